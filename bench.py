@@ -1,0 +1,340 @@
+#!/usr/bin/env python3
+"""Benchmark of the NuFI hot path on GB300: backtraced point-steps/s.
+
+A step is one whole simulation of the workload (default: 1D1V two-stream
+instability, 256 x 1024 quadrature, dt = 1/16, T = 50, i.e. 801 time steps
+and 8.40e10 backtraced point-steps): every time step traces all points back
+through all earlier substeps, reduces rho, and runs the Poisson + spline
+solve that appends the next coefficient slab.  The headline is the
+FP32-split form; the FP64 plain form runs beside it for the error gate
+(max_n |W_split - W_fp64| / max_n |W_fp64| <= 1e-6) and its own rate.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own
+GPU (the path is not split across GPUs in this build); value is the total
+point-steps of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "backtraced point-steps/s FP32-split vs FP64 at ≤1e-6 rel. energy error"
+UNIT = "point-steps/s"
+# Algorithmic work per point-step (one drift + one field evaluation + one
+# kick, order 4, all field components from one gather): 1D 30, 2D 136,
+# 3D 460 flop.
+FLOP_PER_POINT_STEP = {1: 30, 2: 136, 3: 460}
+GATE = 1e-6
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks + throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(self.NAMES, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measure_fma_peaks():
+    """FP32 / FP64 FMA throughput of this GPU (TFLOP/s), from probes/peaks.cu."""
+    import ctypes
+    lib = ctypes.CDLL(str(ROOT / "numericalflowiteration_gb300" / "libnufi_probes.so"))
+    lib.nufi_probe_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    out = {}
+    for name, fp64, iters in (("fp32", 0, 4096), ("fp64", 1, 128)):
+        best = 0.0
+        for _ in range(3):
+            t = ctypes.c_double()
+            ms = ctypes.c_double()
+            if lib.nufi_probe_fma_peak(fp64, iters, ctypes.byref(t), ctypes.byref(ms)) == 0:
+                best = max(best, t.value)
+        out[name] = best
+    return out
+
+
+def cpu_baseline(cfg, n_last: int, threads: int):
+    """Oracle port (test infrastructure) on the host cores: steps 0..n_last."""
+    from oracle import oracle
+    oracle.build()
+    oracle.set_summation(0)
+    t0 = time.perf_counter()
+    oracle.run(cfg, 0, n_last, keep_rho=False, nthreads=threads)
+    dt = time.perf_counter() - t0
+    ps = cfg.point_steps(0, n_last)
+    return {"value": ps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"steps 0..{n_last} of the workload ({ps:.3e} point-steps, {dt:.1f} s, OpenMP over spatial nodes)"}
+
+
+def run_reference(args, cfg):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n_last = args.ref_steps
+    vals = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(cfg, n_last, threads)
+        if k >= args.warmup:
+            vals.append(r["value"])
+    value = statistics.median(vals)
+    ps = cfg.point_steps(0, n_last)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * ps / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial condition)",
+            "config": {"workload": args.workload, "sample_steps": f"0..{n_last}", "threads": threads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"steps 0..{n_last} per step ({ps:.3e} point-steps)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, cfg):
+    import torch
+    import numericalflowiteration_gb300 as nufi
+    from numericalflowiteration_gb300 import build
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    build.build()
+    nufi.load()
+
+    cfg_split = cfg.replace(precision="fp32split")
+    sim = nufi.Simulation(cfg_split, device=local)
+    ext = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        sim.run(energy=False)
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = sim.launches
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            e0.record()
+        sim.run(energy=False)
+        with torch.cuda.stream(ext):
+            e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    barrier()
+    clocks = sampler.stop()
+    launches = sim.launches - launches0
+    total_ms = sum(times)
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    ps = cfg.point_steps()
+    value = ws * ps / (ms_per_step * 1e-3)
+    e_split = sim.energy()
+
+    # FP64 plain form: same workload, for the error gate and its own rate.
+    fp64 = None
+    if not args.no_fp64:
+        sim64 = nufi.Simulation(cfg.replace(precision="fp64"), device=local)
+        ext64 = torch.cuda.ExternalStream(sim64.stream, device=torch.device("cuda", local))
+        sim64.run(energy=False)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext64):
+            e0.record()
+        sim64.run(energy=False)
+        with torch.cuda.stream(ext64):
+            e1.record()
+        e1.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        e64 = sim64.energy()
+        sim64.close()
+        err_max = float(np.max(np.abs(e_split - e64)) / np.max(np.abs(e64)))
+        err_pt = float(np.max(np.abs(e_split - e64) / np.abs(e64)))
+        fp64 = {"value": ps / (ms64 * 1e-3), "ms_per_step": ms64, "speedup_split_vs_fp64": ms64 / ms_per_step,
+                "energy_err_max_normalised": err_max, "energy_err_pointwise_max": err_pt,
+                "gate": GATE, "gate_passed": err_max <= GATE}
+
+    # Dominant kernel (the trace): CUDA events around compute_rho(n) on the
+    # handle's stream at several n (trace + a 1-block rho finalize).
+    ns = [cfg.Nt // 4, cfg.Nt // 2, (3 * cfg.Nt) // 4, cfg.Nt]
+    kt, kps = 0.0, 0
+    for n in ns:
+        for rep in range(2):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(ext):
+                e0.record()
+            sim.compute_rho(n)
+            with torch.cuda.stream(ext):
+                e1.record()
+            e1.synchronize()
+            if rep == 1:
+                kt += e0.elapsed_time(e1)
+                kps += cfg.n_points * n
+    kernel_rate = kps / (kt * 1e-3)
+    peaks = measure_fma_peaks()
+    flop = FLOP_PER_POINT_STEP[cfg.dim]
+    achieved = kernel_rate * flop / 1e12
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32"], "unit": "TFLOP/s",
+                "frac": achieved / peaks["fp32"] if peaks["fp32"] else None, "traffic": None,
+                "peak_source": "measured live: FP32 FMA chains (probes/peaks.cu)",
+                "flop_per_point_step": flop, "kernel": "trace_split_1d_kernel",
+                "kernel_point_steps_per_s": kernel_rate, "fp64_fma_peak_tflops": peaks["fp64"]}
+
+    # End to end through the reference-facing calls with host buffers, the
+    # loop of bin/test_nufi_gpu_1d.cpp:241-252: compute_rho -> download_rho
+    # -> field solve (host rho in, host slab out) -> upload_phi, per step.
+    e2e = None
+    if not args.no_e2e:
+        sim2 = nufi.Simulation(cfg_split, device=local)
+        rho = np.zeros(cfg.n_spatial)
+        coeffs = np.zeros((cfg.Nt + 1) * cfg.stride_t)
+        e2e_times = []
+        for rep in range(1 + max(1, args.steps // 2)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for n in range(cfg.Nt + 1):
+                rho[:] = 0
+                sim2.compute_rho(n)
+                sim2.download_rho(rho)
+                slab, _ = sim2.field_solve(rho)
+                coeffs[n * cfg.stride_t:(n + 1) * cfg.stride_t] = slab
+                sim2.upload_phi(n, coeffs)
+            torch.cuda.synchronize()
+            if rep > 0:
+                e2e_times.append(time.perf_counter() - t0)
+        sim2.close()
+        e2e_s = statistics.median(e2e_times)
+        steps = cfg.Nt + 1
+        e2e = {"value": ws * ps / e2e_s, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
+               "h2d_bytes_per_step": steps * 8 * (cfg.n_spatial + cfg.stride_t),
+               "d2h_bytes_per_step": steps * 8 * (cfg.n_spatial + cfg.stride_t + 1),
+               "path": "drop-in C ABI loop with host buffers (compute_rho, download_rho, field_solve, upload_phi)"}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(cfg.replace(precision="fp64"), args.cpu_steps, os.cpu_count() or 1)
+    sim.close()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (analytic initial condition)",
+                "config": {"workload": args.workload, "Nx": cfg.Nx[0], "Nv": cfg.Nv[0], "Nt": cfg.Nt, "dt": cfg.dt,
+                           "point_steps_per_step": ps, "precision": "fp32-split (FP64 rho/solve)",
+                           "l2": "flushed between timed steps (256 MB write)",
+                           "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                "fp64_plain": fp64, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    from numericalflowiteration_gb300.config import WORKLOADS
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="two_stream_1d_256x1024_T50", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=120, help="CPU baseline sample: steps 0..N")
+    ap.add_argument("--ref-steps", type=int, default=40, help="reference arm sample per step: steps 0..N")
+    args = ap.parse_args(argv)
+    cfg = WORKLOADS[args.workload]()
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+    return run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,149 @@
+/*
+ * nufi_gb300.h — C ABI of the GB300 (sm_103a) NuFI hot path.
+ *
+ * The hot path of Numerical Flow Iteration: at time step n every phase-space
+ * quadrature point (x, v) is traced backwards through n Störmer–Verlet
+ * substeps over the stored B-spline potential coefficients of steps
+ * n-1 .. 0, f0 is evaluated at the foot of the characteristic, and
+ * rho(x) = -sum_v w f~ is formed.  A periodic Poisson + spline
+ * interpolation solve then appends slab n of the coefficient history.
+ *
+ * Every function returns an int status (NUFI_OK = 0).  On failure a message
+ * is kept per handle (nufi_last_error) or per thread for handle-less calls
+ * (nufi_last_error(NULL)).  Nothing here throws; the C++ wrappers in
+ * include/nufi_gb300/ turn the status codes back into the exception types
+ * the reference raises (std::range_error, nufi::cuda::exception,
+ * std::invalid_argument).
+ *
+ * Threading: one handle = one CUDA stream.  Calls on a handle are stream
+ * ordered; the download_* calls and nufi_synchronize block.  A handle must
+ * not be used from two host threads at once (the reference's cuda_kernel is
+ * not thread safe either).
+ *
+ * Grid conventions (reference nufi/cuda_kernel.cu:37-47, 216-231, 398-418):
+ *   x_i = x_min + i*dx      (spatial nodes, dx = (x_max-x_min)/Nx)
+ *   v_j = v_min + j*dv + dv/2  (velocity midpoints, dv = (v_max-v_min)/Nv)
+ *   flattened quadrature index q = s*Nm + m with s the spatial index
+ *   (x fastest, then y, then z) and m the velocity index (u fastest, then
+ *   v, then w); Nm = Nu*Nv*Nw.  This is the reference's q order.
+ *   rho[s] = -(du*dv*dw) * sum_m f~(s, m)   (no +1 background; the Poisson
+ *   solve drops the mean mode).
+ * Coefficient history layout (host side, as the reference keeps it):
+ *   slab n starts at base + n*stride_t, stride_t = prod_d (N_d + order - 1),
+ *   x fastest; each slab is the periodic padding c[i] = c~[i mod N].
+ */
+#ifndef NUFI_GB300_H
+#define NUFI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NUFI_OK              0
+#define NUFI_ERR_INVALID     1  /* bad argument or configuration            */
+#define NUFI_ERR_RANGE       2  /* n > Nt, q range outside the grid, sizes  */
+#define NUFI_ERR_CUDA        3  /* a CUDA runtime call failed               */
+#define NUFI_ERR_UNSUPPORTED 4  /* combination not built (see message)      */
+#define NUFI_ERR_DEVICE      5  /* a device-side check raised its flag      */
+
+/* ---- precision modes --------------------------------------------------- */
+/* FP64 plain: the whole trace in double, same operation order as the
+ * reference's eval_ftilda (nufi/rho.hpp:31-61, 191-232, 318-367).          */
+#define NUFI_PREC_FP64        0
+/* FP32 split: position = integer cell + FP32 fraction, velocity = exact
+ * grid velocity + FP32 kick sum, field tables in FP32, f0 evaluated as a
+ * perturbation of its value at the grid velocity; FP64 only in the rho
+ * accumulator, the Poisson solve and the spline interpolation solve.       */
+#define NUFI_PREC_FP32_SPLIT  1
+
+/* ---- initial conditions (f0) ------------------------------------------- */
+/* params[0] = alpha, params[1] = k (same on every axis)                    */
+/* Landau:      (1 + alpha sum_d cos(k x_d)) exp(-|v|^2/2) / (2 pi)^(dim/2)  */
+#define NUFI_F0_LANDAU        0
+/* Two-stream:  (1 + alpha cos(k x)) v^2 exp(-v^2/2) / sqrt(2 pi)   (1D)    */
+#define NUFI_F0_TWO_STREAM    1
+/* Bump-on-tail:(1 + alpha cos(k x)) [0.9 N(v;0,1) + 0.1 N(v;u_b,sigma_b)]
+ *              params[2] = u_b, params[3] = sigma_b                  (1D)  */
+#define NUFI_F0_BUMP_ON_TAIL  2
+
+typedef struct nufi_config {
+    int32_t dim;          /* 1, 2 or 3                                     */
+    int32_t order;        /* B-spline order (4 = cubic)                    */
+    int32_t precision;    /* NUFI_PREC_*                                   */
+    int32_t f0_kind;      /* NUFI_F0_*                                     */
+    int64_t Nx[3];        /* spline nodes per spatial axis (unused: 1)     */
+    int64_t Nv[3];        /* quadrature nodes per velocity axis (unused: 1)*/
+    int64_t Nt;           /* time steps; slabs 0 .. Nt are kept            */
+    double  dt;           /* time-step size                                */
+    double  x_min[3], x_max[3];
+    double  v_min[3], v_max[3];
+    double  f0_params[8];
+} nufi_config;
+
+typedef struct nufi_handle nufi_handle;
+
+/* Message of the last failed call on h (or of this thread's last failed
+ * handle-less call when h == NULL).  Never NULL. */
+const char *nufi_last_error(const nufi_handle *h);
+
+/* ---- lifetime ----------------------------------------------------------
+ * Replaces the constructor of nufi::dimN::cuda_kernel<real,order>
+ * (nufi/cuda_kernel.hpp:37-38, 82, 124; nufi/cuda_kernel.cu:81-109,
+ * 273-286, 468-483): allocates the coefficient history (Nt+1 slabs),
+ * rho and the metrics accumulators on `device`. */
+int nufi_create(const nufi_config *cfg, int device, nufi_handle **out);
+int nufi_destroy(nufi_handle *h);
+
+/* ---- reference-facing drop-in calls ------------------------------------ */
+/* cuda_kernel::compute_rho (nufi/cuda_kernel.cu:112-132, 289-311, 486-510):
+ * rho := -w * sum over q in [q_begin, q_end) of f~(n, q), using slabs
+ * 0 .. n-1.  NUFI_ERR_RANGE if n > Nt or q_end > Nq.  Asynchronous. */
+int nufi_compute_rho(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end);
+/* cuda_kernel::download_rho (nufi/cuda_kernel.cu:135-145): rho[s] += the
+ * device rho (so the caller zeroes its buffer first).  Blocks. */
+int nufi_download_rho(nufi_handle *h, double *rho);
+int nufi_download_rho_f32(nufi_handle *h, float *rho);
+/* cuda_kernel::upload_phi (nufi/cuda_kernel.cu:147-156): copies slab n from
+ * coeffs_base + n*stride_t of the caller's history to the device. */
+int nufi_upload_phi(nufi_handle *h, int64_t n, const double *coeffs_base);
+int nufi_upload_phi_f32(nufi_handle *h, int64_t n, const float *coeffs_base);
+
+/* ---- device-resident stepping ----------------------------------------- */
+/* One full time step on the device: rho(n) from slabs 0..n-1, then the
+ * Poisson + interpolation solve (FFT-diagonal kernel) writes slab n and the
+ * electric energy W_n = 1/2 int |E|^2 (what poisson::solve returns,
+ * nufi/poisson.cpp:66-89).  energy may be NULL; if given, the call blocks. */
+int nufi_step(nufi_handle *h, int64_t n, double *energy);
+/* Steps n0 .. n1 (inclusive) as one CUDA-graph launch; energy_hist (may be
+ * NULL) receives W_n0 .. W_n1.  Blocks when energy_hist != NULL. */
+int nufi_run(nufi_handle *h, int64_t n0, int64_t n1, double *energy_hist);
+/* Copies slabs n0 .. n1 of the device history into the caller's history
+ * (reference layout, slab n at coeffs_base + n*stride_t).  Blocks. */
+int nufi_download_history(nufi_handle *h, int64_t n0, int64_t n1, double *coeffs_base);
+/* Electric energies W_n0 .. W_n1 recorded by nufi_step / nufi_run. Blocks. */
+int nufi_download_energy(nufi_handle *h, int64_t n0, int64_t n1, double *energy);
+/* Replaces poisson<double>::solve + dimN::interpolate<double,order>
+ * (nufi/poisson.cpp:66-89, 190-219, 328-362; nufi/fields.hpp:63-142,
+ * 186-300, 352-490) on host buffers: rho (N values, x fastest) in,
+ * padded slab (stride_t values) out, returns W in *energy.  Blocks. */
+int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double *energy);
+
+/* ---- information ------------------------------------------------------- */
+int nufi_synchronize(nufi_handle *h);
+/* stride_t (values per slab), number of spatial nodes, number of points */
+int nufi_sizes(const nufi_handle *h, int64_t *stride_t, int64_t *n_spatial, int64_t *n_points);
+/* The CUDA stream the handle launches on (cudaStream_t as void*), so that
+ * callers can time with events on that stream. */
+int nufi_stream(const nufi_handle *h, void **stream);
+/* Number of kernels this handle has launched since creation. */
+int nufi_launch_count(const nufi_handle *h, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NUFI_GB300_H */

@@ -1,0 +1,203 @@
+"""ctypes binding of libnufi_gb300.so (include/nufi_gb300.h).
+
+``Simulation`` mirrors the reference's per-device object
+``nufi::dimN::cuda_kernel<real,order>`` (nufi/cuda_kernel.hpp:33-56): the
+drop-in calls compute_rho / download_rho / upload_phi, plus the
+device-resident step / run / field_solve of this library.  Failures raise
+the exception type the reference raises for the same condition:
+``IndexError`` where it throws std::range_error, ``RuntimeError`` for CUDA
+errors (nufi::cuda::exception), ``ValueError`` for invalid arguments and
+``NotImplementedError`` for configurations this build does not cover.
+
+There is no fallback: if the CUDA library is missing or cannot load,
+``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from .config import Config
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libnufi_gb300.so"
+
+OK, ERR_INVALID, ERR_RANGE, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE = range(6)
+
+# Every exported function of include/nufi_gb300.h with its C signature.
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+SIGNATURES = {
+    "nufi_last_error": (ctypes.c_char_p, [_P]),
+    "nufi_create": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P)]),
+    "nufi_destroy": (ctypes.c_int, [_P]),
+    "nufi_compute_rho": (ctypes.c_int, [_P, _I64, _I64, _I64]),
+    "nufi_download_rho": (ctypes.c_int, [_P, _P]),
+    "nufi_download_rho_f32": (ctypes.c_int, [_P, _P]),
+    "nufi_upload_phi": (ctypes.c_int, [_P, _I64, _P]),
+    "nufi_upload_phi_f32": (ctypes.c_int, [_P, _I64, _P]),
+    "nufi_step": (ctypes.c_int, [_P, _I64, _P]),
+    "nufi_run": (ctypes.c_int, [_P, _I64, _I64, _P]),
+    "nufi_download_history": (ctypes.c_int, [_P, _I64, _I64, _P]),
+    "nufi_download_energy": (ctypes.c_int, [_P, _I64, _I64, _P]),
+    "nufi_field_solve": (ctypes.c_int, [_P, _P, _P, _P]),
+    "nufi_synchronize": (ctypes.c_int, [_P]),
+    "nufi_sizes": (ctypes.c_int, [_P, _P, _P, _P]),
+    "nufi_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "nufi_launch_count": (ctypes.c_int, [_P, _P]),
+}
+
+_lib = None
+
+
+class NufiError(RuntimeError):
+    pass
+
+
+def load(path: Path | None = None):
+    """Load the CUDA library (raises if it is absent: there is no CPU path)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with `python -m numericalflowiteration_gb300.build`")
+    L = ctypes.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _raise(code: int, msg: str):
+    if code == ERR_RANGE:
+        raise IndexError(msg)
+    if code == ERR_INVALID:
+        raise ValueError(msg)
+    if code == ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise NufiError(f"[{code}] {msg}")
+
+
+class Simulation:
+    """One configuration on one GPU (one CUDA stream)."""
+
+    def __init__(self, cfg: Config, device: int = 0):
+        self.cfg = cfg
+        self._lib = load()
+        self._c = cfg.to_c()
+        h = ctypes.c_void_p()
+        st = self._lib.nufi_create(ctypes.byref(self._c), device, ctypes.byref(h))
+        if st:
+            _raise(st, self._lib.nufi_last_error(None).decode())
+        self._h = h
+        self.stride_t = cfg.stride_t
+        self.n_spatial = cfg.n_spatial
+        self.n_points = cfg.n_points
+
+    # -- plumbing ---------------------------------------------------------
+    def _check(self, st: int):
+        if st:
+            _raise(st, self._lib.nufi_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.nufi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._check(self._lib.nufi_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    @property
+    def launches(self) -> int:
+        c = np.zeros(1, dtype=np.int64)
+        self._check(self._lib.nufi_launch_count(self._h, _ptr(c)))
+        return int(c[0])
+
+    # -- drop-in calls (cuda_kernel / cuda_scheduler) ----------------------
+    def compute_rho(self, n: int, q_begin: int = 0, q_end: int | None = None):
+        q_end = self.n_points if q_end is None else q_end
+        self._check(self._lib.nufi_compute_rho(self._h, n, q_begin, q_end))
+
+    def download_rho(self, rho: np.ndarray) -> np.ndarray:
+        """rho += device rho (the caller zeroes it first, as the reference's drivers do)."""
+        if rho.dtype == np.float64:
+            self._check(self._lib.nufi_download_rho(self._h, _ptr(rho)))
+        elif rho.dtype == np.float32:
+            self._check(self._lib.nufi_download_rho_f32(self._h, _ptr(rho)))
+        else:
+            raise TypeError("rho must be float64 or float32")
+        return rho
+
+    def upload_phi(self, n: int, coeffs: np.ndarray):
+        if coeffs.dtype == np.float64:
+            self._check(self._lib.nufi_upload_phi(self._h, n, _ptr(coeffs)))
+        elif coeffs.dtype == np.float32:
+            self._check(self._lib.nufi_upload_phi_f32(self._h, n, _ptr(coeffs)))
+        else:
+            raise TypeError("coeffs must be float64 or float32")
+
+    # -- device-resident stepping ----------------------------------------
+    def step(self, n: int) -> float:
+        e = np.zeros(1)
+        self._check(self._lib.nufi_step(self._h, n, _ptr(e)))
+        return float(e[0])
+
+    def step_async(self, n: int):
+        self._check(self._lib.nufi_step(self._h, n, None))
+
+    def run(self, n0: int = 0, n1: int | None = None, energy: bool = True):
+        n1 = self.cfg.Nt if n1 is None else n1
+        if energy:
+            e = np.zeros(n1 - n0 + 1)
+            self._check(self._lib.nufi_run(self._h, n0, n1, _ptr(e)))
+            return e
+        self._check(self._lib.nufi_run(self._h, n0, n1, None))
+        return None
+
+    def history(self, n0: int = 0, n1: int | None = None, out: np.ndarray | None = None) -> np.ndarray:
+        n1 = self.cfg.Nt if n1 is None else n1
+        if out is None:
+            out = np.zeros((self.cfg.Nt + 1) * self.stride_t)
+        self._check(self._lib.nufi_download_history(self._h, n0, n1, _ptr(out)))
+        return out
+
+    def energy(self, n0: int = 0, n1: int | None = None) -> np.ndarray:
+        n1 = self.cfg.Nt if n1 is None else n1
+        e = np.zeros(n1 - n0 + 1)
+        self._check(self._lib.nufi_download_energy(self._h, n0, n1, _ptr(e)))
+        return e
+
+    def field_solve(self, rho: np.ndarray):
+        r = np.ascontiguousarray(rho, dtype=np.float64)
+        slab = np.zeros(self.stride_t)
+        e = np.zeros(1)
+        self._check(self._lib.nufi_field_solve(self._h, _ptr(r), _ptr(slab), _ptr(e)))
+        return slab, float(e[0])
+
+    def synchronize(self):
+        self._check(self._lib.nufi_synchronize(self._h))

@@ -1,0 +1,671 @@
+// nufi_api.cu — the C ABI of include/nufi_gb300.h: handle lifetime, device
+// memory of the coefficient history, and the launch sequence of the hot
+// path on one CUDA stream.
+//
+// Device memory of a handle (all allocated once, in nufi_create):
+//   hist     (Nt+1) FP64 slabs, reference layout inside a slab, slab pitch
+//            rounded up to 16 bytes; slab n is written by the field solve
+//            (nufi_step / nufi_run) or by nufi_upload_phi.
+//   tables   (Nt+1) FP32 field tables (split mode only): 1D per cell
+//            float4 K(A,B,C) of the spline derivative, 2D/3D the FP32 slab.
+//   partial  [vblocks][Ns] FP64 per-block sums of the trace.
+//   rho      [Ns] FP64, energy [Nt+1] FP64, err (one error word).
+//   solve plan: per-axis twiddles, inverse collocation symbols, |k|^2.
+//   split tables: per-velocity-node constants and per-cell phases.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "nufi_kernels.cuh"
+
+using namespace nufi_gb300;
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+}  // namespace
+
+struct nufi_handle {
+    nufi_config cfg{};
+    Problem p{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    double *hist = nullptr;
+    float *tables = nullptr;
+    double *partial = nullptr;
+    double *rho = nullptr;
+    double *energy = nullptr;
+    double *rho_in = nullptr;     // nufi_field_solve scratch
+    double *slab_out = nullptr;   // nufi_field_solve scratch
+    double *energy_tmp = nullptr; // nufi_field_solve scratch
+    unsigned *err = nullptr;
+    SplitNode *nodes = nullptr;
+    float2 *phase = nullptr;
+    SolvePlan plan;
+    bool solve_ok = false;
+    std::string solve_why;
+    LaunchShape shape;
+    std::string last_error;
+    long long launches = 0;
+    std::map<std::pair<long long, long long>, std::pair<cudaGraphExec_t, long long>> graphs;
+    std::vector<void *> allocations;
+};
+
+namespace {
+
+int fail(nufi_handle *h, int code, const std::string &msg)
+{
+    if (h) h->last_error = msg;
+    else g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(nufi_handle *h, cudaError_t e, const char *where)
+{
+    return fail(h, NUFI_ERR_CUDA, std::string(where) + ": " + cudaGetErrorName(e) + ": " + cudaGetErrorString(e));
+}
+
+#define NUFI_CUDA(h, call)                                         \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #call);   \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(nufi_handle *h, T **ptr, size_t count)
+{
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
+    if (e != cudaSuccess) return e;
+    h->allocations.push_back(p);
+    *ptr = static_cast<T *>(p);
+    return cudaSuccess;
+}
+
+bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
+
+int ilog2(long long v)
+{
+    int l = 0;
+    while ((1LL << l) < v) ++l;
+    return l;
+}
+
+// Host-side B-spline basis at x = 0 (collocation stencil N_j(0)).
+void stencil(int order, double *Nb)
+{
+    switch (order) {
+#define NUFI_STENCIL(O) \
+    case O: bspline_basis<double, O, 0>(0.0, Nb); return;
+        NUFI_STENCIL(2) NUFI_STENCIL(3) NUFI_STENCIL(4) NUFI_STENCIL(5) NUFI_STENCIL(6) NUFI_STENCIL(7)
+        NUFI_STENCIL(8)
+#undef NUFI_STENCIL
+    default: break;
+    }
+}
+
+int validate(const nufi_config *c, std::string &why)
+{
+    if (!c) { why = "null config"; return NUFI_ERR_INVALID; }
+    if (c->dim < 1 || c->dim > 3) { why = "dim must be 1, 2 or 3"; return NUFI_ERR_INVALID; }
+    if (c->order < 2 || c->order > kMaxOrder) { why = "order must be in [2, 8]"; return NUFI_ERR_INVALID; }
+    if (c->Nt < 0) { why = "Nt must be >= 0"; return NUFI_ERR_INVALID; }
+    if (!(c->dt > 0) || !std::isfinite(c->dt)) { why = "dt must be positive and finite"; return NUFI_ERR_INVALID; }
+    for (int a = 0; a < c->dim; ++a) {
+        if (c->Nx[a] < 1 || c->Nv[a] < 1) { why = "grid sizes must be >= 1"; return NUFI_ERR_INVALID; }
+        if (c->Nx[a] > (1 << 20) || c->Nv[a] > kMaxVelocityTable) {
+            why = "grid too large for this build";
+            return NUFI_ERR_RANGE;
+        }
+        if (!(c->x_max[a] > c->x_min[a]) || !(c->v_max[a] > c->v_min[a])) {
+            why = "domain bounds must satisfy min < max";
+            return NUFI_ERR_INVALID;
+        }
+    }
+    if (c->precision != NUFI_PREC_FP64 && c->precision != NUFI_PREC_FP32_SPLIT) {
+        why = "unknown precision mode";
+        return NUFI_ERR_INVALID;
+    }
+    if (c->f0_kind < NUFI_F0_LANDAU || c->f0_kind > NUFI_F0_BUMP_ON_TAIL) {
+        why = "unknown f0 kind";
+        return NUFI_ERR_INVALID;
+    }
+    if (c->dim > 1 && c->f0_kind != NUFI_F0_LANDAU) {
+        why = "f0 kinds other than Landau are 1D only";
+        return NUFI_ERR_UNSUPPORTED;
+    }
+    if (c->precision == NUFI_PREC_FP64 && !fp64_order_supported(c->dim, c->order)) {
+        why = "FP64 trace not built for this (dim, order)";
+        return NUFI_ERR_UNSUPPORTED;
+    }
+    if (c->precision == NUFI_PREC_FP32_SPLIT && !split_supported(c->dim, c->order, c->f0_kind)) {
+        why = "FP32-split trace not built for this (dim, order, f0)";
+        return NUFI_ERR_UNSUPPORTED;
+    }
+    return NUFI_OK;
+}
+
+Problem make_problem(const nufi_config &c)
+{
+    Problem p{};
+    p.dim = c.dim;
+    p.order = c.order;
+    p.f0_kind = c.f0_kind;
+    p.precision = c.precision;
+    p.Ns = 1;
+    p.Nm = 1;
+    p.stride_t = 1;
+    for (int a = 0; a < 3; ++a) {
+        const bool in = a < c.dim;
+        p.N[a] = in ? int(c.Nx[a]) : 1;
+        p.M[a] = in ? int(c.Nv[a]) : 1;
+        p.P[a] = in ? int(c.Nx[a] + c.order - 1) : 1;
+        // config.hpp:67-69
+        p.xmin[a] = in ? c.x_min[a] : 0.0;
+        p.L[a] = in ? c.x_max[a] - c.x_min[a] : 1.0;
+        p.Linv[a] = 1 / p.L[a];
+        p.dx[a] = p.L[a] / p.N[a];
+        p.dxinv[a] = 1 / p.dx[a];
+        p.vmin[a] = in ? c.v_min[a] : 0.0;
+        p.dv[a] = in ? (c.v_max[a] - c.v_min[a]) / p.M[a] : 1.0;
+        if (in) {
+            p.Ns *= p.N[a];
+            p.Nm *= p.M[a];
+            p.stride_t *= p.P[a];
+        }
+    }
+    p.Nq = p.Ns * p.Nm;
+    p.hist_stride = (p.stride_t + 1) / 2 * 2;
+    p.table_stride = c.dim == 1 ? 4LL * p.N[0] : (p.stride_t + 3) / 4 * 4;
+    p.dt = c.dt;
+    for (int i = 0; i < 8; ++i) p.f0p[i] = c.f0_params[i];
+    p.wv = 1;
+    for (int a = 0; a < c.dim; ++a) p.wv *= p.dv[a];
+    return p;
+}
+
+// Trace tiling: the largest points-per-thread that still gives about four
+// resident blocks per SM, then fewer warps per block for small grids.
+LaunchShape choose_shape(const Problem &p, int sms)
+{
+    const long long sblocks = (p.Ns + 31) / 32;
+    const int ppts[3] = {4, 2, 1};
+    const int warps[3] = {4, 2, 1};
+    for (int w : warps)
+        for (int ppt : ppts) {
+            const long long vb = (p.Nm + (long long)w * ppt - 1) / ((long long)w * ppt);
+            if (sblocks * vb >= 4LL * sms) {
+                LaunchShape s;
+                s.warps = w;
+                s.ppt = ppt;
+                s.vblocks = int(vb);
+                return s;
+            }
+        }
+    LaunchShape s;
+    s.warps = 1;
+    s.ppt = 1;
+    s.vblocks = int(p.Nm);
+    return s;
+}
+
+int build_solve_plan(nufi_handle *h)
+{
+    const Problem &p = h->p;
+    h->solve_ok = false;
+    for (int a = 0; a < p.dim; ++a)
+        if (!is_pow2(p.N[a])) {
+            h->solve_why = "device field solve needs power-of-two grid sizes";
+            return NUFI_OK;
+        }
+    const size_t smem = size_t(p.Ns) * sizeof(double2);
+    if (p.Ns > 8192) {
+        h->solve_why = "device field solve holds at most 8192 grid nodes";
+        return NUFI_OK;
+    }
+    double Nb[kMaxOrder] = {0};
+    stencil(p.order, Nb);
+    for (int a = 0; a < p.dim; ++a) {
+        const int N = p.N[a];
+        std::vector<double2> tw(std::max(1, N / 2)), is(N);
+        std::vector<double> ks(N);
+        for (int j = 0; j < N / 2; ++j) {
+            const double ang = -2.0 * M_PI * double(j) / double(N);
+            tw[j] = make_double2(std::cos(ang), std::sin(ang));
+        }
+        for (int k = 0; k < N; ++k) {
+            double re = 0, im = 0;
+            for (int j = 0; j < p.order; ++j) {
+                const double ang = 2.0 * M_PI * double((long long)j * k % N) / double(N);
+                re += Nb[j] * std::cos(ang);
+                im += Nb[j] * std::sin(ang);
+            }
+            const double den = re * re + im * im;
+            is[k] = make_double2(re / den, -im / den);
+            const double kf = (2 * k < N) ? double(k) : double(N - k);
+            const double kk = kf * (2 * M_PI * p.Linv[a]);
+            ks[k] = kk * kk;
+        }
+        NUFI_CUDA(h, dalloc(h, &h->plan.tw[a], tw.size()));
+        NUFI_CUDA(h, dalloc(h, &h->plan.isym[a], is.size()));
+        NUFI_CUDA(h, dalloc(h, &h->plan.ksq[a], ks.size()));
+        NUFI_CUDA(h, cudaMemcpy(h->plan.tw[a], tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
+        NUFI_CUDA(h, cudaMemcpy(h->plan.isym[a], is.data(), is.size() * sizeof(double2), cudaMemcpyHostToDevice));
+        NUFI_CUDA(h, cudaMemcpy(h->plan.ksq[a], ks.data(), ks.size() * sizeof(double), cudaMemcpyHostToDevice));
+        h->plan.log2n[a] = ilog2(N);
+    }
+    h->plan.smem = smem;
+    NUFI_CUDA(h, field_solve_set_smem(smem));
+    h->solve_ok = true;
+    return NUFI_OK;
+}
+
+// Per-velocity-node and per-cell constants of the split form (FP64 here).
+int build_split_tables(nufi_handle *h)
+{
+    const Problem &p = h->p;
+    std::vector<SplitNode> nodes;
+    std::vector<float2> phase;
+    const double c0 = 0.39894228040143267793994;
+    for (int a = 0; a < p.dim; ++a) {
+        for (int j = 0; j < p.M[a]; ++j) {
+            SplitNode nd{};
+            const double u0 = p.vmin[a] + j * p.dv[a] + p.dv[a] / 2;
+            const double w0 = u0 * p.dt / p.dx[a];
+            const double S = std::floor(w0);
+            const double sig = w0 - S;
+            long long S0 = (long long)S % p.N[a];
+            if (S0 < 0) S0 += p.N[a];
+            nd.u0 = u0;
+            nd.u0f = float(u0);
+            nd.sig_hi = float(sig);
+            nd.sig_lo = float(sig - double(nd.sig_hi));
+            nd.S0 = int(S0);
+            const double gm = c0 * std::exp(-u0 * u0 / 2);
+            if (p.f0_kind == NUFI_F0_LANDAU) {
+                nd.g = 0.39894228040143267793994 * std::exp(-u0 * u0 / 2);
+                nd.ga = float(nd.g);
+            } else if (p.f0_kind == NUFI_F0_TWO_STREAM) {
+                nd.g = 0.39894228040143267793994 * std::exp(-u0 * u0 / 2.) * u0 * u0;
+                nd.ga = float(gm);
+            } else {
+                const double sb = p.f0p[3], z = (u0 - p.f0p[2]) / sb;
+                const double g1 = 0.9 * gm, g2 = 0.1 * c0 / sb * std::exp(-z * z / 2);
+                nd.g = g1 + g2;
+                nd.ga = float(g1);
+                nd.gb = float(g2);
+            }
+            nodes.push_back(nd);
+        }
+        for (int i = 0; i < p.N[a]; ++i) {
+            const double th = p.f0p[1] * (p.xmin[a] + i * p.dx[a]);
+            phase.push_back(make_float2(float(std::cos(th)), float(std::sin(th))));
+        }
+    }
+    NUFI_CUDA(h, dalloc(h, &h->nodes, nodes.size()));
+    NUFI_CUDA(h, dalloc(h, &h->phase, phase.size()));
+    NUFI_CUDA(h, cudaMemcpy(h->nodes, nodes.data(), nodes.size() * sizeof(SplitNode), cudaMemcpyHostToDevice));
+    NUFI_CUDA(h, cudaMemcpy(h->phase, phase.data(), phase.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    return NUFI_OK;
+}
+
+// Read and clear the device error word (the stream must be idle).
+int check_device_flags(nufi_handle *h)
+{
+    unsigned flags = 0;
+    NUFI_CUDA(h, cudaMemcpy(&flags, h->err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (flags) {
+        NUFI_CUDA(h, cudaMemset(h->err, 0, sizeof(unsigned)));
+        std::string m = "device check failed:";
+        if (flags & kErrCellIndex) m += " cell index out of range (non-finite position?)";
+        if (flags & kErrKickRange) m += " split-mode kick displacement out of range";
+        if (flags & kErrSolveSize) m += " field-solve size";
+        return fail(h, NUFI_ERR_DEVICE, m);
+    }
+    return NUFI_OK;
+}
+
+int sync_and_check(nufi_handle *h)
+{
+    NUFI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return check_device_flags(h);
+}
+
+// Enqueue the trace of step n over [qb, qe) into h->partial.
+int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int mode)
+{
+    const Problem &p = h->p;
+    cudaError_t e;
+    if (p.precision == NUFI_PREC_FP64)
+        e = launch_trace_fp64(p, h->shape, h->hist, int(n), qb, qe, mode, h->partial, h->err, h->stream);
+    else
+        e = launch_trace_split(p, h->shape, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, h->err,
+                               h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "trace launch");
+    h->launches += 1;
+    return NUFI_OK;
+}
+
+int enqueue_step(nufi_handle *h, long long n)
+{
+    const Problem &p = h->p;
+    int st = enqueue_trace(h, n, 0, p.Nq, 0);
+    if (st) return st;
+    cudaError_t e = launch_field_solve(p, h->plan, h->shape.vblocks, h->partial, nullptr, h->rho,
+                                       h->hist + n * p.hist_stride,
+                                       h->tables ? h->tables + n * p.table_stride : nullptr, h->energy + n, h->err,
+                                       h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
+    h->launches += 1;
+    return NUFI_OK;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+void release(nufi_handle *h)
+{
+    for (auto &g : h->graphs) cudaGraphExecDestroy(g.second.first);
+    h->graphs.clear();
+    for (void *p : h->allocations) cudaFree(p);
+    h->allocations.clear();
+    if (h->stream) cudaStreamDestroy(h->stream);
+    h->stream = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *nufi_last_error(const nufi_handle *h) { return h ? h->last_error.c_str() : g_last_error.c_str(); }
+
+int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
+{
+    if (!out) return fail(nullptr, NUFI_ERR_INVALID, "nufi_create: out is null");
+    *out = nullptr;
+    std::string why;
+    int st = validate(cfg, why);
+    if (st) return fail(nullptr, st, "nufi_create: " + why);
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
+    if (device < 0 || device >= ndev) return fail(nullptr, NUFI_ERR_INVALID, "nufi_create: no such device");
+    std::unique_ptr<nufi_handle> h(new nufi_handle);
+    h->cfg = *cfg;
+    h->device = device;
+    h->p = make_problem(*cfg);
+    DeviceGuard g(device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    h->shape = choose_shape(h->p, sms > 0 ? sms : 1);
+    const Problem &p = h->p;
+    auto bail = [&](int code) {
+        g_last_error = h->last_error;
+        release(h.get());
+        return code;
+    };
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(cuda_fail(h.get(), e, "cudaStreamCreate"));
+    const size_t nslab = size_t(cfg->Nt + 1);
+    if ((e = dalloc(h.get(), &h->hist, nslab * p.hist_stride)) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->partial, size_t(h->shape.vblocks) * p.Ns)) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->rho, size_t(p.Ns))) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->energy, nslab)) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->rho_in, size_t(p.Ns))) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->slab_out, size_t(p.hist_stride))) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->energy_tmp, 1)) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->err, 1)) != cudaSuccess)
+        return bail(cuda_fail(h.get(), e, "cudaMalloc"));
+    if (p.precision == NUFI_PREC_FP32_SPLIT) {
+        if ((e = dalloc(h.get(), &h->tables, nslab * p.table_stride)) != cudaSuccess)
+            return bail(cuda_fail(h.get(), e, "cudaMalloc"));
+        if ((st = build_split_tables(h.get()))) return bail(st);
+        if ((e = cudaMemset(h->tables, 0, nslab * p.table_stride * sizeof(float))) != cudaSuccess)
+            return bail(cuda_fail(h.get(), e, "cudaMemset"));
+    }
+    if ((e = cudaMemset(h->hist, 0, nslab * p.hist_stride * sizeof(double))) != cudaSuccess ||
+        (e = cudaMemset(h->energy, 0, nslab * sizeof(double))) != cudaSuccess ||
+        (e = cudaMemset(h->rho, 0, size_t(p.Ns) * sizeof(double))) != cudaSuccess ||
+        (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess)
+        return bail(cuda_fail(h.get(), e, "cudaMemset"));
+    if ((st = build_solve_plan(h.get()))) return bail(st);
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(cuda_fail(h.get(), e, "nufi_create"));
+    *out = h.release();
+    return NUFI_OK;
+}
+
+int nufi_destroy(nufi_handle *h)
+{
+    if (!h) return NUFI_OK;
+    {
+        DeviceGuard g(h->device);
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        release(h);
+    }
+    delete h;
+    return NUFI_OK;
+}
+
+int nufi_compute_rho(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end)
+{
+    if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
+    if (q_begin < 0 || q_end < q_begin || q_end > h->p.Nq)
+        return fail(h, NUFI_ERR_RANGE, "quadrature range outside [0, Nq]");
+    if (q_begin == q_end) return NUFI_OK;  // as the reference: no launch, rho untouched
+    DeviceGuard g(h->device);
+    int st = enqueue_trace(h, n, q_begin, q_end, 0);
+    if (st) return st;
+    cudaError_t e = launch_finalize_rho(h->p, h->shape.vblocks, h->partial, h->rho, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "finalize launch");
+    h->launches += 1;
+    return NUFI_OK;
+}
+
+static int download_rho_impl(nufi_handle *h, std::vector<double> &tmp)
+{
+    DeviceGuard g(h->device);
+    tmp.resize(size_t(h->p.Ns));
+    NUFI_CUDA(h, cudaMemcpyAsync(tmp.data(), h->rho, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    return sync_and_check(h);
+}
+
+int nufi_download_rho(nufi_handle *h, double *rho)
+{
+    if (!h || !rho) return fail(h, NUFI_ERR_INVALID, "null argument");
+    std::vector<double> tmp;
+    int st = download_rho_impl(h, tmp);
+    if (st) return st;
+    for (size_t i = 0; i < tmp.size(); ++i) rho[i] += tmp[i];
+    return NUFI_OK;
+}
+
+int nufi_download_rho_f32(nufi_handle *h, float *rho)
+{
+    if (!h || !rho) return fail(h, NUFI_ERR_INVALID, "null argument");
+    std::vector<double> tmp;
+    int st = download_rho_impl(h, tmp);
+    if (st) return st;
+    for (size_t i = 0; i < tmp.size(); ++i) rho[i] += float(tmp[i]);
+    return NUFI_OK;
+}
+
+static int upload_slab(nufi_handle *h, int64_t n, const double *slab)
+{
+    const Problem &p = h->p;
+    DeviceGuard g(h->device);
+    NUFI_CUDA(h, cudaMemcpyAsync(h->hist + n * p.hist_stride, slab, size_t(p.stride_t) * sizeof(double),
+                                 cudaMemcpyHostToDevice, h->stream));
+    if (h->tables) {
+        cudaError_t e = launch_derive_table(p, h->hist + n * p.hist_stride, h->tables + n * p.table_stride, h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
+        h->launches += 1;
+    }
+    NUFI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return NUFI_OK;
+}
+
+int nufi_upload_phi(nufi_handle *h, int64_t n, const double *coeffs_base)
+{
+    if (!h || !coeffs_base) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
+    return upload_slab(h, n, coeffs_base + n * h->p.stride_t);
+}
+
+int nufi_upload_phi_f32(nufi_handle *h, int64_t n, const float *coeffs_base)
+{
+    if (!h || !coeffs_base) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
+    std::vector<double> tmp(size_t(h->p.stride_t));
+    const float *src = coeffs_base + n * h->p.stride_t;
+    for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = double(src[i]);
+    return upload_slab(h, n, tmp.data());
+}
+
+int nufi_step(nufi_handle *h, int64_t n, double *energy)
+{
+    if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
+    if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
+    DeviceGuard g(h->device);
+    int st = enqueue_step(h, n);
+    if (st) return st;
+    if (energy) {
+        NUFI_CUDA(h, cudaMemcpyAsync(energy, h->energy + n, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        return sync_and_check(h);
+    }
+    return NUFI_OK;
+}
+
+int nufi_run(nufi_handle *h, int64_t n0, int64_t n1, double *energy_hist)
+{
+    if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (n0 < 0 || n1 < n0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step range outside [0, Nt]");
+    if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
+    DeviceGuard g(h->device);
+    const auto key = std::make_pair((long long)n0, (long long)n1);
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+        cudaGraph_t graph = nullptr;
+        const long long before = h->launches;
+        NUFI_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int st = NUFI_OK;
+        for (int64_t n = n0; n <= n1 && st == NUFI_OK; ++n) st = enqueue_step(h, n);
+        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        const long long per_launch = h->launches - before;
+        h->launches = before;
+        if (st) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+        it = h->graphs.emplace(key, std::make_pair(exec, per_launch)).first;
+    }
+    NUFI_CUDA(h, cudaGraphLaunch(it->second.first, h->stream));
+    h->launches += it->second.second;
+    if (energy_hist) {
+        NUFI_CUDA(h, cudaMemcpyAsync(energy_hist, h->energy + n0, size_t(n1 - n0 + 1) * sizeof(double),
+                                     cudaMemcpyDeviceToHost, h->stream));
+        return sync_and_check(h);
+    }
+    return NUFI_OK;
+}
+
+int nufi_download_history(nufi_handle *h, int64_t n0, int64_t n1, double *coeffs_base)
+{
+    if (!h || !coeffs_base) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (n0 < 0 || n1 < n0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step range outside [0, Nt]");
+    const Problem &p = h->p;
+    DeviceGuard g(h->device);
+    NUFI_CUDA(h, cudaMemcpy2DAsync(coeffs_base + n0 * p.stride_t, size_t(p.stride_t) * sizeof(double),
+                                   h->hist + n0 * p.hist_stride, size_t(p.hist_stride) * sizeof(double),
+                                   size_t(p.stride_t) * sizeof(double), size_t(n1 - n0 + 1),
+                                   cudaMemcpyDeviceToHost, h->stream));
+    return sync_and_check(h);
+}
+
+int nufi_download_energy(nufi_handle *h, int64_t n0, int64_t n1, double *energy)
+{
+    if (!h || !energy) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (n0 < 0 || n1 < n0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step range outside [0, Nt]");
+    DeviceGuard g(h->device);
+    NUFI_CUDA(h, cudaMemcpyAsync(energy, h->energy + n0, size_t(n1 - n0 + 1) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h->stream));
+    return sync_and_check(h);
+}
+
+int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double *energy)
+{
+    if (!h || !rho || !slab_out) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
+    const Problem &p = h->p;
+    DeviceGuard g(h->device);
+    NUFI_CUDA(h, cudaMemcpyAsync(h->rho_in, rho, size_t(p.Ns) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    cudaError_t e = launch_field_solve(p, h->plan, 0, nullptr, h->rho_in, nullptr, h->slab_out, nullptr,
+                                       h->energy_tmp, h->err, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
+    h->launches += 1;
+    NUFI_CUDA(h, cudaMemcpyAsync(slab_out, h->slab_out, size_t(p.stride_t) * sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    double en = 0;
+    NUFI_CUDA(h, cudaMemcpyAsync(&en, h->energy_tmp, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    int st = sync_and_check(h);
+    if (st) return st;
+    if (energy) *energy = en;
+    return NUFI_OK;
+}
+
+int nufi_synchronize(nufi_handle *h)
+{
+    if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return sync_and_check(h);
+}
+
+int nufi_sizes(const nufi_handle *h, int64_t *stride_t, int64_t *n_spatial, int64_t *n_points)
+{
+    if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (stride_t) *stride_t = h->p.stride_t;
+    if (n_spatial) *n_spatial = h->p.Ns;
+    if (n_points) *n_points = h->p.Nq;
+    return NUFI_OK;
+}
+
+int nufi_stream(const nufi_handle *h, void **stream)
+{
+    if (!h || !stream) return fail(nullptr, NUFI_ERR_INVALID, "null argument");
+    *stream = static_cast<void *>(h->stream);
+    return NUFI_OK;
+}
+
+int nufi_launch_count(const nufi_handle *h, int64_t *count)
+{
+    if (!h || !count) return fail(nullptr, NUFI_ERR_INVALID, "null argument");
+    *count = h->launches;
+    return NUFI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,133 @@
+// nufi_common.cuh — device-side problem descriptor and the B-spline
+// arithmetic shared by the trace and field-solve kernels (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/nufi_gb300.h"
+
+namespace nufi_gb300 {
+
+constexpr int kMaxOrder = 8;
+constexpr int kMaxVelocityTable = 4096;  // per-axis velocity nodes kept in tables
+
+// Bits of the device error word (checked by the host after each blocking
+// call).  Kernels set a bit and skip the offending access; they never trap.
+enum : unsigned {
+    kErrCellIndex = 1u << 0,   // a located cell fell outside [0, N)
+    kErrKickRange = 1u << 1,   // split mode: per-substep kick displacement too large
+    kErrSolveSize = 1u << 2,   // field solve: grid larger than its shared-memory plan
+};
+
+// Everything a kernel needs to know about one configuration, by value.
+// Mirrors the reference's config_t (nufi/config.hpp:33-53, 91-114, 167-193)
+// with the derived quantities computed the same way (config.hpp:67-69).
+struct Problem {
+    int dim, order, f0_kind, precision;
+    int N[3];            // spatial nodes per axis (1 when unused)
+    int M[3];            // velocity nodes per axis (1 when unused)
+    int P[3];            // padded slab extents N + order - 1 (1 when unused)
+    long long Ns, Nm, Nq;
+    long long stride_t;  // values per slab, reference layout
+    long long hist_stride;  // doubles between slabs in the device FP64 history
+    long long table_stride; // floats between slabs in the device FP32 tables
+    double dt;
+    double xmin[3], L[3], Linv[3], dx[3], dxinv[3];
+    double vmin[3], dv[3];
+    double f0p[8];
+    double wv;           // prod_d dv_d, the quadrature weight of rho
+};
+
+// Per-velocity-node constants of the split form (one entry per node of
+// each velocity axis).  w0 = u0 dt / dx is the free-streaming shift in
+// cells per substep, split into an integer S0 (reduced mod N) and a
+// fraction sigma = sig_hi + sig_lo in [0, 1).
+struct SplitVel {
+    double u0;        // grid velocity (FP64)
+    float u0f;        // (float)u0
+    float sig_hi, sig_lo;
+    int S0;
+};
+
+__host__ __device__ inline double faculty(int n) { return (n > 1) ? double(n) * faculty(n - 1) : 1.0; }
+
+// splines1d::N<real,order,derivative> (nufi/splines.hpp:39-79), restated:
+// all `order` basis values (or their derivative) at reference coordinate x.
+template <typename real, int ORDER, int DERIV>
+__host__ __device__ __forceinline__ void bspline_basis(real x, real *result)
+{
+    constexpr int n = ORDER, d = DERIV;
+    if (DERIV >= ORDER) {
+#pragma unroll
+        for (int i = 0; i < ORDER; ++i) result[i] = 0;
+        return;
+    }
+    real v[ORDER];
+    v[n - 1] = 1;
+#pragma unroll
+    for (int k = 1; k < n - d; ++k) {
+        v[n - k - 1] = (1 - x) * v[n - k];
+#pragma unroll
+        for (int i = 1 - k; i < 0; ++i) v[n - 1 + i] = (x - i) * v[n - 1 + i] + (k + 1 + i - x) * v[n + i];
+        v[n - 1] *= x;
+    }
+#pragma unroll
+    for (int j = d - 1; j >= 0; --j) {
+        v[j] = -v[j + 1];
+#pragma unroll
+        for (int i = j + 1; i < ORDER - 1; ++i) v[i] = v[i] - v[i + 1];
+    }
+    const real factor = real(1) / real(faculty(ORDER - DERIV - 1));
+#pragma unroll
+    for (int i = 0; i < ORDER; ++i) result[i] = v[i] * factor;
+}
+
+// splines1d::eval<real,order,derivative> (nufi/splines.hpp:81-110) on a
+// window already gathered into c[0..ORDER) (destroyed).
+template <typename real, int ORDER, int DERIV>
+__host__ __device__ __forceinline__ real deboor(real x, real *c)
+{
+    constexpr int n = ORDER, d = DERIV;
+    if (d >= n) return 0;
+#pragma unroll
+    for (int j = 1; j <= d; ++j)
+#pragma unroll
+        for (int i = n - 1; i >= j; --i) c[i] = c[i] - c[i - 1];
+#pragma unroll
+    for (int j = 1; j < n - d; ++j)
+#pragma unroll
+        for (int i = n - d - 1; i >= j; --i)
+            c[d + i] = (x + n - d - 1 - i) * c[d + i] + (i - j + 1 - x) * c[d + i - 1];
+    return (real(1) / real(faculty(ORDER - DERIV - 1))) * c[n - 1];
+}
+
+// Initial conditions in FP64, same expressions as the oracle's and the
+// reference's f0 (nufi/config.hpp:82-83, 148-149, 233-234).
+__device__ __forceinline__ double f0_1d(const Problem &p, double x, double u)
+{
+    const double alpha = p.f0p[0], k = p.f0p[1];
+    if (p.f0_kind == NUFI_F0_LANDAU)
+        return 0.39894228040143267793994 * (1. + alpha * cos(k * x)) * exp(-u * u / 2);
+    if (p.f0_kind == NUFI_F0_TWO_STREAM)
+        return 0.39894228040143267793994 * (1. + alpha * cos(k * x)) * exp(-u * u / 2.) * u * u;
+    const double ub = p.f0p[2], sb = p.f0p[3];
+    const double z = (u - ub) / sb;
+    return (1. + alpha * cos(k * x)) *
+           (0.9 * 0.39894228040143267793994 * exp(-u * u / 2) + 0.1 * 0.39894228040143267793994 / sb * exp(-z * z / 2));
+}
+
+__device__ __forceinline__ double f0_2d(const Problem &p, double x, double y, double u, double v)
+{
+    const double alpha = p.f0p[0], k = p.f0p[1];
+    return 1.0 / (2.0 * 3.14159265358979323846) * exp(-0.5 * (u * u + v * v)) * (1 + alpha * (cos(k * x) + cos(k * y)));
+}
+
+__device__ __forceinline__ double f0_3d(const Problem &p, double x, double y, double z, double u, double v, double w)
+{
+    const double alpha = p.f0p[0], k = p.f0p[1];
+    return 0.06349363593424096978576330493464 * (1. + alpha * cos(k * x) + alpha * cos(k * y) + alpha * cos(k * z)) *
+           exp(-(u * u + v * v + w * w) / 2);
+}
+
+}  // namespace nufi_gb300

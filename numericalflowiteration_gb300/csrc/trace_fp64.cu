@@ -1,0 +1,277 @@
+// trace_fp64.cu — FP64 plain form of the backward characteristic trace.
+//
+// Each thread owns PPT quadrature points with the same spatial node and
+// consecutive velocity nodes; a warp spans 32 consecutive spatial nodes
+// (x fastest), so at small and moderate n the lanes of a warp locate into
+// neighbouring cells and the slab gathers stay coalesced.  The substep loop
+// is outermost and the PPT points innermost, which gives PPT independent
+// dependency chains per thread.
+//
+// Per point the arithmetic is the reference's eval_ftilda
+// (nufi/rho.hpp:31-61, 191-232, 318-367) with dimN::eval
+// (nufi/fields.hpp:36-61, 149-184, 308-350) and the spline kernels
+// (nufi/splines.hpp:39-172): drift x -= dt u, periodic wrap
+// x - L floor(x/L), knot floor(x/dx), de Boor / tensor contraction, kick
+// u += dt E; the first half kick is omitted and the last kick is halved.
+// In 2D/3D the components of E come from one gather of the order^d window
+// and the shared partial contractions; each component is formed by exactly
+// the operations of its own reference eval<> call.
+//
+// rho is reduced without atomics (the reference uses one atomicAdd per
+// point, nufi/cuda_kernel.cu:50): per thread over its PPT points, then over
+// the warps of the block in fixed order into partial[blockIdx.y][s].
+#include "nufi_kernels.cuh"
+
+namespace nufi_gb300 {
+
+namespace {
+
+// fields.hpp wrap + locate on one axis; the knot is remapped when the wrap
+// rounds up to exactly L (the reference would read one value past the
+// padded slab there).
+__device__ __forceinline__ int locate_fp64(const Problem &p, int a, double x, double &xi, unsigned *err)
+{
+    x -= p.xmin[a];
+    x = x - p.L[a] * floor(x * p.Linv[a]);
+    const double xk = floor(x * p.dxinv[a]);
+    int ii = int(xk);
+    xi = x * p.dxinv[a] - xk;
+    if (ii >= p.N[a]) ii -= p.N[a];
+    if (ii < 0 || ii >= p.N[a]) {
+        atomicOr(err, kErrCellIndex);
+        ii = 0;
+    }
+    return ii;
+}
+
+template <int ORDER>
+__device__ __forceinline__ void field_1d(const Problem &p, const double *__restrict__ c, const double *x, double *E,
+                                         unsigned *err)
+{
+    double xi;
+    const int ii = locate_fp64(p, 0, x[0], xi, err);
+    double w[ORDER];
+#pragma unroll
+    for (int j = 0; j < ORDER; ++j) w[j] = __ldg(c + ii + j);
+    const double factor = 1 * p.dxinv[0];
+    E[0] = -(factor * deboor<double, ORDER, 1>(xi, w));
+}
+
+template <int ORDER>
+__device__ __forceinline__ void field_2d(const Problem &p, const double *__restrict__ c, const double *x, double *E,
+                                         unsigned *err)
+{
+    double xi, eta;
+    const int ii = locate_fp64(p, 0, x[0], xi, err);
+    const int jj = locate_fp64(p, 1, x[1], eta, err);
+    const int sy = p.P[0];
+    const double *__restrict__ w = c + (long long)jj * sy + ii;
+    double N0[ORDER], N1[ORDER], c0[ORDER], c1[ORDER];
+    bspline_basis<double, ORDER, 0>(xi, N0);
+    bspline_basis<double, ORDER, 1>(xi, N1);
+#pragma unroll
+    for (int j = 0; j < ORDER; ++j) {
+        c0[j] = 0;
+        c1[j] = 0;
+#pragma unroll
+        for (int i = 0; i < ORDER; ++i) {
+            const double v = __ldg(w + j * sy + i);
+            c1[j] += v * N1[i];
+            c0[j] += v * N0[i];
+        }
+    }
+    const double fx = 1 * p.dxinv[0], fy = 1 * p.dxinv[1];
+    E[0] = -(fx * deboor<double, ORDER, 0>(eta, c1));
+    E[1] = -(fy * deboor<double, ORDER, 1>(eta, c0));
+}
+
+template <int ORDER>
+__device__ __forceinline__ void field_3d(const Problem &p, const double *__restrict__ c, const double *x, double *E,
+                                         unsigned *err)
+{
+    double xi, eta, zeta;
+    const int ii = locate_fp64(p, 0, x[0], xi, err);
+    const int jj = locate_fp64(p, 1, x[1], eta, err);
+    const int kk = locate_fp64(p, 2, x[2], zeta, err);
+    const int sy = p.P[0], sz = p.P[0] * p.P[1];
+    const double *__restrict__ w = c + (long long)kk * sz + (long long)jj * sy + ii;
+    double Nx0[ORDER], Nx1[ORDER];
+    bspline_basis<double, ORDER, 0>(xi, Nx0);
+    bspline_basis<double, ORDER, 1>(xi, Nx1);
+    // czy contracted over x with the value basis (E_y, E_z) and with the
+    // derivative basis (E_x).
+    double czy0[ORDER][ORDER], czy1[ORDER][ORDER];
+#pragma unroll
+    for (int k = 0; k < ORDER; ++k)
+#pragma unroll
+        for (int j = 0; j < ORDER; ++j) {
+            double a0 = 0, a1 = 0;
+#pragma unroll
+            for (int i = 0; i < ORDER; ++i) {
+                const double v = __ldg(w + k * sz + j * sy + i);
+                a1 += v * Nx1[i];
+                a0 += v * Nx0[i];
+            }
+            czy0[k][j] = a0;
+            czy1[k][j] = a1;
+        }
+    double Ny0[ORDER], Ny1[ORDER];
+    bspline_basis<double, ORDER, 0>(eta, Ny0);
+    bspline_basis<double, ORDER, 1>(eta, Ny1);
+    double czx[ORDER], czy[ORDER], czz[ORDER];
+#pragma unroll
+    for (int k = 0; k < ORDER; ++k) {
+        double ax = 0, ay = 0, az = 0;
+#pragma unroll
+        for (int j = 0; j < ORDER; ++j) {
+            ax += czy1[k][j] * Ny0[j];
+            ay += czy0[k][j] * Ny1[j];
+            az += czy0[k][j] * Ny0[j];
+        }
+        czx[k] = ax;
+        czy[k] = ay;
+        czz[k] = az;
+    }
+    const double fx = 1 * p.dxinv[0], fy = 1 * p.dxinv[1], fz = 1 * p.dxinv[2];
+    E[0] = -(fx * deboor<double, ORDER, 0>(zeta, czx));
+    E[1] = -(fy * deboor<double, ORDER, 0>(zeta, czy));
+    E[2] = -(fz * deboor<double, ORDER, 1>(zeta, czz));
+}
+
+template <int D, int ORDER>
+__device__ __forceinline__ void field_fp64(const Problem &p, const double *__restrict__ c, const double *x, double *E,
+                                           unsigned *err)
+{
+    if constexpr (D == 1) field_1d<ORDER>(p, c, x, E, err);
+    else if constexpr (D == 2) field_2d<ORDER>(p, c, x, E, err);
+    else field_3d<ORDER>(p, c, x, E, err);
+}
+
+template <int D>
+__device__ __forceinline__ double f0_fp64(const Problem &p, const double *x, const double *u)
+{
+    if constexpr (D == 1) return f0_1d(p, x[0], u[0]);
+    else if constexpr (D == 2) return f0_2d(p, x[0], x[1], u[0], u[1]);
+    else return f0_3d(p, x[0], x[1], x[2], u[0], u[1], u[2]);
+}
+
+}  // namespace
+
+// eval_ftilda (mode 0) or eval_f (mode 1, with the first half kick from
+// slab n) of PPT points per thread; see the file comment.
+template <int D, int ORDER, int PPT>
+__global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const double *__restrict__ hist, int n,
+                                                         long long q_begin, long long q_end, int mode,
+                                                         double *__restrict__ partial, unsigned *err)
+{
+    const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
+    const long long s = (long long)blockIdx.x * 32 + lane;
+    const long long mb = ((long long)blockIdx.y * W + warp) * PPT;
+    const double dt = p.dt;
+
+    double x[PPT][D], u[PPT][D];
+    bool live[PPT];
+    {
+        long long rs = s < p.Ns ? s : 0;
+        int is[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            is[a] = int(rs % p.N[a]);
+            rs /= p.N[a];
+        }
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const long long m = mb + q;
+            const long long qq = s * p.Nm + m;
+            live[q] = (s < p.Ns) && (m < p.Nm) && (qq >= q_begin) && (qq < q_end);
+            long long rm = m < p.Nm ? m : 0;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                const int im = int(rm % p.M[a]);
+                rm /= p.M[a];
+                x[q][a] = p.xmin[a] + is[a] * p.dx[a];
+                u[q][a] = p.vmin[a] + im * p.dv[a] + p.dv[a] / 2;
+            }
+        }
+    }
+
+    double acc = 0;
+    if (n > 0) {
+        double E[D];
+        if (mode == 1) {  // eval_f: initial half kick with slab n
+            const double *c = hist + (long long)n * p.hist_stride;
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                if (!live[q]) continue;
+                field_fp64<D, ORDER>(p, c, x[q], E, err);
+#pragma unroll
+                for (int a = 0; a < D; ++a) u[q][a] += 0.5 * dt * E[a];
+            }
+        }
+        for (int k = n - 1; k >= 1; --k) {
+            const double *c = hist + (long long)k * p.hist_stride;
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                if (!live[q]) continue;
+#pragma unroll
+                for (int a = 0; a < D; ++a) x[q][a] = x[q][a] - dt * u[q][a];
+                field_fp64<D, ORDER>(p, c, x[q], E, err);
+#pragma unroll
+                for (int a = 0; a < D; ++a) u[q][a] = u[q][a] + dt * E[a];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            if (!live[q]) continue;
+#pragma unroll
+            for (int a = 0; a < D; ++a) x[q][a] -= dt * u[q][a];
+            field_fp64<D, ORDER>(p, hist, x[q], E, err);
+#pragma unroll
+            for (int a = 0; a < D; ++a) u[q][a] += 0.5 * dt * E[a];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < PPT; ++q)
+        if (live[q]) acc += f0_fp64<D>(p, x[q], u[q]);
+
+    block_reduce_partial(acc, s, p.Ns, partial);
+}
+
+// Launch table: dims x orders x points-per-thread.
+template <int D, int ORDER>
+static cudaError_t launch_fp64_order(const Problem &p, const LaunchShape &ls, const double *hist, int n,
+                                     long long qb, long long qe, int mode, double *partial, unsigned *err,
+                                     cudaStream_t st)
+{
+    const dim3 block(32, ls.warps);
+    const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(ls.vblocks));
+    switch (ls.ppt) {
+    case 1: trace_fp64_kernel<D, ORDER, 1><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
+    case 2: trace_fp64_kernel<D, ORDER, 2><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
+    case 4: trace_fp64_kernel<D, ORDER, 4><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
+                              long long qe, int mode, double *partial, unsigned *err, cudaStream_t st)
+{
+#define NUFI_CASE(D, O) \
+    if (p.dim == D && p.order == O) return launch_fp64_order<D, O>(p, ls, hist, n, qb, qe, mode, partial, err, st);
+    NUFI_CASE(1, 3) NUFI_CASE(1, 4) NUFI_CASE(1, 5) NUFI_CASE(1, 6) NUFI_CASE(1, 7) NUFI_CASE(1, 8)
+    NUFI_CASE(2, 3) NUFI_CASE(2, 4) NUFI_CASE(2, 5) NUFI_CASE(2, 6)
+    NUFI_CASE(3, 3) NUFI_CASE(3, 4) NUFI_CASE(3, 5)
+#undef NUFI_CASE
+    return cudaErrorNotSupported;
+}
+
+bool fp64_order_supported(int dim, int order)
+{
+    if (dim == 1) return order >= 3 && order <= 8;
+    if (dim == 2) return order >= 3 && order <= 6;
+    if (dim == 3) return order >= 3 && order <= 5;
+    return false;
+}
+
+}  // namespace nufi_gb300

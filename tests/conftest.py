@@ -1,0 +1,50 @@
+"""Shared helpers of the test suite.
+
+Tests marked ``gpu`` need a CUDA GPU and call the product only through its
+C ABI (libnufi_gb300.so); the others run on the CPU and cover the oracle
+against the reference's golden vectors, the host logic and the C ABI's
+exported surface.
+"""
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+GOLDEN = ROOT / "tests" / "golden"
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+from numericalflowiteration_gb300.config import Config  # noqa: E402
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a kernels)")
+
+
+def golden(name: str):
+    """(config, dict of arrays) of one golden case produced by the reference."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    cfg = Config.from_bytes(z["config"].tobytes())
+    return cfg, {k: z[k] for k in z.files if k != "config"}
+
+
+def golden_manifest():
+    return json.loads((GOLDEN / "manifest.json").read_text())
+
+
+def rel_max(a, b):
+    """max |a - b| / max |b| — the relative error measure of these tests."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / (den if den > 0 else 1.0))
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    from oracle import oracle
+    oracle.build()
+    return oracle

@@ -1,0 +1,120 @@
+"""Generate the golden vectors in tests/golden/ from the REFERENCE's own
+code, built from its sources by oracle/ref/Makefile into oracle/_ref/.
+
+Run here (where the reference sources are mounted):
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+Each case runs `ref_driver run` (the reference's eval_ftilda / eval /
+splines / poisson::solve / interpolate with LSMR, on the configured f0) and
+keeps a compact subset: the whole energy history, rho at a few steps and a
+few coefficient slabs.  Field-solve cases feed a seeded random rho through
+`ref_driver solve`.  The known-answer checks of bin/test_poisson.cpp and
+bin/test_fields.cpp are stored as the numbers the reference prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+sys.path.insert(0, str(REPO))
+
+from numericalflowiteration_gb300.config import (bump_on_tail_1d, landau_1d, landau_2d,  # noqa: E402
+                                                 landau_3d, two_stream_1d)
+
+DRIVER = REPO / "oracle" / "_ref" / "ref_driver"
+
+# name -> (config, n_last, rho steps kept, slab steps kept)
+RUN_CASES = {
+    "landau_1d_64x256_T30": (landau_1d(), 480, [0, 1, 2, 10, 100, 240, 480], [0, 1, 479, 480]),
+    "two_stream_1d_256x1024_n40": (two_stream_1d(), 40, [0, 1, 2, 20, 40], [0, 1, 39, 40]),
+    "two_stream_1d_64x256_T50": (two_stream_1d(Nx=64, Nv=256), 800, [0, 1, 400, 800], [0, 799, 800]),
+    "bump_on_tail_1d_64x256_T20": (bump_on_tail_1d(), 320, [0, 1, 160, 320], [0, 319, 320]),
+    "small_landau_1d_16x32": (landau_1d(Nx=16, Nv=32, Nt=20), 20, list(range(21)), list(range(21))),
+    "order3_landau_1d_32x64": (landau_1d(Nx=32, Nv=64, Nt=12, order=3), 12, [0, 1, 6, 12], [0, 6, 12]),
+    "order5_landau_1d_32x64": (landau_1d(Nx=32, Nv=64, Nt=12, order=5), 12, [0, 1, 6, 12], [0, 6, 12]),
+    "landau_2d_32x64_n20": (landau_2d(), 20, [0, 1, 2, 10, 20], [0, 1, 19, 20]),
+    "landau_2d_16x16_T20": (landau_2d(Nx=16, Nv=16), 160, [0, 1, 80, 160], [0, 159, 160]),
+    "small_landau_2d_8x8": (landau_2d(Nx=8, Nv=8, Nt=10), 10, list(range(11)), list(range(11))),
+    "landau_3d_16x32_n3": (landau_3d(), 3, [0, 1, 2, 3], [0, 1, 2, 3]),
+    "landau_3d_8x8_T2": (landau_3d(Nx=8, Nv=8, Nt=20), 20, [0, 1, 10, 20], [0, 19, 20]),
+    "small_landau_3d_4x4": (landau_3d(Nx=4, Nv=4, Nt=5), 5, list(range(6)), list(range(6))),
+}
+
+SOLVE_CASES = {
+    "solve_1d_64": landau_1d(),
+    "solve_1d_256": two_stream_1d(),
+    "solve_2d_32": landau_2d(),
+    "solve_3d_16": landau_3d(),
+    "solve_1d_64_order3": landau_1d(order=3),
+    "solve_1d_64_order5": landau_1d(order=5),
+}
+
+
+def run_case(name, cfg, n_last, rho_keep, slab_keep, tmp: Path):
+    p = tmp / name
+    (p.with_suffix(".cfg")).write_bytes(cfg.to_bytes())
+    subprocess.run([str(DRIVER), "run", str(p.with_suffix(".cfg")), "0", str(n_last), str(p)], check=True)
+    energy = np.fromfile(str(p) + ".energy")
+    rho = np.fromfile(str(p) + ".rho").reshape(n_last + 1, cfg.n_spatial)
+    coeffs = np.fromfile(str(p) + ".coeffs").reshape(cfg.Nt + 1, cfg.stride_t)
+    np.savez_compressed(HERE / f"{name}.npz", config=np.frombuffer(cfg.to_bytes(), dtype=np.uint8),
+                        n_last=n_last, energy=energy, rho_steps=np.array(rho_keep), rho=rho[rho_keep],
+                        slab_steps=np.array(slab_keep), slabs=coeffs[slab_keep])
+    return {"n_last": n_last, "energy_max": float(np.max(energy)), "energy_last": float(energy[-1])}
+
+
+def solve_case(name, cfg, tmp: Path, seed: int):
+    rng = np.random.default_rng(seed)
+    rho = -1.0 + 1e-2 * rng.standard_normal(cfg.n_spatial)
+    p = tmp / name
+    p.with_suffix(".cfg").write_bytes(cfg.to_bytes())
+    rho.tofile(str(p) + ".rhoin")
+    subprocess.run([str(DRIVER), "solve", str(p.with_suffix(".cfg")), str(p) + ".rhoin", str(p)], check=True)
+    slab = np.fromfile(str(p) + ".slab")
+    energy = np.fromfile(str(p) + ".energy")[0]
+    np.savez_compressed(HERE / f"{name}.npz", config=np.frombuffer(cfg.to_bytes(), dtype=np.uint8),
+                        rho=rho, slab=slab, energy=energy)
+    return {"energy": float(energy)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
+    args = ap.parse_args()
+    subprocess.run(["make", "-s", "-C", str(REPO / "oracle" / "ref"), f"REF={args.ref}"], check=True)
+    manifest = {"generator": "tests/golden/make_golden.py", "driver": "oracle/ref/ref_driver.cpp",
+                "cases": {}}
+    mpath = HERE / "manifest.json"
+    if mpath.exists():
+        manifest = json.loads(mpath.read_text())
+    with tempfile.TemporaryDirectory() as td:
+        tmp = Path(td)
+        for name, (cfg, n_last, rk, sk) in RUN_CASES.items():
+            if args.only and args.only not in name:
+                continue
+            manifest["cases"][name] = run_case(name, cfg, n_last, rk, sk, tmp)
+            print(name, manifest["cases"][name], flush=True)
+        for i, (name, cfg) in enumerate(SOLVE_CASES.items()):
+            if args.only and args.only not in name:
+                continue
+            manifest["cases"][name] = solve_case(name, cfg, tmp, 20261203 + i)
+            print(name, manifest["cases"][name], flush=True)
+    kat_p = json.loads(subprocess.run([str(DRIVER), "poisson_kat"], check=True, capture_output=True,
+                                      text=True).stdout)
+    kat_f = json.loads(subprocess.run([str(DRIVER), "fields_kat"], check=True, capture_output=True,
+                                      text=True).stdout)
+    manifest["kat"] = {"test_poisson_rel_l1": kat_p, "test_fields_2d": kat_f}
+    mpath.write_text(json.dumps(manifest, indent=1, sort_keys=True) + "\n")
+
+
+if __name__ == "__main__":
+    main()

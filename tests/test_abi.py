@@ -1,0 +1,114 @@
+"""The C ABI library without running compute: it loads, exports every
+function include/nufi_gb300.h declares, agrees on the layout of
+nufi_config, and rejects bad configurations before touching the GPU."""
+import ctypes
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+import numericalflowiteration_gb300 as nufi
+from numericalflowiteration_gb300 import _lib
+from numericalflowiteration_gb300.config import NufiConfigC, landau_1d, two_stream_1d
+
+HEADER = ROOT / "include" / "nufi_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(nufi_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from numericalflowiteration_gb300 import build
+    build.build()
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) == set(_lib.SIGNATURES), "binding and header disagree"
+
+
+def test_config_layout_matches_c(tmp_path):
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "nufi_gb300.h"\n'
+        "int main(void){printf(\"%zu %zu %zu %zu %zu\\n\", sizeof(nufi_config), offsetof(nufi_config, Nx),"
+        " offsetof(nufi_config, dt), offsetof(nufi_config, v_max), offsetof(nufi_config, f0_params));return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = list(map(int, subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()))
+    want = [ctypes.sizeof(NufiConfigC), NufiConfigC.Nx.offset, NufiConfigC.dt.offset, NufiConfigC.v_max.offset,
+            NufiConfigC.f0_params.offset]
+    assert got == want
+
+
+def _create_status(lib, cfg_c):
+    h = ctypes.c_void_p()
+    st = lib.nufi_create(ctypes.byref(cfg_c), 0, ctypes.byref(h))
+    msg = lib.nufi_last_error(None).decode()
+    if st == 0:
+        lib.nufi_destroy(h)
+    return st, msg
+
+
+@pytest.mark.parametrize("mutate,code", [
+    (lambda c: setattr(c, "dim", 4), _lib.ERR_INVALID),
+    (lambda c: setattr(c, "order", 9), _lib.ERR_INVALID),
+    (lambda c: setattr(c, "dt", -1.0), _lib.ERR_INVALID),
+    (lambda c: setattr(c, "precision", 7), _lib.ERR_INVALID),
+    (lambda c: c.Nx.__setitem__(0, 0), _lib.ERR_INVALID),
+])
+def test_invalid_configs_rejected_before_cuda(lib, mutate, code):
+    c = landau_1d().to_c()
+    mutate(c)
+    st, msg = _create_status(lib, c)
+    assert st == code and msg.startswith("nufi_create:")
+
+
+def test_unbuilt_combinations_report_unsupported(lib):
+    c = landau_1d(order=5, precision="fp32split").to_c()
+    st, msg = _create_status(lib, c)
+    assert st == _lib.ERR_UNSUPPORTED and "FP32-split" in msg
+    c = landau_1d().to_c()
+    c.dim = 2
+    c.f0_kind = 1
+    c.Nx[1] = 8
+    c.Nv[1] = 8
+    c.x_max[1] = 1.0
+    c.v_max[1] = 1.0
+    st, msg = _create_status(lib, c)
+    assert st == _lib.ERR_UNSUPPORTED
+
+
+def test_python_errors_map_to_reference_exception_types(lib):
+    with pytest.raises(ValueError):
+        nufi.Simulation(landau_1d(order=12))
+    with pytest.raises(NotImplementedError):
+        nufi.Simulation(two_stream_1d(order=3, precision="fp32split"))
+
+
+def test_null_handle_calls_fail_cleanly(lib):
+    assert lib.nufi_compute_rho(None, 0, 0, 1) == _lib.ERR_INVALID
+    assert lib.nufi_destroy(None) == 0
+    assert lib.nufi_last_error(None) is not None
+
+
+def test_point_step_count():
+    cfg = two_stream_1d()
+    assert cfg.n_points == 262144
+    assert cfg.point_steps() == 262144 * 800 * 801 // 2
+    assert cfg.point_steps(10, 20) == 262144 * sum(range(10, 21))

@@ -1,0 +1,169 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the
+reference's golden vectors (tests/golden/) and the CPU oracle.
+
+Measures: max |d| / max |ref| for rho, slabs and energy histories.
+FP64 plain must agree with the reference to 1e-12 (2e-12 for the
+alpha = 1e-3 two-stream case, whose FP64 summation floor is ~1e-12, see
+tests/test_oracle_golden.py).  FP32-split must stay within 1e-6 of the
+FP64 energy history (the metric's gate).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_max
+
+pytestmark = pytest.mark.gpu
+
+ENERGY_TOL = {"two_stream_1d_256x1024_n40": 2e-12}
+
+
+@pytest.fixture(scope="module")
+def nufi():
+    import numericalflowiteration_gb300 as m
+    from numericalflowiteration_gb300 import build
+    build.build()
+    m.load()
+    return m
+
+
+def _slabs_ok(cfg, hist, g, tol=1e-11):
+    st = cfg.stride_t
+    for i, n in enumerate(g["slab_steps"]):
+        if n <= int(g["n_last"]):
+            assert rel_max(hist[n * st:(n + 1) * st], g["slabs"][i]) <= tol, f"slab {n}"
+
+
+@pytest.mark.parametrize("name", ["small_landau_1d_16x32", "small_landau_2d_8x8", "small_landau_3d_4x4",
+                                  "order3_landau_1d_32x64", "order5_landau_1d_32x64"])
+def test_fp64_stepwise_rho_energy_slabs(nufi, name):
+    cfg, g = golden(name)
+    with nufi.Simulation(cfg) as sim:
+        energies = []
+        for n in range(int(g["n_last"]) + 1):
+            energies.append(sim.step(n))
+            rho = sim.download_rho(np.zeros(cfg.n_spatial))
+            if n in list(g["rho_steps"]):
+                i = list(g["rho_steps"]).index(n)
+                assert rel_max(rho, g["rho"][i]) <= 1e-12, f"rho step {n}"
+        assert rel_max(energies, g["energy"]) <= 1e-12
+        _slabs_ok(cfg, sim.history(), g)
+        assert sim.launches >= 2 * (int(g["n_last"]) + 1)
+
+
+@pytest.mark.parametrize("name", ["landau_1d_64x256_T30", "bump_on_tail_1d_64x256_T20",
+                                  "two_stream_1d_256x1024_n40", "landau_2d_16x16_T20", "landau_3d_8x8_T2",
+                                  "landau_2d_32x64_n20", "landau_3d_16x32_n3"])
+def test_fp64_graph_run_matches_reference(nufi, name):
+    cfg, g = golden(name)
+    n_last = int(g["n_last"])
+    with nufi.Simulation(cfg) as sim:
+        e = sim.run(0, n_last)
+        assert rel_max(e, g["energy"]) <= ENERGY_TOL.get(name, 1e-12)
+        _slabs_ok(cfg, sim.history(), g)
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+        assert rel_max(rho, g["rho"][list(g["rho_steps"]).index(n_last)]) <= 1e-12
+
+
+def test_fp64_two_stream_through_saturation(nufi):
+    cfg, g = golden("two_stream_1d_64x256_T50")
+    with nufi.Simulation(cfg) as sim:
+        e = sim.run()
+    assert rel_max(e[:200], g["energy"][:200]) <= 2e-12
+    assert rel_max(e, g["energy"]) <= 1e-9
+
+
+@pytest.mark.parametrize("name", ["solve_1d_64", "solve_1d_256", "solve_2d_32", "solve_3d_16",
+                                  "solve_1d_64_order3", "solve_1d_64_order5"])
+def test_device_field_solve_matches_reference(nufi, name):
+    cfg, g = golden(name)
+    with nufi.Simulation(cfg) as sim:
+        slab, e = sim.field_solve(g["rho"])
+    assert rel_max(slab, g["slab"]) <= 1e-12
+    assert abs(e - float(g["energy"])) <= 1e-12 * abs(float(g["energy"]))
+
+
+def test_dropin_upload_compute_download(nufi, oracle_mod):
+    """The reference drivers' loop: upload_phi the reference's slabs, then
+    compute_rho over a split q range and download_rho (which accumulates)."""
+    cfg, g = golden("small_landau_1d_16x32")
+    st = cfg.stride_t
+    coeffs = np.zeros((cfg.Nt + 1) * st)
+    for i, n in enumerate(g["slab_steps"]):
+        coeffs[n * st:(n + 1) * st] = g["slabs"][i]
+    with nufi.Simulation(cfg) as sim:
+        for n in range(cfg.Nt + 1):
+            sim.upload_phi(n, coeffs)
+        for n in [0, 1, 7, cfg.Nt]:
+            acc = np.zeros(cfg.n_spatial)
+            cuts = [0, 37, 200, cfg.n_points]
+            for a, b in zip(cuts[:-1], cuts[1:]):
+                sim.compute_rho(n, a, b)
+                sim.download_rho(acc)
+            oracle_mod.set_summation(1)
+            want = oracle_mod.rho(cfg, n, coeffs)
+            oracle_mod.set_summation(0)
+            assert rel_max(acc, want) <= 1e-13
+            assert rel_max(acc, g["rho"][list(g["rho_steps"]).index(n)]) <= 1e-12
+        # float buffers of the <float, order> instantiation
+        acc32 = np.zeros(cfg.n_spatial, dtype=np.float32)
+        sim.compute_rho(3)
+        sim.download_rho(acc32)
+        assert rel_max(acc32, g["rho"][3]) <= 1e-6
+
+
+def test_dropin_errors_and_empty_range(nufi):
+    cfg, _ = golden("small_landau_1d_16x32")
+    with nufi.Simulation(cfg) as sim:
+        with pytest.raises(IndexError):
+            sim.compute_rho(cfg.Nt + 1)
+        with pytest.raises(IndexError):
+            sim.compute_rho(0, 0, cfg.n_points + 1)
+        sim.compute_rho(0)
+        a = sim.download_rho(np.zeros(cfg.n_spatial))
+        sim.compute_rho(0, 5, 5)  # empty: the reference returns without touching rho
+        b = sim.download_rho(np.zeros(cfg.n_spatial))
+        assert np.array_equal(a, b)
+        with pytest.raises(IndexError):
+            sim.upload_phi(cfg.Nt + 1, np.zeros((cfg.Nt + 2) * cfg.stride_t))
+
+
+def test_fp64_run_is_deterministic(nufi):
+    cfg, _ = golden("landau_1d_64x256_T30")
+    with nufi.Simulation(cfg) as a, nufi.Simulation(cfg) as b:
+        ea, eb = a.run(), b.run()
+        ea2 = a.run()
+    assert np.array_equal(ea, eb) and np.array_equal(ea, ea2)
+
+
+@pytest.mark.parametrize("name,tol", [("landau_1d_64x256_T30", 1e-6), ("bump_on_tail_1d_64x256_T20", 1e-6),
+                                      ("small_landau_1d_16x32", 1e-6)])
+def test_split_energy_within_gate(nufi, name, tol):
+    cfg, g = golden(name)
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        e = sim.run(0, int(g["n_last"]))
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+    assert rel_max(e, g["energy"]) <= tol
+    assert rel_max(rho, g["rho"][-1]) <= 1e-6
+
+
+def test_split_two_stream_linear_phase(nufi):
+    cfg, g = golden("two_stream_1d_64x256_T50")
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        e = sim.run()
+    assert rel_max(e[:400], g["energy"][:400]) <= 1e-6
+
+
+def test_split_dropin_matches_fp64(nufi):
+    """The split form behind the drop-in calls: same slabs uploaded, rho
+    within FP32-split accuracy of the FP64 rho."""
+    cfg, g = golden("landau_1d_64x256_T30")
+    st = cfg.stride_t
+    with nufi.Simulation(cfg) as ref:
+        ref.run(0, 100)
+        coeffs = ref.history()
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        for n in range(101):
+            sim.upload_phi(n, coeffs)
+        sim.compute_rho(100)
+        got = sim.download_rho(np.zeros(cfg.n_spatial))
+    assert rel_max(got, g["rho"][list(g["rho_steps"]).index(100)]) <= 1e-6

@@ -1,0 +1,125 @@
+"""The CPU oracle against golden vectors produced by the reference's own
+code (tests/golden/make_golden.py runs oracle/_ref/ref_driver, built from
+nufi/rho.hpp, fields.hpp, splines.hpp, lsmr.tpp and poisson.cpp).
+
+Tolerances: rho(0) involves only f0 and the point convention and must be
+bit-identical; later steps go through the field solve, where the reference
+iterates LSMR to machine precision and the oracle solves directly, so they
+agree to ~1e-14 and the tests use 1e-12 (max |d| / max |ref|).  Energy
+histories are compared the same way, normalised by their maximum (with
+alpha = 1e-3 the energy is a difference of O(1) terms and pointwise
+relative errors near its minima say nothing about the solver).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, golden_manifest, rel_max
+
+RUN_CASES_FAST = [
+    "small_landau_1d_16x32",
+    "small_landau_2d_8x8",
+    "small_landau_3d_4x4",
+    "order3_landau_1d_32x64",
+    "order5_landau_1d_32x64",
+    "landau_1d_64x256_T30",
+    "bump_on_tail_1d_64x256_T20",
+    "two_stream_1d_256x1024_n40",
+    "landau_3d_8x8_T2",
+    "landau_2d_16x16_T20",
+]
+
+# Energy tolerance per case (max |dW| / max |W|).  With alpha = 1e-3 the
+# field is driven by a 1e-3 perturbation of rho ~ -1, so the rounding of
+# the O(1) sum over 1024 velocities (~3e-15 absolute) is ~1e-12 of the
+# energy: summing the same f~ values in order or compensated differs by
+# 9.7e-13 after 40 steps, and the reference's own GPU kernel (atomics in
+# arbitrary order) is not reproducible below that.
+ENERGY_TOL = {"two_stream_1d_256x1024_n40": 2e-12}
+
+# Long two-stream run: chaotic after saturation, so agreement is looser
+# once the instability has saturated (see test below).
+TWO_STREAM_LONG = "two_stream_1d_64x256_T50"
+
+
+@pytest.mark.parametrize("name", RUN_CASES_FAST)
+def test_oracle_run_matches_reference(name, oracle_mod):
+    cfg, g = golden(name)
+    n_last = int(g["n_last"])
+    energy, rho, coeffs = oracle_mod.run(cfg, 0, n_last)
+    assert rel_max(energy, g["energy"]) <= ENERGY_TOL.get(name, 1e-12)
+    for i, n in enumerate(g["rho_steps"]):
+        assert rel_max(rho[n], g["rho"][i]) <= 1e-12, f"rho step {n}"
+    assert np.array_equal(rho[0], g["rho"][0]), "rho(0) must be bit-identical (f0 + point convention)"
+    st = cfg.stride_t
+    for i, n in enumerate(g["slab_steps"]):
+        assert rel_max(coeffs[n * st:(n + 1) * st], g["slabs"][i]) <= 1e-11, f"slab {n}"
+
+
+def test_oracle_two_stream_long(oracle_mod):
+    """Linear phase to the alpha = 1e-3 summation floor (ENERGY_TOL); through
+    saturation the two codes stay within 1e-9 of the peak energy (rounding
+    differences are amplified by the instability, as between any two FP64
+    implementations)."""
+    cfg, g = golden(TWO_STREAM_LONG)
+    energy, rho, _ = oracle_mod.run(cfg, 0, int(g["n_last"]), keep_rho=True)
+    e_ref = g["energy"]
+    assert rel_max(energy[:200], e_ref[:200]) <= 2e-12
+    assert rel_max(energy, e_ref) <= 1e-9
+    assert np.array_equal(rho[0], g["rho"][0])
+
+
+@pytest.mark.parametrize("name", ["solve_1d_64", "solve_1d_256", "solve_2d_32", "solve_3d_16",
+                                  "solve_1d_64_order3", "solve_1d_64_order5"])
+def test_oracle_field_solve_matches_reference(name, oracle_mod):
+    cfg, g = golden(name)
+    slab, e = oracle_mod.field_solve(cfg, g["rho"])
+    assert rel_max(slab, g["slab"]) <= 1e-12
+    assert abs(e - float(g["energy"])) <= 1e-13 * abs(float(g["energy"]))
+
+
+def test_oracle_poisson_known_answer(oracle_mod):
+    """bin/test_poisson.cpp:36-119: rho = cos2z + sin8y + cos42x on 128x64x32
+    over [0, 2pi)^3; the reference prints a relative l1 error of ~4e-15."""
+    from numericalflowiteration_gb300.config import Config
+    cfg = Config(3, [128, 64, 32], [1, 1, 1], 0, 1.0, [0.0] * 3, [2 * np.pi] * 3, [0.0] * 3, [1.0] * 3)
+    dx = 2 * np.pi / np.array([128, 64, 32])
+    z, y, x = np.meshgrid(np.arange(32) * dx[2], np.arange(64) * dx[1], np.arange(128) * dx[0], indexing="ij")
+    rho = np.cos(2 * z) + np.sin(8 * y) + np.cos(42 * x)
+    phi = np.cos(2 * z) / 4 + np.sin(8 * y) / 64 + np.cos(42 * x) / (42 * 42)
+    out, _ = oracle_mod.poisson(cfg, rho.ravel())
+    err = np.sum(np.abs(out - phi.ravel())) / np.sum(np.abs(phi))
+    ref = golden_manifest()["kat"]["test_poisson_rel_l1"]["double"]
+    assert err < 1e-13 and ref < 1e-13
+
+
+def test_oracle_fields_known_answer(oracle_mod):
+    """bin/test_fields.cpp:129-190: interpolate sin3x + sin3y on 128x128 and
+    evaluate back at the nodes (the reference's max error is ~1.6e-14)."""
+    from numericalflowiteration_gb300.config import Config
+    cfg = Config(2, [128, 128], [1, 1], 0, 1.0, [0.0, -np.pi], [4 * np.pi, np.pi], [0.0] * 2, [1.0] * 2)
+    dx, dy = 4 * np.pi / 128, 2 * np.pi / 128
+    j, i = np.meshgrid(np.arange(128), np.arange(128), indexing="ij")
+    x, y = i * dx, -np.pi + j * dy
+    vals = np.sin(3 * x) + np.sin(3 * y)
+    slab = oracle_mod.interpolate(cfg, vals.ravel())
+    pts = np.stack([x.ravel(), y.ravel()], axis=1)
+    back = oracle_mod.eval_field(cfg, slab, pts)
+    err = np.max(np.abs(back - vals.ravel()))
+    ref = golden_manifest()["kat"]["test_fields_2d"]["max_node_error_2d"]
+    assert err < 1e-12 and ref < 1e-12
+
+
+def test_oracle_q_range_partition(oracle_mod):
+    """rho over a split q range adds up to rho over the whole range, as the
+    reference's multi-device split relies on (nufi/cuda_scheduler.hpp:88-118)."""
+    cfg, g = golden("small_landau_1d_16x32")
+    coeffs = np.zeros((cfg.Nt + 1) * cfg.stride_t)
+    st = cfg.stride_t
+    for i, n in enumerate(g["slab_steps"]):
+        coeffs[n * st:(n + 1) * st] = g["slabs"][i]
+    n = 7
+    full = oracle_mod.rho(cfg, n, coeffs)
+    cuts = [0, 37, 200, cfg.n_points]
+    parts = sum(oracle_mod.rho(cfg, n, coeffs, a, b) for a, b in zip(cuts[:-1], cuts[1:]))
+    assert rel_max(parts, full) <= 1e-14
+    assert rel_max(full, g["rho"][n]) <= 1e-12

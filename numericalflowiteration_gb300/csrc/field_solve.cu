@@ -1,6 +1,6 @@
 // field_solve.cu — periodic Poisson solve fused with the B-spline
 // collocation solve, as one diagonal in Fourier space, plus the small
-// kernels around it (rho from partials, FP32 field tables).
+// kernels around it (FP32 field tables).
 //
 // The reference (a) transforms rho with FFTW's separable DHT, scales mode
 // k by 1/(N |k|^2), zeroes the mean and transforms back
@@ -86,22 +86,6 @@ __device__ __forceinline__ float4 cubic_kick_poly(double c0, double c1, double c
 
 }  // namespace
 
-__global__ void finalize_rho_kernel(const Problem p, int nvb, const double *__restrict__ partial,
-                                    double *__restrict__ rho)
-{
-    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= p.Ns) return;
-    double t = 0;
-    for (int b = 0; b < nvb; ++b) t += partial[(long long)b * p.Ns + s];
-    rho[s] = -p.wv * t;
-}
-
-cudaError_t launch_finalize_rho(const Problem &p, int nvb, const double *partial, double *rho, cudaStream_t st)
-{
-    finalize_rho_kernel<<<unsigned((p.Ns + 255) / 256), 256, 0, st>>>(p, nvb, partial, rho);
-    return cudaGetLastError();
-}
-
 struct SolveArgs {
     const double2 *tw[3];
     const double2 *isym[3];
@@ -109,29 +93,16 @@ struct SolveArgs {
     int lg[3];
 };
 
-__global__ void __launch_bounds__(1024) field_solve_kernel(const Problem p, const SolveArgs a, int nvb,
-                                                           const double *__restrict__ partial,
-                                                           const double *__restrict__ rho_in,
-                                                           double *__restrict__ rho_out, double *__restrict__ slab,
+__global__ void __launch_bounds__(1024) field_solve_kernel(const Problem p, const SolveArgs a,
+                                                           const double *__restrict__ rho, double *__restrict__ slab,
                                                            float *__restrict__ table, double *__restrict__ energy_out,
                                                            unsigned *err)
 {
     extern __shared__ double2 z[];
     __shared__ double red[1024];
     const long long ntot = p.Ns;
-    // 1. rho (fixed-order sum of the trace partials, or a given rho)
-    for (long long s = threadIdx.x; s < ntot; s += blockDim.x) {
-        double r;
-        if (rho_in) {
-            r = rho_in[s];
-        } else {
-            double t = 0;
-            for (int b = 0; b < nvb; ++b) t += partial[(long long)b * ntot + s];
-            r = -p.wv * t;
-        }
-        if (rho_out) rho_out[s] = r;
-        z[s] = make_double2(r, 0.0);
-    }
+    // 1. rho (written by the trace kernel, or copied in by the caller)
+    for (long long s = threadIdx.x; s < ntot; s += blockDim.x) z[s] = make_double2(rho[s], 0.0);
     __syncthreads();
     // 2. forward DFT, axis by axis (x fastest)
     long long S = 1;
@@ -198,9 +169,8 @@ __global__ void __launch_bounds__(1024) field_solve_kernel(const Problem p, cons
     }
 }
 
-cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, int nvb, const double *partial,
-                               const double *rho_in, double *rho_out, double *hist_slab, float *table_slab,
-                               double *energy_out, unsigned *err, cudaStream_t st)
+cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
+                               float *table_slab, double *energy_out, unsigned *err, cudaStream_t st)
 {
     SolveArgs a;
     for (int i = 0; i < 3; ++i) {
@@ -209,8 +179,7 @@ cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, int nvb,
         a.ksq[i] = plan.ksq[i];
         a.lg[i] = plan.log2n[i];
     }
-    field_solve_kernel<<<1, 1024, plan.smem, st>>>(p, a, nvb, partial, rho_in, rho_out, hist_slab, table_slab,
-                                                   energy_out, err);
+    field_solve_kernel<<<1, 1024, plan.smem, st>>>(p, a, rho, hist_slab, table_slab, energy_out, err);
     return cudaGetLastError();
 }
 

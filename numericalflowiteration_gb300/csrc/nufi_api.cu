@@ -8,13 +8,16 @@
 //            (nufi_step / nufi_run) or by nufi_upload_phi.
 //   tables   (Nt+1) FP32 field tables (split mode only): 1D per cell
 //            float4 K(A,B,C) of the spline derivative, 2D/3D the FP32 slab.
-//   partial  [vblocks][Ns] FP64 per-block sums of the trace.
+//   partial  [vblocks][Ns] FP64 per-block sums of the trace, and one
+//            arrival counter per 32-node spatial tile (finish_rho).
 //   rho      [Ns] FP64, energy [Nt+1] FP64, err (one error word).
 //   solve plan: per-axis twiddles, inverse collocation symbols, |k|^2.
 //   split tables: per-velocity-node constants and per-cell phases.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <string>
@@ -39,6 +42,7 @@ struct nufi_handle {
     double *hist = nullptr;
     float *tables = nullptr;
     double *partial = nullptr;
+    unsigned *counter = nullptr;
     double *rho = nullptr;
     double *energy = nullptr;
     double *rho_in = nullptr;     // nufi_field_solve scratch
@@ -187,6 +191,8 @@ Problem make_problem(const nufi_config &c)
     for (int i = 0; i < 8; ++i) p.f0p[i] = c.f0_params[i];
     p.wv = 1;
     for (int a = 0; a < c.dim; ++a) p.wv *= p.dv[a];
+    const char *plain = std::getenv("NUFI_SPLIT_PLAIN_KICK");
+    p.split_plain_kick = (plain && plain[0] == '1') ? 1 : 0;
     return p;
 }
 
@@ -239,6 +245,12 @@ int build_solve_plan(nufi_handle *h)
             const double ang = -2.0 * M_PI * double(j) / double(N);
             tw[j] = make_double2(std::cos(ang), std::sin(ang));
         }
+        // Symbol of the collocation circulant; even-degree splines (orders
+        // 3, 5) make it vanish at the Nyquist mode, where the reference's
+        // LSMR from a zero start returns the minimum-norm solution, i.e.
+        // that mode is dropped (pseudo-inverse).
+        std::vector<double2> lam(N);
+        double lmax = 0;
         for (int k = 0; k < N; ++k) {
             double re = 0, im = 0;
             for (int j = 0; j < p.order; ++j) {
@@ -246,8 +258,13 @@ int build_solve_plan(nufi_handle *h)
                 re += Nb[j] * std::cos(ang);
                 im += Nb[j] * std::sin(ang);
             }
+            lam[k] = make_double2(re, im);
+            lmax = std::max(lmax, std::sqrt(re * re + im * im));
+        }
+        for (int k = 0; k < N; ++k) {
+            const double re = lam[k].x, im = lam[k].y;
             const double den = re * re + im * im;
-            is[k] = make_double2(re / den, -im / den);
+            is[k] = std::sqrt(den) <= 1e-12 * lmax ? make_double2(0.0, 0.0) : make_double2(re / den, -im / den);
             const double kf = (2 * k < N) ? double(k) : double(N - k);
             const double kk = kf * (2 * M_PI * p.Linv[a]);
             ks[k] = kk * kk;
@@ -342,10 +359,11 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
 {
     const Problem &p = h->p;
     cudaError_t e;
+    RhoScratch scr{h->partial, h->counter};
     if (p.precision == NUFI_PREC_FP64)
-        e = launch_trace_fp64(p, h->shape, h->hist, int(n), qb, qe, mode, h->partial, h->err, h->stream);
+        e = launch_trace_fp64(p, h->shape, h->hist, int(n), qb, qe, mode, scr, h->rho, h->err, h->stream);
     else
-        e = launch_trace_split(p, h->shape, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, h->err,
+        e = launch_trace_split(p, h->shape, h->tables, h->nodes, h->phase, int(n), qb, qe, scr, h->rho, h->err,
                                h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "trace launch");
     h->launches += 1;
@@ -357,8 +375,7 @@ int enqueue_step(nufi_handle *h, long long n)
     const Problem &p = h->p;
     int st = enqueue_trace(h, n, 0, p.Nq, 0);
     if (st) return st;
-    cudaError_t e = launch_field_solve(p, h->plan, h->shape.vblocks, h->partial, nullptr, h->rho,
-                                       h->hist + n * p.hist_stride,
+    cudaError_t e = launch_field_solve(p, h->plan, h->rho, h->hist + n * p.hist_stride,
                                        h->tables ? h->tables + n * p.table_stride : nullptr, h->energy + n, h->err,
                                        h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
@@ -427,6 +444,7 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     const size_t nslab = size_t(cfg->Nt + 1);
     if ((e = dalloc(h.get(), &h->hist, nslab * p.hist_stride)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->partial, size_t(h->shape.vblocks) * p.Ns)) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->counter, size_t((p.Ns + 31) / 32))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->rho, size_t(p.Ns))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->energy, nslab)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->rho_in, size_t(p.Ns))) != cudaSuccess ||
@@ -444,7 +462,8 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     if ((e = cudaMemset(h->hist, 0, nslab * p.hist_stride * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->energy, 0, nslab * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->rho, 0, size_t(p.Ns) * sizeof(double))) != cudaSuccess ||
-        (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess)
+        (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMemset(h->counter, 0, size_t((p.Ns + 31) / 32) * sizeof(unsigned))) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMemset"));
     if ((st = build_solve_plan(h.get()))) return bail(st);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(cuda_fail(h.get(), e, "nufi_create"));
@@ -472,12 +491,7 @@ int nufi_compute_rho(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end)
         return fail(h, NUFI_ERR_RANGE, "quadrature range outside [0, Nq]");
     if (q_begin == q_end) return NUFI_OK;  // as the reference: no launch, rho untouched
     DeviceGuard g(h->device);
-    int st = enqueue_trace(h, n, q_begin, q_end, 0);
-    if (st) return st;
-    cudaError_t e = launch_finalize_rho(h->p, h->shape.vblocks, h->partial, h->rho, h->stream);
-    if (e != cudaSuccess) return cuda_fail(h, e, "finalize launch");
-    h->launches += 1;
-    return NUFI_OK;
+    return enqueue_trace(h, n, q_begin, q_end, 0);
 }
 
 static int download_rho_impl(nufi_handle *h, std::vector<double> &tmp)
@@ -624,8 +638,8 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
     const Problem &p = h->p;
     DeviceGuard g(h->device);
     NUFI_CUDA(h, cudaMemcpyAsync(h->rho_in, rho, size_t(p.Ns) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    cudaError_t e = launch_field_solve(p, h->plan, 0, nullptr, h->rho_in, nullptr, h->slab_out, nullptr,
-                                       h->energy_tmp, h->err, h->stream);
+    cudaError_t e = launch_field_solve(p, h->plan, h->rho_in, h->slab_out, nullptr, h->energy_tmp, h->err,
+                                       h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
     h->launches += 1;
     NUFI_CUDA(h, cudaMemcpyAsync(slab_out, h->slab_out, size_t(p.stride_t) * sizeof(double), cudaMemcpyDeviceToHost,

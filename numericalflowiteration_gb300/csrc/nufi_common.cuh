@@ -37,17 +37,9 @@ struct Problem {
     double vmin[3], dv[3];
     double f0p[8];
     double wv;           // prod_d dv_d, the quadrature weight of rho
-};
-
-// Per-velocity-node constants of the split form (one entry per node of
-// each velocity axis).  w0 = u0 dt / dx is the free-streaming shift in
-// cells per substep, split into an integer S0 (reduced mod N) and a
-// fraction sigma = sig_hi + sig_lo in [0, 1).
-struct SplitVel {
-    double u0;        // grid velocity (FP64)
-    float u0f;        // (float)u0
-    float sig_hi, sig_lo;
-    int S0;
+    int split_plain_kick;  // split mode: 1 = uncompensated FP32 kick sum
+                           // (NUFI_SPLIT_PLAIN_KICK=1 at create; for measuring
+                           // what the compensation buys)
 };
 
 __host__ __device__ inline double faculty(int n) { return (n > 1) ? double(n) * faculty(n - 1) : 1.0; }

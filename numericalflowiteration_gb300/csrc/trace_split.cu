@@ -11,6 +11,9 @@
 // 2^-24 |x| of a plain FP32 trace, and the large constant part of the
 // velocity never meets FP32 rounding.  floor(t) comes from one
 // round-down add of 1.5 * 2^23 (valid for |t| < 2^22).
+// The kick sum dw is compensated (Kahan: dwc carries the rounding lost by
+// each add and is fed back into the next drift), because an uncompensated
+// FP32 velocity sum puts O(n^1.5 eps |dw|) into the positions.
 //
 // The field of slab k is held as, per cell i, the quadratic
 // K (A + B xi + C xi^2) = K dS/dxi of the cubic spline on that cell with
@@ -35,10 +38,10 @@ constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 
 template <bool POW2>
-__device__ __forceinline__ void drift_split(int &I, float &xi, float dw, float shi, float slo, int S0, int N,
-                                            unsigned *err)
+__device__ __forceinline__ void drift_split(int &I, float &xi, float dw, float dwc, float shi, float slo, int S0,
+                                            int N, unsigned *err)
 {
-    const float t = (xi - shi) - (slo + dw);
+    const float t = (xi - shi) - ((slo - dwc) + dw);
     const float mg = __fadd_rd(t, kMagic);
     const int fi = __float_as_int(mg) - kMagicBits;
     xi = t - (mg - kMagic);
@@ -86,12 +89,26 @@ __device__ __forceinline__ float delta_f0_1d(const F0Split &f, const SplitNode &
 
 }  // namespace
 
-template <int PPT, bool POW2>
+// dw += k with Kahan compensation (dwc = -(low bits lost so far)).
+template <bool COMP>
+__device__ __forceinline__ void kick_split(float &dw, float &dwc, float k)
+{
+    if constexpr (COMP) {
+        const float y = k - dwc;
+        const float t = dw + y;
+        dwc = (t - dw) - y;
+        dw = t;
+    } else {
+        dw += k;
+    }
+}
+
+template <int PPT, bool POW2, bool COMP>
 __global__ void __launch_bounds__(256) trace_split_1d_kernel(const Problem p, const float *__restrict__ tables,
                                                              const SplitNode *__restrict__ nodes,
                                                              const float2 *__restrict__ phase, int n,
                                                              long long q_begin, long long q_end,
-                                                             double *__restrict__ partial, unsigned *err)
+                                                             RhoScratch scr, double *__restrict__ rho, unsigned *err)
 {
     const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
     const long long s = (long long)blockIdx.x * 32 + lane;
@@ -99,7 +116,7 @@ __global__ void __launch_bounds__(256) trace_split_1d_kernel(const Problem p, co
     const int N = p.N[0];
 
     int I[PPT], S0[PPT];
-    float xi[PPT], dw[PPT], shi[PPT], slo[PPT];
+    float xi[PPT], dw[PPT], dwc[PPT], shi[PPT], slo[PPT];
     bool live[PPT];
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
@@ -113,6 +130,7 @@ __global__ void __launch_bounds__(256) trace_split_1d_kernel(const Problem p, co
         I[q] = int(s < p.Ns ? s : 0);
         xi[q] = 0.0f;
         dw[q] = 0.0f;
+        dwc[q] = 0.0f;
     }
 
     if (n > 0) {
@@ -120,17 +138,17 @@ __global__ void __launch_bounds__(256) trace_split_1d_kernel(const Problem p, co
             const float4 *__restrict__ tk = reinterpret_cast<const float4 *>(tables + (long long)k * p.table_stride);
 #pragma unroll
             for (int q = 0; q < PPT; ++q) {
-                drift_split<POW2>(I[q], xi[q], dw[q], shi[q], slo[q], S0[q], N, err);
+                drift_split<POW2>(I[q], xi[q], dw[q], dwc[q], shi[q], slo[q], S0[q], N, err);
                 const float4 T = __ldg(tk + I[q]);
-                dw[q] += fmaf(xi[q], fmaf(xi[q], T.z, T.y), T.x);
+                kick_split<COMP>(dw[q], dwc[q], fmaf(xi[q], fmaf(xi[q], T.z, T.y), T.x));
             }
         }
         const float4 *__restrict__ t0 = reinterpret_cast<const float4 *>(tables);
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
-            drift_split<POW2>(I[q], xi[q], dw[q], shi[q], slo[q], S0[q], N, err);
+            drift_split<POW2>(I[q], xi[q], dw[q], dwc[q], shi[q], slo[q], S0[q], N, err);
             const float4 T = __ldg(t0 + I[q]);
-            dw[q] += 0.5f * fmaf(xi[q], fmaf(xi[q], T.z, T.y), T.x);
+            kick_split<COMP>(dw[q], dwc[q], 0.5f * fmaf(xi[q], fmaf(xi[q], T.z, T.y), T.x));
         }
     }
 
@@ -146,10 +164,10 @@ __global__ void __launch_bounds__(256) trace_split_1d_kernel(const Problem p, co
     for (int q = 0; q < PPT; ++q) {
         if (!live[q]) continue;
         const SplitNode nd = nodes[mb + q];
-        const float df = delta_f0_1d(f, nd, __ldg(phase + I[q]), xi[q], dw[q]);
+        const float df = delta_f0_1d(f, nd, __ldg(phase + I[q]), xi[q], dw[q] - dwc[q]);
         acc += double(df) + nd.g;
     }
-    block_reduce_partial(acc, s, p.Ns, partial);
+    finish_rho(acc, s, p.Ns, p.wv, scr, rho);
 }
 
 bool split_supported(int dim, int order, int f0_kind)
@@ -160,16 +178,21 @@ bool split_supported(int dim, int order, int f0_kind)
 }
 
 cudaError_t launch_trace_split(const Problem &p, const LaunchShape &ls, const float *tables, const SplitNode *nodes,
-                               const float2 *phase, int n, long long qb, long long qe, double *partial, unsigned *err,
-                               cudaStream_t st)
+                               const float2 *phase, int n, long long qb, long long qe, RhoScratch scr, double *rho,
+                               unsigned *err, cudaStream_t st)
 {
     if (p.dim != 1) return cudaErrorNotSupported;
     const dim3 block(32, ls.warps);
     const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(ls.vblocks));
     const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
-#define NUFI_LAUNCH(PPT)                                                                                          \
-    if (pow2) trace_split_1d_kernel<PPT, true><<<grid, block, 0, st>>>(p, tables, nodes, phase, n, qb, qe, partial, err); \
-    else trace_split_1d_kernel<PPT, false><<<grid, block, 0, st>>>(p, tables, nodes, phase, n, qb, qe, partial, err);
+#define NUFI_LAUNCH3(PPT, P2, C) \
+    trace_split_1d_kernel<PPT, P2, C><<<grid, block, 0, st>>>(p, tables, nodes, phase, n, qb, qe, scr, rho, err);
+#define NUFI_LAUNCH(PPT)                                                  \
+    if (p.split_plain_kick) {                                             \
+        if (pow2) NUFI_LAUNCH3(PPT, true, false) else NUFI_LAUNCH3(PPT, false, false) \
+    } else {                                                              \
+        if (pow2) NUFI_LAUNCH3(PPT, true, true) else NUFI_LAUNCH3(PPT, false, true) \
+    }
     switch (ls.ppt) {
     case 1: NUFI_LAUNCH(1) break;
     case 2: NUFI_LAUNCH(2) break;
@@ -177,6 +200,7 @@ cudaError_t launch_trace_split(const Problem &p, const LaunchShape &ls, const fl
     default: return cudaErrorInvalidValue;
     }
 #undef NUFI_LAUNCH
+#undef NUFI_LAUNCH3
     return cudaGetLastError();
 }
 

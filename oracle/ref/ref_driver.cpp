@@ -9,6 +9,8 @@
 // explicit specialisation of that member for real = double, declared
 // before any use; everything else is the reference's code unchanged.
 //
+// NUFI_REF_SUMMATION=1 in the environment sums rho compensated (see
+// rho_sum); the default is the reference's in-order sum.
 // Usage:
 //   ref_driver run   <cfg.bin> <n0> <n1> <out_prefix> [threads]
 //       steps n0..n1 of the loop of bin/test_nufi_gpu_{1d,2d,3d}.cpp with
@@ -21,6 +23,7 @@
 //       <out>.slab and <out>.energy.
 //   ref_driver poisson_kat        bin/test_poisson.cpp's analytic check
 //   ref_driver fields_kat         bin/test_fields.cpp's checks at nodes
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -34,6 +37,24 @@
 #include "../nufi_f0.h"
 
 static nufi_f0_params g_f0;
+// 0: rho summed in q order (as the reference's CPU loop); 1: Neumaier
+// compensated, i.e. the same f~ values summed to ~1 ulp.
+static int g_sum_mode = 0;
+
+struct rho_sum {
+    double acc = 0, comp = 0;
+    void add(double f)
+    {
+        if (g_sum_mode == 1) {
+            const double t = acc + f;
+            comp += (std::abs(acc) >= std::abs(f)) ? (acc - t) + f : (f - t) + acc;
+            acc = t;
+        } else {
+            acc += f;
+        }
+    }
+    double value() const { return acc + comp; }
+};
 
 namespace nufi {
 namespace dim1 {
@@ -121,13 +142,13 @@ void rho_1d(size_t n, const double *coeffs, const nufi::dim1::config_t<double> &
 {
 #pragma omp parallel for schedule(dynamic, 1)
     for (size_t ix = 0; ix < conf.Nx; ++ix) {
-        double acc = 0;
+        rho_sum acc;
         for (size_t iu = 0; iu < conf.Nu; ++iu) {
             const double x = conf.x_min + ix * conf.dx;
             const double u = conf.u_min + iu * conf.du + conf.du / 2;
-            acc += nufi::dim1::eval_ftilda<double, order>(n, x, u, coeffs, conf);
+            acc.add(nufi::dim1::eval_ftilda<double, order>(n, x, u, coeffs, conf));
         }
-        rho[ix] = -conf.du * acc;
+        rho[ix] = -conf.du * acc.value();
     }
 }
 
@@ -138,16 +159,16 @@ void rho_2d(size_t n, const double *coeffs, const nufi::dim2::config_t<double> &
 #pragma omp parallel for schedule(dynamic, 1)
     for (size_t s = 0; s < Ns; ++s) {
         const size_t ix = s % conf.Nx, iy = s / conf.Nx;
-        double acc = 0;
+        rho_sum acc;
         for (size_t iv = 0; iv < conf.Nv; ++iv)
             for (size_t iu = 0; iu < conf.Nu; ++iu) {
                 const double x = conf.x_min + ix * conf.dx;
                 const double y = conf.y_min + iy * conf.dy;
                 const double u = conf.u_min + iu * conf.du + conf.du / 2;
                 const double v = conf.v_min + iv * conf.dv + conf.dv / 2;
-                acc += nufi::dim2::eval_ftilda<double, order>(n, x, y, u, v, coeffs, conf);
+                acc.add(nufi::dim2::eval_ftilda<double, order>(n, x, y, u, v, coeffs, conf));
             }
-        rho[s] = -(conf.du * conf.dv) * acc;
+        rho[s] = -(conf.du * conf.dv) * acc.value();
     }
 }
 
@@ -158,7 +179,7 @@ void rho_3d(size_t n, const double *coeffs, const nufi::dim3::config_t<double> &
 #pragma omp parallel for schedule(dynamic, 1)
     for (size_t s = 0; s < Ns; ++s) {
         const size_t ix = s % conf.Nx, iy = (s / conf.Nx) % conf.Ny, iz = s / (conf.Nx * conf.Ny);
-        double acc = 0;
+        rho_sum acc;
         for (size_t iw = 0; iw < conf.Nw; ++iw)
             for (size_t iv = 0; iv < conf.Nv; ++iv)
                 for (size_t iu = 0; iu < conf.Nu; ++iu) {
@@ -168,9 +189,9 @@ void rho_3d(size_t n, const double *coeffs, const nufi::dim3::config_t<double> &
                     const double u = conf.u_min + iu * conf.du + conf.du / 2;
                     const double v = conf.v_min + iv * conf.dv + conf.dv / 2;
                     const double w = conf.w_min + iw * conf.dw + conf.dw / 2;
-                    acc += nufi::dim3::eval_ftilda<double, order>(n, x, y, z, u, v, w, coeffs, conf);
+                    acc.add(nufi::dim3::eval_ftilda<double, order>(n, x, y, z, u, v, w, coeffs, conf));
                 }
-        rho[s] = -(conf.du * conf.dv * conf.dw) * acc;
+        rho[s] = -(conf.du * conf.dv * conf.dw) * acc.value();
     }
 }
 
@@ -339,6 +360,7 @@ int main(int argc, char **argv)
         std::fprintf(stderr, "usage: ref_driver run|solve|poisson_kat|fields_kat ...\n");
         return 2;
     }
+    if (const char *m = std::getenv("NUFI_REF_SUMMATION")) g_sum_mode = std::atoi(m);
     const std::string cmd = argv[1];
     if (cmd == "run") return cmd_run(argc, argv);
     if (cmd == "solve") return cmd_solve(argc, argv);

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import subprocess
 import sys
 import tempfile
@@ -58,17 +59,30 @@ SOLVE_CASES = {
 }
 
 
-def run_case(name, cfg, n_last, rho_keep, slab_keep, tmp: Path):
-    p = tmp / name
-    (p.with_suffix(".cfg")).write_bytes(cfg.to_bytes())
-    subprocess.run([str(DRIVER), "run", str(p.with_suffix(".cfg")), "0", str(n_last), str(p)], check=True)
+def _driver_run(cfg, n_last, p: Path, summation: int):
+    env = dict(os.environ, NUFI_REF_SUMMATION=str(summation))
+    subprocess.run([str(DRIVER), "run", str(p.with_suffix(".cfg")), "0", str(n_last), str(p)], check=True, env=env)
     energy = np.fromfile(str(p) + ".energy")
     rho = np.fromfile(str(p) + ".rho").reshape(n_last + 1, cfg.n_spatial)
     coeffs = np.fromfile(str(p) + ".coeffs").reshape(cfg.Nt + 1, cfg.stride_t)
+    return energy, rho, coeffs
+
+
+def run_case(name, cfg, n_last, rho_keep, slab_keep, tmp: Path):
+    """The reference's loop twice: rho summed in q order (its CPU loop) and
+    compensated (the exact sum of the same f~ values); the gap between the
+    two energy histories is the FP64 summation floor of the case."""
+    p = tmp / name
+    (p.with_suffix(".cfg")).write_bytes(cfg.to_bytes())
+    energy, rho, coeffs = _driver_run(cfg, n_last, p, 0)
+    energy_c, rho_c, coeffs_c = _driver_run(cfg, n_last, p, 1)
+    floor = float(np.max(np.abs(energy - energy_c)) / np.max(np.abs(energy_c)))
     np.savez_compressed(HERE / f"{name}.npz", config=np.frombuffer(cfg.to_bytes(), dtype=np.uint8),
                         n_last=n_last, energy=energy, rho_steps=np.array(rho_keep), rho=rho[rho_keep],
-                        slab_steps=np.array(slab_keep), slabs=coeffs[slab_keep])
-    return {"n_last": n_last, "energy_max": float(np.max(energy)), "energy_last": float(energy[-1])}
+                        slab_steps=np.array(slab_keep), slabs=coeffs[slab_keep], energy_comp=energy_c,
+                        rho_comp=rho_c[rho_keep], slabs_comp=coeffs_c[slab_keep], summation_floor=floor)
+    return {"n_last": n_last, "energy_max": float(np.max(energy)), "energy_last": float(energy[-1]),
+            "summation_floor": floor}
 
 
 def solve_case(name, cfg, tmp: Path, seed: int):

@@ -2,19 +2,18 @@
 reference's golden vectors (tests/golden/) and the CPU oracle.
 
 Measures: max |d| / max |ref| for rho, slabs and energy histories.
-FP64 plain must agree with the reference to 1e-12 (2e-12 for the
-alpha = 1e-3 two-stream case, whose FP64 summation floor is ~1e-12, see
-tests/test_oracle_golden.py).  FP32-split must stay within 1e-6 of the
-FP64 energy history (the metric's gate).
+FP64 plain must agree with the reference to 1e-12: against the reference
+run with compensated rho sums (the GPU sums in a fixed, compensated tree)
+and, against the reference's in-order sums, within 1e-12 or 3x that case's
+measured FP64 summation floor (conftest.energy_tol).  FP32-split must stay
+within 1e-6 of the FP64 energy history (the metric's gate).
 """
 import numpy as np
 import pytest
 
-from conftest import golden, rel_max
+from conftest import energy_tol, golden, rel_max
 
 pytestmark = pytest.mark.gpu
-
-ENERGY_TOL = {"two_stream_1d_256x1024_n40": 2e-12}
 
 
 @pytest.fixture(scope="module")
@@ -45,7 +44,8 @@ def test_fp64_stepwise_rho_energy_slabs(nufi, name):
             if n in list(g["rho_steps"]):
                 i = list(g["rho_steps"]).index(n)
                 assert rel_max(rho, g["rho"][i]) <= 1e-12, f"rho step {n}"
-        assert rel_max(energies, g["energy"]) <= 1e-12
+        assert rel_max(energies, g["energy_comp"]) <= 1e-12
+        assert rel_max(energies, g["energy"]) <= energy_tol(g)
         _slabs_ok(cfg, sim.history(), g)
         assert sim.launches >= 2 * (int(g["n_last"]) + 1)
 
@@ -58,7 +58,8 @@ def test_fp64_graph_run_matches_reference(nufi, name):
     n_last = int(g["n_last"])
     with nufi.Simulation(cfg) as sim:
         e = sim.run(0, n_last)
-        assert rel_max(e, g["energy"]) <= ENERGY_TOL.get(name, 1e-12)
+        assert rel_max(e, g["energy_comp"]) <= 1e-12
+        assert rel_max(e, g["energy"]) <= energy_tol(g)
         _slabs_ok(cfg, sim.history(), g)
         rho = sim.download_rho(np.zeros(cfg.n_spatial))
         assert rel_max(rho, g["rho"][list(g["rho_steps"]).index(n_last)]) <= 1e-12
@@ -68,7 +69,8 @@ def test_fp64_two_stream_through_saturation(nufi):
     cfg, g = golden("two_stream_1d_64x256_T50")
     with nufi.Simulation(cfg) as sim:
         e = sim.run()
-    assert rel_max(e[:200], g["energy"][:200]) <= 2e-12
+    assert rel_max(e[:200], g["energy_comp"][:200]) <= 1e-12
+    assert rel_max(e[:200], g["energy"][:200]) <= max(2e-12, energy_tol(g))
     assert rel_max(e, g["energy"]) <= 1e-9
 
 

@@ -132,6 +132,28 @@ int nufi_download_energy(nufi_handle *h, int64_t n0, int64_t n1, double *energy)
  * padded slab (stride_t values) out, returns W in *energy.  Blocks. */
 int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double *energy);
 
+/* ---- allocation-free rho ------------------------------------------------
+ * No counterpart in the reference.  rho of step n over [q_begin, q_end)
+ * for callers that must not allocate device memory (no cudaMalloc, no
+ * allocating library call): for example code running inside someone
+ * else's CUDA-graph capture or memory pool, or a real-time loop whose
+ * device memory is reserved up front.  FP64 plain form only.  The caller
+ * passes device buffers: hist (slab k at hist + k*hist_stride doubles,
+ * reference layout inside a slab, hist_stride >= stride_t) and rho (Ns
+ * doubles, overwritten, not accumulated).  Enqueued on `stream` (a
+ * cudaStream_t, NULL = legacy default stream) on the current device;
+ * returns without waiting.
+ * Scratch: a fixed 8 MiB array inside the library (held by every GPU that
+ * loads it until the process exits) for the per-block partial sums; about
+ * Nm * Ns / 16 * 8 bytes must fit, larger problems get NUFI_ERR_RANGE.
+ * The first call on a device looks up the array's device address; make
+ * that first call before any stream capture.  All calls share the array,
+ * so calls that overlap on the GPU (other streams, other threads) race;
+ * serialise them.  Device-side range flags are not reported here.
+ * Handle-less: errors via nufi_last_error(NULL). */
+int nufi_compute_rho_noalloc(const nufi_config *cfg, int64_t n, const double *hist, int64_t hist_stride,
+                             int64_t q_begin, int64_t q_end, double *rho, void *stream);
+
 /* ---- information ------------------------------------------------------- */
 int nufi_synchronize(nufi_handle *h);
 /* stride_t (values per slab), number of spatial nodes, number of points */

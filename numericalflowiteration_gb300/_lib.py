@@ -47,6 +47,7 @@ SIGNATURES = {
     "nufi_sizes": (ctypes.c_int, [_P, _P, _P, _P]),
     "nufi_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "nufi_launch_count": (ctypes.c_int, [_P, _P]),
+    "nufi_compute_rho_noalloc": (ctypes.c_int, [_P, _I64, _P, _I64, _I64, _I64, _P, _P]),
 }
 
 _lib = None

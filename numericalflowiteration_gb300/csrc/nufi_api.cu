@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -683,3 +684,95 @@ int nufi_launch_count(const nufi_handle *h, int64_t *count)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free rho (nufi_compute_rho_noalloc).
+//
+// For callers that must not allocate device memory: code that runs while
+// allocations are forbidden or would stall (a host thread inside another
+// library's CUDA-graph capture or memory pool, a real-time loop that
+// pre-reserves everything, an embedding that owns the device memory
+// budget).  The caller passes the coefficient history and rho as device
+// buffers; the trace's scratch (per-block partial sums, per-tile arrival
+// counters) lives in the file-scope array below, which every GPU that loads
+// this library holds until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_addr[kMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device, looked up
+// once per device.  (In host code the symbol's name is only a host-side
+// stand-in; a kernel must be given this address instead.)
+int noalloc_scratch(int dev, unsigned char **out)
+{
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_addr[dev] = static_cast<unsigned char *>(ptr);
+    }
+    *out = g_noalloc_addr[dev];
+    return NUFI_OK;
+}
+
+}  // namespace
+
+extern "C" int nufi_compute_rho_noalloc(const nufi_config *cfg, int64_t n, const double *hist, int64_t hist_stride,
+                                        int64_t q_begin, int64_t q_end, double *rho, void *stream)
+{
+    std::string why;
+    int st = validate(cfg, why);
+    if (st) return fail(nullptr, st, "nufi_compute_rho_noalloc: " + why);
+    if (cfg->precision != NUFI_PREC_FP64)
+        return fail(nullptr, NUFI_ERR_UNSUPPORTED, "nufi_compute_rho_noalloc: FP64 plain form only");
+    if (!hist || !rho) return fail(nullptr, NUFI_ERR_INVALID, "nufi_compute_rho_noalloc: null buffer");
+    Problem p = make_problem(*cfg);
+    if (hist_stride < p.stride_t)
+        return fail(nullptr, NUFI_ERR_INVALID, "nufi_compute_rho_noalloc: hist_stride smaller than one slab");
+    p.hist_stride = hist_stride;
+    if (n < 0 || n > cfg->Nt) return fail(nullptr, NUFI_ERR_RANGE, "nufi_compute_rho_noalloc: Time-step out of range.");
+    if (q_begin < 0 || q_end < q_begin || q_end > p.Nq)
+        return fail(nullptr, NUFI_ERR_RANGE, "nufi_compute_rho_noalloc: quadrature range outside [0, Nq]");
+    if (q_begin == q_end) return NUFI_OK;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return fail(nullptr, NUFI_ERR_INVALID, "nufi_compute_rho_noalloc: device id");
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    LaunchShape shape = choose_shape(p, sms > 0 ? sms : 1);
+    // Scratch layout: [error word | pad to 256 B][tile counters | pad][partials]
+    const size_t ntiles = size_t((p.Ns + 31) / 32);
+    const size_t off_counter = 256;
+    const size_t off_partial = (off_counter + ntiles * sizeof(unsigned) + 255) / 256 * 256;
+    auto need = [&](const LaunchShape &s) { return off_partial + size_t(s.vblocks) * size_t(p.Ns) * sizeof(double); };
+    if (need(shape) > kNoAllocScratchBytes) {
+        // fewest velocity blocks: 4 warps x 4 points per thread
+        shape.warps = 4;
+        shape.ppt = 4;
+        shape.vblocks = int((p.Nm + 15) / 16);
+    }
+    if (need(shape) > kNoAllocScratchBytes)
+        return fail(nullptr, NUFI_ERR_RANGE,
+                    "nufi_compute_rho_noalloc: needs " + std::to_string(need(shape)) +
+                        " bytes of scratch; the allocation-free entry point holds " +
+                        std::to_string(kNoAllocScratchBytes) + " (about Nm * Ns / 16 * 8 bytes must fit)");
+    unsigned char *base = nullptr;
+    if ((st = noalloc_scratch(dev, &base))) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // The previous call's contents stay in the array: the error word and the
+    // tile counters must start at zero.
+    if ((e = cudaMemsetAsync(base, 0, off_partial, s)) != cudaSuccess)
+        return cuda_fail(nullptr, e, "cudaMemsetAsync(scratch)");
+    RhoScratch scr{reinterpret_cast<double *>(base + off_partial), reinterpret_cast<unsigned *>(base + off_counter)};
+    e = launch_trace_fp64(p, shape, hist, int(n), q_begin, q_end, 0, scr, rho, reinterpret_cast<unsigned *>(base), s);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "nufi_compute_rho_noalloc launch");
+    return NUFI_OK;
+}

@@ -1,0 +1,64 @@
+"""The allocation-free rho entry point, nufi_compute_rho_noalloc, against
+the regular drop-in path (nufi_compute_rho + nufi_download_rho).
+
+It serves callers that must not allocate device memory: code running
+inside another library's CUDA-graph capture or memory pool, or a loop that
+reserves all of its device memory up front.  Such a caller hands in its own
+device buffers (the test makes them with torch); the entry point keeps its
+scratch in a fixed 8 MiB array inside the library.  The file name sorts
+last so that a stop-at-first-failure run has already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import rel_max
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_rho_matches_compute_rho_on_consecutive_calls():
+    torch = pytest.importorskip("torch")
+    import numericalflowiteration_gb300 as nufi
+    from numericalflowiteration_gb300 import build
+    from numericalflowiteration_gb300.config import landau_1d, two_stream_1d
+
+    build.build()
+    lib = nufi.load()
+    torch.cuda.init()
+    for cfg in (landau_1d(Nx=64, Nv=256, Nt=40), two_stream_1d(Nx=128, Nv=512, Nt=30)):
+        steps = (17, cfg.Nt)
+        with nufi.Simulation(cfg) as sim:
+            sim.run()
+            hist = sim.history()
+            want = {}
+            for n in steps:
+                sim.compute_rho(n)
+                want[n] = sim.download_rho(np.zeros(cfg.n_spatial))
+        dev_hist = torch.from_numpy(hist).cuda()
+        rho = torch.full((cfg.n_spatial,), float("nan"), dtype=torch.float64, device="cuda")
+        c = cfg.to_c()
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        for n in steps:  # two calls in a row share the library's scratch
+            st = lib.nufi_compute_rho_noalloc(ctypes.byref(c), n, ctypes.c_void_p(dev_hist.data_ptr()),
+                                              cfg.stride_t, 0, cfg.n_points, ctypes.c_void_p(rho.data_ptr()),
+                                              stream)
+            assert st == 0, lib.nufi_last_error(None).decode()
+            torch.cuda.synchronize()
+            assert rel_max(rho.cpu().numpy(), want[n]) <= 1e-13
+
+
+def test_noalloc_rejects_problems_beyond_its_scratch():
+    torch = pytest.importorskip("torch")
+    import numericalflowiteration_gb300 as nufi
+    from numericalflowiteration_gb300.config import landau_3d
+
+    lib = nufi.load()
+    torch.cuda.init()
+    cfg = landau_3d()  # 16^3 x 32^3: partial sums need ~64 MiB
+    c = cfg.to_c()
+    buf = torch.zeros(16, dtype=torch.float64, device="cuda")
+    st = lib.nufi_compute_rho_noalloc(ctypes.byref(c), 1, ctypes.c_void_p(buf.data_ptr()), cfg.stride_t, 0,
+                                      cfg.n_points, ctypes.c_void_p(buf.data_ptr()), None)
+    assert st == 2 and b"bytes of scratch" in lib.nufi_last_error(None)

@@ -1,6 +1,6 @@
-// field_solve.cu — periodic Poisson solve fused with the B-spline
-// collocation solve, as one diagonal in Fourier space, plus the small
-// kernels around it (FP32 field tables).
+// field_solve.cu — the per-step work around the trace: rho from the trace's
+// partial sums, then the periodic Poisson solve fused with the B-spline
+// collocation solve, the padded slab, the FP32 field table and W_n.
 //
 // The reference (a) transforms rho with FFTW's separable DHT, scales mode
 // k by 1/(N |k|^2), zeroes the mean and transforms back
@@ -8,71 +8,201 @@
 // W = prod L / 2 * sum_{k != 0} |k|^2 phi_k^2; then (b) solves the circulant
 // collocation system sum_j N_j(0) c[(i+j) mod N] = phi_i by LSMR
 // (nufi/fields.hpp:63-142, 186-300, 352-490) and writes the periodically
-// padded slab c[i] = c~[i mod N].  Because the Poisson scaling depends only
-// on the folded |k| per axis, the DHT sandwich equals a DFT sandwich, and
-// the collocation matrix is circulant with symbol
-// lambda(k) = prod_a sum_j N_j(0) exp(+2 pi i j k_a / N_a).  So
-//     c^(k) = rho^(k) / (N_tot |k|^2 lambda(k)),  c^(0) = 0,
-//     W     = prod L / 2 * sum_{k != 0} |rho^(k)|^2 / (N_tot^2 |k|^2)
-// with rho^ the unnormalised DFT.  Everything here is FP64.
-//
-// One block does the whole solve in shared memory (N_tot <= 8192 complex
-// values): radix-2 FFTs along each axis, then the diagonal, then the
-// inverse.  FP64 throughput is low on this part, but the solve is
-// O(N log N) per time step against O(N_points * n) for the trace.
+// padded slab c[i] = c~[i mod N].  Both are diagonal in Fourier space
+// (the Poisson scaling depends only on the folded |k| per axis, so the DHT
+// sandwich equals a DFT sandwich; the collocation matrix is circulant with
+// symbol lambda(k) = prod_a sum_j N_j(0) exp(+2 pi i j k_a / N_a)):
+//     c = IDFT[ rho^ / (N |k|^2 lambda) ],   phi = IDFT[ rho^ / (N |k|^2) ].
+// The host turns each diagonal into its circulant kernel (the inverse DFT
+// of the diagonal, computed once per configuration), so a step is a set of
+// dense circulant products c_i = sum_j G_c[i - j] rho'_j, spread over many
+// blocks.  On this part FP64 runs at 1/64 of the FP32 rate, and a
+// single-block FFT per step was serial; the product instead spreads the
+// O(N^2) FP64 FMAs over all SMs.  rho' = rho - mean(rho): the kernels sum
+// to zero, and removing the O(1) background first keeps the rounding
+// relative to the perturbation.  W = prod L / (2 N) * sum_i rho'_i phi_i
+// (Parseval), equal to the reference's spectral sum.  Everything is FP64.
 #include "nufi_kernels.cuh"
 
 namespace nufi_gb300 {
 
+__global__ void reduce_rho_kernel(const Problem p, int rows, const double *__restrict__ partial,
+                                  double *__restrict__ rho)
+{
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int Ns = int(p.Ns);
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < Ns; s += warps) {
+        double sum = 0, comp = 0;
+        for (int r = lane; r < rows; r += 32) neumaier_add(sum, comp, partial[(long long)r * Ns + s]);
+        for (int off = 16; off > 0; off >>= 1) {
+            const double os = __shfl_down_sync(0xffffffffu, sum, off);
+            const double oc = __shfl_down_sync(0xffffffffu, comp, off);
+            neumaier_add(sum, comp, os);
+            comp += oc;
+        }
+        if (lane == 0) rho[s] = -p.wv * (sum + comp);
+    }
+}
+
+cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st)
+{
+    const int warps_per_block = 4;
+    const int blocks = int((p.Ns + warps_per_block - 1) / warps_per_block);
+    reduce_rho_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(p, rows, partial, rho);
+    return cudaGetLastError();
+}
+
 namespace {
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b)
-{
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
+constexpr int kSolveThreads = 256;
+constexpr int kSolveWarps = kSolveThreads / 32;
 
-// In-place radix-2 FFT of every line along axis a (length N = 2^lg,
-// element stride S) of the N_tot-element array z.  sign = -1 forward
-// (twiddles as stored), +1 inverse (conjugated twiddles).
-__device__ void fft_axis(double2 *z, long long ntot, int N, int lg, long long S, const double2 *__restrict__ tw,
-                         bool inverse)
+// Sum of one value per thread, fixed-order tree over the block.
+__device__ __forceinline__ double block_sum_fixed(double v, double *red)
 {
-    if (N <= 1) return;
-    const long long lines = ntot / N;
-    // bit reversal along the axis
-    for (long long e = threadIdx.x; e < ntot; e += blockDim.x) {
-        const long long line = e / N;
-        const int i = int(e % N);
-        const int r = int(__brev(unsigned(i)) >> (32 - lg));
-        if (i < r) {
-            const long long base = (line / S) * (S * N) + (line % S);
-            const long long a = base + (long long)i * S, b = base + (long long)r * S;
-            const double2 t = z[a];
-            z[a] = z[b];
-            z[b] = t;
-        }
-    }
+    red[threadIdx.x] = v;
     __syncthreads();
-    const long long nb = lines * (N / 2);
-    for (int len = 2; len <= N; len <<= 1) {
-        const int half = len >> 1, step = N / len;
-        for (long long b = threadIdx.x; b < nb; b += blockDim.x) {
-            const long long line = b / (N / 2);
-            const int j = int(b % (N / 2));
-            const int pos = j % half;
-            const int i0 = (j / half) * len + pos;
-            const long long base = (line / S) * (S * N) + (line % S);
-            const long long e0 = base + (long long)i0 * S, e1 = e0 + (long long)half * S;
-            double2 w = tw[pos * step];
-            if (inverse) w.y = -w.y;
-            const double2 a = z[e0];
-            const double2 t = cmul(z[e1], w);
-            z[e0] = make_double2(a.x + t.x, a.y + t.y);
-            z[e1] = make_double2(a.x - t.x, a.y - t.y);
-        }
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
     }
+    const double r = red[0];
+    __syncthreads();
+    return r;
 }
+
+}  // namespace
+
+// One warp per node i (nodes strided over all warps of the grid):
+//   acc[c] = sum_j green[c][(i - j) mod N] * rho'[j]      (mod per axis)
+// then the slab (all padded positions of i), the table, and rho'_i phi_i.
+template <int NCONV>
+__global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
+    const Problem p, const double *__restrict__ rho, const double *__restrict__ green, int green_in_smem,
+    double *__restrict__ slab, float *__restrict__ table, double *__restrict__ energy_partial,
+    unsigned *__restrict__ energy_counter, double *__restrict__ energy_out)
+{
+    extern __shared__ double sm[];
+    __shared__ double red[kSolveThreads];
+    __shared__ bool last;
+    const int Ns = int(p.Ns);
+    const int N0 = p.N[0], N1 = p.N[1], N2 = p.N[2];
+    double *rs = sm;                                    // rho' [Ns]
+    const double *G = green_in_smem ? sm + Ns : green;  // [NCONV][Ns]
+    // 1. rho' = rho - mean(rho), the mean in fixed order (every block alike)
+    double part = 0;
+    for (int j = threadIdx.x; j < Ns; j += blockDim.x) {
+        const double r = rho[j];
+        rs[j] = r;
+        part += r;
+    }
+    if (green_in_smem)
+        for (int j = threadIdx.x; j < NCONV * Ns; j += blockDim.x) sm[Ns + j] = green[j];
+    const double mean = block_sum_fixed(part, red) / double(Ns);
+    for (int j = threadIdx.x; j < Ns; j += blockDim.x) rs[j] -= mean;
+    __syncthreads();
+
+    // 2. circulant products, one warp per node
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int total_warps = gridDim.x * kSolveWarps;
+    const int step0 = 32 % N0, step1 = (32 / N0) % N1, step2 = 32 / (N0 * N1);
+    double e_local = 0;
+    for (int i = blockIdx.x * kSolveWarps + warp; i < Ns; i += total_warps) {
+        const int i0 = i % N0, i1 = (i / N0) % N1, i2 = i / (N0 * N1);
+        double acc[NCONV];
+#pragma unroll
+        for (int c = 0; c < NCONV; ++c) acc[c] = 0;
+        int j0 = lane % N0, j1 = (lane / N0) % N1, j2 = lane / (N0 * N1);
+        for (int j = lane; j < Ns; j += 32) {
+            int m0 = i0 - j0, m1 = i1 - j1, m2 = i2 - j2;
+            m0 += m0 < 0 ? N0 : 0;
+            m1 += m1 < 0 ? N1 : 0;
+            m2 += m2 < 0 ? N2 : 0;
+            const int m = (m2 * N1 + m1) * N0 + m0;
+            const double r = rs[j];
+#pragma unroll
+            for (int c = 0; c < NCONV; ++c) acc[c] = fma(G[c * Ns + m], r, acc[c]);
+            // (j0, j1, j2) of j + 32
+            j0 += step0;
+            j1 += step1;
+            j2 += step2;
+            if (j0 >= N0) { j0 -= N0; ++j1; }
+            if (j1 >= N1) { j1 -= N1; ++j2; }
+        }
+#pragma unroll
+        for (int c = 0; c < NCONV; ++c)
+            for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
+        if (lane == 0) {
+            const double cval = acc[0];
+            // every padded position of node i: i_a and i_a + N_a while < P_a
+            for (int dz = 0; dz < 2; ++dz) {
+                const int k = i2 + dz * N2;
+                if (k >= p.P[2]) continue;
+                for (int dy = 0; dy < 2; ++dy) {
+                    const int jj = i1 + dy * N1;
+                    if (jj >= p.P[1]) continue;
+                    for (int dx = 0; dx < 2; ++dx) {
+                        const int ii = i0 + dx * N0;
+                        if (ii >= p.P[0]) continue;
+                        const int idx = (k * p.P[1] + jj) * p.P[0] + ii;
+                        slab[idx] = cval;
+                        if (table && p.dim > 1) table[idx] = float(cval);
+                    }
+                }
+            }
+            if constexpr (NCONV == 5) {
+                if (table)
+                    reinterpret_cast<float4 *>(table)[i] =
+                        make_float4(float(acc[2]), float(acc[3]), float(acc[4]), 0.0f);
+            }
+            e_local += rs[i] * acc[1];
+        }
+    }
+    // 3. energy: block partial (fixed order), the last block sums the blocks
+    const double eb = block_sum_fixed(e_local, red);
+    if (threadIdx.x == 0) energy_partial[blockIdx.x] = eb;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(energy_counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double v = 0;
+    for (int b = threadIdx.x; b < int(gridDim.x); b += blockDim.x) v += __ldcg(energy_partial + b);
+    const double tot = block_sum_fixed(v, red);
+    if (threadIdx.x == 0) {
+        double Lp = 1;
+        for (int ax = 0; ax < p.dim; ++ax) Lp *= p.L[ax];
+        if (energy_out) energy_out[0] = tot * (Lp / (2.0 * double(Ns)));
+        energy_counter[0] = 0u;
+    }
+}
+
+cudaError_t field_solve_prepare(const SolvePlan &plan)
+{
+    cudaError_t e = cudaFuncSetAttribute(circulant_solve_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(plan.smem));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(circulant_solve_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(plan.smem));
+}
+
+cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
+                               float *table_slab, double *energy_out, cudaStream_t st)
+{
+    if (plan.nconv == 5)
+        circulant_solve_kernel<5><<<plan.blocks, kSolveThreads, plan.smem, st>>>(
+            p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
+            energy_out);
+    else
+        circulant_solve_kernel<2><<<plan.blocks, kSolveThreads, plan.smem, st>>>(
+            p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
+            energy_out);
+    return cudaGetLastError();
+}
+
+namespace {
 
 // K (A, B, C) of cell i from c[i..i+3]: the derivative of the cubic
 // B-spline sum on [i, i+1) as a quadratic in xi, times K = -dt^2/dx^2.
@@ -85,103 +215,6 @@ __device__ __forceinline__ float4 cubic_kick_poly(double c0, double c1, double c
 }
 
 }  // namespace
-
-struct SolveArgs {
-    const double2 *tw[3];
-    const double2 *isym[3];
-    const double *ksq[3];
-    int lg[3];
-};
-
-__global__ void __launch_bounds__(1024) field_solve_kernel(const Problem p, const SolveArgs a,
-                                                           const double *__restrict__ rho, double *__restrict__ slab,
-                                                           float *__restrict__ table, double *__restrict__ energy_out,
-                                                           unsigned *err)
-{
-    extern __shared__ double2 z[];
-    __shared__ double red[1024];
-    const long long ntot = p.Ns;
-    // 1. rho (written by the trace kernel, or copied in by the caller)
-    for (long long s = threadIdx.x; s < ntot; s += blockDim.x) z[s] = make_double2(rho[s], 0.0);
-    __syncthreads();
-    // 2. forward DFT, axis by axis (x fastest)
-    long long S = 1;
-    for (int ax = 0; ax < p.dim; ++ax) {
-        fft_axis(z, ntot, p.N[ax], a.lg[ax], S, a.tw[ax], false);
-        S *= p.N[ax];
-    }
-    // 3. diagonal + energy
-    double e = 0;
-    const double inv_ntot = 1.0 / double(ntot);
-    for (long long s = threadIdx.x; s < ntot; s += blockDim.x) {
-        if (s == 0) {
-            z[0] = make_double2(0.0, 0.0);
-            continue;
-        }
-        long long r = s;
-        double ksq = 0;
-        double2 is = make_double2(1.0, 0.0);
-        for (int ax = 0; ax < p.dim; ++ax) {
-            const int k = int(r % p.N[ax]);
-            r /= p.N[ax];
-            ksq += a.ksq[ax][k];
-            is = cmul(is, a.isym[ax][k]);
-        }
-        const double2 F = z[s];
-        e += (F.x * F.x + F.y * F.y) / ksq;
-        const double scale = inv_ntot / ksq;
-        const double2 c = cmul(F, is);
-        z[s] = make_double2(c.x * scale, c.y * scale);
-    }
-    red[threadIdx.x] = e;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    // 4. inverse DFT
-    S = 1;
-    for (int ax = 0; ax < p.dim; ++ax) {
-        fft_axis(z, ntot, p.N[ax], a.lg[ax], S, a.tw[ax], true);
-        S *= p.N[ax];
-    }
-    // 5. padded slab (reference layout) and the FP32 field table
-    const long long P0 = p.P[0], P1 = p.P[1], P2 = p.P[2];
-    const long long npad = P0 * P1 * P2;
-    for (long long idx = threadIdx.x; idx < npad; idx += blockDim.x) {
-        const long long i = idx % P0, j = (idx / P0) % P1, k = idx / (P0 * P1);
-        const long long src = ((k % p.N[2]) * p.N[1] + (j % p.N[1])) * p.N[0] + (i % p.N[0]);
-        const double c = z[src].x;
-        slab[idx] = c;
-        if (table && p.dim > 1) table[idx] = float(c);
-    }
-    if (table && p.dim == 1) {
-        const int N = p.N[0];
-        const double K = -p.dt * p.dt * p.dxinv[0] * p.dxinv[0];
-        float4 *t4 = reinterpret_cast<float4 *>(table);
-        for (int i = threadIdx.x; i < N; i += blockDim.x)
-            t4[i] = cubic_kick_poly(z[i].x, z[(i + 1) % N].x, z[(i + 2) % N].x, z[(i + 3) % N].x, K);
-    }
-    if (threadIdx.x == 0 && energy_out) {
-        double Lp = 1;
-        for (int ax = 0; ax < p.dim; ++ax) Lp *= p.L[ax];
-        energy_out[0] = red[0] * inv_ntot * inv_ntot * (Lp / 2);
-    }
-}
-
-cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
-                               float *table_slab, double *energy_out, unsigned *err, cudaStream_t st)
-{
-    SolveArgs a;
-    for (int i = 0; i < 3; ++i) {
-        a.tw[i] = plan.tw[i];
-        a.isym[i] = plan.isym[i];
-        a.ksq[i] = plan.ksq[i];
-        a.lg[i] = plan.log2n[i];
-    }
-    field_solve_kernel<<<1, 1024, plan.smem, st>>>(p, a, rho, hist_slab, table_slab, energy_out, err);
-    return cudaGetLastError();
-}
 
 __global__ void derive_table_kernel(const Problem p, const double *__restrict__ slab, float *__restrict__ table)
 {
@@ -204,11 +237,4 @@ cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float
     return cudaGetLastError();
 }
 
-}  // namespace nufi_gb300
-
-namespace nufi_gb300 {
-cudaError_t field_solve_set_smem(size_t smem)
-{
-    return cudaFuncSetAttribute(field_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-}
 }  // namespace nufi_gb300

@@ -8,12 +8,13 @@
 //            (nufi_step / nufi_run) or by nufi_upload_phi.
 //   tables   (Nt+1) FP32 field tables (split mode only): 1D per cell
 //            float4 K(A,B,C) of the spline derivative, 2D/3D the FP32 slab.
-//   partial  [vblocks][Ns] FP64 per-block sums of the trace, and one
-//            arrival counter per 32-node spatial tile (finish_rho).
+//   partial  [rows][Ns] FP64 per-block sums of the trace (reduce_rho sums
+//            the rows into rho).
 //   rho      [Ns] FP64, energy [Nt+1] FP64, err (one error word).
-//   solve plan: per-axis twiddles, inverse collocation symbols, |k|^2.
+//   solve plan: circulant kernels of the Poisson + collocation diagonal.
 //   split tables: per-velocity-node constants and per-cell phases.
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -43,7 +44,6 @@ struct nufi_handle {
     double *hist = nullptr;
     float *tables = nullptr;
     double *partial = nullptr;
-    unsigned *counter = nullptr;
     double *rho = nullptr;
     double *energy = nullptr;
     double *rho_in = nullptr;     // nufi_field_solve scratch
@@ -56,6 +56,7 @@ struct nufi_handle {
     bool solve_ok = false;
     std::string solve_why;
     LaunchShape shape;
+    StagedShape staged;
     std::string last_error;
     long long launches = 0;
     std::map<std::pair<long long, long long>, std::pair<cudaGraphExec_t, long long>> graphs;
@@ -222,64 +223,127 @@ LaunchShape choose_shape(const Problem &p, int sms)
     return s;
 }
 
-int build_solve_plan(nufi_handle *h)
+// The field solve's circulant kernels (see field_solve.cu): for every mode
+// k the diagonal D(k) of Poisson (1 / (N |k|^2)) and of Poisson followed by
+// the collocation solve (divided by the symbol lambda(k)), then the inverse
+// DFT of D, separable per axis, summed in long double.  Even-degree splines
+// (orders 3, 5) make lambda vanish at the Nyquist mode, where the
+// reference's LSMR from a zero start returns the minimum-norm solution,
+// i.e. drops that mode: the same pseudo-inverse here.  In 1D split mode
+// three more kernels give K (A, B, C) of the per-cell quadratic directly
+// (shifts of c are phase factors of its diagonal).
+int build_solve_plan(nufi_handle *h, int sms)
 {
     const Problem &p = h->p;
     h->solve_ok = false;
-    for (int a = 0; a < p.dim; ++a)
-        if (!is_pow2(p.N[a])) {
-            h->solve_why = "device field solve needs power-of-two grid sizes";
-            return NUFI_OK;
-        }
-    const size_t smem = size_t(p.Ns) * sizeof(double2);
-    if (p.Ns > 8192) {
-        h->solve_why = "device field solve holds at most 8192 grid nodes";
+    const long long Ns = p.Ns;
+    if (Ns > 16384) {
+        h->solve_why = "device field solve holds at most 16384 grid nodes";
         return NUFI_OK;
     }
+    using cld = std::complex<long double>;
+    const long double two_pi = 6.283185307179586476925286766559005768L;
     double Nb[kMaxOrder] = {0};
     stencil(p.order, Nb);
+    // per-axis symbols and |k|^2
+    std::vector<std::vector<cld>> lam(p.dim);
+    std::vector<std::vector<long double>> ks(p.dim);
     for (int a = 0; a < p.dim; ++a) {
         const int N = p.N[a];
-        std::vector<double2> tw(std::max(1, N / 2)), is(N);
-        std::vector<double> ks(N);
-        for (int j = 0; j < N / 2; ++j) {
-            const double ang = -2.0 * M_PI * double(j) / double(N);
-            tw[j] = make_double2(std::cos(ang), std::sin(ang));
-        }
-        // Symbol of the collocation circulant; even-degree splines (orders
-        // 3, 5) make it vanish at the Nyquist mode, where the reference's
-        // LSMR from a zero start returns the minimum-norm solution, i.e.
-        // that mode is dropped (pseudo-inverse).
-        std::vector<double2> lam(N);
-        double lmax = 0;
+        lam[a].resize(N);
+        ks[a].resize(N);
         for (int k = 0; k < N; ++k) {
-            double re = 0, im = 0;
+            cld z(0, 0);
             for (int j = 0; j < p.order; ++j) {
-                const double ang = 2.0 * M_PI * double((long long)j * k % N) / double(N);
-                re += Nb[j] * std::cos(ang);
-                im += Nb[j] * std::sin(ang);
+                const long double ang = two_pi * (long double)((long long)j * k % N) / (long double)N;
+                z += (long double)Nb[j] * cld(cosl(ang), sinl(ang));
             }
-            lam[k] = make_double2(re, im);
-            lmax = std::max(lmax, std::sqrt(re * re + im * im));
+            lam[a][k] = z;
+            const long double kf = (2 * k < N) ? (long double)k : (long double)(N - k);
+            const long double kk = kf * (two_pi / (long double)p.L[a]);
+            ks[a][k] = kk * kk;
         }
-        for (int k = 0; k < N; ++k) {
-            const double re = lam[k].x, im = lam[k].y;
-            const double den = re * re + im * im;
-            is[k] = std::sqrt(den) <= 1e-12 * lmax ? make_double2(0.0, 0.0) : make_double2(re / den, -im / den);
-            const double kf = (2 * k < N) ? double(k) : double(N - k);
-            const double kk = kf * (2 * M_PI * p.Linv[a]);
-            ks[k] = kk * kk;
-        }
-        NUFI_CUDA(h, dalloc(h, &h->plan.tw[a], tw.size()));
-        NUFI_CUDA(h, dalloc(h, &h->plan.isym[a], is.size()));
-        NUFI_CUDA(h, dalloc(h, &h->plan.ksq[a], ks.size()));
-        NUFI_CUDA(h, cudaMemcpy(h->plan.tw[a], tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
-        NUFI_CUDA(h, cudaMemcpy(h->plan.isym[a], is.data(), is.size() * sizeof(double2), cudaMemcpyHostToDevice));
-        NUFI_CUDA(h, cudaMemcpy(h->plan.ksq[a], ks.data(), ks.size() * sizeof(double), cudaMemcpyHostToDevice));
-        h->plan.log2n[a] = ilog2(N);
     }
-    h->plan.smem = smem;
-    NUFI_CUDA(h, field_solve_set_smem(smem));
+    const bool split1d = p.precision == NUFI_PREC_FP32_SPLIT && p.dim == 1;
+    const int nconv = split1d ? 5 : 2;
+    std::vector<cld> D((size_t)nconv * Ns, cld(0, 0));
+    long double lmax = 0;
+    for (long long s = 0; s < Ns; ++s) {
+        long long r = s;
+        cld l(1, 0);
+        for (int a = 0; a < p.dim; ++a) {
+            l *= lam[a][r % p.N[a]];
+            r /= p.N[a];
+        }
+        lmax = std::max(lmax, std::abs(l));
+    }
+    const long double K = -(long double)p.dt * p.dt * p.dxinv[0] * p.dxinv[0];
+    for (long long s = 1; s < Ns; ++s) {
+        long long r = s;
+        long double ksq = 0;
+        cld l(1, 0);
+        int k0 = 0;
+        for (int a = 0; a < p.dim; ++a) {
+            const int k = int(r % p.N[a]);
+            if (a == 0) k0 = k;
+            r /= p.N[a];
+            ksq += ks[a][k];
+            l *= lam[a][k];
+        }
+        const long double dphi = 1.0L / ((long double)Ns * ksq);
+        const cld dc = std::abs(l) <= 1e-12L * lmax ? cld(0, 0) : cld(dphi, 0) / l;
+        D[s] = dc;
+        D[Ns + s] = cld(dphi, 0);
+        if (split1d) {
+            const int N = p.N[0];
+            auto w = [&](int m) {
+                const long double ang = two_pi * (long double)((long long)m * k0 % N) / (long double)N;
+                return cld(cosl(ang), sinl(ang));
+            };
+            D[2 * Ns + s] = (K / 2) * (w(2) - cld(1, 0)) * dc;
+            D[3 * Ns + s] = K * (cld(1, 0) - 2.0L * w(1) + w(2)) * dc;
+            D[4 * Ns + s] = (K / 2) * (cld(-1, 0) + 3.0L * w(1) - 3.0L * w(2) + w(3)) * dc;
+        }
+    }
+    // inverse DFT (sign +, unnormalised), axis by axis, all kernels
+    long long stride = 1;
+    for (int a = 0; a < p.dim; ++a) {
+        const int N = p.N[a];
+        std::vector<cld> tw(N), line(N), out(N);
+        for (int k = 0; k < N; ++k) {
+            const long double ang = two_pi * (long double)k / (long double)N;
+            tw[k] = cld(cosl(ang), sinl(ang));
+        }
+        for (int c = 0; c < nconv; ++c) {
+            cld *base = D.data() + (size_t)c * Ns;
+            for (long long l = 0; l < Ns / N; ++l) {
+                const long long lo = l % stride, hi = l / stride;
+                cld *ptr = base + hi * stride * N + lo;
+                for (int k = 0; k < N; ++k) line[k] = ptr[(long long)k * stride];
+                for (int i = 0; i < N; ++i) {
+                    cld acc(0, 0);
+                    for (int k = 0; k < N; ++k) acc += line[k] * tw[(long long)i * k % N];
+                    out[i] = acc;
+                }
+                for (int i = 0; i < N; ++i) ptr[(long long)i * stride] = out[i];
+            }
+        }
+        stride *= N;
+    }
+    std::vector<double> green((size_t)nconv * Ns);
+    for (size_t i = 0; i < green.size(); ++i) green[i] = double(D[i].real());
+    SolvePlan &pl = h->plan;
+    pl.nconv = nconv;
+    pl.blocks = int(std::max<long long>(1, std::min<long long>((Ns + 7) / 8, sms)));
+    const size_t with_green = size_t(Ns) * 8 * (1 + nconv);
+    pl.green_in_smem = with_green <= 160 * 1024;
+    pl.smem = pl.green_in_smem ? with_green : size_t(Ns) * 8;
+    NUFI_CUDA(h, dalloc(h, &pl.green, green.size()));
+    NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(pl.blocks)));
+    NUFI_CUDA(h, dalloc(h, &pl.energy_counter, 1));
+    NUFI_CUDA(h, cudaMemcpy(pl.green, green.data(), green.size() * sizeof(double), cudaMemcpyHostToDevice));
+    NUFI_CUDA(h, cudaMemset(pl.energy_counter, 0, sizeof(unsigned)));
+    NUFI_CUDA(h, field_solve_prepare(pl));
     h->solve_ok = true;
     return NUFI_OK;
 }
@@ -344,6 +408,7 @@ int check_device_flags(nufi_handle *h)
         if (flags & kErrCellIndex) m += " cell index out of range (non-finite position?)";
         if (flags & kErrKickRange) m += " split-mode kick displacement out of range";
         if (flags & kErrSolveSize) m += " field-solve size";
+        if (flags & kErrStageTimeout) m += " shared-memory staging wait timed out";
         return fail(h, NUFI_ERR_DEVICE, m);
     }
     return NUFI_OK;
@@ -355,18 +420,24 @@ int sync_and_check(nufi_handle *h)
     return check_device_flags(h);
 }
 
-// Enqueue the trace of step n over [qb, qe) into h->partial.
+// Enqueue the trace of step n over [qb, qe) and the reduction into h->rho.
 int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int mode)
 {
     const Problem &p = h->p;
     cudaError_t e;
-    RhoScratch scr{h->partial, h->counter};
+    int rows = 0;
     if (p.precision == NUFI_PREC_FP64)
-        e = launch_trace_fp64(p, h->shape, h->hist, int(n), qb, qe, mode, scr, h->rho, h->err, h->stream);
+        e = launch_trace_fp64(p, h->shape, h->hist, int(n), qb, qe, mode, h->partial, &rows, h->err, h->stream);
+    else if (h->staged.ok)
+        e = launch_trace_split_staged(p, h->staged, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows,
+                                      h->err, h->stream);
     else
-        e = launch_trace_split(p, h->shape, h->tables, h->nodes, h->phase, int(n), qb, qe, scr, h->rho, h->err,
+        e = launch_trace_split(p, h->shape, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows, h->err,
                                h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "trace launch");
+    h->launches += 1;
+    e = launch_reduce_rho(p, rows, h->partial, h->rho, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "reduce launch");
     h->launches += 1;
     return NUFI_OK;
 }
@@ -377,7 +448,7 @@ int enqueue_step(nufi_handle *h, long long n)
     int st = enqueue_trace(h, n, 0, p.Nq, 0);
     if (st) return st;
     cudaError_t e = launch_field_solve(p, h->plan, h->rho, h->hist + n * p.hist_stride,
-                                       h->tables ? h->tables + n * p.table_stride : nullptr, h->energy + n, h->err,
+                                       h->tables ? h->tables + n * p.table_stride : nullptr, h->energy + n,
                                        h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
     h->launches += 1;
@@ -435,6 +506,11 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     h->shape = choose_shape(h->p, sms > 0 ? sms : 1);
     const Problem &p = h->p;
+    if (p.precision == NUFI_PREC_FP32_SPLIT && !p.split_plain_kick) {
+        const char *staged = std::getenv("NUFI_SPLIT_STAGED");
+        if (!(staged && staged[0] == '0')) h->staged = staged_shape_1d(p, sms > 0 ? sms : 1);
+    }
+    const size_t partial_rows = size_t(std::max(h->shape.vblocks, h->staged.ok ? h->staged.ctas : 0));
     auto bail = [&](int code) {
         g_last_error = h->last_error;
         release(h.get());
@@ -444,8 +520,7 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
         return bail(cuda_fail(h.get(), e, "cudaStreamCreate"));
     const size_t nslab = size_t(cfg->Nt + 1);
     if ((e = dalloc(h.get(), &h->hist, nslab * p.hist_stride)) != cudaSuccess ||
-        (e = dalloc(h.get(), &h->partial, size_t(h->shape.vblocks) * p.Ns)) != cudaSuccess ||
-        (e = dalloc(h.get(), &h->counter, size_t((p.Ns + 31) / 32))) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->partial, partial_rows * p.Ns)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->rho, size_t(p.Ns))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->energy, nslab)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->rho_in, size_t(p.Ns))) != cudaSuccess ||
@@ -463,10 +538,9 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     if ((e = cudaMemset(h->hist, 0, nslab * p.hist_stride * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->energy, 0, nslab * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->rho, 0, size_t(p.Ns) * sizeof(double))) != cudaSuccess ||
-        (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMemset(h->counter, 0, size_t((p.Ns + 31) / 32) * sizeof(unsigned))) != cudaSuccess)
+        (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMemset"));
-    if ((st = build_solve_plan(h.get()))) return bail(st);
+    if ((st = build_solve_plan(h.get(), sms > 0 ? sms : 1))) return bail(st);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(cuda_fail(h.get(), e, "nufi_create"));
     *out = h.release();
     return NUFI_OK;
@@ -639,8 +713,7 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
     const Problem &p = h->p;
     DeviceGuard g(h->device);
     NUFI_CUDA(h, cudaMemcpyAsync(h->rho_in, rho, size_t(p.Ns) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    cudaError_t e = launch_field_solve(p, h->plan, h->rho_in, h->slab_out, nullptr, h->energy_tmp, h->err,
-                                       h->stream);
+    cudaError_t e = launch_field_solve(p, h->plan, h->rho_in, h->slab_out, nullptr, h->energy_tmp, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
     h->launches += 1;
     NUFI_CUDA(h, cudaMemcpyAsync(slab_out, h->slab_out, size_t(p.stride_t) * sizeof(double), cudaMemcpyDeviceToHost,
@@ -693,8 +766,8 @@ int nufi_launch_count(const nufi_handle *h, int64_t *count)
 // library's CUDA-graph capture or memory pool, a real-time loop that
 // pre-reserves everything, an embedding that owns the device memory
 // budget).  The caller passes the coefficient history and rho as device
-// buffers; the trace's scratch (per-block partial sums, per-tile arrival
-// counters) lives in the file-scope array below, which every GPU that loads
+// buffers; the trace's scratch (per-block partial sums and an error word)
+// lives in the file-scope array below, which every GPU that loads
 // this library holds until the process exits.
 // ---------------------------------------------------------------------------
 namespace {
@@ -748,11 +821,9 @@ extern "C" int nufi_compute_rho_noalloc(const nufi_config *cfg, int64_t n, const
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     LaunchShape shape = choose_shape(p, sms > 0 ? sms : 1);
-    // Scratch layout: [error word | pad to 256 B][tile counters | pad][partials]
-    const size_t ntiles = size_t((p.Ns + 31) / 32);
-    const size_t off_counter = 256;
-    const size_t off_partial = (off_counter + ntiles * sizeof(unsigned) + 255) / 256 * 256;
-    auto need = [&](const LaunchShape &s) { return off_partial + size_t(s.vblocks) * size_t(p.Ns) * sizeof(double); };
+    // Scratch layout: [error word | pad to 256 B][partial sums]
+    const size_t off_partial = 256;
+    auto need = [&](const LaunchShape &sh) { return off_partial + size_t(sh.vblocks) * size_t(p.Ns) * sizeof(double); };
     if (need(shape) > kNoAllocScratchBytes) {
         // fewest velocity blocks: 4 warps x 4 points per thread
         shape.warps = 4;
@@ -767,12 +838,16 @@ extern "C" int nufi_compute_rho_noalloc(const nufi_config *cfg, int64_t n, const
     unsigned char *base = nullptr;
     if ((st = noalloc_scratch(dev, &base))) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // The previous call's contents stay in the array: the error word and the
-    // tile counters must start at zero.
+    // The previous call's contents stay in the array: the error word must
+    // start at zero (the partial sums are overwritten before they are read).
     if ((e = cudaMemsetAsync(base, 0, off_partial, s)) != cudaSuccess)
         return cuda_fail(nullptr, e, "cudaMemsetAsync(scratch)");
-    RhoScratch scr{reinterpret_cast<double *>(base + off_partial), reinterpret_cast<unsigned *>(base + off_counter)};
-    e = launch_trace_fp64(p, shape, hist, int(n), q_begin, q_end, 0, scr, rho, reinterpret_cast<unsigned *>(base), s);
-    if (e != cudaSuccess) return cuda_fail(nullptr, e, "nufi_compute_rho_noalloc launch");
+    double *partial = reinterpret_cast<double *>(base + off_partial);
+    int rows = 0;
+    e = launch_trace_fp64(p, shape, hist, int(n), q_begin, q_end, 0, partial, &rows,
+                          reinterpret_cast<unsigned *>(base), s);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "nufi_compute_rho_noalloc trace launch");
+    e = launch_reduce_rho(p, rows, partial, rho, s);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "nufi_compute_rho_noalloc reduce launch");
     return NUFI_OK;
 }

@@ -18,6 +18,7 @@ enum : unsigned {
     kErrCellIndex = 1u << 0,   // a located cell fell outside [0, N)
     kErrKickRange = 1u << 1,   // split mode: per-substep kick displacement too large
     kErrSolveSize = 1u << 2,   // field solve: grid larger than its shared-memory plan
+    kErrStageTimeout = 1u << 3, // a bounded wait on a shared-memory staging barrier gave up
 };
 
 // Everything a kernel needs to know about one configuration, by value.

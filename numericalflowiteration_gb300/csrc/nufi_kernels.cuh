@@ -26,14 +26,6 @@ struct SplitNode {
     int S0;         // integer free-streaming shift, reduced mod N
 };
 
-// Scratch of the trace kernels: per-block partial sums and one arrival
-// counter per 32-node spatial tile (zero between launches: the block that
-// completes a tile resets its counter).
-struct RhoScratch {
-    double *partial;     // [vblocks][Ns]
-    unsigned *counter;   // [ceil(Ns / 32)]
-};
-
 __device__ __forceinline__ void neumaier_add(double &sum, double &comp, double x)
 {
     const double t = sum + x;
@@ -41,83 +33,75 @@ __device__ __forceinline__ void neumaier_add(double &sum, double &comp, double x
     sum = t;
 }
 
-// rho[s] = -wv * sum over the velocity nodes of one value per thread.
-// 1. per block, fixed order: lane = spatial node, warps summed in order,
-//    into partial[blockIdx.y][s];
-// 2. the last block to arrive for spatial tile blockIdx.x (ticket counter
-//    after a fence) sums that tile's gridDim.y partials in fixed order,
-//    compensated, and writes rho; so the result does not depend on which
-//    block arrives last, and no atomics touch rho.
-__device__ __forceinline__ void finish_rho(double acc, long long s, long long Ns, double wv, RhoScratch scr,
-                                           double *__restrict__ rho)
+// Trace blocks of (32 lanes = spatial nodes) x W warps: the warps' values
+// are summed in fixed order into partial[blockIdx.y][s]; reduce_rho then
+// sums the rows.  No atomics touch rho, so runs are bitwise reproducible
+// (the reference uses one atomicAdd per point, nufi/cuda_kernel.cu:50).
+__device__ __forceinline__ void write_partial_tiled(double acc, long long s, long long Ns,
+                                                    double *__restrict__ partial)
 {
     __shared__ double red[8][32];
-    __shared__ double red_c[8][32];
-    __shared__ bool last;
-    const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
-    red[warp][lane] = acc;
+    red[threadIdx.y][threadIdx.x] = acc;
     __syncthreads();
-    if (warp == 0 && s < Ns) {
-        double t = red[0][lane];
-        for (int w = 1; w < W; ++w) t += red[w][lane];
-        scr.partial[(long long)blockIdx.y * Ns + s] = t;
-    }
-    __threadfence();
-    __syncthreads();
-    if (lane == 0 && warp == 0) {
-        const unsigned prev = atomicAdd(scr.counter + blockIdx.x, 1u);
-        last = (prev == gridDim.y - 1);
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    const int nb = int(gridDim.y);
-    const int chunk = (nb + W - 1) / W;
-    const int b0 = warp * chunk, b1 = min(nb, b0 + chunk);
-    double sum = 0, comp = 0;
-    if (s < Ns)
-        for (int b = b0; b < b1; ++b) neumaier_add(sum, comp, __ldcg(scr.partial + (long long)b * Ns + s));
-    red[warp][lane] = sum;
-    red_c[warp][lane] = comp;
-    __syncthreads();
-    if (warp == 0) {
-        if (s < Ns) {
-            double t = 0, c = 0;
-            for (int w = 0; w < W; ++w) {
-                neumaier_add(t, c, red[w][lane]);
-                c += red_c[w][lane];
-            }
-            rho[s] = -wv * (t + c);
-        }
-        if (lane == 0) scr.counter[blockIdx.x] = 0u;
+    if (threadIdx.y == 0 && s < Ns) {
+        double t = red[0][threadIdx.x];
+        for (int w = 1; w < int(blockDim.y); ++w) t += red[w][threadIdx.x];
+        partial[(long long)blockIdx.y * Ns + s] = t;
     }
 }
 
+// The trace kernels write per-block partial sums of f~ ([rows][Ns]); the
+// launchers return the row count through *rows.
 cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
-                              long long qe, int mode, RhoScratch scr, double *rho, unsigned *err, cudaStream_t st);
+                              long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st);
 bool fp64_order_supported(int dim, int order);
 
 cudaError_t launch_trace_split(const Problem &p, const LaunchShape &ls, const float *tables, const SplitNode *nodes,
-                               const float2 *phase, int n, long long qb, long long qe, RhoScratch scr, double *rho,
+                               const float2 *phase, int n, long long qb, long long qe, double *partial, int *rows,
                                unsigned *err, cudaStream_t st);
 bool split_supported(int dim, int order, int f0_kind);
 
-
-// Field-solve resources (twiddles and inverse symbols per axis).
-struct SolvePlan {
-    double2 *tw[3] = {nullptr, nullptr, nullptr};      // exp(-2 pi i j / N), j < N/2
-    double2 *isym[3] = {nullptr, nullptr, nullptr};    // 1 / lambda_a(k)
-    double *ksq[3] = {nullptr, nullptr, nullptr};      // (2 pi kfold / L)^2
-    int log2n[3] = {0, 0, 0};
+// Staged FP32-split 1D trace (trace_split_staged.cu): persistent grid of
+// `ctas` blocks of `threads` (one spatial node each) with `ppt` velocity
+// chains per thread; tables streamed through shared memory in chunks of
+// `slabs_per_chunk` slabs.
+constexpr int kStagedMaxPPT = 8;
+struct StagedShape {
+    bool ok = false;
+    int ctas = 0, threads = 0, ppt = 0, slabs_per_chunk = 0;
     size_t smem = 0;
 };
+StagedShape staged_shape_1d(const Problem &p, int sms);
+cudaError_t launch_trace_split_staged(const Problem &p, const StagedShape &sh, const float *tables,
+                                      const SplitNode *nodes, const float2 *phase, int n, long long qb, long long qe,
+                                      double *partial, int *rows, unsigned *err, cudaStream_t st);
 
-// One block: FFT of rho, Poisson + spline diagonal, inverse FFT, padded
-// slab n (FP64) + FP32 table n (when table_slab != null), energy n.
+// rho[s] = -wv * sum over the rows of partial[row][s]: one warp per node,
+// lanes take rows in a fixed stride with Neumaier compensation, then a
+// fixed xor-shuffle tree; deterministic.
+cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st);
+
+
+// Field solve as circulant products (field_solve.cu).  green holds
+// nconv kernels of Ns values each: [0] spline coefficients c, [1] Poisson
+// potential phi at the nodes, and for the 1D split table [2..4] the
+// coefficients K A, K B, K C of the per-cell quadratic.
+struct SolvePlan {
+    double *green = nullptr;
+    int nconv = 0;
+    int blocks = 0;              // grid of the solve kernel
+    size_t smem = 0;             // rho' (+ green when staged) in shared memory
+    bool green_in_smem = false;
+    double *energy_partial = nullptr;  // [blocks]
+    unsigned *energy_counter = nullptr;
+};
+
+// Poisson + collocation solve of one step: padded slab n (FP64), the FP32
+// table n (when table_slab != null) and the electric energy W_n.
 cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
-                               float *table_slab, double *energy_out, unsigned *err, cudaStream_t st);
+                               float *table_slab, double *energy_out, cudaStream_t st);
+cudaError_t field_solve_prepare(const SolvePlan &plan);
 // FP32 table of one FP64 slab (after upload_phi).
-cudaError_t field_solve_set_smem(size_t smem);
 cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st);
 
 }  // namespace nufi_gb300

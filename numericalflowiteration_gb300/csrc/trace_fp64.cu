@@ -17,10 +17,10 @@
 // and the shared partial contractions; each component is formed by exactly
 // the operations of its own reference eval<> call.
 //
-// rho is reduced without atomics on rho (the reference uses one atomicAdd
-// per point, nufi/cuda_kernel.cu:50): per thread over its PPT points, then
-// in fixed order per block and across blocks (finish_rho), so repeated runs
-// are bitwise identical.
+// rho is reduced without atomics (the reference uses one atomicAdd per
+// point, nufi/cuda_kernel.cu:50): per thread over its PPT points, in fixed
+// order per block (write_partial_tiled) and across blocks (reduce_rho), so
+// repeated runs are bitwise identical.
 #include "nufi_kernels.cuh"
 
 namespace nufi_gb300 {
@@ -163,7 +163,7 @@ __device__ __forceinline__ double f0_fp64(const Problem &p, const double *x, con
 template <int D, int ORDER, int PPT>
 __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const double *__restrict__ hist, int n,
                                                          long long q_begin, long long q_end, int mode,
-                                                         RhoScratch scr, double *__restrict__ rho, unsigned *err)
+                                                         double *__restrict__ partial, unsigned *err)
 {
     const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
     const long long s = (long long)blockIdx.x * 32 + lane;
@@ -235,31 +235,32 @@ __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const 
     for (int q = 0; q < PPT; ++q)
         if (live[q]) acc += f0_fp64<D>(p, x[q], u[q]);
 
-    finish_rho(acc, s, p.Ns, p.wv, scr, rho);
+    write_partial_tiled(acc, s, p.Ns, partial);
 }
 
 // Launch table: dims x orders x points-per-thread.
 template <int D, int ORDER>
 static cudaError_t launch_fp64_order(const Problem &p, const LaunchShape &ls, const double *hist, int n,
-                                     long long qb, long long qe, int mode, RhoScratch scr, double *rho,
-                                     unsigned *err, cudaStream_t st)
+                                     long long qb, long long qe, int mode, double *partial, unsigned *err,
+                                     cudaStream_t st)
 {
     const dim3 block(32, ls.warps);
     const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(ls.vblocks));
     switch (ls.ppt) {
-    case 1: trace_fp64_kernel<D, ORDER, 1><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, scr, rho, err); break;
-    case 2: trace_fp64_kernel<D, ORDER, 2><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, scr, rho, err); break;
-    case 4: trace_fp64_kernel<D, ORDER, 4><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, scr, rho, err); break;
+    case 1: trace_fp64_kernel<D, ORDER, 1><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
+    case 2: trace_fp64_kernel<D, ORDER, 2><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
+    case 4: trace_fp64_kernel<D, ORDER, 4><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
-                              long long qe, int mode, RhoScratch scr, double *rho, unsigned *err, cudaStream_t st)
+                              long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st)
 {
+    *rows = ls.vblocks;
 #define NUFI_CASE(D, O) \
-    if (p.dim == D && p.order == O) return launch_fp64_order<D, O>(p, ls, hist, n, qb, qe, mode, scr, rho, err, st);
+    if (p.dim == D && p.order == O) return launch_fp64_order<D, O>(p, ls, hist, n, qb, qe, mode, partial, err, st);
     NUFI_CASE(1, 3) NUFI_CASE(1, 4) NUFI_CASE(1, 5) NUFI_CASE(1, 6) NUFI_CASE(1, 7) NUFI_CASE(1, 8)
     NUFI_CASE(2, 3) NUFI_CASE(2, 4) NUFI_CASE(2, 5) NUFI_CASE(2, 6)
     NUFI_CASE(3, 3) NUFI_CASE(3, 4) NUFI_CASE(3, 5)

@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) trace_split_1d_kernel(const Problem p, co
                                                              const SplitNode *__restrict__ nodes,
                                                              const float2 *__restrict__ phase, int n,
                                                              long long q_begin, long long q_end,
-                                                             RhoScratch scr, double *__restrict__ rho, unsigned *err)
+                                                             double *__restrict__ partial, unsigned *err)
 {
     const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
     const long long s = (long long)blockIdx.x * 32 + lane;
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256) trace_split_1d_kernel(const Problem p, co
         const float df = delta_f0_1d(f, nd, __ldg(phase + I[q]), xi[q], dw[q] - dwc[q]);
         acc += double(df) + nd.g;
     }
-    finish_rho(acc, s, p.Ns, p.wv, scr, rho);
+    write_partial_tiled(acc, s, p.Ns, partial);
 }
 
 bool split_supported(int dim, int order, int f0_kind)
@@ -178,15 +178,16 @@ bool split_supported(int dim, int order, int f0_kind)
 }
 
 cudaError_t launch_trace_split(const Problem &p, const LaunchShape &ls, const float *tables, const SplitNode *nodes,
-                               const float2 *phase, int n, long long qb, long long qe, RhoScratch scr, double *rho,
+                               const float2 *phase, int n, long long qb, long long qe, double *partial, int *rows,
                                unsigned *err, cudaStream_t st)
 {
+    *rows = ls.vblocks;
     if (p.dim != 1) return cudaErrorNotSupported;
     const dim3 block(32, ls.warps);
     const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(ls.vblocks));
     const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
 #define NUFI_LAUNCH3(PPT, P2, C) \
-    trace_split_1d_kernel<PPT, P2, C><<<grid, block, 0, st>>>(p, tables, nodes, phase, n, qb, qe, scr, rho, err);
+    trace_split_1d_kernel<PPT, P2, C><<<grid, block, 0, st>>>(p, tables, nodes, phase, n, qb, qe, partial, err);
 #define NUFI_LAUNCH(PPT)                                                  \
     if (p.split_plain_kick) {                                             \
         if (pow2) NUFI_LAUNCH3(PPT, true, false) else NUFI_LAUNCH3(PPT, false, false) \

@@ -169,3 +169,19 @@ def test_split_dropin_matches_fp64(nufi):
         sim.compute_rho(100)
         got = sim.download_rho(np.zeros(cfg.n_spatial))
     assert rel_max(got, g["rho"][list(g["rho_steps"]).index(100)]) <= 1e-6
+
+
+@pytest.mark.parametrize("cfgname", ["two_stream_1d_64x256_T50", "landau_1d_64x256_T30"])
+def test_split_staged_matches_unstaged(nufi, cfgname, monkeypatch):
+    """The shared-memory staged split trace (default) against the plain
+    global-load form of the same arithmetic: only the order of the FP64 rho
+    sums differs."""
+    cfg, g = golden(cfgname)
+    cfg = cfg.replace(precision="fp32split", Nt=min(cfg.Nt, 300))
+    with nufi.Simulation(cfg) as a:
+        ea = a.run()
+    monkeypatch.setenv("NUFI_SPLIT_STAGED", "0")
+    with nufi.Simulation(cfg) as b:
+        eb = b.run()
+    assert rel_max(ea, eb) <= 1e-9
+    assert rel_max(ea, g["energy"][:cfg.Nt + 1]) <= 1e-6

@@ -47,7 +47,8 @@ __global__ void reduce_rho_kernel(const Problem p, int rows, const double *__res
 
 cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st)
 {
-    const int warps_per_block = 4;
+    // one warp per block: the FP64 work of the few nodes spreads over all SMs
+    const int warps_per_block = 1;
     const int blocks = int((p.Ns + warps_per_block - 1) / warps_per_block);
     reduce_rho_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(p, rows, partial, rho);
     return cudaGetLastError();
@@ -74,17 +75,20 @@ __device__ __forceinline__ double block_sum_fixed(double v, double *red)
 
 }  // namespace
 
-// One warp per node i (nodes strided over all warps of the grid):
+// Each block owns `nodes_per_block` nodes; each node's sum over j is split
+// across wpn = 8 / nodes_per_block warps (warp w of a node takes the j-range
+// quarter w), the warps' sums combined in fixed order:
 //   acc[c] = sum_j green[c][(i - j) mod N] * rho'[j]      (mod per axis)
 // then the slab (all padded positions of i), the table, and rho'_i phi_i.
 template <int NCONV>
 __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     const Problem p, const double *__restrict__ rho, const double *__restrict__ green, int green_in_smem,
-    double *__restrict__ slab, float *__restrict__ table, double *__restrict__ energy_partial,
+    int nodes_per_block, double *__restrict__ slab, float *__restrict__ table, double *__restrict__ energy_partial,
     unsigned *__restrict__ energy_counter, double *__restrict__ energy_out)
 {
     extern __shared__ double sm[];
     __shared__ double red[kSolveThreads];
+    __shared__ double wacc[kSolveWarps][NCONV];
     __shared__ bool last;
     const int Ns = int(p.Ns);
     const int N0 = p.N[0], N1 = p.N[1], N2 = p.N[2];
@@ -103,18 +107,22 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     for (int j = threadIdx.x; j < Ns; j += blockDim.x) rs[j] -= mean;
     __syncthreads();
 
-    // 2. circulant products, one warp per node
+    // 2. circulant products
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int total_warps = gridDim.x * kSolveWarps;
-    const int step0 = 32 % N0, step1 = (32 / N0) % N1, step2 = 32 / (N0 * N1);
-    double e_local = 0;
-    for (int i = blockIdx.x * kSolveWarps + warp; i < Ns; i += total_warps) {
-        const int i0 = i % N0, i1 = (i / N0) % N1, i2 = i / (N0 * N1);
-        double acc[NCONV];
+    const int wpn = kSolveWarps / nodes_per_block;  // warps per node
+    const int slot = warp / wpn, part_w = warp % wpn;
+    const int i = blockIdx.x * nodes_per_block + slot;
+    const int jlen = (Ns + wpn - 1) / wpn;
+    const int jbeg = part_w * jlen, jend = min(Ns, jbeg + jlen);
+    double acc[NCONV];
 #pragma unroll
-        for (int c = 0; c < NCONV; ++c) acc[c] = 0;
-        int j0 = lane % N0, j1 = (lane / N0) % N1, j2 = lane / (N0 * N1);
-        for (int j = lane; j < Ns; j += 32) {
+    for (int c = 0; c < NCONV; ++c) acc[c] = 0;
+    if (i < Ns) {
+        const int i0 = i % N0, i1 = (i / N0) % N1, i2 = i / (N0 * N1);
+        const int step0 = 32 % N0, step1 = (32 / N0) % N1, step2 = 32 / (N0 * N1);
+        int j = jbeg + lane;
+        int j0 = j % N0, j1 = (j / N0) % N1, j2 = j / (N0 * N1);
+        for (; j < jend; j += 32) {
             int m0 = i0 - j0, m1 = i1 - j1, m2 = i2 - j2;
             m0 += m0 < 0 ? N0 : 0;
             m1 += m1 < 0 ? N1 : 0;
@@ -130,34 +138,45 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
             if (j0 >= N0) { j0 -= N0; ++j1; }
             if (j1 >= N1) { j1 -= N1; ++j2; }
         }
+    }
 #pragma unroll
-        for (int c = 0; c < NCONV; ++c)
-            for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
-        if (lane == 0) {
-            const double cval = acc[0];
-            // every padded position of node i: i_a and i_a + N_a while < P_a
-            for (int dz = 0; dz < 2; ++dz) {
-                const int k = i2 + dz * N2;
-                if (k >= p.P[2]) continue;
-                for (int dy = 0; dy < 2; ++dy) {
-                    const int jj = i1 + dy * N1;
-                    if (jj >= p.P[1]) continue;
-                    for (int dx = 0; dx < 2; ++dx) {
-                        const int ii = i0 + dx * N0;
-                        if (ii >= p.P[0]) continue;
-                        const int idx = (k * p.P[1] + jj) * p.P[0] + ii;
-                        slab[idx] = cval;
-                        if (table && p.dim > 1) table[idx] = float(cval);
-                    }
+    for (int c = 0; c < NCONV; ++c)
+        for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < NCONV; ++c) wacc[warp][c] = acc[c];
+    __syncthreads();
+    double e_local = 0;
+    if (part_w == 0 && lane == 0 && i < Ns) {
+        double a[NCONV];
+#pragma unroll
+        for (int c = 0; c < NCONV; ++c) {
+            a[c] = wacc[warp][c];
+            for (int w = 1; w < wpn; ++w) a[c] += wacc[warp + w][c];
+        }
+        const int i0 = i % N0, i1 = (i / N0) % N1, i2 = i / (N0 * N1);
+        const double cval = a[0];
+        // every padded position of node i: i_a and i_a + N_a while < P_a
+        for (int dz = 0; dz < 2; ++dz) {
+            const int k = i2 + dz * N2;
+            if (k >= p.P[2]) continue;
+            for (int dy = 0; dy < 2; ++dy) {
+                const int jj = i1 + dy * N1;
+                if (jj >= p.P[1]) continue;
+                for (int dx = 0; dx < 2; ++dx) {
+                    const int ii = i0 + dx * N0;
+                    if (ii >= p.P[0]) continue;
+                    const int idx = (k * p.P[1] + jj) * p.P[0] + ii;
+                    slab[idx] = cval;
+                    if (table && p.dim > 1) table[idx] = float(cval);
                 }
             }
-            if constexpr (NCONV == 5) {
-                if (table)
-                    reinterpret_cast<float4 *>(table)[i] =
-                        make_float4(float(acc[2]), float(acc[3]), float(acc[4]), 0.0f);
-            }
-            e_local += rs[i] * acc[1];
         }
+        if constexpr (NCONV == 5) {
+            if (table)
+                reinterpret_cast<float4 *>(table)[i] = make_float4(float(a[2]), float(a[3]), float(a[4]), 0.0f);
+        }
+        e_local = rs[i] * a[1];
     }
     // 3. energy: block partial (fixed order), the last block sums the blocks
     const double eb = block_sum_fixed(e_local, red);
@@ -193,12 +212,12 @@ cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const do
 {
     if (plan.nconv == 5)
         circulant_solve_kernel<5><<<plan.blocks, kSolveThreads, plan.smem, st>>>(
-            p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
-            energy_out);
+            p, rho, plan.green, plan.green_in_smem, plan.nodes_per_block, hist_slab, table_slab, plan.energy_partial,
+            plan.energy_counter, energy_out);
     else
         circulant_solve_kernel<2><<<plan.blocks, kSolveThreads, plan.smem, st>>>(
-            p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
-            energy_out);
+            p, rho, plan.green, plan.green_in_smem, plan.nodes_per_block, hist_slab, table_slab, plan.energy_partial,
+            plan.energy_counter, energy_out);
     return cudaGetLastError();
 }
 

@@ -57,6 +57,7 @@ struct nufi_handle {
     std::string solve_why;
     LaunchShape shape;
     StagedShape staged;
+    PersistentRun persist;
     std::string last_error;
     long long launches = 0;
     std::map<std::pair<long long, long long>, std::pair<cudaGraphExec_t, long long>> graphs;
@@ -334,12 +335,17 @@ int build_solve_plan(nufi_handle *h, int sms)
     for (size_t i = 0; i < green.size(); ++i) green[i] = double(D[i].real());
     SolvePlan &pl = h->plan;
     pl.nconv = nconv;
-    pl.blocks = int(std::max<long long>(1, std::min<long long>((Ns + 7) / 8, sms)));
+    // nodes per block: enough blocks to cover the SMs, up to 8 warps per node
+    int npb = 8;
+    while (npb > 1 && (Ns + npb - 1) / npb < sms) npb /= 2;
+    pl.nodes_per_block = npb;
+    pl.blocks = int((Ns + npb - 1) / npb);
     const size_t with_green = size_t(Ns) * 8 * (1 + nconv);
     pl.green_in_smem = with_green <= 160 * 1024;
     pl.smem = pl.green_in_smem ? with_green : size_t(Ns) * 8;
     NUFI_CUDA(h, dalloc(h, &pl.green, green.size()));
-    NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(pl.blocks)));
+    // also holds one part per CTA of the persistent run kernel
+    NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(std::max(pl.blocks, sms))));
     NUFI_CUDA(h, dalloc(h, &pl.energy_counter, 1));
     NUFI_CUDA(h, cudaMemcpy(pl.green, green.data(), green.size() * sizeof(double), cudaMemcpyHostToDevice));
     NUFI_CUDA(h, cudaMemset(pl.energy_counter, 0, sizeof(unsigned)));
@@ -541,6 +547,14 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
         (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMemset"));
     if ((st = build_solve_plan(h.get(), sms > 0 ? sms : 1))) return bail(st);
+    if (h->solve_ok && h->staged.ok) {
+        const char *pers = std::getenv("NUFI_PERSISTENT");
+        if (!(pers && pers[0] == '0')) {
+            h->persist = persistent_shape_1d(p, h->staged, h->plan, sms > 0 ? sms : 1);
+            if (h->persist.ok && (e = dalloc(h.get(), &h->persist.sync, 2)) != cudaSuccess)
+                return bail(cuda_fail(h.get(), e, "cudaMalloc"));
+        }
+    }
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(cuda_fail(h.get(), e, "nufi_create"));
     *out = h.release();
     return NUFI_OK;
@@ -651,6 +665,25 @@ int nufi_run(nufi_handle *h, int64_t n0, int64_t n1, double *energy_hist)
     if (n0 < 0 || n1 < n0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step range outside [0, Nt]");
     if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
     DeviceGuard g(h->device);
+    if (h->persist.ok) {
+        // one cooperative launch for all steps (run_split_1d.cu)
+        const Problem &p = h->p;
+        cudaError_t e = launch_run_split_1d(p, h->persist, h->plan, h->tables, h->hist, h->nodes, h->phase, h->partial,
+                                            h->rho, h->energy, int(n0), int(n1), h->err, h->stream);
+        if (e == cudaSuccess) {
+            h->launches += 1;
+            if (energy_hist) {
+                NUFI_CUDA(h, cudaMemcpyAsync(energy_hist, h->energy + n0, size_t(n1 - n0 + 1) * sizeof(double),
+                                             cudaMemcpyDeviceToHost, h->stream));
+                return sync_and_check(h);
+            }
+            return NUFI_OK;
+        }
+        if (e != cudaErrorCooperativeLaunchTooLarge && e != cudaErrorNotSupported)
+            return cuda_fail(h, e, "persistent run launch");
+        cudaGetLastError();
+        h->persist.ok = false;  // fall back to the graph of per-step launches
+    }
     const auto key = std::make_pair((long long)n0, (long long)n1);
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {

@@ -19,6 +19,7 @@ enum : unsigned {
     kErrKickRange = 1u << 1,   // split mode: per-substep kick displacement too large
     kErrSolveSize = 1u << 2,   // field solve: grid larger than its shared-memory plan
     kErrStageTimeout = 1u << 3, // a bounded wait on a shared-memory staging barrier gave up
+    kErrBarrierTimeout = 1u << 4, // a bounded wait on the persistent kernel's grid barrier gave up
 };
 
 // Everything a kernel needs to know about one configuration, by value.

@@ -69,12 +69,23 @@ constexpr int kStagedMaxPPT = 8;
 struct StagedShape {
     bool ok = false;
     int ctas = 0, threads = 0, ppt = 0, slabs_per_chunk = 0;
+    int tpn = 1;  // threads per spatial node (chain groups)
     size_t smem = 0;
 };
 StagedShape staged_shape_1d(const Problem &p, int sms);
 cudaError_t launch_trace_split_staged(const Problem &p, const StagedShape &sh, const float *tables,
                                       const SplitNode *nodes, const float2 *phase, int n, long long qb, long long qe,
                                       double *partial, int *rows, unsigned *err, cudaStream_t st);
+
+// Whole FP32-split 1D simulation in one cooperative launch
+// (run_split_1d.cu): staged trace, rho, circulant solve and W_n per step,
+// separated by bounded grid barriers.  sync = {barrier count, abort flag}.
+struct PersistentRun {
+    bool ok = false;
+    int ctas = 0, threads = 0, ppt = 0, slabs_per_chunk = 0, tpn = 1;
+    size_t smem = 0;
+    unsigned *sync = nullptr;
+};
 
 // rho[s] = -wv * sum over the rows of partial[row][s]: one warp per node,
 // lanes take rows in a fixed stride with Neumaier compensation, then a
@@ -90,9 +101,10 @@ struct SolvePlan {
     double *green = nullptr;
     int nconv = 0;
     int blocks = 0;              // grid of the solve kernel
+    int nodes_per_block = 8;     // 1, 2, 4 or 8 (8 / warps per node)
     size_t smem = 0;             // rho' (+ green when staged) in shared memory
     bool green_in_smem = false;
-    double *energy_partial = nullptr;  // [blocks]
+    double *energy_partial = nullptr;  // [max(blocks, SMs)]
     unsigned *energy_counter = nullptr;
 };
 
@@ -101,6 +113,11 @@ struct SolvePlan {
 cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
                                float *table_slab, double *energy_out, cudaStream_t st);
 cudaError_t field_solve_prepare(const SolvePlan &plan);
+
+PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const SolvePlan &plan, int sms);
+cudaError_t launch_run_split_1d(const Problem &p, const PersistentRun &pr, const SolvePlan &plan, float *tables,
+                                double *hist, const SplitNode *nodes, const float2 *phase, double *partial,
+                                double *rho, double *energy, int n0, int n1, unsigned *err, cudaStream_t st);
 // FP32 table of one FP64 slab (after upload_phi).
 cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st);
 

@@ -1,0 +1,364 @@
+// run_split_1d.cu — a whole FP32-split 1D simulation (steps n0..n1) in one
+// cooperative launch.
+//
+// The per-step work outside the trace is small (Ns <= 256 nodes) but a
+// chain of dependent phases: partial sums -> rho -> circulant solve ->
+// slab, table and W_n.  As separate launches each phase costs a launch gap
+// and a cold start (about 20 us per step in total, against ~100 us of trace
+// at mid-run).  Here the grid stays resident (one CTA per SM, co-resident
+// by the cooperative launch) and the phases are separated by a bounded grid
+// barrier:
+//   trace    each CTA: its velocity chains through slabs n-1..0, streamed
+//            through the shared-memory ring (as trace_split_staged.cu);
+//            writes partial[cta][s]
+//   barrier
+//   reduce   node s is reduced by CTA s mod G, one warp per node, lanes in
+//            fixed stride with Neumaier compensation, fixed shuffle tree
+//   barrier
+//   solve    every CTA loads rho, removes the mean (fixed order) and
+//            computes its nodes' circulant products c, phi, K(A,B,C) from
+//            the Green's kernels held in shared memory for the whole run;
+//            writes slab n (FP64), table n (float4 per cell) and its part
+//            of sum rho' phi
+//   barrier
+//   energy   CTA 0 sums the parts in CTA order -> W_n
+// The next step's trace reads table n through the async proxy (bulk
+// copies) after the barrier; fence.proxy.async.global orders that read
+// after the generic-proxy writes made visible by the barrier.
+// All arithmetic is that of trace_split_staged.cu and field_solve.cu.
+#include "split_device.cuh"
+
+namespace nufi_gb300 {
+
+using namespace split;
+
+namespace {
+
+// Fixed-order sum over the block of one value per thread (any multiple of
+// 32 threads): shuffle tree per warp, then warp sums in order.
+__device__ __forceinline__ double block_sum(double v, double *red)
+{
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) t += red[w];
+    __syncthreads();
+    if (threadIdx.x == 0) red[0] = t;
+    __syncthreads();
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+}  // namespace
+
+template <int PPT, bool POW2>
+__global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
+    const Problem p, float *__restrict__ tables, double *__restrict__ hist, const SplitNode *__restrict__ nodes,
+    const float2 *__restrict__ phase, const double *__restrict__ green, double *__restrict__ partial,
+    double *__restrict__ rho, double *__restrict__ energy, double *__restrict__ epart, int n0, int n1, int S, int Nr,
+    unsigned *sync, unsigned *err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long full_bar[kRing];
+    __shared__ double red[32];
+    __shared__ double wacc[16][5];
+    __shared__ double combine[256];
+
+    const int N = p.N[0];
+    const int G = gridDim.x;
+    const int W = blockDim.x >> 5;
+    const int s = threadIdx.x % Nr;    // spatial node of this thread
+    const int grp = threadIdx.x / Nr;  // its chain group
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float4 *ring = reinterpret_cast<float4 *>(smem_raw);
+    double *rs = reinterpret_cast<double *>(smem_raw + size_t(kRing) * S * N * sizeof(float4));  // rho' [N]
+    double *gs = rs + N;                                                                       // green [5][N]
+    unsigned *count = sync, *abort = sync + 1;
+
+    const long long m0 = (long long)blockIdx.x * p.Nm / G;
+    const long long m1 = (long long)(blockIdx.x + 1) * p.Nm / G;
+    int S0m[PPT];
+    float shi[PPT], slo[PPT];
+    bool live[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        const long long m = m0 + grp * PPT + q;
+        live[q] = (s < N) && (m < m1);
+        const SplitNode nd = nodes[m < m1 ? m : m0];
+        S0m[q] = nd.S0 + kMagicBits;
+        shi[q] = nd.sig_hi;
+        slo[q] = nd.sig_lo;
+    }
+    for (int j = threadIdx.x; j < 5 * N; j += blockDim.x) gs[j] = green[j];
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < kRing; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    const F0 f = make_f0(p);
+    const unsigned slab_bytes = unsigned(p.table_stride) * 4u;
+    unsigned uses[kRing] = {0, 0, 0};
+    unsigned target = 0;
+    // nodes of this CTA in the reduce and solve phases: blockIdx.x + k*G
+    const int K = blockIdx.x < N ? (N - 1 - int(blockIdx.x)) / G + 1 : 0;
+    int Kp = 1;
+    while (Kp < K) Kp <<= 1;
+    const int wpn = K > 0 ? W / Kp : W;  // warps per node in the solve
+    const double Lfac = p.L[0] / (2.0 * double(N));
+
+    // Chunk j of step n holds slabs [k_lo, k_hi], k_hi = n-1-j*S, in ring
+    // slot j % kRing.  Chunk 0 contains slab n-1, written by the solve of
+    // the previous step; its older slabs and chunks 1..kRing-1 are fetched
+    // ahead (prefetch), before the barriers of the previous step.
+    auto chunk_range = [&](int n, int j, int &k_lo, int &k_hi) {
+        k_hi = n - 1 - j * S;
+        k_lo = max(0, k_hi - S + 1);
+    };
+    auto issue_part = [&](int n, int j, int k_from, int k_to) {  // slabs k_from..k_to of chunk j
+        int k_lo, k_hi;
+        chunk_range(n, j, k_lo, k_hi);
+        const unsigned bar = smem_addr(&full_bar[j % kRing]);
+        bulk_g2s(smem_addr(ring + (j % kRing) * S * N + (k_from - k_lo) * N), tables + (long long)k_from * p.table_stride,
+                 unsigned(k_to - k_from + 1) * slab_bytes, bar);
+    };
+    auto expect_chunk = [&](int n, int j) {
+        int k_lo, k_hi;
+        chunk_range(n, j, k_lo, k_hi);
+        mbar_expect_tx(smem_addr(&full_bar[j % kRing]), unsigned(k_hi - k_lo + 1) * slab_bytes);
+    };
+    // for step n: everything but slab n-1 of chunk 0 (thread 0 only)
+    auto prefetch = [&](int n) {
+        const int nchunks = (n + S - 1) / S;
+        for (int j = 0; j < kRing && j < nchunks; ++j) {
+            expect_chunk(n, j);
+            int k_lo, k_hi;
+            chunk_range(n, j, k_lo, k_hi);
+            if (j == 0) {
+                if (k_hi - 1 >= k_lo) issue_part(n, 0, k_lo, k_hi - 1);
+            } else {
+                issue_part(n, j, k_lo, k_hi);
+            }
+        }
+    };
+    bool prefetched = false;
+    // Grid barrier; if it gives up, first complete and drain any copies
+    // still in flight into this block's shared memory, then leave.
+    auto barrier = [&](int n) -> bool {
+        if (grid_barrier(count, target, abort, err)) return true;
+        if (prefetched && threadIdx.x == 0) {
+            issue_part(n + 1, 0, n, n);
+            const int nch = (n + 1 + S - 1) / S;
+            for (int j = 0; j < kRing && j < nch; ++j) mbar_wait(smem_addr(&full_bar[j % kRing]), uses[j % kRing] & 1u);
+        }
+        return false;
+    };
+
+    for (int n = n0; n <= n1; ++n) {
+        // ---------------- trace of step n ----------------
+        int I[PPT];
+        float xi[PPT], dwT[PPT], dwTc[PPT];
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            I[q] = s < N ? s : 0;
+            xi[q] = 0.0f;
+            dwT[q] = slo[q];
+            dwTc[q] = 0.0f;
+        }
+        if (n > 0) {
+            const int nchunks = (n + S - 1) / S;
+            if (threadIdx.x == 0) {
+                fence_proxy_async_global();
+                if (!prefetched) prefetch(n);
+                issue_part(n, 0, n - 1, n - 1);  // the newest slab
+            }
+            bool ok = true;
+            for (int j = 0; j < nchunks; ++j) {
+                const int slot = j % kRing;
+                ok &= mbar_wait(smem_addr(&full_bar[slot]), uses[slot] & 1u);
+                const float4 *__restrict__ chunk = ring + slot * S * N;
+                int k_lo, k_hi;
+                chunk_range(n, j, k_lo, k_hi);
+                trace_chunk<PPT, POW2>(chunk, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err);
+                __syncthreads();  // everyone is done with this slot
+                ++uses[slot];
+                if (threadIdx.x == 0 && j + kRing < nchunks) {
+                    expect_chunk(n, j + kRing);
+                    int lo, hi;
+                    chunk_range(n, j + kRing, lo, hi);
+                    issue_part(n, j + kRing, lo, hi);
+                }
+            }
+            if (!ok) atomicOr(err, kErrStageTimeout);
+        }
+        // the next step's older slabs load during this step's barriers
+        prefetched = false;
+        if (n + 1 <= n1 && n + 1 > 0) {
+            if (threadIdx.x == 0) prefetch(n + 1);
+            prefetched = true;
+        }
+        double acc = 0;
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            if (!live[q]) continue;
+            const SplitNode nd = nodes[m0 + grp * PPT + q];
+            acc += double(delta_f0(f, nd, __ldg(phase + I[q]), xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
+        }
+        if (blockDim.x > unsigned(Nr)) {
+            if (grp == 1) combine[s] = acc;
+            __syncthreads();
+            if (grp == 0) acc += combine[s];
+        }
+        if (grp == 0 && s < N) partial[(long long)blockIdx.x * N + s] = acc;
+        if (!barrier(n)) return;
+
+        // ---------------- rho: node blockIdx.x + warp*G ----------------
+        if (warp < K) {
+            const int node = int(blockIdx.x) + warp * G;
+            double sum = 0, comp = 0;
+            for (int r = lane; r < G; r += 32) neumaier_add(sum, comp, __ldcg(partial + (long long)r * N + node));
+            for (int off = 16; off > 0; off >>= 1) {
+                const double os = __shfl_down_sync(0xffffffffu, sum, off);
+                const double oc = __shfl_down_sync(0xffffffffu, comp, off);
+                neumaier_add(sum, comp, os);
+                comp += oc;
+            }
+            if (lane == 0) rho[node] = -p.wv * (sum + comp);
+        }
+        if (!barrier(n)) return;
+
+        // ---------------- field solve ----------------
+        double part = 0;
+        for (int j = threadIdx.x; j < N; j += blockDim.x) {
+            const double r = __ldcg(rho + j);
+            rs[j] = r;
+            part += r;
+        }
+        const double mean = block_sum(part, red) / double(N);
+        for (int j = threadIdx.x; j < N; j += blockDim.x) rs[j] -= mean;
+        __syncthreads();
+        const int slotn = warp / wpn, pw = warp % wpn;
+        double a[5] = {0, 0, 0, 0, 0};
+        if (slotn < K) {
+            const int node = int(blockIdx.x) + slotn * G;
+            const int jlen = (N + wpn - 1) / wpn;
+            const int jb = pw * jlen, je = min(N, jb + jlen);
+            for (int j = jb + lane; j < je; j += 32) {
+                int m = node - j;
+                m += m < 0 ? N : 0;
+                const double r = rs[j];
+#pragma unroll
+                for (int c = 0; c < 5; ++c) a[c] = fma(gs[c * N + m], r, a[c]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 5; ++c)
+            for (int off = 16; off > 0; off >>= 1) a[c] += __shfl_down_sync(0xffffffffu, a[c], off);
+        if (lane == 0)
+#pragma unroll
+            for (int c = 0; c < 5; ++c) wacc[warp][c] = a[c];
+        __syncthreads();
+        double e_local = 0;
+        if (lane == 0 && pw == 0 && slotn < K) {
+            const int node = int(blockIdx.x) + slotn * G;
+            double v[5];
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+                v[c] = wacc[warp][c];
+                for (int w = 1; w < wpn; ++w) v[c] += wacc[warp + w][c];
+            }
+            double *slab = hist + (long long)n * p.hist_stride;
+            slab[node] = v[0];
+            if (node + N < p.P[0]) slab[node + N] = v[0];
+            reinterpret_cast<float4 *>(tables + (long long)n * p.table_stride)[node] =
+                make_float4(float(v[2]), float(v[3]), float(v[4]), 0.0f);
+            e_local = rs[node] * v[1];
+        }
+        const double eb = block_sum(e_local, red);
+        if (threadIdx.x == 0) epart[blockIdx.x] = eb;
+        if (!barrier(n)) return;
+
+        // ---------------- W_n ----------------
+        if (blockIdx.x == 0) {
+            double v = 0;
+            for (int b = threadIdx.x; b < G; b += blockDim.x) v += __ldcg(epart + b);
+            const double tot = block_sum(v, red);
+            if (threadIdx.x == 0) energy[n] = tot * Lfac;
+        }
+    }
+    // no bulk copy may be in flight when the block exits
+    if (prefetched) {
+        bool ok = true;
+        for (int r = 0; r < kRing; ++r) ok &= mbar_wait(smem_addr(&full_bar[r]), uses[r] & 1u);
+        if (!ok) atomicOr(err, kErrStageTimeout);
+    }
+}
+
+namespace {
+
+template <int PPT>
+cudaError_t launch_run_ppt(const Problem &p, const PersistentRun &pr, const SolvePlan &plan, float *tables,
+                           double *hist, const SplitNode *nodes, const float2 *phase, double *partial, double *rho,
+                           double *energy, int n0, int n1, unsigned *err, cudaStream_t st)
+{
+    const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
+    void (*fn)(const Problem, float *, double *, const SplitNode *, const float2 *, const double *, double *,
+               double *, double *, double *, int, int, int, int, unsigned *, unsigned *) =
+        pow2 ? run_split_1d_kernel<PPT, true> : run_split_1d_kernel<PPT, false>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(pr.smem));
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(pr.ctas);
+    cfg.blockDim = dim3(pr.threads);
+    cfg.dynamicSmemBytes = pr.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaMemsetAsync(pr.sync, 0, 2 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernelEx(&cfg, fn, p, tables, hist, nodes, phase, (const double *)plan.green, partial, rho,
+                              energy, plan.energy_partial, n0, n1, pr.slabs_per_chunk, pr.threads / pr.tpn, pr.sync,
+                              err);
+}
+
+}  // namespace
+
+PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const SolvePlan &plan, int sms)
+{
+    PersistentRun pr;
+    if (!sh.ok || p.dim != 1 || plan.nconv != 5 || sh.threads > 512 || sh.threads < 32) return pr;
+    const int W = sh.threads / 32;
+    const int K = (p.N[0] + sh.ctas - 1) / sh.ctas;  // nodes per CTA in reduce/solve
+    if (K > W || sh.ctas > sms) return pr;
+    pr.ctas = sh.ctas;
+    pr.threads = sh.threads;
+    pr.tpn = sh.tpn;
+    pr.ppt = sh.ppt;
+    pr.slabs_per_chunk = sh.slabs_per_chunk;
+    const size_t ring = size_t(kRing) * sh.slabs_per_chunk * p.N[0] * sizeof(float4);
+    pr.smem = std::max(ring + size_t(6) * p.N[0] * sizeof(double), sh.smem);
+    if (pr.smem > 220 * 1024) return pr;
+    pr.ok = true;
+    return pr;
+}
+
+cudaError_t launch_run_split_1d(const Problem &p, const PersistentRun &pr, const SolvePlan &plan, float *tables,
+                                double *hist, const SplitNode *nodes, const float2 *phase, double *partial,
+                                double *rho, double *energy, int n0, int n1, unsigned *err, cudaStream_t st)
+{
+    switch (pr.ppt) {
+#define NUFI_CASE(K) \
+    case K: return launch_run_ppt<K>(p, pr, plan, tables, hist, nodes, phase, partial, rho, energy, n0, n1, err, st);
+        NUFI_CASE(1) NUFI_CASE(2) NUFI_CASE(3) NUFI_CASE(4) NUFI_CASE(5) NUFI_CASE(6) NUFI_CASE(7) NUFI_CASE(8)
+#undef NUFI_CASE
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace nufi_gb300

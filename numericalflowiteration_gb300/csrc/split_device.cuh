@@ -1,0 +1,236 @@
+// split_device.cuh — device pieces shared by the FP32-split kernels:
+// shared-memory staging (mbarrier + cp.async.bulk), a bounded grid
+// barrier for the persistent kernel, and the split-form drift / kick / f0.
+#pragma once
+
+#include "nufi_kernels.cuh"
+
+namespace nufi_gb300 {
+namespace split {
+
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+constexpr int kRing = 3;
+constexpr unsigned kWaitLimit = 1u << 22;      // polls of an mbarrier
+constexpr unsigned kBarrierLimit = 1u << 26;   // polls of the grid barrier
+
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait; false on timeout.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    for (unsigned it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned)
+// from global memory into this CTA's shared memory, completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+// Orders this thread's earlier (generic-proxy) view of global memory before
+// its later bulk copies (async proxy) read it.
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier of a cooperative launch: every block adds 1 to *count
+// (monotonic over the launch), then waits until it reaches `target`
+// (incremented by gridDim.x per barrier).  The wait is bounded; on timeout
+// or when another block has already given up (*abort != 0) it raises
+// kErrBarrierTimeout, sets *abort and returns false, and the caller leaves
+// the kernel (no hang).
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned &target, unsigned *abort, unsigned *err)
+{
+    __shared__ int ok;
+    __syncthreads();
+    target += gridDim.x;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        int good = 1;
+        for (unsigned it = 0; ld_acquire_gpu(count) < target; ++it) {
+            if (it > kBarrierLimit || ld_acquire_gpu(abort) != 0u) {
+                good = 0;
+                break;
+            }
+        }
+        if (!good) {
+            atomicOr(err, kErrBarrierTimeout);
+            atomicExch(abort, 1u);
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <bool POW2>
+__device__ __forceinline__ void drift(int &I, float &xi, float dw, float dwc, float shi, float slo, int S0, int N,
+                                      unsigned *err)
+{
+    const float t = (xi - shi) - ((slo - dwc) + dw);
+    const float mg = __fadd_rd(t, kMagic);
+    const int fi = __float_as_int(mg) - kMagicBits;
+    xi = t - (mg - kMagic);
+    int J = I - S0 + fi;
+    if constexpr (POW2) {
+        J &= N - 1;
+    } else {
+        J += (J < 0) ? N : 0;
+        J -= (J >= N) ? N : 0;
+        if ((unsigned)J >= (unsigned)N) {
+            atomicOr(err, kErrKickRange);
+            J = ((J % N) + N) % N;
+        }
+    }
+    I = J;
+}
+
+// dw += k with Kahan compensation (dwc = -(low bits lost so far)).
+__device__ __forceinline__ void kick(float &dw, float &dwc, float k)
+{
+    const float y = k - dwc;
+    const float t = dw + y;
+    dwc = (t - dw) - y;
+    dw = t;
+}
+
+struct F0 {
+    int kind;
+    float alpha, kdx, dx_dt, ub, inv_s2;
+};
+
+__device__ __forceinline__ F0 make_f0(const Problem &p)
+{
+    F0 f;
+    f.kind = p.f0_kind;
+    f.alpha = float(p.f0p[0]);
+    f.kdx = float(p.f0p[1] * p.dx[0]);
+    f.dx_dt = float(p.dx[0] / p.dt);
+    f.ub = float(p.f0p[2]);
+    f.inv_s2 = p.f0_kind == NUFI_F0_BUMP_ON_TAIL ? float(1.0 / (p.f0p[3] * p.f0p[3])) : 0.0f;
+    return f;
+}
+
+// f0(foot) - G(u0) in FP32: f0 = (1 + alpha cos kx) G(u), expm1 form so
+// the rounding is relative to the perturbation (see trace_split.cu).
+__device__ __forceinline__ float delta_f0(const F0 &f, const SplitNode &nd, float2 cs, float xi, float dw)
+{
+    float sp, cp;
+    sincosf(f.kdx * xi, &sp, &cp);
+    const float c = cs.x * cp - cs.y * sp;  // cos(k x_foot)
+    const float du = dw * f.dx_dt;
+    if (f.kind == NUFI_F0_LANDAU) {
+        const float em = expm1f(-(du * (nd.u0f + 0.5f * du)));
+        return nd.ga * (em + f.alpha * c * (1.0f + em));
+    }
+    if (f.kind == NUFI_F0_TWO_STREAM) {
+        const float u = nd.u0f + du;
+        const float em = expm1f(-(du * (nd.u0f + 0.5f * du)));
+        const float diff = nd.ga * (u * u * em + du * (2.0f * nd.u0f + du));
+        return diff + f.alpha * c * (nd.ga * u * u * (1.0f + em));
+    }
+    const float em1 = expm1f(-(du * (nd.u0f + 0.5f * du)));
+    const float em2 = expm1f(-(du * ((nd.u0f - f.ub) + 0.5f * du)) * f.inv_s2);
+    return nd.ga * em1 + nd.gb * em2 + f.alpha * c * (nd.ga * (1.0f + em1) + nd.gb * (1.0f + em2));
+}
+
+}  // namespace split
+}  // namespace nufi_gb300
+
+namespace nufi_gb300 {
+namespace split {
+
+// Substeps k_hi..k_lo (descending) of PPT chains over a chunk of tables in
+// shared memory (slab k at chunk + (k - k_lo) * N, float4 per cell).
+// State per chain: cell I, fraction xi, and the kick sum in two levels:
+// dwT (+ Kahan term dwTc) holds the sum up to the previous chunk and
+// starts at sig_lo, the low part of the free-streaming fraction; dwC sums
+// this chunk's kicks in plain FP32 and is folded into dwT at the end.
+//   drift:  t = ((xi - sig_hi) - dwT) - dwC
+//           floor(t) by a round-down add of 1.5*2^23, whose bit pattern
+//           minus S0m = S0 + bits(1.5*2^23) moves the cell
+//   kick:   dwC += K (A + B xi + C xi^2) of the cell (halved for k = 0)
+// 13 FP32/INT instructions and one 16-byte shared load per substep.
+template <int PPT, bool POW2>
+__device__ __forceinline__ void trace_chunk(const float4 *__restrict__ chunk, int k_hi, int k_lo, int N,
+                                            int (&I)[PPT], float (&xi)[PPT], float (&dwT)[PPT], float (&dwTc)[PPT],
+                                            const float (&shi)[PPT], const int (&S0m)[PPT], unsigned *err)
+{
+    float dwC[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) dwC[q] = 0.0f;
+    auto substep = [&](const float4 *__restrict__ tk, float h) {
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const float t = ((xi[q] - shi[q]) - dwT[q]) - dwC[q];
+            const float mg = __fadd_rd(t, kMagic);
+            int J = I[q] - S0m[q] + __float_as_int(mg);
+            if constexpr (POW2) {
+                J &= N - 1;
+            } else {
+                J += (J < 0) ? N : 0;
+                J -= (J >= N) ? N : 0;
+                if ((unsigned)J >= (unsigned)N) {
+                    atomicOr(err, kErrKickRange);
+                    J = ((J % N) + N) % N;
+                }
+            }
+            I[q] = J;
+            xi[q] = t - (mg - kMagic);
+            const float4 T = tk[J];
+            const float kq = fmaf(xi[q], fmaf(xi[q], T.z, T.y), T.x);
+            dwC[q] = (h == 1.0f) ? dwC[q] + kq : fmaf(h, kq, dwC[q]);
+        }
+    };
+    const int k_stop = max(k_lo, 1);
+    for (int k = k_hi; k >= k_stop; --k) substep(chunk + (k - k_lo) * N, 1.0f);
+    if (k_lo == 0) substep(chunk, 0.5f);
+    // fold this chunk's kicks into the compensated total
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) kick(dwT[q], dwTc[q], dwC[q]);
+}
+
+}  // namespace split
+}  // namespace nufi_gb300

@@ -434,6 +434,9 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
     int rows = 0;
     if (p.precision == NUFI_PREC_FP64)
         e = launch_trace_fp64(p, h->shape, h->hist, int(n), qb, qe, mode, h->partial, &rows, h->err, h->stream);
+    else if (p.dim > 1)
+        e = launch_trace_split_nd(p, h->staged, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows,
+                                  h->err, h->stream);
     else if (h->staged.ok)
         e = launch_trace_split_staged(p, h->staged, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows,
                                       h->err, h->stream);
@@ -512,7 +515,14 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     h->shape = choose_shape(h->p, sms > 0 ? sms : 1);
     const Problem &p = h->p;
-    if (p.precision == NUFI_PREC_FP32_SPLIT && !p.split_plain_kick) {
+    if (p.precision == NUFI_PREC_FP32_SPLIT && p.dim > 1) {
+        h->staged = staged_shape_nd(p, sms > 0 ? sms : 1);
+        const char *staged = std::getenv("NUFI_SPLIT_STAGED");
+        if (staged && staged[0] == '0') {  // tables read from global memory
+            h->staged.ring = 0;
+            h->staged.smem = 0;
+        }
+    } else if (p.precision == NUFI_PREC_FP32_SPLIT && !p.split_plain_kick) {
         const char *staged = std::getenv("NUFI_SPLIT_STAGED");
         if (!(staged && staged[0] == '0')) h->staged = staged_shape_1d(p, sms > 0 ? sms : 1);
     }

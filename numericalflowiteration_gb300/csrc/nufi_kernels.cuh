@@ -70,9 +70,15 @@ struct StagedShape {
     bool ok = false;
     int ctas = 0, threads = 0, ppt = 0, slabs_per_chunk = 0;
     int tpn = 1;  // threads per spatial node (chain groups)
+    int ring = 3;  // shared-memory ring slots (0: 2D/3D tables read from global memory)
     size_t smem = 0;
 };
 StagedShape staged_shape_1d(const Problem &p, int sms);
+// FP32-split 2D/3D trace (trace_split_nd.cu).
+StagedShape staged_shape_nd(const Problem &p, int sms);
+cudaError_t launch_trace_split_nd(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
+                                  const float2 *phase, int n, long long qb, long long qe, double *partial, int *rows,
+                                  unsigned *err, cudaStream_t st);
 cudaError_t launch_trace_split_staged(const Problem &p, const StagedShape &sh, const float *tables,
                                       const SplitNode *nodes, const float2 *phase, int n, long long qb, long long qe,
                                       double *partial, int *rows, unsigned *err, cudaStream_t st);

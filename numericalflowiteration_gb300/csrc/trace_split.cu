@@ -174,7 +174,7 @@ bool split_supported(int dim, int order, int f0_kind)
 {
     if (order != 4) return false;
     if (dim == 1) return f0_kind == NUFI_F0_LANDAU || f0_kind == NUFI_F0_TWO_STREAM || f0_kind == NUFI_F0_BUMP_ON_TAIL;
-    return false;
+    return (dim == 2 || dim == 3) && f0_kind == NUFI_F0_LANDAU;
 }
 
 cudaError_t launch_trace_split(const Problem &p, const LaunchShape &ls, const float *tables, const SplitNode *nodes,

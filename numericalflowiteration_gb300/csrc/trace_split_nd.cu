@@ -1,0 +1,374 @@
+// trace_split_nd.cu — FP32-split trace in 2D2V and 3D3V.
+//
+// Per axis a the state is the 1D split form (split_device.cuh): integer
+// cell I_a, FP32 fraction xi_a in [0, 1), and the kick sum in cells per
+// substep in two levels (plain FP32 within a chunk of slabs, Kahan-
+// compensated across chunks; the sum starts at the low part of the free-
+// streaming fraction).  The field of slab k is its FP32 padded copy (the
+// reference layout, x fastest) written by the field solve.  All components
+// of E come from one gather of the 4^D window, contracted with the cubic
+// B-spline value and derivative bases per axis (the arithmetic of
+// splines2d / splines3d::eval and of the reference's separate eval<1,0> /
+// eval<0,1> calls, nufi/splines.hpp:117-172, nufi/rho.hpp:213-214, 343-345,
+// in FP32):  kick_a = -(dt / dx_a)^2 * dS/dxi_a  (cells per substep).
+// f0 is the Landau form (1 + alpha sum_a cos(k x_a)) prod_a g(u_a)
+// (nufi/config.hpp:148-149, 233-234), evaluated as f0(foot) - G(u0) with
+// expm1; G(u0) is added back in FP64.
+//
+// Geometry: about one CTA per SM; CTA c owns the velocity nodes
+// [c*Nm/G, (c+1)*Nm/G) for every spatial node.  Thread t owns the spatial
+// nodes s = t + T j and visits its items in (j, m) order, PPT at a time
+// (one full trace per batch), so the 32 lanes of a warp hold 32
+// consecutive spatial nodes (x fastest) at one velocity: neighbouring
+// cells, conflict-free shared-memory gathers.  Each thread is the only one
+// in the CTA to touch its nodes, and its items of one node are consecutive,
+// so rho is a register sum flushed to partial[c][s] when j changes (FP64,
+// fixed order: deterministic).
+//
+// Tables: with ring > 0 the history is streamed through `ring` shared-
+// memory slots of S slabs (cp.async.bulk completing on an mbarrier), one
+// chunk stream over all batches so the copies run ahead across batch
+// boundaries; with ring == 0 (slabs too large for shared memory) the
+// gathers read the tables in global memory.  Every mbarrier wait is
+// bounded; a timeout raises kErrStageTimeout (no trap, no hang).
+#include <algorithm>
+
+#include "split_device.cuh"
+
+namespace nufi_gb300 {
+
+using namespace split;
+
+namespace {
+
+// Cubic B-spline basis values N[i] and derivatives D[i] on [0, 1)
+// (splines1d::N<real,4,0> and <real,4,1>, nufi/splines.hpp:39-79).
+__device__ __forceinline__ void cubic_basis(float x, float (&Nv)[4], float (&Dv)[4])
+{
+    const float x2 = x * x, x3 = x2 * x, u = 1.0f - x;
+    constexpr float s6 = 1.0f / 6.0f;
+    Nv[0] = u * u * u * s6;
+    Nv[1] = fmaf(x2, fmaf(3.0f, x, -6.0f), 4.0f) * s6;
+    Nv[3] = x3 * s6;
+    Nv[2] = 1.0f - (Nv[0] + Nv[1] + Nv[3]);
+    Dv[0] = -0.5f * u * u;
+    Dv[1] = x * fmaf(1.5f, x, -2.0f);
+    Dv[3] = 0.5f * x2;
+    Dv[2] = -(Dv[0] + Dv[1] + Dv[3]);
+}
+
+template <int D>
+struct Chain {
+    int I[D], S0m[D];
+    float xi[D], dwT[D], dwTc[D], dwC[D], shi[D];
+};
+
+// Drift of one axis: as the 1D chunk loop (split_device.cuh).
+template <bool POW2>
+__device__ __forceinline__ void drift_axis(int &I, float &xi, float dwT, float dwC, float shi, int S0m, int N,
+                                           unsigned *err)
+{
+    const float t = ((xi - shi) - dwT) - dwC;
+    const float mg = __fadd_rd(t, kMagic);
+    int J = I - S0m + __float_as_int(mg);
+    if constexpr (POW2) {
+        J &= N - 1;
+    } else {
+        J += (J < 0) ? N : 0;
+        J -= (J >= N) ? N : 0;
+        if ((unsigned)J >= (unsigned)N) {
+            atomicOr(err, kErrKickRange);
+            J = ((J % N) + N) % N;
+        }
+    }
+    I = J;
+    xi = t - (mg - kMagic);
+}
+
+// dS/dxi_a of the FP32 slab window at the chain's cells and fractions.
+template <int D>
+__device__ __forceinline__ void field_grad(const float *__restrict__ slab, int sy, int sz, const Chain<D> &c,
+                                           float (&g)[D])
+{
+    float Nx[4], Dx[4], Ny[4], Dy[4];
+    cubic_basis(c.xi[0], Nx, Dx);
+    cubic_basis(c.xi[1], Ny, Dy);
+    if constexpr (D == 2) {
+        const float *w = slab + c.I[1] * sy + c.I[0];
+        float gx = 0.0f, gy = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float r0 = 0.0f, r1 = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float v = w[j * sy + i];
+                r0 = fmaf(v, Nx[i], r0);
+                r1 = fmaf(v, Dx[i], r1);
+            }
+            gx = fmaf(r1, Ny[j], gx);
+            gy = fmaf(r0, Dy[j], gy);
+        }
+        g[0] = gx;
+        g[1] = gy;
+    } else {
+        float Nz[4], Dz[4];
+        cubic_basis(c.xi[2], Nz, Dz);
+        const float *w = slab + c.I[2] * sz + c.I[1] * sy + c.I[0];
+        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float ax = 0.0f, ay = 0.0f, az = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float r0 = 0.0f, r1 = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float v = w[k * sz + j * sy + i];
+                    r0 = fmaf(v, Nx[i], r0);
+                    r1 = fmaf(v, Dx[i], r1);
+                }
+                ax = fmaf(r1, Ny[j], ax);
+                ay = fmaf(r0, Dy[j], ay);
+                az = fmaf(r0, Ny[j], az);
+            }
+            gx = fmaf(ax, Nz[k], gx);
+            gy = fmaf(ay, Nz[k], gy);
+            gz = fmaf(az, Dz[k], gz);
+        }
+        g[0] = gx;
+        g[1] = gy;
+        g[2] = gz;
+    }
+}
+
+}  // namespace
+
+template <int D, int PPT, bool POW2, bool STAGED>
+__global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p, const float *__restrict__ tables,
+                                                                const SplitNode *__restrict__ nodes,
+                                                                const float2 *__restrict__ phase, int n,
+                                                                long long q_begin, long long q_end, int S, int R,
+                                                                double *__restrict__ partial, unsigned *err)
+{
+    extern __shared__ __align__(128) float ring[];
+    __shared__ __align__(8) unsigned long long full_bar[kRing];
+
+    const int T = blockDim.x;
+    const int t = threadIdx.x;
+    const int G = gridDim.x;
+    const long long Ns = p.Ns;
+    const long long m0 = (long long)blockIdx.x * p.Nm / G;
+    const long long Mc = (long long)(blockIdx.x + 1) * p.Nm / G - m0;
+    const long long nj = t < Ns ? (Ns - t + T - 1) / T : 0;  // spatial nodes of this thread
+    const long long nj0 = (Ns + T - 1) / T;                  // ... of thread 0 (the most)
+    const long long batches = (nj0 * Mc + PPT - 1) / PPT;
+    const int sy = p.P[0], sz = p.P[0] * p.P[1];
+    float K[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) K[a] = float(-p.dt * p.dt * p.dxinv[a] * p.dxinv[a]);
+    const long long slab_f = p.table_stride;
+
+    // chunk stream: chunk g covers slabs [k_lo, k_hi] of batch g / nchunks
+    const int nchunks = n > 0 ? (n + S - 1) / S : 0;
+    const long long total_chunks = batches * nchunks;
+    auto chunk_range = [&](long long g, int &k_hi, int &k_lo) {
+        const int j = int(g % nchunks);
+        k_hi = n - 1 - j * S;
+        k_lo = max(0, k_hi - S + 1);
+    };
+    auto issue = [&](long long g) {
+        int k_hi, k_lo;
+        chunk_range(g, k_hi, k_lo);
+        const int slot = int(g % R);
+        const unsigned bar = smem_addr(&full_bar[slot]);
+        const unsigned bytes = unsigned(k_hi - k_lo + 1) * unsigned(slab_f) * 4u;
+        mbar_expect_tx(bar, bytes);
+        bulk_g2s(smem_addr(ring + (long long)slot * S * slab_f), tables + (long long)k_lo * slab_f, bytes, bar);
+    };
+    if constexpr (STAGED) {
+        if (t == 0) {
+            for (int r = 0; r < R; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
+            mbar_fence_init();
+        }
+        __syncthreads();
+        if (t == 0)
+            for (long long g = 0; g < R && g < total_chunks; ++g) issue(g);
+    }
+    bool ok = true;
+    long long g = 0;  // next chunk of the stream
+
+    long long cur_j = 0;
+    double acc = 0;
+    for (long long b = 0; b < batches; ++b) {
+        Chain<D> ch[PPT];
+        bool live[PPT];
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const long long k = b * PPT + q;
+            const long long j = k / Mc;
+            const long long m = m0 + k % Mc;
+            const long long s = t + j * T;
+            const bool inside = j < nj;
+            const long long qq = s * p.Nm + m;
+            live[q] = inside && qq >= q_begin && qq < q_end;
+            long long rs = inside ? s : 0, rm = m;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                const SplitNode nd = nodes[(a > 0 ? p.M[0] : 0) + (a > 1 ? p.M[1] : 0) + int(rm % p.M[a])];
+                ch[q].I[a] = int(rs % p.N[a]);
+                rs /= p.N[a];
+                rm /= p.M[a];
+                ch[q].S0m[a] = nd.S0 + kMagicBits;
+                ch[q].shi[a] = nd.sig_hi;
+                ch[q].xi[a] = 0.0f;
+                ch[q].dwT[a] = nd.sig_lo;
+                ch[q].dwTc[a] = 0.0f;
+                ch[q].dwC[a] = 0.0f;
+            }
+        }
+        auto substep = [&](const float *__restrict__ sl, float h) {
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+#pragma unroll
+                for (int a = 0; a < D; ++a)
+                    drift_axis<POW2>(ch[q].I[a], ch[q].xi[a], ch[q].dwT[a], ch[q].dwC[a], ch[q].shi[a], ch[q].S0m[a],
+                                     p.N[a], err);
+                float gr[D];
+                field_grad<D>(sl, sy, sz, ch[q], gr);
+#pragma unroll
+                for (int a = 0; a < D; ++a) ch[q].dwC[a] = fmaf(h * K[a], gr[a], ch[q].dwC[a]);
+            }
+        };
+        for (int j = 0; j < nchunks; ++j, ++g) {
+            int k_hi, k_lo;
+            chunk_range(g, k_hi, k_lo);
+            const float *__restrict__ base;
+            if constexpr (STAGED) {
+                const int slot = int(g % R);
+                ok &= mbar_wait(smem_addr(&full_bar[slot]), unsigned((g / R) & 1));
+                base = ring + (long long)slot * S * slab_f;
+            } else {
+                base = tables + (long long)k_lo * slab_f;
+            }
+            const int k_stop = max(k_lo, 1);
+            for (int k = k_hi; k >= k_stop; --k) substep(base + (k - k_lo) * slab_f, 1.0f);
+            if (k_lo == 0) substep(base, 0.5f);
+#pragma unroll
+            for (int q = 0; q < PPT; ++q)
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    kick(ch[q].dwT[a], ch[q].dwTc[a], ch[q].dwC[a]);
+                    ch[q].dwC[a] = 0.0f;
+                }
+            if constexpr (STAGED) {
+                __syncthreads();  // everyone is done with this slot
+                if (t == 0 && g + R < total_chunks) issue(g + R);
+            }
+        }
+        // f0(foot) - G(u0) in FP32, the FP64 background G(u0) added back
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const long long k = b * PPT + q;
+            const long long j = k / Mc;
+            if (j != cur_j) {
+                if (cur_j < nj) partial[(long long)blockIdx.x * Ns + t + cur_j * T] = acc;
+                acc = 0;
+                cur_j = j;
+            }
+            if (!live[q]) continue;
+            long long rm = m0 + k % Mc;
+            float delta = 0.0f, csum = 0.0f, Gf = 1.0f;
+            double Gd = 1.0;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                const SplitNode nd = nodes[(a > 0 ? p.M[0] : 0) + (a > 1 ? p.M[1] : 0) + int(rm % p.M[a])];
+                rm /= p.M[a];
+                const float du = ((ch[q].dwT[a] - ch[q].dwTc[a]) - nd.sig_lo) * float(p.dx[a] / p.dt);
+                delta = fmaf(du, nd.u0f + 0.5f * du, delta);
+                const float2 cs = __ldg(phase + (a > 0 ? p.N[0] : 0) + (a > 1 ? p.N[1] : 0) + ch[q].I[a]);
+                float sp, cp;
+                sincosf(float(p.f0p[1] * p.dx[a]) * ch[q].xi[a], &sp, &cp);
+                csum += cs.x * cp - cs.y * sp;
+                Gf *= nd.ga;
+                Gd *= nd.g;
+            }
+            const float em = expm1f(-delta);
+            const float df = Gf * (em + float(p.f0p[0]) * csum * (1.0f + em));
+            acc += double(df) + Gd;
+        }
+    }
+    if (cur_j < nj) partial[(long long)blockIdx.x * Ns + t + cur_j * T] = acc;
+    if (!ok) atomicOr(err, kErrStageTimeout);
+}
+
+namespace {
+
+template <int D, int PPT, bool STAGED>
+cudaError_t launch_nd(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
+                      const float2 *phase, int n, long long qb, long long qe, double *partial, unsigned *err,
+                      cudaStream_t st)
+{
+    bool pow2 = true;
+    for (int a = 0; a < D; ++a) pow2 = pow2 && ((p.N[a] & (p.N[a] - 1)) == 0);
+    void (*fn)(const Problem, const float *, const SplitNode *, const float2 *, int, long long, long long, int, int,
+               double *, unsigned *) =
+        pow2 ? trace_split_nd_kernel<D, PPT, true, STAGED> : trace_split_nd_kernel<D, PPT, false, STAGED>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sh.smem));
+    if (e != cudaSuccess) return e;
+    fn<<<sh.ctas, sh.threads, sh.smem, st>>>(p, tables, nodes, phase, n, qb, qe, sh.slabs_per_chunk,
+                                             STAGED ? sh.ring : 1, partial, err);
+    return cudaGetLastError();
+}
+
+template <int D, int PPT>
+cudaError_t launch_nd_mode(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
+                           const float2 *phase, int n, long long qb, long long qe, double *partial, unsigned *err,
+                           cudaStream_t st)
+{
+    if (sh.ring > 0) return launch_nd<D, PPT, true>(p, sh, tables, nodes, phase, n, qb, qe, partial, err, st);
+    return launch_nd<D, PPT, false>(p, sh, tables, nodes, phase, n, qb, qe, partial, err, st);
+}
+
+}  // namespace
+
+// One CTA per SM (at most Nm), T = min(512, Ns rounded up to a warp)
+// threads; S slabs per ring slot from a 120 KB budget (more than half of
+// an SM's shared memory, so no SM holds two CTAs), 3 slots, or 2 when 3 do
+// not fit in 200 KB, else the tables stay in global memory.
+StagedShape staged_shape_nd(const Problem &p, int sms)
+{
+    StagedShape sh;
+    if (p.dim < 2 || p.order != 4) return sh;
+    const size_t slab_bytes = size_t(p.table_stride) * 4;
+    const size_t kOneCtaPerSm = 120 * 1024, kMaxSmem = 200 * 1024;
+    sh.ctas = int(std::min<long long>(p.Nm, sms));
+    sh.threads = int(std::min<long long>(512, (p.Ns + 31) / 32 * 32));
+    sh.ppt = p.dim == 2 ? 2 : 1;
+    sh.tpn = 1;
+    if (size_t(kRing) * slab_bytes <= kMaxSmem) {
+        sh.ring = kRing;
+        sh.slabs_per_chunk =
+            int(std::max<size_t>(1, std::min<size_t>(16, kOneCtaPerSm / (size_t(kRing) * slab_bytes))));
+    } else if (2 * slab_bytes <= kMaxSmem) {
+        sh.ring = 2;
+        sh.slabs_per_chunk = 1;
+    } else {
+        sh.ring = 0;
+        sh.slabs_per_chunk = 16;
+    }
+    sh.smem = sh.ring > 0 ? std::max(size_t(sh.ring) * sh.slabs_per_chunk * slab_bytes, kOneCtaPerSm) : 0;
+    sh.ok = true;
+    return sh;
+}
+
+cudaError_t launch_trace_split_nd(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
+                                  const float2 *phase, int n, long long qb, long long qe, double *partial, int *rows,
+                                  unsigned *err, cudaStream_t st)
+{
+    *rows = sh.ctas;
+    if (p.dim == 2) return launch_nd_mode<2, 2>(p, sh, tables, nodes, phase, n, qb, qe, partial, err, st);
+    if (p.dim == 3) return launch_nd_mode<3, 1>(p, sh, tables, nodes, phase, n, qb, qe, partial, err, st);
+    return cudaErrorNotSupported;
+}
+
+}  // namespace nufi_gb300

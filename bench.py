@@ -38,6 +38,9 @@ UNIT = "point-steps/s"
 # kick, order 4, all field components from one gather): 1D 30, 2D 136,
 # 3D 460 flop.
 FLOP_PER_POINT_STEP = {1: 30, 2: 136, 3: 460}
+# Shared-memory bytes the FP32-split trace loads per point-step: the 1D
+# per-cell table entry (one float4), the 4x4 / 4x4x4 FP32 slab window.
+SMEM_BYTES_PER_POINT_STEP = {1: 16, 2: 64, 3: 256}
 GATE = 1e-6
 
 
@@ -104,11 +107,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def measure_fma_peaks():
-    """FP32 / FP64 FMA throughput of this GPU (TFLOP/s), from probes/peaks.cu."""
+def measure_peaks():
+    """FP32 / FP64 FMA throughput (TFLOP/s) and shared-memory load bandwidth
+    (GB/s) of this GPU, from probes/peaks.cu (best of 3 each)."""
     import ctypes
     lib = ctypes.CDLL(str(ROOT / "numericalflowiteration_gb300" / "libnufi_probes.so"))
     lib.nufi_probe_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.nufi_probe_smem_bw.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     out = {}
     for name, fp64, iters in (("fp32", 0, 4096), ("fp64", 1, 128)):
         best = 0.0
@@ -118,7 +123,26 @@ def measure_fma_peaks():
             if lib.nufi_probe_fma_peak(fp64, iters, ctypes.byref(t), ctypes.byref(ms)) == 0:
                 best = max(best, t.value)
         out[name] = best
+    best = 0.0
+    for _ in range(3):
+        g = ctypes.c_double()
+        ms = ctypes.c_double()
+        if lib.nufi_probe_smem_bw(2048, ctypes.byref(g), ctypes.byref(ms)) == 0:
+            best = max(best, g.value)
+    out["smem_gbs"] = best
     return out
+
+
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        return json.loads(p.read_text()).get(f"{kernel}@{workload}")
+    except (ValueError, OSError):
+        return None
 
 
 def cpu_baseline(cfg, n_last: int, threads: int):
@@ -238,8 +262,8 @@ def run_ours(args, cfg):
                 "energy_err_max_normalised": err_max, "energy_err_pointwise_max": err_pt,
                 "gate": GATE, "gate_passed": err_max <= GATE}
 
-    # Dominant kernel (the trace): CUDA events around compute_rho(n) on the
-    # handle's stream at several n (trace + a 1-block rho finalize).
+    # Per-step trace launches: CUDA events around compute_rho(n) on the
+    # handle's stream at several n (trace + rho reduction).
     ns = [cfg.Nt // 4, cfg.Nt // 2, (3 * cfg.Nt) // 4, cfg.Nt]
     kt, kps = 0.0, 0
     for n in ns:
@@ -256,14 +280,31 @@ def run_ours(args, cfg):
                 kt += e0.elapsed_time(e1)
                 kps += cfg.n_points * n
     kernel_rate = kps / (kt * 1e-3)
-    peaks = measure_fma_peaks()
+    peaks = measure_peaks()
     flop = FLOP_PER_POINT_STEP[cfg.dim]
-    achieved = kernel_rate * flop / 1e12
+    desc = sim.describe()
+    # The dominant kernel of the timed region: with the whole-run kernel one
+    # launch is one timed step (all Nt+1 time steps), so its launch duration
+    # is ms_per_step; otherwise the per-step trace launches above.
+    if desc["persistent"]["ok"]:
+        kname, krate, launch_ms = desc["run"], ps / (ms_per_step * 1e-3), ms_per_step
+    else:
+        kname, krate, launch_ms = desc["trace"], kernel_rate, kt / len(ns)
+    achieved = krate * flop / 1e12
+    smem_bytes = SMEM_BYTES_PER_POINT_STEP[cfg.dim]
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32"], "unit": "TFLOP/s",
-                "frac": achieved / peaks["fp32"] if peaks["fp32"] else None, "traffic": None,
-                "peak_source": "measured live: FP32 FMA chains (probes/peaks.cu)",
-                "flop_per_point_step": flop, "kernel": "trace_split_1d_kernel",
-                "kernel_point_steps_per_s": kernel_rate, "fp64_fma_peak_tflops": peaks["fp64"]}
+                "frac": achieved / peaks["fp32"] if peaks["fp32"] else None,
+                "traffic": profiled_traffic(kname, args.workload),
+                "kernel": kname, "launch_ms": launch_ms, "point_steps_per_s": krate,
+                "flop_per_point_step": flop,
+                "peak_source": "measured live in this run: FP32 FMA chains (probes/peaks.cu); "
+                               "MEASURED_PEAKS.json holds no SIMT peak",
+                "smem_cobound": {"bytes_per_point_step": smem_bytes, "achieved_gbs": krate * smem_bytes / 1e9,
+                                 "peak_gbs": peaks["smem_gbs"],
+                                 "frac": krate * smem_bytes / 1e9 / peaks["smem_gbs"] if peaks["smem_gbs"] else None},
+                "per_step_trace": {"kernel": desc["trace"], "point_steps_per_s": kernel_rate},
+                "fp64_fma_peak_tflops": peaks["fp64"],
+                "traffic_source": "profiles/traffic.json (ncu dram__bytes_read.sum + dram__bytes_write.sum per launch)"}
 
     # End to end through the reference-facing calls with host buffers, the
     # loop of bin/test_nufi_gpu_1d.cpp:241-252: compute_rho -> download_rho
@@ -316,6 +357,21 @@ def run_ours(args, cfg):
     return 0
 
 
+def profile_case(args, cfg):
+    """One run of steps 0..nt in one precision; prints the chosen kernels."""
+    import numericalflowiteration_gb300 as nufi
+    from numericalflowiteration_gb300 import build
+    build.build()
+    nufi.load()
+    nt = cfg.Nt if args.nt is None else args.nt
+    c = cfg.replace(precision=args.precision, Nt=nt)
+    with nufi.Simulation(c) as sim:
+        e = sim.run()
+        print(json.dumps({"workload": args.workload, "precision": args.precision, "nt": nt,
+                          "energy_last": float(e[-1]), "kernels": sim.describe()}), flush=True)
+    return 0
+
+
 def main(argv=None):
     from numericalflowiteration_gb300.config import WORKLOADS
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
@@ -329,8 +385,14 @@ def main(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=120, help="CPU baseline sample: steps 0..N")
     ap.add_argument("--ref-steps", type=int, default=40, help="reference arm sample per step: steps 0..N")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run steps 0..--nt of the workload once in --precision and exit (a small case for ncu)")
+    ap.add_argument("--precision", default="fp32split", choices=["fp32split", "fp64"])
+    ap.add_argument("--nt", type=int, default=None, help="with --profile-case: last step")
     args = ap.parse_args(argv)
     cfg = WORKLOADS[args.workload]()
+    if args.profile_case:
+        return profile_case(args, cfg)
     if args.impl == "reference":
         return run_reference(args, cfg)
     return run_ours(args, cfg)

@@ -111,6 +111,25 @@ int nufi_download_rho_f32(nufi_handle *h, float *rho);
  * coeffs_base + n*stride_t of the caller's history to the device. */
 int nufi_upload_phi(nufi_handle *h, int64_t n, const double *coeffs_base);
 int nufi_upload_phi_f32(nufi_handle *h, int64_t n, const float *coeffs_base);
+/* cuda_kernel::compute_metrics (nufi/cuda_kernel.cu:158-175, 341-358,
+ * 543-560; kernels :53-79, 239-271, 428-466): over q in [q_begin, q_end)
+ * of f(n, q) = f0 at the foot of the full backward trace from step n
+ * (eval_f, nufi/rho.hpp:63-93: initial half kick with slab n, so slabs
+ * 0 .. n must be present), with u0 the point's grid velocity:
+ *   m[0] = sum w f            (L1 norm)
+ *   m[1] = sum w f^2          (the caller takes the square root)
+ *   m[2] = sum w |u0|^2 f / 2 (kinetic energy)
+ *   m[3] = sum -w f log f over f > 0 (entropy)
+ * w = du dx (1D), dx dy du dv (2D), du dv dw (3D: as the reference, without
+ * dx dy dz).  The metrics grid is the rho grid (the reference drivers set
+ * conf_metrics to the same Nx, Nu; bin/test_nufi_gpu_1d.cpp:216-221).  Always
+ * evaluated in FP64 on the FP64 history, also for FP32-split handles.  An
+ * empty range returns without touching the device sums (as the reference);
+ * n > Nt is NUFI_ERR_RANGE (the reference does not check).  Asynchronous. */
+int nufi_compute_metrics(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end);
+/* cuda_kernel::download_metrics (nufi/cuda_kernel.cu:177-189): m[k] += the
+ * device sums.  Blocks. */
+int nufi_download_metrics(nufi_handle *h, double *metrics4);
 
 /* ---- device-resident stepping ----------------------------------------- */
 /* One full time step on the device: rho(n) from slabs 0..n-1, then the
@@ -163,6 +182,11 @@ int nufi_sizes(const nufi_handle *h, int64_t *stride_t, int64_t *n_spatial, int6
 int nufi_stream(const nufi_handle *h, void **stream);
 /* Number of kernels this handle has launched since creation. */
 int nufi_launch_count(const nufi_handle *h, int64_t *count);
+/* No counterpart in the reference: a JSON object naming the kernels and
+ * launch shapes this handle chose (trace, whole-run kernel, field solve),
+ * NUL-terminated into buf; NUFI_ERR_RANGE if len is too small (the text is
+ * cut). */
+int nufi_describe(const nufi_handle *h, char *buf, size_t len);
 
 #ifdef __cplusplus
 }

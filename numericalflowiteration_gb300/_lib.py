@@ -38,6 +38,9 @@ SIGNATURES = {
     "nufi_download_rho_f32": (ctypes.c_int, [_P, _P]),
     "nufi_upload_phi": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_upload_phi_f32": (ctypes.c_int, [_P, _I64, _P]),
+    "nufi_compute_metrics": (ctypes.c_int, [_P, _I64, _I64, _I64]),
+    "nufi_describe": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    "nufi_download_metrics": (ctypes.c_int, [_P, _P]),
     "nufi_step": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_run": (ctypes.c_int, [_P, _I64, _I64, _P]),
     "nufi_download_history": (ctypes.c_int, [_P, _I64, _I64, _P]),
@@ -143,6 +146,26 @@ class Simulation:
     def compute_rho(self, n: int, q_begin: int = 0, q_end: int | None = None):
         q_end = self.n_points if q_end is None else q_end
         self._check(self._lib.nufi_compute_rho(self._h, n, q_begin, q_end))
+
+    def describe(self) -> dict:
+        """Kernels and launch shapes this handle chose."""
+        import json
+        buf = ctypes.create_string_buffer(4096)
+        self._check(self._lib.nufi_describe(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def compute_metrics(self, n: int, q_begin: int = 0, q_end: int | None = None):
+        """L1 norm, sum w f^2, kinetic energy and entropy of f(n) (eval_f)."""
+        q_end = self.n_points if q_end is None else q_end
+        self._check(self._lib.nufi_compute_metrics(self._h, n, q_begin, q_end))
+
+    def download_metrics(self, metrics: np.ndarray | None = None) -> np.ndarray:
+        """metrics += device sums (4 doubles); a new zeroed array if None."""
+        m = np.zeros(4) if metrics is None else metrics
+        if m.dtype != np.float64 or m.shape != (4,) or not m.flags.c_contiguous:
+            raise TypeError("metrics must be a contiguous float64 array of 4")
+        self._check(self._lib.nufi_download_metrics(self._h, _ptr(m)))
+        return m
 
     def download_rho(self, rho: np.ndarray) -> np.ndarray:
         """rho += device rho (the caller zeroes it first, as the reference's drivers do)."""

@@ -54,6 +54,26 @@ cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial,
     return cudaGetLastError();
 }
 
+__global__ void reduce_metrics_kernel(long long blocks, const double *__restrict__ partial, double *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31, k = threadIdx.x >> 5;
+    double sum = 0, comp = 0;
+    for (long long r = lane; r < blocks; r += 32) neumaier_add(sum, comp, partial[k * blocks + r]);
+    for (int off = 16; off > 0; off >>= 1) {
+        const double os = __shfl_down_sync(0xffffffffu, sum, off);
+        const double oc = __shfl_down_sync(0xffffffffu, comp, off);
+        neumaier_add(sum, comp, os);
+        comp += oc;
+    }
+    if (lane == 0) out[k] = sum + comp;
+}
+
+cudaError_t launch_reduce_metrics(long long blocks, const double *partial, double *metrics, cudaStream_t st)
+{
+    reduce_metrics_kernel<<<1, 128, 0, st>>>(blocks, partial, metrics);
+    return cudaGetLastError();
+}
+
 namespace {
 
 constexpr int kSolveThreads = 256;
@@ -168,7 +188,7 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
                     if (ii >= p.P[0]) continue;
                     const int idx = (k * p.P[1] + jj) * p.P[0] + ii;
                     slab[idx] = cval;
-                    if (table && p.dim > 1) table[idx] = float(cval);
+                    if (table && p.dim > 1) table[(k * p.P[1] + jj) * p.table_sx + ii] = float(cval);
                 }
             }
         }
@@ -245,7 +265,8 @@ __global__ void derive_table_kernel(const Problem p, const double *__restrict__ 
             cubic_kick_poly(slab[idx], slab[idx + 1], slab[idx + 2], slab[idx + 3], K);
     } else {
         if (idx >= p.stride_t) return;
-        table[idx] = float(slab[idx]);
+        const long long row = idx / p.P[0];
+        table[row * p.table_sx + idx % p.P[0]] = float(slab[idx]);
     }
 }
 

@@ -52,6 +52,8 @@ struct nufi_handle {
     unsigned *err = nullptr;
     SplitNode *nodes = nullptr;
     float2 *phase = nullptr;
+    double *mpartial = nullptr;  // [4][trace blocks] metrics block sums
+    double *metrics = nullptr;   // [4]
     SolvePlan plan;
     bool solve_ok = false;
     std::string solve_why;
@@ -189,7 +191,15 @@ Problem make_problem(const nufi_config &c)
     }
     p.Nq = p.Ns * p.Nm;
     p.hist_stride = (p.stride_t + 1) / 2 * 2;
-    p.table_stride = c.dim == 1 ? 4LL * p.N[0] : (p.stride_t + 3) / 4 * 4;
+    // 2D/3D FP32 tables: x rows of table_sx floats.  A warp holds 32
+    // consecutive spatial nodes, i.e. 32 / N[0] rows when N[0] < 32; with
+    // table_sx = N[0] (mod 32) those rows fall on disjoint shared-memory
+    // banks (with P[0] = N[0] + 3 two 16-node rows would share 3 banks and
+    // every gather would take two wavefronts).
+    p.table_sx = p.P[0];
+    if (c.dim > 1 && p.N[0] < 32)
+        while (p.table_sx % 32 != p.N[0] % 32) ++p.table_sx;
+    p.table_stride = c.dim == 1 ? 4LL * p.N[0] : (1LL * p.table_sx * p.P[1] * p.P[2] + 3) / 4 * 4;
     p.dt = c.dt;
     for (int i = 0; i < 8; ++i) p.f0p[i] = c.f0_params[i];
     p.wv = 1;
@@ -542,6 +552,8 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
         (e = dalloc(h.get(), &h->rho_in, size_t(p.Ns))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->slab_out, size_t(p.hist_stride))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->energy_tmp, 1)) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->mpartial, size_t(4 * ((p.Ns + 31) / 32) * h->shape.vblocks))) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->metrics, 4)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->err, 1)) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMalloc"));
     if (p.precision == NUFI_PREC_FP32_SPLIT) {
@@ -554,6 +566,7 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     if ((e = cudaMemset(h->hist, 0, nslab * p.hist_stride * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->energy, 0, nslab * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->rho, 0, size_t(p.Ns) * sizeof(double))) != cudaSuccess ||
+        (e = cudaMemset(h->metrics, 0, 4 * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMemset"));
     if ((st = build_solve_plan(h.get(), sms > 0 ? sms : 1))) return bail(st);
@@ -609,6 +622,38 @@ int nufi_download_rho(nufi_handle *h, double *rho)
     int st = download_rho_impl(h, tmp);
     if (st) return st;
     for (size_t i = 0; i < tmp.size(); ++i) rho[i] += tmp[i];
+    return NUFI_OK;
+}
+
+int nufi_compute_metrics(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end)
+{
+    if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
+    if (q_begin < 0 || q_end < q_begin || q_end > h->p.Nq)
+        return fail(h, NUFI_ERR_RANGE, "quadrature range outside [0, Nq]");
+    if (q_begin == q_end) return NUFI_OK;  // as the reference: no launch, sums untouched
+    DeviceGuard g(h->device);
+    const Problem &p = h->p;
+    int rows = 0;
+    cudaError_t e = launch_trace_fp64(p, h->shape, h->hist, int(n), q_begin, q_end, 2, h->mpartial, &rows, h->err,
+                                      h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "metrics launch");
+    h->launches += 1;
+    e = launch_reduce_metrics((p.Ns + 31) / 32 * (long long)rows, h->mpartial, h->metrics, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "metrics reduce launch");
+    h->launches += 1;
+    return NUFI_OK;
+}
+
+int nufi_download_metrics(nufi_handle *h, double *metrics4)
+{
+    if (!h || !metrics4) return fail(h, NUFI_ERR_INVALID, "null argument");
+    DeviceGuard g(h->device);
+    double tmp[4];
+    NUFI_CUDA(h, cudaMemcpyAsync(tmp, h->metrics, sizeof(tmp), cudaMemcpyDeviceToHost, h->stream));
+    int st = sync_and_check(h);
+    if (st) return st;
+    for (int k = 0; k < 4; ++k) metrics4[k] += tmp[k];
     return NUFI_OK;
 }
 
@@ -797,6 +842,32 @@ int nufi_launch_count(const nufi_handle *h, int64_t *count)
     if (!h || !count) return fail(nullptr, NUFI_ERR_INVALID, "null argument");
     *count = h->launches;
     return NUFI_OK;
+}
+
+int nufi_describe(const nufi_handle *h, char *buf, size_t len)
+{
+    if (!h || !buf || len == 0) return fail(nullptr, NUFI_ERR_INVALID, "null argument");
+    const Problem &p = h->p;
+    char tmp[1024];
+    const char *trace = p.precision == NUFI_PREC_FP64 ? "trace_fp64_kernel"
+                        : p.dim > 1                   ? "trace_split_nd_kernel"
+                        : h->staged.ok                ? "trace_split_1d_staged_kernel"
+                                                      : "trace_split_1d_kernel";
+    int k = std::snprintf(
+        tmp, sizeof(tmp),
+        "{\"trace\": \"%s\", \"fp64_shape\": {\"warps\": %d, \"ppt\": %d, \"vblocks\": %d}, "
+        "\"staged\": {\"ok\": %d, \"ctas\": %d, \"threads\": %d, \"ppt\": %d, \"slabs_per_chunk\": %d, "
+        "\"ring\": %d, \"smem\": %zu}, \"run\": \"%s\", \"persistent\": {\"ok\": %d, \"ctas\": %d, "
+        "\"threads\": %d, \"ppt\": %d, \"smem\": %zu}, \"solve\": {\"ok\": %d, \"kernel\": "
+        "\"circulant_solve_kernel<%d>\", \"blocks\": %d, \"nodes_per_block\": %d}}",
+        trace, h->shape.warps, h->shape.ppt, h->shape.vblocks, int(h->staged.ok), h->staged.ctas,
+        h->staged.threads, h->staged.ppt, h->staged.slabs_per_chunk, h->staged.ring, h->staged.smem,
+        h->persist.ok ? "run_split_1d_kernel" : "graph of per-step launches", int(h->persist.ok), h->persist.ctas,
+        h->persist.threads, h->persist.ppt, h->persist.smem, int(h->solve_ok), h->plan.nconv, h->plan.blocks,
+        h->plan.nodes_per_block);
+    if (k < 0) return fail(nullptr, NUFI_ERR_INVALID, "describe");
+    std::snprintf(buf, len, "%s", tmp);
+    return size_t(k) < len ? NUFI_OK : fail(nullptr, NUFI_ERR_RANGE, "describe: buffer too small");
 }
 
 }  // extern "C"

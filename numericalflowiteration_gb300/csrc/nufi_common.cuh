@@ -34,6 +34,7 @@ struct Problem {
     long long stride_t;  // values per slab, reference layout
     long long hist_stride;  // doubles between slabs in the device FP64 history
     long long table_stride; // floats between slabs in the device FP32 tables
+    int table_sx;           // 2D/3D FP32 table: floats per x row (>= P[0], see make_problem)
     double dt;
     double xmin[3], L[3], Linv[3], dx[3], dxinv[3];
     double vmin[3], dv[3];

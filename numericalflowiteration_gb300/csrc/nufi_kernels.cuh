@@ -50,8 +50,31 @@ __device__ __forceinline__ void write_partial_tiled(double acc, long long s, lon
     }
 }
 
+// Block sums of the four metrics into partial[k * blocks + block] (fixed
+// xor-shuffle tree per warp, warps summed in order: deterministic).
+__device__ __forceinline__ void write_metrics_block(const double (&m4)[4], double *__restrict__ partial)
+{
+    __shared__ double red[4][8];
+    const int lane = threadIdx.x, warp = threadIdx.y;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        double v = m4[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (warp == 0 && lane < 4) {
+        double t = red[lane][0];
+        for (int w = 1; w < int(blockDim.y); ++w) t += red[lane][w];
+        const long long blocks = (long long)gridDim.x * gridDim.y;
+        partial[lane * blocks + (long long)blockIdx.y * gridDim.x + blockIdx.x] = t;
+    }
+}
+
 // The trace kernels write per-block partial sums of f~ ([rows][Ns]); the
-// launchers return the row count through *rows.
+// launchers return the row count through *rows.  mode 0: f~ (eval_ftilda);
+// mode 2: the four metrics of f (eval_f) into [4][blocks] block sums.
 cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
                               long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st);
 bool fp64_order_supported(int dim, int order);
@@ -97,6 +120,9 @@ struct PersistentRun {
 // lanes take rows in a fixed stride with Neumaier compensation, then a
 // fixed xor-shuffle tree; deterministic.
 cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st);
+// metrics[k] = sum over the blocks of partial[k][block] (one warp per
+// metric, Neumaier lanes and a fixed shuffle tree).
+cudaError_t launch_reduce_metrics(long long blocks, const double *partial, double *metrics, cudaStream_t st);
 
 
 // Field solve as circulant products (field_solve.cu).  green holds

@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const 
     double acc = 0;
     if (n > 0) {
         double E[D];
-        if (mode == 1) {  // eval_f: initial half kick with slab n
+        if (mode >= 1) {  // eval_f: initial half kick with slab n
             const double *c = hist + (long long)n * p.hist_stride;
 #pragma unroll
             for (int q = 0; q < PPT; ++q) {
@@ -230,6 +230,37 @@ __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const 
 #pragma unroll
             for (int a = 0; a < D; ++a) u[q][a] += 0.5 * dt * E[a];
         }
+    }
+    if (mode == 2) {
+        // metrics of cuda_eval_metrics (nufi/cuda_kernel.cu:53-79, 239-271,
+        // 428-466): weight * f, weight * f^2, weight * |u0|^2 f / 2 and
+        // -weight f log f, u0 the point's initial velocity; weight du (dx)
+        // in 1D, dx dy du dv in 2D, du dv dw in 3D (the reference's 3D
+        // kernel leaves out dx dy dz).
+        double w = p.wv;
+        if (D < 3)
+            for (int a = 0; a < D; ++a) w *= p.dx[a];
+        double m4[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            if (!live[q]) continue;
+            const double f = f0_fp64<D>(p, x[q], u[q]);
+            long long rm = mb + q;
+            double uu = 0;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+                const double u0 = p.vmin[a] + int(rm % p.M[a]) * p.dv[a] + p.dv[a] / 2;
+                rm /= p.M[a];
+                uu += u0 * u0;
+            }
+            const double wf = w * f;
+            m4[0] += wf;
+            m4[1] += wf * f;
+            m4[2] += w * (uu * f / 2);
+            m4[3] += (f > 0) ? -wf * log(f) : 0.0;
+        }
+        write_metrics_block(m4, partial);
+        return;
     }
 #pragma unroll
     for (int q = 0; q < PPT; ++q)

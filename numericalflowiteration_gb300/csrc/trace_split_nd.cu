@@ -4,8 +4,10 @@
 // cell I_a, FP32 fraction xi_a in [0, 1), and the kick sum in cells per
 // substep in two levels (plain FP32 within a chunk of slabs, Kahan-
 // compensated across chunks; the sum starts at the low part of the free-
-// streaming fraction).  The field of slab k is its FP32 padded copy (the
-// reference layout, x fastest) written by the field solve.  All components
+// streaming fraction).  The field of slab k is its FP32 padded copy written
+// by the field solve: the reference layout (x fastest, periodic padding to
+// N + 3 per axis) with x rows widened to table_sx floats so that the rows
+// one warp spans use disjoint shared-memory banks.  All components
 // of E come from one gather of the 4^D window, contracted with the cubic
 // B-spline value and derivative bases per axis (the arithmetic of
 // splines2d / splines3d::eval and of the reference's separate eval<1,0> /
@@ -162,7 +164,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
     const long long nj = t < Ns ? (Ns - t + T - 1) / T : 0;  // spatial nodes of this thread
     const long long nj0 = (Ns + T - 1) / T;                  // ... of thread 0 (the most)
     const long long batches = (nj0 * Mc + PPT - 1) / PPT;
-    const int sy = p.P[0], sz = p.P[0] * p.P[1];
+    const int sy = p.table_sx, sz = p.table_sx * p.P[1];
     float K[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) K[a] = float(-p.dt * p.dt * p.dxinv[a] * p.dxinv[a]);
@@ -334,13 +336,13 @@ cudaError_t launch_nd_mode(const Problem &p, const StagedShape &sh, const float 
 // One CTA per SM (at most Nm), T = min(512, Ns rounded up to a warp)
 // threads; S slabs per ring slot from a 120 KB budget (more than half of
 // an SM's shared memory, so no SM holds two CTAs), 3 slots, or 2 when 3 do
-// not fit in 200 KB, else the tables stay in global memory.
+// not fit in 220 KB, else the tables stay in global memory.
 StagedShape staged_shape_nd(const Problem &p, int sms)
 {
     StagedShape sh;
     if (p.dim < 2 || p.order != 4) return sh;
     const size_t slab_bytes = size_t(p.table_stride) * 4;
-    const size_t kOneCtaPerSm = 120 * 1024, kMaxSmem = 200 * 1024;
+    const size_t kOneCtaPerSm = 120 * 1024, kMaxSmem = 220 * 1024;
     sh.ctas = int(std::min<long long>(p.Nm, sms));
     sh.threads = int(std::min<long long>(512, (p.Ns + 31) / 32 * 32));
     sh.ppt = p.dim == 2 ? 2 : 1;

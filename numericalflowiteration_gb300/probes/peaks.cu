@@ -1,8 +1,12 @@
 // peaks.cu — measured denominators for the roofline of the trace kernels,
-// which are bound by FP32 / FP64 FMA issue (not by HBM or tensor cores).
-// Each thread runs 8 independent FMA chains for `iters` rounds; the peak
-// is 2 flop per FMA over the kernel's CUDA-event time.  Built into
-// libnufi_probes.so, used by bench.py only.
+// which are bound by FP32 / FP64 FMA issue and shared-memory load
+// bandwidth (not by HBM or tensor cores).
+//   nufi_probe_fma_peak: each thread runs 8 independent FMA chains for
+//     `iters` rounds; 2 flop per FMA over the kernel's CUDA-event time.
+//   nufi_probe_smem_bw: every warp reads 32 consecutive float4 (512 B,
+//     conflict-free) of a 64 KB shared buffer per load, `iters` x 16 loads
+//     per thread; bytes read over the kernel's CUDA-event time.
+// Built into libnufi_probes.so, used by bench.py only.
 #include <cuda_runtime.h>
 #include <cstdio>
 
@@ -52,7 +56,58 @@ int run(double *tflops, double *ms_out, int iters)
     return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
+__global__ void __launch_bounds__(1024) smem_reads(float *out, int iters)
+{
+    extern __shared__ float4 buf[];  // 4096 float4
+    for (int i = threadIdx.x; i < 4096; i += blockDim.x) buf[i] = make_float4(i, i + 1, i + 2, i + 3);
+    __syncthreads();
+    float4 acc = make_float4(0, 0, 0, 0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int base = warp * 32;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const float4 v = buf[((base + r * 256) & 4095) + lane];
+            acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
+        }
+        base = (base + 32 * 33) & 4095;
+    }
+    const float s = (acc.x + acc.y) + (acc.z + acc.w);
+    if (s == -12345.678f) out[threadIdx.x] = s;
+}
+
+int run_smem(double *gbs, double *ms_out, int iters)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    float *out = nullptr;
+    if (cudaMalloc(&out, 1024 * sizeof(float)) != cudaSuccess) return 1;
+    const size_t smem = 4096 * sizeof(float4);
+    cudaFuncSetAttribute(smem_reads, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    const int blocks = sms * 2, threads = 1024;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    smem_reads<<<blocks, threads, smem>>>(out, iters / 8 + 1);  // warm-up
+    cudaEventRecord(e0);
+    smem_reads<<<blocks, threads, smem>>>(out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double bytes = double(blocks) * threads * double(iters) * 16.0 * 16.0;
+    *gbs = bytes / (double(ms) * 1e-3) / 1e9;
+    *ms_out = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
 }  // namespace
+
+extern "C" int nufi_probe_smem_bw(int iters, double *gbs, double *ms) { return run_smem(gbs, ms, iters); }
 
 extern "C" int nufi_probe_fma_peak(int fp64, int iters, double *tflops, double *ms)
 {

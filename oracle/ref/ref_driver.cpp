@@ -21,6 +21,11 @@
 //   ref_driver solve <cfg.bin> <rho.bin> <out_prefix>
 //       poisson<double>::solve + interpolate<double,order>; writes
 //       <out>.slab and <out>.energy.
+//   ref_driver metrics <cfg.bin> <coeffs.bin> <n> <out_prefix>
+//       the four sums of cuda_eval_metrics (nufi/cuda_kernel.cu:53-79,
+//       239-271, 428-466) over all q, f from the reference's eval_f
+//       (nufi/rho.hpp:63-93, 234-, 369-); per-node sums in q order, nodes
+//       summed in order; writes <out>.metrics (4 doubles).
 //   ref_driver poisson_kat        bin/test_poisson.cpp's analytic check
 //   ref_driver fields_kat         bin/test_fields.cpp's checks at nodes
 #include <cmath>
@@ -212,6 +217,97 @@ void rho_any(const nufi_config &k, size_t n, const double *coeffs, double *rho)
 #undef NUFI_REF_ORDER_CASE
 }
 
+// Metrics by the GPU kernels' point order, weights and expressions.
+struct metric_sums {
+    double m[4] = {0, 0, 0, 0};
+    void add(double weight, double f, double uu)
+    {
+        m[0] += weight * f;
+        m[1] += weight * f * f;
+        m[2] += weight * (uu * f / 2);
+        m[3] += (f > 0) ? -weight * f * std::log(f) : 0;
+    }
+};
+
+template <size_t order>
+void metrics_1d(size_t n, const double *coeffs, const nufi::dim1::config_t<double> &conf, double *out)
+{
+    std::vector<metric_sums> per(conf.Nx);
+    const double weight = conf.du * conf.dx;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (size_t ix = 0; ix < conf.Nx; ++ix)
+        for (size_t iu = 0; iu < conf.Nu; ++iu) {
+            const double x = conf.x_min + ix * conf.dx;
+            const double u = conf.u_min + iu * conf.du + conf.du / 2;
+            per[ix].add(weight, nufi::dim1::eval_f<double, order>(n, x, u, coeffs, conf), u * u);
+        }
+    for (auto &p : per)
+        for (int k = 0; k < 4; ++k) out[k] += p.m[k];
+}
+
+template <size_t order>
+void metrics_2d(size_t n, const double *coeffs, const nufi::dim2::config_t<double> &conf, double *out)
+{
+    const size_t Ns = conf.Nx * conf.Ny;
+    std::vector<metric_sums> per(Ns);
+    const double weight = conf.dx * conf.dy * conf.du * conf.dv;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (size_t s = 0; s < Ns; ++s) {
+        const size_t ix = s % conf.Nx, iy = s / conf.Nx;
+        for (size_t iv = 0; iv < conf.Nv; ++iv)
+            for (size_t iu = 0; iu < conf.Nu; ++iu) {
+                const double x = conf.x_min + ix * conf.dx, y = conf.y_min + iy * conf.dy;
+                const double u = conf.u_min + iu * conf.du + conf.du / 2;
+                const double v = conf.v_min + iv * conf.dv + conf.dv / 2;
+                per[s].add(weight, nufi::dim2::eval_f<double, order>(n, x, y, u, v, coeffs, conf), u * u + v * v);
+            }
+    }
+    for (auto &p : per)
+        for (int k = 0; k < 4; ++k) out[k] += p.m[k];
+}
+
+template <size_t order>
+void metrics_3d(size_t n, const double *coeffs, const nufi::dim3::config_t<double> &conf, double *out)
+{
+    const size_t Ns = conf.Nx * conf.Ny * conf.Nz;
+    std::vector<metric_sums> per(Ns);
+    const double weight = conf.du * conf.dv * conf.dw;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (size_t s = 0; s < Ns; ++s) {
+        const size_t ix = s % conf.Nx, iy = (s / conf.Nx) % conf.Ny, iz = s / (conf.Nx * conf.Ny);
+        for (size_t iw = 0; iw < conf.Nw; ++iw)
+            for (size_t iv = 0; iv < conf.Nv; ++iv)
+                for (size_t iu = 0; iu < conf.Nu; ++iu) {
+                    const double x = conf.x_min + ix * conf.dx, y = conf.y_min + iy * conf.dy;
+                    const double z = conf.z_min + iz * conf.dz;
+                    const double u = conf.u_min + iu * conf.du + conf.du / 2;
+                    const double v = conf.v_min + iv * conf.dv + conf.dv / 2;
+                    const double w = conf.w_min + iw * conf.dw + conf.dw / 2;
+                    per[s].add(weight, nufi::dim3::eval_f<double, order>(n, x, y, z, u, v, w, coeffs, conf),
+                               u * u + v * v + w * w);
+                }
+    }
+    for (auto &p : per)
+        for (int k = 0; k < 4; ++k) out[k] += p.m[k];
+}
+
+void metrics_any(const nufi_config &k, size_t n, const double *coeffs, double *out)
+{
+#define NUFI_REF_ORDER_CASE(O)                                               \
+    case O:                                                                   \
+        if (k.dim == 1) { nufi::dim1::config_t<double> c; fill(c, k); metrics_1d<O>(n, coeffs, c, out); } \
+        else if (k.dim == 2) { nufi::dim2::config_t<double> c; fill(c, k); metrics_2d<O>(n, coeffs, c, out); } \
+        else { nufi::dim3::config_t<double> c; fill(c, k); metrics_3d<O>(n, coeffs, c, out); } \
+        return;
+    switch (k.order) {
+        NUFI_REF_ORDER_CASE(3)
+        NUFI_REF_ORDER_CASE(4)
+        NUFI_REF_ORDER_CASE(5)
+    default: std::fprintf(stderr, "order %d not built\n", k.order); std::exit(2);
+    }
+#undef NUFI_REF_ORDER_CASE
+}
+
 // poisson<double>::solve then interpolate<double,order>, as the drivers do
 // (bin/test_nufi_gpu_1d.cpp:248-249; _2d.cpp:156-157; _3d.cpp:160-161).
 double solve_any(const nufi_config &k, double *rho, double *slab)
@@ -291,6 +387,22 @@ int cmd_solve(int argc, char **argv)
     return 0;
 }
 
+int cmd_metrics(int argc, char **argv)
+{
+    if (argc < 6) return 2;
+    nufi_config k;
+    if (!read_file(argv[2], &k, sizeof(k))) return 2;
+    g_f0.kind = k.f0_kind;
+    for (int i = 0; i < 8; ++i) g_f0.p[i] = k.f0_params[i];
+    std::vector<double> coeffs((k.Nt + 1) * slab_size(k));
+    if (!read_file(argv[3], coeffs.data(), sizeof(double) * coeffs.size())) return 2;
+    const size_t n = std::strtoull(argv[4], nullptr, 10);
+    double m[4] = {0, 0, 0, 0};
+    metrics_any(k, n, coeffs.data(), m);
+    write_file(std::string(argv[5]) + ".metrics", m, sizeof(m));
+    return 0;
+}
+
 // bin/test_poisson.cpp:36-119: rho = cos2z + sin8y + cos42x on 128x64x32.
 template <typename real>
 double poisson_kat()
@@ -364,6 +476,7 @@ int main(int argc, char **argv)
     const std::string cmd = argv[1];
     if (cmd == "run") return cmd_run(argc, argv);
     if (cmd == "solve") return cmd_solve(argc, argv);
+    if (cmd == "metrics") return cmd_metrics(argc, argv);
     if (cmd == "poisson_kat") {
         std::printf("{\"float\": %.17g, \"double\": %.17g}\n", poisson_kat<float>(), poisson_kat<double>());
         return 0;

@@ -49,6 +49,20 @@ RUN_CASES = {
     "small_landau_3d_4x4": (landau_3d(Nx=4, Nv=4, Nt=5), 5, list(range(6)), list(range(6))),
 }
 
+# name -> (config, metrics steps): the reference's eval_f metrics of its own
+# in-order run, at the listed steps (ref_driver metrics)
+METRICS_CASES = {
+    "metrics_small_landau_1d_16x32": (landau_1d(Nx=16, Nv=32, Nt=20), [0, 1, 10, 20]),
+    "metrics_landau_1d_64x256_T30": (landau_1d(), [0, 100, 480]),
+    "metrics_two_stream_1d_64x256_T50": (two_stream_1d(Nx=64, Nv=256), [0, 400, 800]),
+    "metrics_bump_on_tail_1d_64x256_n80": (bump_on_tail_1d(Nt=80), [0, 80]),
+    "metrics_order5_landau_1d_32x64": (landau_1d(Nx=32, Nv=64, Nt=12, order=5), [0, 12]),
+    "metrics_small_landau_2d_8x8": (landau_2d(Nx=8, Nv=8, Nt=10), [0, 1, 10]),
+    "metrics_landau_2d_16x16_n40": (landau_2d(Nx=16, Nv=16, Nt=40), [0, 20, 40]),
+    "metrics_small_landau_3d_4x4": (landau_3d(Nx=4, Nv=4, Nt=5), [0, 1, 5]),
+    "metrics_landau_3d_8x8_T2": (landau_3d(Nx=8, Nv=8, Nt=20), [0, 10, 20]),
+}
+
 SOLVE_CASES = {
     "solve_1d_64": landau_1d(),
     "solve_1d_256": two_stream_1d(),
@@ -85,6 +99,26 @@ def run_case(name, cfg, n_last, rho_keep, slab_keep, tmp: Path):
             "summation_floor": floor}
 
 
+def metrics_case(name, cfg, steps, tmp: Path):
+    """The reference's run to the last listed step, then its eval_f metrics
+    at each listed step on that history."""
+    p = tmp / name
+    (p.with_suffix(".cfg")).write_bytes(cfg.to_bytes())
+    n_last = max(steps)
+    _, _, coeffs = _driver_run(cfg, n_last, p, 0)
+    coeffs.tofile(str(p) + ".hist")
+    out = []
+    for n in steps:
+        subprocess.run([str(DRIVER), "metrics", str(p.with_suffix(".cfg")), str(p) + ".hist", str(n), str(p)],
+                       check=True)
+        out.append(np.fromfile(str(p) + ".metrics"))
+    keep = list(range(n_last + 1))  # eval_f at step n reads slabs 0 .. n
+    np.savez_compressed(HERE / f"{name}.npz", config=np.frombuffer(cfg.to_bytes(), dtype=np.uint8),
+                        steps=np.array(steps), metrics=np.array(out), n_last=n_last,
+                        slab_steps=np.array(keep), slabs=coeffs[keep])
+    return {"steps": steps, "metrics_last": [float(v) for v in out[-1]]}
+
+
 def solve_case(name, cfg, tmp: Path, seed: int):
     rng = np.random.default_rng(seed)
     rho = -1.0 + 1e-2 * rng.standard_normal(cfg.n_spatial)
@@ -116,6 +150,11 @@ def main():
             if args.only and args.only not in name:
                 continue
             manifest["cases"][name] = run_case(name, cfg, n_last, rk, sk, tmp)
+            print(name, manifest["cases"][name], flush=True)
+        for name, (cfg, steps) in METRICS_CASES.items():
+            if args.only and args.only not in name:
+                continue
+            manifest["cases"][name] = metrics_case(name, cfg, steps, tmp)
             print(name, manifest["cases"][name], flush=True)
         for i, (name, cfg) in enumerate(SOLVE_CASES.items()):
             if args.only and args.only not in name:

@@ -131,3 +131,20 @@ def test_oracle_q_range_partition(oracle_mod):
     parts = sum(oracle_mod.rho(cfg, n, coeffs, a, b) for a, b in zip(cuts[:-1], cuts[1:]))
     assert rel_max(parts, full) <= 1e-14
     assert rel_max(full, g["rho"][n]) <= 1e-12
+
+
+METRICS_CASES = ["metrics_small_landau_1d_16x32", "metrics_landau_1d_64x256_T30", "metrics_two_stream_1d_64x256_T50",
+                 "metrics_bump_on_tail_1d_64x256_n80", "metrics_order5_landau_1d_32x64",
+                 "metrics_small_landau_2d_8x8", "metrics_landau_2d_16x16_n40", "metrics_small_landau_3d_4x4",
+                 "metrics_landau_3d_8x8_T2"]
+
+
+@pytest.mark.parametrize("name", METRICS_CASES)
+def test_oracle_metrics_match_reference(name, oracle_mod):
+    """eval_f metrics (L1, sum f^2, kinetic energy, entropy) of the oracle on
+    the reference's own history against the reference's eval_f metrics."""
+    cfg, g = golden(name)
+    hist = np.ascontiguousarray(g["slabs"].reshape(-1))
+    for n, ref in zip(g["steps"], g["metrics"]):
+        got = oracle_mod.metrics(cfg, int(n), hist)
+        assert np.max(np.abs(got - ref) / np.abs(ref)) <= 1e-12, (int(n), got, ref)

@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
         }
         if constexpr (NCONV == 5) {
             if (table)
-                reinterpret_cast<float4 *>(table)[i] = make_float4(float(a[2]), float(a[3]), float(a[4]), 0.0f);
+                store_kick_entry(table, N0, i, float(a[2]), float(a[3]), float(a[4]));
         }
         e_local = rs[i] * a[1];
     }
@@ -245,12 +245,13 @@ namespace {
 
 // K (A, B, C) of cell i from c[i..i+3]: the derivative of the cubic
 // B-spline sum on [i, i+1) as a quadratic in xi, times K = -dt^2/dx^2.
-__device__ __forceinline__ float4 cubic_kick_poly(double c0, double c1, double c2, double c3, double K)
+__device__ __forceinline__ void cubic_kick_poly(double c0, double c1, double c2, double c3, double K, float *slab,
+                                                int N, int i)
 {
     const double A = (c2 - c0) * 0.5;
     const double B = (c0 - 2.0 * c1) + c2;
     const double C = ((3.0 * (c1 - c2) - c0) + c3) * 0.5;
-    return make_float4(float(K * A), float(K * B), float(K * C), 0.0f);
+    store_kick_entry(slab, N, i, float(K * A), float(K * B), float(K * C));
 }
 
 }  // namespace
@@ -261,8 +262,7 @@ __global__ void derive_table_kernel(const Problem p, const double *__restrict__ 
     if (p.dim == 1) {
         if (idx >= p.N[0]) return;
         const double K = -p.dt * p.dt * p.dxinv[0] * p.dxinv[0];
-        reinterpret_cast<float4 *>(table)[idx] =
-            cubic_kick_poly(slab[idx], slab[idx + 1], slab[idx + 2], slab[idx + 3], K);
+        cubic_kick_poly(slab[idx], slab[idx + 1], slab[idx + 2], slab[idx + 3], K, table, p.N[0], int(idx));
     } else {
         if (idx >= p.stride_t) return;
         const long long row = idx / p.P[0];

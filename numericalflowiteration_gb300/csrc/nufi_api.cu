@@ -7,7 +7,7 @@
 //            rounded up to 16 bytes; slab n is written by the field solve
 //            (nufi_step / nufi_run) or by nufi_upload_phi.
 //   tables   (Nt+1) FP32 field tables (split mode only): 1D per cell
-//            float4 K(A,B,C) of the spline derivative, 2D/3D the FP32 slab.
+//            K(A,B), K C of the spline derivative (store_kick_entry), 2D/3D the FP32 slab.
 //   partial  [rows][Ns] FP64 per-block sums of the trace (reduce_rho sums
 //            the rows into rho).
 //   rho      [Ns] FP64, energy [Nt+1] FP64, err (one error word).
@@ -199,7 +199,7 @@ Problem make_problem(const nufi_config &c)
     p.table_sx = p.P[0];
     if (c.dim > 1 && p.N[0] < 32)
         while (p.table_sx % 32 != p.N[0] % 32) ++p.table_sx;
-    p.table_stride = c.dim == 1 ? 4LL * p.N[0] : (1LL * p.table_sx * p.P[1] * p.P[2] + 3) / 4 * 4;
+    p.table_stride = c.dim == 1 ? (3LL * p.N[0] + 3) / 4 * 4 : (1LL * p.table_sx * p.P[1] * p.P[2] + 3) / 4 * 4;
     p.dt = c.dt;
     for (int i = 0; i < 8; ++i) p.f0p[i] = c.f0_params[i];
     p.wv = 1;

@@ -18,7 +18,7 @@
 //   solve    every CTA loads rho, removes the mean (fixed order) and
 //            computes its nodes' circulant products c, phi, K(A,B,C) from
 //            the Green's kernels held in shared memory for the whole run;
-//            writes slab n (FP64), table n (float4 per cell) and its part
+//            writes slab n (FP64), table n (store_kick_entry) and its part
 //            of sum rho' phi
 //   barrier
 //   energy   CTA 0 sums the parts in CTA order -> W_n
@@ -55,7 +55,7 @@ __device__ __forceinline__ double block_sum(double v, double *red)
 }  // namespace
 
 template <int PPT, bool POW2>
-__global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
+__global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     const Problem p, float *__restrict__ tables, double *__restrict__ hist, const SplitNode *__restrict__ nodes,
     const float2 *__restrict__ phase, const double *__restrict__ green, double *__restrict__ partial,
     double *__restrict__ rho, double *__restrict__ energy, double *__restrict__ epart, int n0, int n1, int S, int Nr,
@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long full_bar[kRing];
+    __shared__ unsigned released[kRing];  // warps done with the slot's chunk
     __shared__ double red[32];
     __shared__ double wacc[16][5];
     __shared__ double combine[256];
@@ -73,8 +74,9 @@ __global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
     const int s = threadIdx.x % Nr;    // spatial node of this thread
     const int grp = threadIdx.x / Nr;  // its chain group
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float4 *ring = reinterpret_cast<float4 *>(smem_raw);
-    double *rs = reinterpret_cast<double *>(smem_raw + size_t(kRing) * S * N * sizeof(float4));  // rho' [N]
+    const int TS = int(p.table_stride);  // floats per slab table
+    float *ring = reinterpret_cast<float *>(smem_raw);
+    double *rs = reinterpret_cast<double *>(smem_raw + size_t(kRing) * S * TS * sizeof(float));  // rho' [N]
     double *gs = rs + N;                                                                       // green [5][N]
     unsigned *count = sync, *abort = sync + 1;
 
@@ -94,14 +96,16 @@ __global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
     }
     for (int j = threadIdx.x; j < 5 * N; j += blockDim.x) gs[j] = green[j];
     if (threadIdx.x == 0) {
-        for (int r = 0; r < kRing; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
+        for (int r = 0; r < kRing; ++r) {
+            mbar_init(smem_addr(&full_bar[r]), 1);
+            released[r] = 0;
+        }
         mbar_fence_init();
     }
     __syncthreads();
 
     const F0 f = make_f0(p);
     const unsigned slab_bytes = unsigned(p.table_stride) * 4u;
-    unsigned uses[kRing] = {0, 0, 0};
     unsigned target = 0;
     // nodes of this CTA in the reduce and solve phases: blockIdx.x + k*G
     const int K = blockIdx.x < N ? (N - 1 - int(blockIdx.x)) / G + 1 : 0;
@@ -110,50 +114,86 @@ __global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
     const int wpn = K > 0 ? W / Kp : W;  // warps per node in the solve
     const double Lfac = p.L[0] / (2.0 * double(N));
 
-    // Chunk j of step n holds slabs [k_lo, k_hi], k_hi = n-1-j*S, in ring
-    // slot j % kRing.  Chunk 0 contains slab n-1, written by the solve of
-    // the previous step; its older slabs and chunks 1..kRing-1 are fetched
-    // ahead (prefetch), before the barriers of the previous step.
+    // The ring as one stream of chunks over the whole run: chunk g (global
+    // count from n0) sits in slot g % kRing, phase parity (g / kRing) & 1.
+    // Chunk j of step n holds slabs [k_lo, k_hi], k_hi = n-1-j*S.  A slot
+    // is refilled by the last warp to release it (a per-slot count in
+    // shared memory), with chunk g + kRing: of this step, or of step n+1
+    // (its chunk 0 without its newest slab n-1+1 = n, which the field solve
+    // of step n has not written yet).  After the grid barriers of step n,
+    // thread 0 issues that newest slab, and the first chunks of step n+1
+    // whose predecessors were not in step n.  No warp waits for another in
+    // the trace; it waits only for its data.
+    auto nchunks_of = [&](int n) { return n > 0 ? (n + S - 1) / S : 0; };
     auto chunk_range = [&](int n, int j, int &k_lo, int &k_hi) {
         k_hi = n - 1 - j * S;
         k_lo = max(0, k_hi - S + 1);
     };
-    auto issue_part = [&](int n, int j, int k_from, int k_to) {  // slabs k_from..k_to of chunk j
+    // bulk copy of slabs k_from..k_to of chunk (n, j) in slot `slot`
+    auto copy_part = [&](int n, int j, unsigned slot, int k_from, int k_to) {
         int k_lo, k_hi;
         chunk_range(n, j, k_lo, k_hi);
-        const unsigned bar = smem_addr(&full_bar[j % kRing]);
-        bulk_g2s(smem_addr(ring + (j % kRing) * S * N + (k_from - k_lo) * N), tables + (long long)k_from * p.table_stride,
-                 unsigned(k_to - k_from + 1) * slab_bytes, bar);
+        bulk_g2s(smem_addr(ring + slot * S * TS + (k_from - k_lo) * TS), tables + (long long)k_from * p.table_stride,
+                 unsigned(k_to - k_from + 1) * slab_bytes, smem_addr(&full_bar[slot]));
     };
-    auto expect_chunk = [&](int n, int j) {
+    // arm slot for the whole chunk (n, j), then copy slabs k_lo..k_last
+    auto issue = [&](int n, int j, unsigned slot, int k_last) {
         int k_lo, k_hi;
         chunk_range(n, j, k_lo, k_hi);
-        mbar_expect_tx(smem_addr(&full_bar[j % kRing]), unsigned(k_hi - k_lo + 1) * slab_bytes);
+        mbar_expect_tx(smem_addr(&full_bar[slot]), unsigned(k_hi - k_lo + 1) * slab_bytes);
+        if (k_last >= k_lo) copy_part(n, j, slot, k_lo, k_last);
     };
-    // for step n: everything but slab n-1 of chunk 0 (thread 0 only)
-    auto prefetch = [&](int n) {
-        const int nchunks = (n + S - 1) / S;
-        for (int j = 0; j < kRing && j < nchunks; ++j) {
-            expect_chunk(n, j);
+    // Thread 0 at the start of step m (after the barriers of step m-1, or
+    // at launch): complete chunk 0's newest slab, issue the first chunks
+    // whose predecessor chunk g - kRing is older than step m-1.
+    unsigned gbase = 0, gbase_prev = 0;  // first chunk of this / the previous step
+    auto start_step = [&](int m, bool first) {
+        const int nch = nchunks_of(m);
+        for (int j = 0; j < kRing && j < nch; ++j) {
+            const unsigned g = gbase + j;
+            const bool pred_prev = !first && g >= unsigned(kRing) && g - kRing >= gbase_prev;
             int k_lo, k_hi;
-            chunk_range(n, j, k_lo, k_hi);
-            if (j == 0) {
-                if (k_hi - 1 >= k_lo) issue_part(n, 0, k_lo, k_hi - 1);
-            } else {
-                issue_part(n, j, k_lo, k_hi);
-            }
+            chunk_range(m, j, k_lo, k_hi);
+            if (!pred_prev)
+                issue(m, j, g % kRing, k_hi);
+            else if (j == 0)
+                copy_part(m, 0, g % kRing, k_hi, k_hi);
         }
     };
-    bool prefetched = false;
-    // Grid barrier; if it gives up, first complete and drain any copies
-    // still in flight into this block's shared memory, then leave.
+    // The last warp to release chunk g of step n (local j) refills its slot.
+    auto refill = [&](int n, int j, unsigned g) {
+        const unsigned slot = g % kRing;
+        const int nch = nchunks_of(n);
+        const int jj = j + kRing;
+        if (jj < nch) {
+            int k_lo, k_hi;
+            chunk_range(n, jj, k_lo, k_hi);
+            issue(n, jj, slot, k_hi);
+        } else if (n + 1 <= n1 && jj - nch < nchunks_of(n + 1)) {
+            const int j1 = jj - nch;
+            int k_lo, k_hi;
+            chunk_range(n + 1, j1, k_lo, k_hi);
+            issue(n + 1, j1, slot, j1 == 0 ? k_hi - 1 : k_hi);  // slab n comes after the barriers
+        }
+    };
+    // Drain on a failed barrier during step n (gbase already advanced to
+    // step n+1): copies of step n+1 issued by refill are completed (chunk
+    // 0's newest slab issued too) and waited for.
+    auto drain = [&](int n) {
+        if (threadIdx.x != 0 || n + 1 > n1) return;
+        const int nch1 = nchunks_of(n + 1);
+        for (int j = 0; j < kRing && j < nch1; ++j) {
+            const unsigned g = gbase + j;
+            if (g < unsigned(kRing) || g - kRing < gbase_prev) continue;  // not issued by refill
+            int k_lo, k_hi;
+            chunk_range(n + 1, j, k_lo, k_hi);
+            if (j == 0) copy_part(n + 1, 0, g % kRing, k_hi, k_hi);
+            mbar_wait(smem_addr(&full_bar[g % kRing]), (g / kRing) & 1u);
+        }
+    };
     auto barrier = [&](int n) -> bool {
         if (grid_barrier(count, target, abort, err)) return true;
-        if (prefetched && threadIdx.x == 0) {
-            issue_part(n + 1, 0, n, n);
-            const int nch = (n + 1 + S - 1) / S;
-            for (int j = 0; j < kRing && j < nch; ++j) mbar_wait(smem_addr(&full_bar[j % kRing]), uses[j % kRing] & 1u);
-        }
+        drain(n);
         return false;
     };
 
@@ -168,38 +208,31 @@ __global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
             dwT[q] = slo[q];
             dwTc[q] = 0.0f;
         }
-        if (n > 0) {
-            const int nchunks = (n + S - 1) / S;
-            if (threadIdx.x == 0) {
-                fence_proxy_async_global();
-                if (!prefetched) prefetch(n);
-                issue_part(n, 0, n - 1, n - 1);  // the newest slab
-            }
+        const int nchunks = nchunks_of(n);
+        if (threadIdx.x == 0 && nchunks > 0) {
+            fence_proxy_async_global();
+            start_step(n, n == n0);
+        }
+        if (nchunks > 0) {
             bool ok = true;
             for (int j = 0; j < nchunks; ++j) {
-                const int slot = j % kRing;
-                ok &= mbar_wait(smem_addr(&full_bar[slot]), uses[slot] & 1u);
-                const float4 *__restrict__ chunk = ring + slot * S * N;
+                const unsigned g = gbase + j, slot = g % kRing;
+                ok &= mbar_wait(smem_addr(&full_bar[slot]), (g / kRing) & 1u);
+                const float *__restrict__ chunk = ring + slot * S * TS;
                 int k_lo, k_hi;
                 chunk_range(n, j, k_lo, k_hi);
-                trace_chunk<PPT, POW2>(chunk, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err);
-                __syncthreads();  // everyone is done with this slot
-                ++uses[slot];
-                if (threadIdx.x == 0 && j + kRing < nchunks) {
-                    expect_chunk(n, j + kRing);
-                    int lo, hi;
-                    chunk_range(n, j + kRing, lo, hi);
-                    issue_part(n, j + kRing, lo, hi);
+                trace_chunk<PPT, POW2>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err);
+                __syncwarp();
+                if (lane == 0 && atom_add_acq_rel_cta(&released[slot], 1u) == unsigned(W - 1)) {
+                    released[slot] = 0;
+                    fence_proxy_async_shared();
+                    refill(n, j, g);
                 }
             }
             if (!ok) atomicOr(err, kErrStageTimeout);
         }
-        // the next step's older slabs load during this step's barriers
-        prefetched = false;
-        if (n + 1 <= n1 && n + 1 > 0) {
-            if (threadIdx.x == 0) prefetch(n + 1);
-            prefetched = true;
-        }
+        gbase_prev = gbase;
+        gbase += nchunks;
         double acc = 0;
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
@@ -273,8 +306,7 @@ __global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
             double *slab = hist + (long long)n * p.hist_stride;
             slab[node] = v[0];
             if (node + N < p.P[0]) slab[node + N] = v[0];
-            reinterpret_cast<float4 *>(tables + (long long)n * p.table_stride)[node] =
-                make_float4(float(v[2]), float(v[3]), float(v[4]), 0.0f);
+            store_kick_entry(tables + (long long)n * p.table_stride, N, node, float(v[2]), float(v[3]), float(v[4]));
             e_local = rs[node] * v[1];
         }
         const double eb = block_sum(e_local, red);
@@ -289,12 +321,7 @@ __global__ void __launch_bounds__(512, 1) run_split_1d_kernel(
             if (threadIdx.x == 0) energy[n] = tot * Lfac;
         }
     }
-    // no bulk copy may be in flight when the block exits
-    if (prefetched) {
-        bool ok = true;
-        for (int r = 0; r < kRing; ++r) ok &= mbar_wait(smem_addr(&full_bar[r]), uses[r] & 1u);
-        if (!ok) atomicOr(err, kErrStageTimeout);
-    }
+    // refill issues nothing past step n1: no bulk copy is in flight here
 }
 
 namespace {
@@ -333,6 +360,7 @@ PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const
 {
     PersistentRun pr;
     if (!sh.ok || p.dim != 1 || plan.nconv != 5 || sh.threads > 512 || sh.threads < 32) return pr;
+    if (sh.ppt > 4 && sh.threads > 256) return pr;  // launch bounds of the PPT > 4 instances
     const int W = sh.threads / 32;
     const int K = (p.N[0] + sh.ctas - 1) / sh.ctas;  // nodes per CTA in reduce/solve
     if (K > W || sh.ctas > sms) return pr;
@@ -341,7 +369,7 @@ PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const
     pr.tpn = sh.tpn;
     pr.ppt = sh.ppt;
     pr.slabs_per_chunk = sh.slabs_per_chunk;
-    const size_t ring = size_t(kRing) * sh.slabs_per_chunk * p.N[0] * sizeof(float4);
+    const size_t ring = size_t(kRing) * sh.slabs_per_chunk * size_t(p.table_stride) * sizeof(float);
     pr.smem = std::max(ring + size_t(6) * p.N[0] * sizeof(double), sh.smem);
     if (pr.smem > 220 * 1024) return pr;
     pr.ok = true;

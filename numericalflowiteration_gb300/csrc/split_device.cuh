@@ -66,6 +66,22 @@ __device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned
 // its later bulk copies (async proxy) read it.
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
+// Orders this thread's (and, after a __syncwarp, its warp's) earlier
+// generic-proxy accesses to shared memory before its later bulk copies.
+__device__ __forceinline__ void fence_proxy_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Shared-memory atomic add with acquire-release semantics at CTA scope;
+// returns the old value.
+__device__ __forceinline__ unsigned atom_add_acq_rel_cta(unsigned *p, unsigned v)
+{
+    unsigned old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;"
+                 : "=r"(old)
+                 : "r"(smem_addr(p)), "r"(v)
+                 : "memory");
+    return old;
+}
+
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p)
 {
     unsigned v;
@@ -183,7 +199,7 @@ namespace nufi_gb300 {
 namespace split {
 
 // Substeps k_hi..k_lo (descending) of PPT chains over a chunk of tables in
-// shared memory (slab k at chunk + (k - k_lo) * N, float4 per cell).
+// shared memory (slab k at chunk + (k - k_lo) * TS floats, kick_lookup layout).
 // State per chain: cell I, fraction xi, and the kick sum in two levels:
 // dwT (+ Kahan term dwTc) holds the sum up to the previous chunk and
 // starts at sig_lo, the low part of the free-streaming fraction; dwC sums
@@ -192,16 +208,16 @@ namespace split {
 //           floor(t) by a round-down add of 1.5*2^23, whose bit pattern
 //           minus S0m = S0 + bits(1.5*2^23) moves the cell
 //   kick:   dwC += K (A + B xi + C xi^2) of the cell (halved for k = 0)
-// 13 FP32/INT instructions and one 16-byte shared load per substep.
+// 13 FP32/INT instructions and two shared loads (8 + 4 bytes) per substep.
 template <int PPT, bool POW2>
-__device__ __forceinline__ void trace_chunk(const float4 *__restrict__ chunk, int k_hi, int k_lo, int N,
+__device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int TS, int k_hi, int k_lo, int N,
                                             int (&I)[PPT], float (&xi)[PPT], float (&dwT)[PPT], float (&dwTc)[PPT],
                                             const float (&shi)[PPT], const int (&S0m)[PPT], unsigned *err)
 {
     float dwC[PPT];
 #pragma unroll
     for (int q = 0; q < PPT; ++q) dwC[q] = 0.0f;
-    auto substep = [&](const float4 *__restrict__ tk, float h) {
+    auto substep = [&](const float *__restrict__ tk, float h) {
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
             const float t = ((xi[q] - shi[q]) - dwT[q]) - dwC[q];
@@ -219,13 +235,12 @@ __device__ __forceinline__ void trace_chunk(const float4 *__restrict__ chunk, in
             }
             I[q] = J;
             xi[q] = t - (mg - kMagic);
-            const float4 T = tk[J];
-            const float kq = fmaf(xi[q], fmaf(xi[q], T.z, T.y), T.x);
+            const float kq = kick_lookup(tk, N, J, xi[q]);
             dwC[q] = (h == 1.0f) ? dwC[q] + kq : fmaf(h, kq, dwC[q]);
         }
     };
     const int k_stop = max(k_lo, 1);
-    for (int k = k_hi; k >= k_stop; --k) substep(chunk + (k - k_lo) * N, 1.0f);
+    for (int k = k_hi; k >= k_stop; --k) substep(chunk + (k - k_lo) * TS, 1.0f);
     if (k_lo == 0) substep(chunk, 0.5f);
     // fold this chunk's kicks into the compensated total
 #pragma unroll

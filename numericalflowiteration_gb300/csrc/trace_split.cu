@@ -135,20 +135,17 @@ __global__ void __launch_bounds__(256) trace_split_1d_kernel(const Problem p, co
 
     if (n > 0) {
         for (int k = n - 1; k >= 1; --k) {
-            const float4 *__restrict__ tk = reinterpret_cast<const float4 *>(tables + (long long)k * p.table_stride);
+            const float *__restrict__ tk = tables + (long long)k * p.table_stride;
 #pragma unroll
             for (int q = 0; q < PPT; ++q) {
                 drift_split<POW2>(I[q], xi[q], dw[q], dwc[q], shi[q], slo[q], S0[q], N, err);
-                const float4 T = __ldg(tk + I[q]);
-                kick_split<COMP>(dw[q], dwc[q], fmaf(xi[q], fmaf(xi[q], T.z, T.y), T.x));
+                kick_split<COMP>(dw[q], dwc[q], kick_lookup_ldg(tk, N, I[q], xi[q]));
             }
         }
-        const float4 *__restrict__ t0 = reinterpret_cast<const float4 *>(tables);
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
             drift_split<POW2>(I[q], xi[q], dw[q], dwc[q], shi[q], slo[q], S0[q], N, err);
-            const float4 T = __ldg(t0 + I[q]);
-            kick_split<COMP>(dw[q], dwc[q], 0.5f * fmaf(xi[q], fmaf(xi[q], T.z, T.y), T.x));
+            kick_split<COMP>(dw[q], dwc[q], 0.5f * kick_lookup_ldg(tables, N, I[q], xi[q]));
         }
     }
 

@@ -12,7 +12,7 @@
 //
 // Geometry: a persistent grid of about one CTA per SM.  Each thread owns
 // one spatial node (x-lanes, so the 32 lanes of a warp read neighbouring
-// cells: conflict-free float4 reads) and PPT velocity nodes, i.e. PPT
+// cells: few bank conflicts) and PPT velocity nodes, i.e. PPT
 // independent dependency chains.  CTA c owns velocity nodes
 // [c*Nm/G, (c+1)*Nm/G).  rho: per thread over its chains (FP64) into
 // partial[c][s]; reduce_rho sums the G rows.
@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
                                                                      int Nr, double *__restrict__ partial,
                                                                      unsigned *err)
 {
-    extern __shared__ __align__(128) float4 ring[];
+    extern __shared__ __align__(128) float ring[];
     __shared__ __align__(8) unsigned long long full_bar[kRing];
     __shared__ double combine[256];
 
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
     }
 
     if (n > 0) {
-        const int slab_f4 = N;                    // float4 per slab
+        const int TS = int(p.table_stride);       // floats per slab
         const int nchunks = (n + S - 1) / S;
         const unsigned slab_bytes = unsigned(p.table_stride) * 4u;
         if (threadIdx.x == 0) {
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
             const unsigned bytes = unsigned(k_hi - k_lo + 1) * slab_bytes;
             const unsigned bar = smem_addr(&full_bar[j % kRing]);
             mbar_expect_tx(bar, bytes);
-            bulk_g2s(smem_addr(ring + (j % kRing) * S * slab_f4), tables + (long long)k_lo * p.table_stride, bytes,
+            bulk_g2s(smem_addr(ring + (j % kRing) * S * TS), tables + (long long)k_lo * p.table_stride, bytes,
                      bar);
         };
         if (threadIdx.x == 0)
@@ -93,10 +93,10 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
         for (int j = 0; j < nchunks; ++j) {
             const int slot = j % kRing;
             ok &= mbar_wait(smem_addr(&full_bar[slot]), unsigned((j / kRing) & 1));
-            const float4 *__restrict__ chunk = ring + slot * S * slab_f4;
+            const float *__restrict__ chunk = ring + slot * S * TS;
             const int k_hi = n - 1 - j * S;
             const int k_lo = max(0, k_hi - S + 1);
-            trace_chunk<PPT, POW2>(chunk, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err);
+            trace_chunk<PPT, POW2>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err);
             __syncthreads();  // everyone is done with this slot
             if (threadIdx.x == 0 && j + kRing < nchunks) issue(j + kRing);
         }

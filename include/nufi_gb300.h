@@ -151,6 +151,24 @@ int nufi_download_energy(nufi_handle *h, int64_t n0, int64_t n1, double *energy)
  * padded slab (stride_t values) out, returns W in *energy.  Blocks. */
 int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double *energy);
 
+/* ---- gradient of the time-integrated field energy ----------------------
+ * No counterpart in the reference.  Objective J = 2 dt sum_{n=0}^{n1} W_n
+ * (the time integral of int |E|^2 dx as a rectangle sum over the steps),
+ * parameters theta = f0_params[0..3] = (alpha, k, u_b, sigma_b) of the 1D
+ * initial conditions (k inside f0 only: the domain stays as configured;
+ * u_b, sigma_b only for the bump-on-tail, else their derivatives are 0).
+ * nufi_forward: steps 0..n1 (as nufi_run) and J.  nufi_objective: J from
+ * the recorded W_n.  nufi_backward: dJ/dtheta (4 doubles) by the adjoint
+ * of the whole backward-traced trajectory in FP64: the coefficient history
+ * of the forward is the only checkpoint, the characteristics are recomputed
+ * and walked back substep by substep (Stormer-Verlet inverted exactly).
+ * 1D, orders 4 and 6; NUFI_ERR_RANGE if the forward has not computed slabs
+ * 0..n1.  Blocks.  The order of the FP64 additions into the slab adjoints
+ * is not fixed: results vary in the last bits between calls. */
+int nufi_forward(nufi_handle *h, int64_t n1, double *J);
+int nufi_objective(nufi_handle *h, int64_t n1, double *J);
+int nufi_backward(nufi_handle *h, int64_t n1, double *grad4);
+
 /* ---- allocation-free rho ------------------------------------------------
  * No counterpart in the reference.  rho of step n over [q_begin, q_end)
  * for callers that must not allocate device memory (no cudaMalloc, no

@@ -40,6 +40,9 @@ SIGNATURES = {
     "nufi_upload_phi_f32": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_compute_metrics": (ctypes.c_int, [_P, _I64, _I64, _I64]),
     "nufi_describe": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    "nufi_forward": (ctypes.c_int, [_P, _I64, _P]),
+    "nufi_objective": (ctypes.c_int, [_P, _I64, _P]),
+    "nufi_backward": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_download_metrics": (ctypes.c_int, [_P, _P]),
     "nufi_step": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_run": (ctypes.c_int, [_P, _I64, _I64, _P]),
@@ -146,6 +149,27 @@ class Simulation:
     def compute_rho(self, n: int, q_begin: int = 0, q_end: int | None = None):
         q_end = self.n_points if q_end is None else q_end
         self._check(self._lib.nufi_compute_rho(self._h, n, q_begin, q_end))
+
+    # -- gradient of J = 2 dt sum_n W_n (no reference counterpart) ----------
+    def forward(self, n1: int | None = None) -> float:
+        """Steps 0..n1 and J = 2 dt sum_{n<=n1} W_n."""
+        n1 = self.cfg.Nt if n1 is None else n1
+        J = ctypes.c_double()
+        self._check(self._lib.nufi_forward(self._h, n1, ctypes.byref(J)))
+        return J.value
+
+    def objective(self, n1: int | None = None) -> float:
+        n1 = self.cfg.Nt if n1 is None else n1
+        J = ctypes.c_double()
+        self._check(self._lib.nufi_objective(self._h, n1, ctypes.byref(J)))
+        return J.value
+
+    def backward(self, n1: int | None = None) -> np.ndarray:
+        """dJ/d(alpha, k, u_b, sigma_b) by the adjoint of the forward run."""
+        n1 = self.cfg.Nt if n1 is None else n1
+        g = np.zeros(4)
+        self._check(self._lib.nufi_backward(self._h, n1, _ptr(g)))
+        return g
 
     def describe(self) -> dict:
         """Kernels and launch shapes this handle chose."""

@@ -54,6 +54,14 @@ struct nufi_handle {
     float2 *phase = nullptr;
     double *mpartial = nullptr;  // [4][trace blocks] metrics block sums
     double *metrics = nullptr;   // [4]
+    // adjoint (allocated on first nufi_backward)
+    AdjointPlan aplan;
+    double *mu = nullptr;         // (Nt+1) x P slab adjoints
+    double *lambda = nullptr;     // [Ns]
+    double *theta_acc = nullptr;  // [4][adjoint blocks]
+    double *grad = nullptr;       // [4]
+    std::vector<char> slab_set;   // slab n written (step, run, upload_phi)
+    std::vector<char> energy_set; // W_n recorded (step, run)
     SolvePlan plan;
     bool solve_ok = false;
     std::string solve_why;
@@ -430,6 +438,14 @@ int check_device_flags(nufi_handle *h)
     return NUFI_OK;
 }
 
+void mark_steps(nufi_handle *h, int64_t n0, int64_t n1, bool energy)
+{
+    for (int64_t n = n0; n <= n1; ++n) {
+        h->slab_set[size_t(n)] = 1;
+        if (energy) h->energy_set[size_t(n)] = 1;
+    }
+}
+
 int sync_and_check(nufi_handle *h)
 {
     NUFI_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -570,6 +586,9 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
         (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMemset"));
     if ((st = build_solve_plan(h.get(), sms > 0 ? sms : 1))) return bail(st);
+    h->slab_set.assign(nslab, 0);
+    h->energy_set.assign(nslab, 0);
+    h->aplan = adjoint_plan_1d(p);
     if (h->solve_ok && h->staged.ok) {
         const char *pers = std::getenv("NUFI_PERSISTENT");
         if (!(pers && pers[0] == '0')) {
@@ -678,6 +697,7 @@ static int upload_slab(nufi_handle *h, int64_t n, const double *slab)
         if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
         h->launches += 1;
     }
+    h->slab_set[size_t(n)] = 1;
     NUFI_CUDA(h, cudaStreamSynchronize(h->stream));
     return NUFI_OK;
 }
@@ -707,6 +727,7 @@ int nufi_step(nufi_handle *h, int64_t n, double *energy)
     DeviceGuard g(h->device);
     int st = enqueue_step(h, n);
     if (st) return st;
+    mark_steps(h, n, n, true);
     if (energy) {
         NUFI_CUDA(h, cudaMemcpyAsync(energy, h->energy + n, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         return sync_and_check(h);
@@ -727,6 +748,7 @@ int nufi_run(nufi_handle *h, int64_t n0, int64_t n1, double *energy_hist)
                                             h->rho, h->energy, int(n0), int(n1), h->err, h->stream);
         if (e == cudaSuccess) {
             h->launches += 1;
+            mark_steps(h, n0, n1, true);
             if (energy_hist) {
                 NUFI_CUDA(h, cudaMemcpyAsync(energy_hist, h->energy + n0, size_t(n1 - n0 + 1) * sizeof(double),
                                              cudaMemcpyDeviceToHost, h->stream));
@@ -763,6 +785,7 @@ int nufi_run(nufi_handle *h, int64_t n0, int64_t n1, double *energy_hist)
     }
     NUFI_CUDA(h, cudaGraphLaunch(it->second.first, h->stream));
     h->launches += it->second.second;
+    mark_steps(h, n0, n1, true);
     if (energy_hist) {
         NUFI_CUDA(h, cudaMemcpyAsync(energy_hist, h->energy + n0, size_t(n1 - n0 + 1) * sizeof(double),
                                      cudaMemcpyDeviceToHost, h->stream));
@@ -842,6 +865,65 @@ int nufi_launch_count(const nufi_handle *h, int64_t *count)
     if (!h || !count) return fail(nullptr, NUFI_ERR_INVALID, "null argument");
     *count = h->launches;
     return NUFI_OK;
+}
+
+int nufi_objective(nufi_handle *h, int64_t n1, double *J)
+{
+    if (!h || !J) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (n1 < 0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step outside [0, Nt]");
+    for (int64_t n = 0; n <= n1; ++n)
+        if (!h->energy_set[size_t(n)])
+            return fail(h, NUFI_ERR_RANGE, "objective: W_n of steps 0..n1 not computed (run the forward first)");
+    DeviceGuard g(h->device);
+    std::vector<double> w(size_t(n1 + 1));
+    NUFI_CUDA(h, cudaMemcpyAsync(w.data(), h->energy, w.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    int st = sync_and_check(h);
+    if (st) return st;
+    double s = 0;
+    for (double v : w) s += v;
+    *J = 2.0 * h->cfg.dt * s;
+    return NUFI_OK;
+}
+
+int nufi_forward(nufi_handle *h, int64_t n1, double *J)
+{
+    int st = nufi_run(h, 0, n1, nullptr);
+    if (st) return st;
+    return J ? nufi_objective(h, n1, J) : NUFI_OK;
+}
+
+int nufi_backward(nufi_handle *h, int64_t n1, double *grad)
+{
+    if (!h || !grad) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (n1 < 0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step outside [0, Nt]");
+    if (!h->aplan.ok)
+        return fail(h, NUFI_ERR_UNSUPPORTED, "backward: built for 1D, orders 4 and 6 (odd-degree splines)");
+    if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
+    for (int64_t n = 0; n <= n1; ++n)
+        if (!h->slab_set[size_t(n)])
+            return fail(h, NUFI_ERR_RANGE, "backward: slabs 0..n1 not present (run the forward first)");
+    DeviceGuard g(h->device);
+    const Problem &p = h->p;
+    const AdjointPlan &ap = h->aplan;
+    const size_t blocks = size_t(ap.grid_x) * ap.grid_y;
+    const size_t mu_n = size_t(h->cfg.Nt + 1) * p.P[0];
+    if (!h->mu) {
+        cudaError_t e;
+        if ((e = dalloc(h, &h->mu, mu_n)) != cudaSuccess || (e = dalloc(h, &h->lambda, size_t(p.Ns))) != cudaSuccess ||
+            (e = dalloc(h, &h->theta_acc, 4 * blocks)) != cudaSuccess || (e = dalloc(h, &h->grad, 4)) != cudaSuccess)
+            return cuda_fail(h, e, "cudaMalloc");
+    }
+    NUFI_CUDA(h, cudaMemsetAsync(h->mu, 0, mu_n * sizeof(double), h->stream));
+    NUFI_CUDA(h, cudaMemsetAsync(h->theta_acc, 0, 4 * blocks * sizeof(double), h->stream));
+    cudaError_t e = launch_adjoint_1d(p, ap, h->hist, h->plan.green, h->mu, h->lambda, h->theta_acc, int(n1), h->err,
+                                      h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "adjoint launch");
+    h->launches += 2 * (n1 + 1);
+    e = launch_reduce_metrics((long long)blocks, h->theta_acc, h->grad, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "adjoint reduce launch");
+    h->launches += 1;
+    NUFI_CUDA(h, cudaMemcpyAsync(grad, h->grad, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return sync_and_check(h);
 }
 
 int nufi_describe(const nufi_handle *h, char *buf, size_t len)

@@ -171,6 +171,19 @@ PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const
 cudaError_t launch_run_split_1d(const Problem &p, const PersistentRun &pr, const SolvePlan &plan, float *tables,
                                 double *hist, const SplitNode *nodes, const float2 *phase, double *partial,
                                 double *rho, double *energy, int n0, int n1, unsigned *err, cudaStream_t st);
+// Reverse-mode gradient of J = 2 dt sum_n W_n with respect to f0's
+// (alpha, k, u_b, sigma_b), 1D, FP64 (adjoint_1d.cu).  mu: (Nt+1) x P
+// slab adjoints (zeroed by the caller), theta_acc: [4][grid_x*grid_y]
+// (zeroed by the caller).
+constexpr int kAdjointPPT = 4;
+struct AdjointPlan {
+    bool ok = false;
+    int threads = 0, grid_x = 0, grid_y = 0, chunk = 1;
+};
+AdjointPlan adjoint_plan_1d(const Problem &p);
+cudaError_t launch_adjoint_1d(const Problem &p, const AdjointPlan &ap, const double *hist, const double *gc,
+                              double *mu, double *lambda, double *theta_acc, int n1, unsigned *err, cudaStream_t st);
+
 // FP32 table of one FP64 slab (after upload_phi).
 cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st);
 

@@ -652,6 +652,127 @@ int oracle_run(const nufi_config *cfg, int64_t n0, int64_t n1, double *coeffs, d
     return st;
 }
 
+/* ---- forward-mode derivative of J = 2 dt sum_{n<=n1} W_n (1D) ------------
+ * The check of the GPU adjoint: every quantity of the 1D loop carries its
+ * derivative with respect to theta = (alpha, k, u_b, sigma_b) (4 tangent
+ * directions at once):  per point (x, u) and (dx_i, du_i) through the trace,
+ *   x -= dt u              dx_i -= dt du_i
+ *   E = -S'_k(x)/dx        dE_i = -S''_k(x)/dx^2 dx_i - dS'_k[dc_k,i](x)/dx
+ *   u += h dt E            du_i += h dt dE_i
+ * then df~_i = f0_x dx_i + f0_u du_i + df0/dtheta_i at the foot,
+ * drho_i = -w sum df~_i, dc_n,i = the (linear) field solve of drho_i, and
+ * dW_n,i = L/N sum_s (drho_i - mean drho_i) phi_n (W = L/(2N) rho'.G rho'
+ * with G symmetric).  The foot derivatives of f0 are those of nufi_f0.h
+ * (k inside f0 only, the domain fixed; x unwrapped, as the reference
+ * evaluates f0). */
+static void oc_f0_grad_1d(const oc_t *o, double x, double u, double *fx, double *fu, double *dth)
+{
+    const double alpha = o->p[0], k = o->p[1], c0 = 0.39894228040143267793994;
+    const double ck = cos(k * x), sk = sin(k * x), sp = 1. + alpha * ck;
+    double g, gu, gub = 0, gsb = 0;
+    if (o->f0_kind == NUFI_F0_LANDAU) {
+        g = c0 * exp(-u * u / 2); gu = -u * g;
+    } else if (o->f0_kind == NUFI_F0_TWO_STREAM) {
+        const double e = c0 * exp(-u * u / 2.);
+        g = e * u * u; gu = e * u * (2. - u * u);
+    } else {
+        const double ub = o->p[2], sb = o->p[3], z = (u - ub) / sb;
+        const double e1 = c0 * exp(-u * u / 2), e2 = c0 / sb * exp(-z * z / 2);
+        g = 0.9 * e1 + 0.1 * e2;
+        gu = -0.9 * u * e1 - 0.1 * z / sb * e2;
+        gub = 0.1 * z / sb * e2;
+        gsb = 0.1 * (z * z - 1.) / sb * e2;
+    }
+    *fx = -alpha * k * sk * g;
+    *fu = sp * gu;
+    dth[0] = ck * g; dth[1] = -alpha * x * sk * g; dth[2] = sp * gub; dth[3] = sp * gsb;
+}
+
+int oracle_objective_tangent(const nufi_config *cfg, int64_t n1, double *J, double *dJ, int nthreads)
+{
+    oc_t o; int st = oc_setup(cfg, &o); int64_t n; int i;
+    double *coeffs, *dco[4], *rho, *drho[4], *phi, *work;
+    if (st) return st;
+    if (o.dim != 1) return NUFI_ERR_UNSUPPORTED;
+    if (n1 < 0 || (size_t)n1 > o.Nt) return NUFI_ERR_RANGE;
+    coeffs = (double *)calloc((o.Nt + 1) * o.stride_t, sizeof(double));
+    rho = (double *)malloc(sizeof(double) * o.Ns);
+    phi = (double *)malloc(sizeof(double) * o.Ns);
+    work = (double *)malloc(sizeof(double) * o.stride_t);
+    for (i = 0; i < 4; ++i) {
+        dco[i] = (double *)calloc((o.Nt + 1) * o.stride_t, sizeof(double));
+        drho[i] = (double *)malloc(sizeof(double) * o.Ns);
+    }
+    *J = 0;
+    for (i = 0; i < 4; ++i) dJ[i] = 0;
+    for (n = 0; n <= n1 && !st; ++n) {
+        const double w = oc_weight_v(&o);
+        long long s;
+        double W, mean[4] = {0, 0, 0, 0};
+        (void)nthreads;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
+        for (s = 0; s < (long long)o.Ns; ++s) {
+            double acc = 0, dacc[4] = {0, 0, 0, 0};
+            size_t m;
+            for (m = 0; m < o.Nm; ++m) {
+                double x, u, dx[4] = {0, 0, 0, 0}, du[4] = {0, 0, 0, 0}, fx, fu, dth[4];
+                size_t k;
+                int a;
+                { double xx[3], uu[3]; oc_point(&o, (size_t)s, m, xx, uu); x = xx[0]; u = uu[0]; }
+                for (k = (size_t)n; k-- > 0;) {
+                    const double h = k == 0 ? 0.5 : 1.0;
+                    const double *c = coeffs + k * o.stride_t;
+                    size_t ii; double xi, w1[OC_MAX_ORDER], w2[OC_MAX_ORDER], S1 = 0, S2 = 0, E, Ep;
+                    int j;
+                    x = x - o.dt * u;
+                    for (a = 0; a < 4; ++a) dx[a] = dx[a] - o.dt * du[a];
+                    oc_locate(&o, 0, x, &ii, &xi);
+                    oc_N(o.order, 1, xi, w1);
+                    oc_N(o.order, 2, xi, w2);
+                    for (j = 0; j < o.order; ++j) { S1 += c[ii + j] * w1[j]; S2 += c[ii + j] * w2[j]; }
+                    E = -o.dxinv[0] * S1;
+                    Ep = -o.dxinv[0] * o.dxinv[0] * S2;
+                    for (a = 0; a < 4; ++a) {
+                        const double *dc = dco[a] + k * o.stride_t;
+                        double dS1 = 0;
+                        for (j = 0; j < o.order; ++j) dS1 += dc[ii + j] * w1[j];
+                        du[a] = du[a] + h * o.dt * (Ep * dx[a] - o.dxinv[0] * dS1);
+                    }
+                    u = u + h * o.dt * E;
+                }
+                { double xx[3] = {x, 0, 0}, uu[3] = {u, 0, 0}; acc += oc_f0(&o, xx, uu); }
+                oc_f0_grad_1d(&o, x, u, &fx, &fu, dth);
+                for (a = 0; a < 4; ++a) dacc[a] += fx * dx[a] + fu * du[a] + dth[a];
+            }
+            rho[s] = -w * acc;
+            for (i = 0; i < 4; ++i) drho[i][s] = -w * dacc[i];
+        }
+        /* primal: phi (Poisson in place on a copy) and slab n */
+        memcpy(phi, rho, sizeof(double) * o.Ns);
+        W = oc_poisson(&o, phi);
+        st = oc_interpolate(&o, phi, coeffs + (size_t)n * o.stride_t);
+        *J += 2.0 * o.dt * W;
+        for (i = 0; i < 4 && !st; ++i) {
+            double dW = 0; long long l;
+            for (l = 0; l < (long long)o.Ns; ++l) mean[i] += drho[i][l];
+            mean[i] /= (double)o.Ns;
+            for (l = 0; l < (long long)o.Ns; ++l) dW += (drho[i][l] - mean[i]) * phi[l];
+            dJ[i] += 2.0 * o.dt * o.L[0] / (double)o.Ns * dW;
+            /* tangent slab: the same linear solve of drho */
+            {
+                double e;
+                memcpy(work, drho[i], sizeof(double) * o.Ns);
+                e = oc_poisson(&o, work);
+                (void)e;
+                st = oc_interpolate(&o, work, dco[i] + (size_t)n * o.stride_t);
+            }
+        }
+    }
+    free(coeffs); free(rho); free(phi); free(work);
+    for (i = 0; i < 4; ++i) { free(dco[i]); free(drho[i]); }
+    return st;
+}
+
 int oracle_sizes(const nufi_config *cfg, int64_t *stride_t, int64_t *ns, int64_t *nq)
 {
     oc_t o; int st = oc_setup(cfg, &o);

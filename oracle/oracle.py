@@ -56,6 +56,7 @@ def lib():
         L.oracle_run.argtypes = [P, i64, i64, P, P, P, ctypes.c_int]
         L.oracle_sizes.argtypes = [P, P, P, P]
         L.oracle_set_summation.argtypes = [ctypes.c_int]
+        L.oracle_objective_tangent.argtypes = [P, i64, P, P, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -97,6 +98,24 @@ def run(cfg, n0: int = 0, n1: int | None = None, coeffs: np.ndarray | None = Non
                           nthreads or threads())
     _check(st, "run")
     return energy, (rho.reshape(n1 - n0 + 1, cfg.n_spatial) if keep_rho else None), coeffs
+
+
+def objective(cfg, n1: int | None = None, nthreads=None) -> float:
+    """J = 2 dt sum_{n<=n1} W_n of the reference loop (oracle_run)."""
+    n1 = cfg.Nt if n1 is None else n1
+    energy, _, _ = run(cfg, 0, n1, keep_rho=False, nthreads=nthreads)
+    return 2.0 * cfg.dt * float(np.sum(energy))
+
+
+def objective_tangent(cfg, n1: int | None = None, nthreads=None):
+    """(J, dJ/d(alpha, k, u_b, sigma_b)) by forward-mode differentiation of
+    the 1D loop in FP64 (oracle_objective_tangent)."""
+    n1 = cfg.Nt if n1 is None else n1
+    c, p = _cfg(cfg)
+    J = np.zeros(1)
+    dJ = np.zeros(4)
+    _check(lib().oracle_objective_tangent(p, n1, _ptr(J), _ptr(dJ), nthreads or threads()), "objective_tangent")
+    return float(J[0]), dJ
 
 
 def rho(cfg, n: int, coeffs: np.ndarray, q_begin: int = 0, q_end: int | None = None, nthreads=None):

@@ -169,6 +169,29 @@ int nufi_forward(nufi_handle *h, int64_t n1, double *J);
 int nufi_objective(nufi_handle *h, int64_t n1, double *J);
 int nufi_backward(nufi_handle *h, int64_t n1, double *grad4);
 
+/* ---- batches of 1D instances --------------------------------------------
+ * No counterpart in the reference.  Many 1D1V parameter sets of uneven
+ * grid sizes (Nx dividing 256, any Nv, Nt; one precision, order 4) advanced
+ * together: each time step is one trace launch over the work units of all
+ * instances (256 threads x the tuned chains per thread over one instance's
+ * velocity slice), one rho reduction and one field solve for all; the
+ * whole run (and the whole adjoint sweep) is one CUDA-graph launch.
+ * nufi_batch_create runs the autotuner (launch shapes timed on the device;
+ * NUFI_BATCH_TUNE=0 keeps defaults) and reports its choice through
+ * nufi_batch_describe.  nufi_batch_forward: J_i = 2 dt sum_n W_n of every
+ * instance (count doubles, may be NULL).  nufi_batch_backward: dJ_i/d(alpha,
+ * k, u_b, sigma_b) (count x 4 doubles; the FP64 adjoint of nufi_backward).
+ * Errors: nufi_batch_last_error(batch) (or NULL after a failed create). */
+typedef struct nufi_batch nufi_batch;
+int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_batch **out);
+int nufi_batch_destroy(nufi_batch *b);
+const char *nufi_batch_last_error(const nufi_batch *b);
+int nufi_batch_forward(nufi_batch *b, double *J);
+int nufi_batch_backward(nufi_batch *b, double *grad);
+int nufi_batch_energy(nufi_batch *b, int32_t i, double *energy);
+int nufi_batch_stream(const nufi_batch *b, void **stream);
+int nufi_batch_describe(const nufi_batch *b, char *buf, size_t len);
+
 /* ---- allocation-free rho ------------------------------------------------
  * No counterpart in the reference.  rho of step n over [q_begin, q_end)
  * for callers that must not allocate device memory (no cudaMalloc, no

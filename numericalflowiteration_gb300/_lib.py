@@ -19,7 +19,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .config import Config
+from .config import Config, NufiConfigC
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "libnufi_gb300.so"
@@ -43,6 +43,14 @@ SIGNATURES = {
     "nufi_forward": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_objective": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_backward": (ctypes.c_int, [_P, _I64, _P]),
+    "nufi_batch_create": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int, _P]),
+    "nufi_batch_destroy": (ctypes.c_int, [_P]),
+    "nufi_batch_last_error": (ctypes.c_char_p, [_P]),
+    "nufi_batch_forward": (ctypes.c_int, [_P, _P]),
+    "nufi_batch_backward": (ctypes.c_int, [_P, _P]),
+    "nufi_batch_energy": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+    "nufi_batch_stream": (ctypes.c_int, [_P, _P]),
+    "nufi_batch_describe": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "nufi_download_metrics": (ctypes.c_int, [_P, _P]),
     "nufi_step": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_run": (ctypes.c_int, [_P, _I64, _I64, _P]),
@@ -249,3 +257,72 @@ class Simulation:
 
     def synchronize(self):
         self._check(self._lib.nufi_synchronize(self._h))
+
+
+class Batch:
+    """Many 1D instances advanced together (nufi_batch_*): one graph launch
+    for the whole forward, one for the whole adjoint."""
+
+    def __init__(self, cfgs, device: int = 0):
+        self.cfgs = list(cfgs)
+        self._lib = load()
+        arr = (NufiConfigC * len(self.cfgs))(*[c.to_c() for c in self.cfgs])
+        self._arr = arr
+        h = ctypes.c_void_p()
+        st = self._lib.nufi_batch_create(arr, len(self.cfgs), device, ctypes.byref(h))
+        if st:
+            _raise(st, self._lib.nufi_batch_last_error(None).decode())
+        self._h = h
+
+    def _check(self, st: int):
+        if st:
+            _raise(st, self._lib.nufi_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.nufi_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.cfgs)
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._check(self._lib.nufi_batch_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def forward(self) -> np.ndarray:
+        """All steps of every instance; J_i = 2 dt sum_n W_n."""
+        J = np.zeros(len(self.cfgs))
+        self._check(self._lib.nufi_batch_forward(self._h, _ptr(J)))
+        return J
+
+    def backward(self) -> np.ndarray:
+        """dJ_i/d(alpha, k, u_b, sigma_b), shape (count, 4)."""
+        g = np.zeros((len(self.cfgs), 4))
+        self._check(self._lib.nufi_batch_backward(self._h, _ptr(g)))
+        return g
+
+    def energy(self, i: int) -> np.ndarray:
+        e = np.zeros(self.cfgs[i].Nt + 1)
+        self._check(self._lib.nufi_batch_energy(self._h, i, _ptr(e)))
+        return e
+
+    def describe(self) -> dict:
+        import json
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self._lib.nufi_batch_describe(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())

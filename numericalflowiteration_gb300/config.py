@@ -166,6 +166,27 @@ def landau_3d(Nx=16, Nv=32, Nt=100, dt=0.1, alpha=0.01, k=0.5, **kw) -> Config:
                   "landau", [alpha, k], **kw)
 
 
+def batched_bump_on_tail(count=256, seed=20261203, Nt=320, dt=1.0 / 16, nx=(64, 128, 256), nv=(256, 512, 1024),
+                         precision="fp64", **kw):
+    """The batched adjoint configuration: `count` bump-on-tail instances
+    with seeded uniform alpha in [0.01, 0.05], k in [0.3, 0.5], u_b in
+    [4, 5], sigma_b in [0.4, 0.6] and grid sizes drawn from nx x nv
+    (dt = 1/16, T = 20)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        a = float(rng.uniform(0.01, 0.05))
+        k = float(rng.uniform(0.3, 0.5))
+        ub = float(rng.uniform(4.0, 5.0))
+        sb = float(rng.uniform(0.4, 0.6))
+        Nx = int(rng.choice(nx))
+        Nv = int(rng.choice(nv))
+        out.append(bump_on_tail_1d(Nx=Nx, Nv=Nv, Nt=Nt, dt=dt, alpha=a, k=k, u_b=ub, sigma_b=sb,
+                                   precision=precision, **kw))
+    return out
+
+
 WORKLOADS = {
     "landau_1d_64x256_T30": landau_1d,
     "two_stream_1d_256x1024_T50": two_stream_1d,

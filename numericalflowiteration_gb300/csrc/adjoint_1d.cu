@@ -27,83 +27,11 @@
 // so the gradient varies in the last bits from run to run).
 #include <algorithm>
 
-#include "nufi_kernels.cuh"
+#include "adjoint_device.cuh"
 
 namespace nufi_gb300 {
 
-namespace {
-
-struct F0Grad {
-    double fx, fu, dth[4];
-};
-
-// Partial derivatives of the 1D initial conditions (nufi/config.hpp:82-83;
-// the bump-on-tail of the batched configuration) at the foot (x unwrapped,
-// as the reference evaluates f0 there).
-__device__ __forceinline__ F0Grad f0_grad_1d(const Problem &p, double x, double u)
-{
-    const double alpha = p.f0p[0], k = p.f0p[1];
-    const double c0 = 0.39894228040143267793994;
-    double sk, ck;
-    sincos(k * x, &sk, &ck);
-    const double sp = 1. + alpha * ck;
-    double g, gu, gub = 0, gsb = 0;
-    if (p.f0_kind == NUFI_F0_LANDAU) {
-        const double e = c0 * exp(-u * u / 2);
-        g = e;
-        gu = -u * e;
-    } else if (p.f0_kind == NUFI_F0_TWO_STREAM) {
-        const double e = c0 * exp(-u * u / 2.);
-        g = e * u * u;
-        gu = e * u * (2. - u * u);
-    } else {
-        const double ubv = p.f0p[2], sb = p.f0p[3];
-        const double z = (u - ubv) / sb;
-        const double e1 = c0 * exp(-u * u / 2), e2 = c0 / sb * exp(-z * z / 2);
-        g = 0.9 * e1 + 0.1 * e2;
-        gu = -0.9 * u * e1 - 0.1 * z / sb * e2;
-        gub = 0.1 * z / sb * e2;
-        gsb = 0.1 * (z * z - 1.) / sb * e2;
-    }
-    F0Grad r;
-    r.fx = -alpha * k * sk * g;
-    r.fu = sp * gu;
-    r.dth[0] = ck * g;
-    r.dth[1] = -alpha * x * sk * g;
-    r.dth[2] = sp * gub;
-    r.dth[3] = sp * gsb;
-    return r;
-}
-
-// fields.hpp wrap + knot (as trace_fp64.cu's locate_fp64).
-__device__ __forceinline__ int locate_adj(const Problem &p, double x, double &xi, unsigned *err)
-{
-    x -= p.xmin[0];
-    x = x - p.L[0] * floor(x * p.Linv[0]);
-    const double xk = floor(x * p.dxinv[0]);
-    int ii = int(xk);
-    xi = x * p.dxinv[0] - xk;
-    if (ii >= p.N[0]) ii -= p.N[0];
-    if (ii < 0 || ii >= p.N[0]) {
-        atomicOr(err, kErrCellIndex);
-        ii = 0;
-    }
-    return ii;
-}
-
-// E = -dS/dx at x with the primal's arithmetic (trace_fp64.cu field_1d).
-template <int ORDER>
-__device__ __forceinline__ double efield_primal(const Problem &p, const double *__restrict__ c, double x, unsigned *err)
-{
-    double xi;
-    const int ii = locate_adj(p, x, xi, err);
-    double w[ORDER];
-#pragma unroll
-    for (int j = 0; j < ORDER; ++j) w[j] = __ldg(c + ii + j);
-    return -((1 * p.dxinv[0]) * deboor<double, ORDER, 1>(xi, w));
-}
-
-}  // namespace
+using namespace adj;
 
 // Per step m: rebuild the feet, seed, reverse through slabs 0..m-1.
 // Block (T threads = spatial nodes blockIdx.x*T + t), PPT velocity nodes
@@ -116,16 +44,10 @@ __global__ void __launch_bounds__(256) adjoint_trace_1d_kernel(const Problem p, 
                                                                unsigned *err)
 {
     extern __shared__ double mu_s[];  // [chunk][P]
-    __shared__ double red[4][8];
-    const int P = p.P[0], N = p.N[0];
+    const int N = p.N[0];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const long long mb = (long long)blockIdx.y * PPT;
-    const double dt = p.dt, dxinv = p.dxinv[0];
-    const long long hs = p.hist_stride;
-
-    for (int i = threadIdx.x; i < chunk * P; i += blockDim.x) mu_s[i] = 0;
-
-    double x[PPT], u[PPT], xb[PPT], ub[PPT];
+    double x[PPT], u[PPT];
     bool live[PPT];
     const double a = s < N ? -p.wv * lambda[s] : 0.0;
 #pragma unroll
@@ -135,98 +57,10 @@ __global__ void __launch_bounds__(256) adjoint_trace_1d_kernel(const Problem p, 
         x[q] = p.xmin[0] + (s < N ? s : 0) * p.dx[0];
         u[q] = p.vmin[0] + (jm < p.Nm ? jm : 0) * p.dv[0] + p.dv[0] / 2;
     }
-    // 1. the primal trace to the foot (eval_ftilda, same operations)
-    for (int k = m - 1; k >= 1; --k) {
-        const double *c = hist + k * hs;
-#pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            if (!live[q]) continue;
-            x[q] = x[q] - dt * u[q];
-            u[q] = u[q] + dt * efield_primal<ORDER>(p, c, x[q], err);
-        }
-    }
-    if (m > 0) {
-#pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            if (!live[q]) continue;
-            x[q] -= dt * u[q];
-            u[q] += 0.5 * dt * efield_primal<ORDER>(p, hist, x[q], err);
-        }
-    }
-    // 2. seed at the foot
     double th[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int q = 0; q < PPT; ++q) {
-        xb[q] = 0;
-        ub[q] = 0;
-        if (!live[q]) continue;
-        const F0Grad g = f0_grad_1d(p, x[q], u[q]);
-        xb[q] = a * g.fx;
-        ub[q] = a * g.fu;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) th[i] += a * g.dth[i];
-    }
-    __syncthreads();
-    // 3. reverse sweep, slabs 0..m-1 in chunks staged in shared memory
-    for (int k0 = 0; k0 < m; k0 += chunk) {
-        const int k1 = min(m, k0 + chunk);
-        for (int k = k0; k < k1; ++k) {
-            const double h = k == 0 ? 0.5 : 1.0;
-            const double *c = hist + k * hs;
-            double *ms = mu_s + (k - k0) * P;
-#pragma unroll
-            for (int q = 0; q < PPT; ++q) {
-                if (!live[q]) continue;
-                double xi;
-                const int ii = locate_adj(p, x[q], xi, err);
-                double N1[ORDER], N2[ORDER];
-                bspline_basis<double, ORDER, 1>(xi, N1);
-                bspline_basis<double, ORDER, 2>(xi, N2);
-                double s1 = 0, s2 = 0;
-#pragma unroll
-                for (int j = 0; j < ORDER; ++j) {
-                    const double w = __ldg(c + ii + j);
-                    s1 = fma(w, N1[j], s1);
-                    s2 = fma(w, N2[j], s2);
-                }
-                const double E = -dxinv * s1;
-                const double Ep = -dxinv * dxinv * s2;
-                const double coef = ub[q] * h * dt * (-dxinv);
-#pragma unroll
-                for (int j = 0; j < ORDER; ++j) atomicAdd(ms + ii + j, coef * N1[j]);
-                const double xt = xb[q] + ub[q] * h * dt * Ep;
-                xb[q] = xt;
-                ub[q] = ub[q] - dt * xt;
-                u[q] = u[q] - h * dt * E;
-                x[q] = x[q] + dt * u[q];
-            }
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < (k1 - k0) * P; i += blockDim.x) {
-            const double v = mu_s[i];
-            if (v != 0) {
-                atomicAdd(mu + (long long)(k0 + i / P) * P + i % P, v);
-                mu_s[i] = 0;
-            }
-        }
-        __syncthreads();
-    }
-    // 4. this block's dJ/dtheta (fixed-order shuffle tree, warps in order)
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        double v = th[i];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[i][warp] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 4) {
-        double t = red[threadIdx.x][0];
-        for (int w = 1; w < int(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
-        const long long blocks = (long long)gridDim.x * gridDim.y;
-        theta_acc[threadIdx.x * blocks + (long long)blockIdx.y * gridDim.x + blockIdx.x] += t;
-    }
+    adjoint_chains<ORDER, PPT>(p, hist, m, chunk, a, x, u, live, mu_s, mu, th, err);
+    const long long blocks = (long long)gridDim.x * gridDim.y;
+    block_theta_add(th, theta_acc, blocks, (long long)blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // lambda_m = scale * phi_m + G_c^T fold(mu_m), one thread per node.

@@ -955,6 +955,451 @@ int nufi_describe(const nufi_handle *h, char *buf, size_t len)
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
+// Batches of 1D instances (batch_1d.cu): one handle per instance for its
+// buffers, the batch for the unit maps, the autotuned launch shapes and
+// the CUDA graphs of the whole forward and backward.
+// ---------------------------------------------------------------------------
+struct nufi_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int precision = 0;
+    std::vector<nufi_handle *> inst;
+    std::vector<BatchInst> hi;  // host copies of the descriptors
+    BatchInst *d_inst = nullptr;
+    int *unit_inst = nullptr, *node_inst = nullptr, *solve_inst = nullptr, *adj_unit_inst = nullptr;
+    double *theta_acc = nullptr, *grad = nullptr;
+    unsigned *err = nullptr;
+    BatchLaunch L;
+    int maxNt = 0;
+    long long point_steps = 0;
+    cudaGraphExec_t fwd = nullptr, bwd = nullptr;
+    bool forward_done = false;
+    std::string last_error, tune;
+    std::vector<void *> allocations;
+};
+
+namespace {
+
+int bfail(nufi_batch *b, int code, const std::string &msg)
+{
+    if (b) b->last_error = msg;
+    g_last_error = msg;
+    return code;
+}
+
+int bcuda(nufi_batch *b, cudaError_t e, const char *where)
+{
+    return bfail(b, NUFI_ERR_CUDA, std::string(where) + ": " + cudaGetErrorName(e) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+cudaError_t balloc(nufi_batch *b, T **ptr, size_t count)
+{
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(count * sizeof(T), 16));
+    if (e != cudaSuccess) return e;
+    b->allocations.push_back(p);
+    *ptr = static_cast<T *>(p);
+    return cudaSuccess;
+}
+
+void batch_release(nufi_batch *b)
+{
+    if (b->fwd) cudaGraphExecDestroy(b->fwd);
+    if (b->bwd) cudaGraphExecDestroy(b->bwd);
+    b->fwd = b->bwd = nullptr;
+    for (void *p : b->allocations) cudaFree(p);
+    b->allocations.clear();
+    for (nufi_handle *h : b->inst) nufi_destroy(h);
+    b->inst.clear();
+    if (b->stream) cudaStreamDestroy(b->stream);
+    b->stream = nullptr;
+}
+
+int units_of(const nufi_handle *h, int ppt)
+{
+    const int tpn = 256 / h->p.N[0];
+    return int((h->p.Nm + (long long)tpn * ppt - 1) / ((long long)tpn * ppt));
+}
+
+// Forward units for `ppt` chains per thread (descriptors and map uploaded).
+int batch_set_units(nufi_batch *b, int ppt, bool adjoint)
+{
+    std::vector<int> map;
+    for (size_t i = 0; i < b->inst.size(); ++i) {
+        const int u = units_of(b->inst[i], ppt);
+        if (adjoint) {
+            b->hi[i].adj_unit_begin = int(map.size());
+            b->hi[i].adj_units = u;
+        } else {
+            b->hi[i].unit_begin = int(map.size());
+            b->hi[i].units = u;
+        }
+        map.insert(map.end(), size_t(u), int(i));
+    }
+    int *dst = adjoint ? b->adj_unit_inst : b->unit_inst;
+    cudaError_t e = cudaMemcpy(dst, map.data(), map.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_inst, b->hi.data(), b->hi.size() * sizeof(BatchInst), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bcuda(b, e, "batch maps");
+    if (adjoint) {
+        b->L.adj_ppt = ppt;
+        b->L.adj_units = int(map.size());
+    } else {
+        b->L.ppt = ppt;
+        b->L.units = int(map.size());
+    }
+    return NUFI_OK;
+}
+
+// Event time (ms) of `reps` runs of fn on the batch stream after one warm-up.
+template <typename F>
+float batch_time(nufi_batch *b, F fn, int reps)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    if (fn() != cudaSuccess) return -1;
+    cudaEventRecord(e0, b->stream);
+    for (int r = 0; r < reps; ++r)
+        if (fn() != cudaSuccess) return -1;
+    cudaEventRecord(e1, b->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / reps;
+}
+
+// The autotuner: times the candidate launch shapes of the batched trace
+// (chains per thread, slabs per ring chunk) at a mid-run step and of the
+// adjoint trace (chains per thread), keeps the fastest.  NUFI_BATCH_TUNE=0
+// keeps the defaults.
+int batch_autotune(nufi_batch *b)
+{
+    const char *env = std::getenv("NUFI_BATCH_TUNE");
+    const bool tune = !(env && env[0] == '0');
+    const int n_t = std::max(1, b->maxNt / 2);
+    size_t ts_max = 0;
+    for (nufi_handle *h : b->inst) ts_max = std::max<size_t>(ts_max, size_t(h->p.table_stride));
+    std::string log = "{\"trace\": [";
+    struct Cand { int ppt, S; };
+    std::vector<Cand> cands;
+    if (b->precision == NUFI_PREC_FP32_SPLIT) {
+        for (int ppt : {2, 4, 8})
+            for (int S : {4, 8, 16}) cands.push_back({ppt, S});
+    } else {
+        for (int ppt : {1, 2, 4}) cands.push_back({ppt, 0});
+    }
+    if (!tune) cands = {b->precision == NUFI_PREC_FP32_SPLIT ? Cand{4, 8} : Cand{2, 0}};
+    float best = -1;
+    Cand bc = cands[0];
+    for (size_t c = 0; c < cands.size(); ++c) {
+        int st = batch_set_units(b, cands[c].ppt, false);
+        if (st) return st;
+        b->L.slabs_per_chunk = std::max(1, cands[c].S);
+        b->L.smem = size_t(kRingSlots) * b->L.slabs_per_chunk * ts_max * sizeof(float);
+        float ms = tune ? batch_time(b, [&] { return launch_batch_trace(b->L, n_t, b->stream); }, 2) : 0.0f;
+        if (ms < 0) return bcuda(b, cudaGetLastError(), "autotune trace");
+        char item[128];
+        std::snprintf(item, sizeof(item), "%s{\"ppt\": %d, \"slabs_per_chunk\": %d, \"ms\": %.4f}", c ? ", " : "",
+                      cands[c].ppt, cands[c].S, ms);
+        log += item;
+        if (best < 0 || ms < best) {
+            best = ms;
+            bc = cands[c];
+        }
+    }
+    int st = batch_set_units(b, bc.ppt, false);
+    if (st) return st;
+    b->L.slabs_per_chunk = std::max(1, bc.S);
+    b->L.smem = size_t(kRingSlots) * b->L.slabs_per_chunk * ts_max * sizeof(float);
+    log += "], \"adjoint\": [";
+    std::vector<int> acands = tune ? std::vector<int>{1, 2, 4} : std::vector<int>{2};
+    float abest = -1;
+    int abc = acands[0];
+    for (size_t c = 0; c < acands.size(); ++c) {
+        st = batch_set_units(b, acands[c], true);
+        if (st) return st;
+        float ms = tune ? batch_time(b, [&] { return launch_batch_adjoint_step(b->L, n_t, b->stream); }, 1) : 0.0f;
+        if (ms < 0) return bcuda(b, cudaGetLastError(), "autotune adjoint");
+        char item[96];
+        std::snprintf(item, sizeof(item), "%s{\"ppt\": %d, \"ms\": %.4f}", c ? ", " : "", acands[c], ms);
+        log += item;
+        if (abest < 0 || ms < abest) {
+            abest = ms;
+            abc = acands[c];
+        }
+    }
+    st = batch_set_units(b, abc, true);
+    if (st) return st;
+    char tail[160];
+    std::snprintf(tail, sizeof(tail), "], \"chosen\": {\"ppt\": %d, \"slabs_per_chunk\": %d, \"adjoint_ppt\": %d, "
+                  "\"tuned_at_step\": %d}}", b->L.ppt, b->L.slabs_per_chunk, b->L.adj_ppt, n_t);
+    log += tail;
+    b->tune = log;
+    // the tuning runs wrote into the adjoint scratch and the error word
+    cudaMemsetAsync(b->err, 0, sizeof(unsigned), b->stream);
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    return e == cudaSuccess ? NUFI_OK : bcuda(b, e, "autotune");
+}
+
+int batch_check(nufi_batch *b)
+{
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "batch");
+    unsigned flags = 0;
+    if ((e = cudaMemcpy(&flags, b->err, sizeof(unsigned), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return bcuda(b, e, "batch flags");
+    if (flags) {
+        cudaMemset(b->err, 0, sizeof(unsigned));
+        return bfail(b, NUFI_ERR_DEVICE, "batch: device check failed (flags " + std::to_string(flags) + ")");
+    }
+    return NUFI_OK;
+}
+
+template <typename F>
+int capture(nufi_batch *b, cudaGraphExec_t *exec, F body)
+{
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return bcuda(b, e, "begin capture");
+    cudaError_t eb = body();
+    e = cudaStreamEndCapture(b->stream, &g);
+    if (eb != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return bcuda(b, eb, "batch launch");
+    }
+    if (e != cudaSuccess) return bcuda(b, e, "end capture");
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    return e == cudaSuccess ? NUFI_OK : bcuda(b, e, "graph instantiate");
+}
+
+}  // namespace
+
+extern "C" {
+
+int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_batch **out)
+{
+    if (!out || !cfgs || count <= 0) return bfail(nullptr, NUFI_ERR_INVALID, "nufi_batch_create: bad arguments");
+    *out = nullptr;
+    for (int32_t i = 0; i < count; ++i) {
+        const nufi_config &c = cfgs[i];
+        if (c.dim != 1 || c.order != 4 || c.precision != cfgs[0].precision)
+            return bfail(nullptr, NUFI_ERR_UNSUPPORTED, "nufi_batch_create: 1D, order 4, one precision per batch");
+        if (c.Nx[0] < 1 || c.Nx[0] > kBatchMaxN || kBatchMaxN % c.Nx[0] != 0)
+            return bfail(nullptr, NUFI_ERR_UNSUPPORTED, "nufi_batch_create: Nx must divide 256");
+    }
+    std::unique_ptr<nufi_batch> b(new nufi_batch);
+    b->device = device;
+    b->precision = cfgs[0].precision;
+    auto bail = [&](int code) {
+        const std::string msg = b->last_error;
+        batch_release(b.get());
+        g_last_error = msg;
+        return code;
+    };
+    for (int32_t i = 0; i < count; ++i) {
+        nufi_handle *h = nullptr;
+        int st = nufi_create(&cfgs[i], device, &h);
+        if (st) {
+            b->last_error = "instance " + std::to_string(i) + ": " + g_last_error;
+            return bail(st);
+        }
+        b->inst.push_back(h);
+        if (!h->solve_ok) {
+            b->last_error = "instance " + std::to_string(i) + ": " + h->solve_why;
+            return bail(NUFI_ERR_UNSUPPORTED);
+        }
+    }
+    DeviceGuard g(device);
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail(bcuda(b.get(), e, "cudaStreamCreate"));
+    long long max_units = 0, max_adj = 0, nodes = 0;
+    int solve_blocks = 0, max_P = 0;
+    b->hi.resize(size_t(count));
+    std::vector<int> node_map, solve_map;
+    bool pow2 = true;
+    for (int32_t i = 0; i < count; ++i) {
+        nufi_handle *h = b->inst[size_t(i)];
+        const Problem &p = h->p;
+        BatchInst &I = b->hi[size_t(i)];
+        std::memset(&I, 0, sizeof(I));
+        I.p = p;
+        I.hist = h->hist;
+        I.tables = h->tables;
+        I.nodes = h->nodes;
+        I.phase = h->phase;
+        I.green = h->plan.green;
+        I.rho = h->rho;
+        I.energy = h->energy;
+        I.Nt = int(h->cfg.Nt);
+        I.tpn = kBatchMaxN / p.N[0];
+        const int u1 = units_of(h, 1);
+        const int nsb = (p.N[0] + 7) / 8;
+        if ((e = balloc(b.get(), &I.partial, size_t(u1) * p.N[0])) != cudaSuccess ||
+            (e = balloc(b.get(), &I.epart, size_t(nsb))) != cudaSuccess ||
+            (e = balloc(b.get(), &I.ecount, 1)) != cudaSuccess ||
+            (e = balloc(b.get(), &I.mu, size_t(I.Nt + 1) * p.P[0])) != cudaSuccess ||
+            (e = balloc(b.get(), &I.lambda, size_t(p.N[0]))) != cudaSuccess)
+            return bail(bcuda(b.get(), e, "cudaMalloc"));
+        if ((e = cudaMemset(I.ecount, 0, sizeof(unsigned))) != cudaSuccess ||
+            (e = cudaMemset(I.mu, 0, size_t(I.Nt + 1) * p.P[0] * sizeof(double))) != cudaSuccess)
+            return bail(bcuda(b.get(), e, "cudaMemset"));
+        I.node_begin = nodes;
+        node_map.insert(node_map.end(), size_t(p.N[0]), i);
+        nodes += p.N[0];
+        I.solve_begin = solve_blocks;
+        I.solve_blocks = nsb;
+        solve_map.insert(solve_map.end(), size_t(nsb), i);
+        solve_blocks += nsb;
+        max_units += u1;
+        max_adj += u1;
+        max_P = std::max(max_P, p.P[0]);
+        b->maxNt = std::max(b->maxNt, I.Nt);
+        b->point_steps += p.Nq * ((long long)I.Nt * (I.Nt + 1) / 2);
+        pow2 = pow2 && ((p.N[0] & (p.N[0] - 1)) == 0);
+    }
+    if ((e = balloc(b.get(), &b->d_inst, size_t(count))) != cudaSuccess ||
+        (e = balloc(b.get(), &b->unit_inst, size_t(max_units))) != cudaSuccess ||
+        (e = balloc(b.get(), &b->adj_unit_inst, size_t(max_adj))) != cudaSuccess ||
+        (e = balloc(b.get(), &b->node_inst, size_t(nodes))) != cudaSuccess ||
+        (e = balloc(b.get(), &b->solve_inst, size_t(solve_blocks))) != cudaSuccess ||
+        (e = balloc(b.get(), &b->theta_acc, size_t(4 * max_adj))) != cudaSuccess ||
+        (e = balloc(b.get(), &b->grad, size_t(4 * count))) != cudaSuccess ||
+        (e = balloc(b.get(), &b->err, 1)) != cudaSuccess)
+        return bail(bcuda(b.get(), e, "cudaMalloc"));
+    if ((e = cudaMemcpy(b->node_inst, node_map.data(), node_map.size() * sizeof(int), cudaMemcpyHostToDevice)) !=
+            cudaSuccess ||
+        (e = cudaMemcpy(b->solve_inst, solve_map.data(), solve_map.size() * sizeof(int), cudaMemcpyHostToDevice)) !=
+            cudaSuccess ||
+        (e = cudaMemset(b->err, 0, sizeof(unsigned))) != cudaSuccess)
+        return bail(bcuda(b.get(), e, "batch setup"));
+    BatchLaunch &L = b->L;
+    L.inst = b->d_inst;
+    L.unit_inst = b->unit_inst;
+    L.node_inst = b->node_inst;
+    L.solve_inst = b->solve_inst;
+    L.adj_unit_inst = b->adj_unit_inst;
+    L.count = count;
+    L.precision = b->precision;
+    L.pow2 = pow2;
+    L.total_nodes = nodes;
+    L.solve_blocks = solve_blocks;
+    L.max_P = max_P;
+    L.adj_chunk = 8;
+    L.theta_acc = b->theta_acc;
+    L.err = b->err;
+    int st = batch_autotune(b.get());
+    if (st) return bail(st);
+    *out = b.release();
+    return NUFI_OK;
+}
+
+int nufi_batch_destroy(nufi_batch *b)
+{
+    if (!b) return NUFI_OK;
+    DeviceGuard g(b->device);
+    batch_release(b);
+    delete b;
+    return NUFI_OK;
+}
+
+const char *nufi_batch_last_error(const nufi_batch *b) { return b ? b->last_error.c_str() : g_last_error.c_str(); }
+
+int nufi_batch_forward(nufi_batch *b, double *J)
+{
+    if (!b) return bfail(nullptr, NUFI_ERR_INVALID, "null batch");
+    DeviceGuard g(b->device);
+    if (!b->fwd) {
+        int st = capture(b, &b->fwd, [&] {
+            cudaError_t e = cudaSuccess;
+            for (int n = 0; n <= b->maxNt && e == cudaSuccess; ++n) e = launch_batch_step(b->L, n, b->stream);
+            return e;
+        });
+        if (st) return st;
+    }
+    cudaError_t e = cudaGraphLaunch(b->fwd, b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "graph launch");
+    int st = batch_check(b);
+    if (st) return st;
+    for (nufi_handle *h : b->inst) mark_steps(h, 0, h->cfg.Nt, true);
+    b->forward_done = true;
+    if (J) {
+        for (size_t i = 0; i < b->inst.size(); ++i) {
+            nufi_handle *h = b->inst[i];
+            std::vector<double> w(size_t(h->cfg.Nt + 1));
+            e = cudaMemcpy(w.data(), h->energy, w.size() * sizeof(double), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return bcuda(b, e, "energy download");
+            double s = 0;
+            for (double v : w) s += v;
+            J[i] = 2.0 * h->cfg.dt * s;
+        }
+    }
+    return NUFI_OK;
+}
+
+int nufi_batch_backward(nufi_batch *b, double *grad)
+{
+    if (!b || !grad) return bfail(b, NUFI_ERR_INVALID, "null argument");
+    if (!b->forward_done) return bfail(b, NUFI_ERR_RANGE, "batch backward: run the forward first");
+    DeviceGuard g(b->device);
+    if (!b->bwd) {
+        int st = capture(b, &b->bwd, [&] {
+            cudaError_t e = cudaSuccess;
+            for (const BatchInst &I : b->hi)
+                if (e == cudaSuccess)
+                    e = cudaMemsetAsync(I.mu, 0, size_t(I.Nt + 1) * I.p.P[0] * sizeof(double), b->stream);
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(b->theta_acc, 0, size_t(4) * b->L.adj_units * sizeof(double), b->stream);
+            for (int m = b->maxNt; m >= 0 && e == cudaSuccess; --m) e = launch_batch_adjoint_step(b->L, m, b->stream);
+            if (e == cudaSuccess) e = launch_batch_theta_reduce(b->L, b->grad, b->stream);
+            return e;
+        });
+        if (st) return st;
+    }
+    cudaError_t e = cudaGraphLaunch(b->bwd, b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "graph launch");
+    e = cudaMemcpyAsync(grad, b->grad, size_t(4) * b->L.count * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+    if (e != cudaSuccess) return bcuda(b, e, "grad download");
+    return batch_check(b);
+}
+
+int nufi_batch_energy(nufi_batch *b, int32_t i, double *energy)
+{
+    if (!b || !energy) return bfail(b, NUFI_ERR_INVALID, "null argument");
+    if (i < 0 || i >= b->L.count) return bfail(b, NUFI_ERR_RANGE, "instance out of range");
+    DeviceGuard g(b->device);
+    nufi_handle *h = b->inst[size_t(i)];
+    cudaError_t e = cudaMemcpy(energy, h->energy, size_t(h->cfg.Nt + 1) * sizeof(double), cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? NUFI_OK : bcuda(b, e, "energy download");
+}
+
+int nufi_batch_stream(const nufi_batch *b, void **stream)
+{
+    if (!b || !stream) return bfail(nullptr, NUFI_ERR_INVALID, "null argument");
+    *stream = b->stream;
+    return NUFI_OK;
+}
+
+int nufi_batch_describe(const nufi_batch *b, char *buf, size_t len)
+{
+    if (!b || !buf || len == 0) return bfail(nullptr, NUFI_ERR_INVALID, "null argument");
+    const std::string s = "{\"instances\": " + std::to_string(b->L.count) + ", \"units\": " +
+                          std::to_string(b->L.units) + ", \"adjoint_units\": " + std::to_string(b->L.adj_units) +
+                          ", \"solve_blocks\": " + std::to_string(b->L.solve_blocks) + ", \"max_Nt\": " +
+                          std::to_string(b->maxNt) + ", \"point_steps\": " + std::to_string(b->point_steps) +
+                          ", \"autotune\": " + b->tune + "}";
+    std::snprintf(buf, len, "%s", s.c_str());
+    return s.size() < len ? NUFI_OK : bfail(nullptr, NUFI_ERR_RANGE, "describe: buffer too small");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
 // Allocation-free rho (nufi_compute_rho_noalloc).
 //
 // For callers that must not allocate device memory: code that runs while

@@ -184,6 +184,47 @@ AdjointPlan adjoint_plan_1d(const Problem &p);
 cudaError_t launch_adjoint_1d(const Problem &p, const AdjointPlan &ap, const double *hist, const double *gc,
                               double *mu, double *lambda, double *theta_acc, int n1, unsigned *err, cudaStream_t st);
 
+// Batched 1D instances (batch_1d.cu).  One descriptor per instance; the
+// unit, node and solve-block maps give each CTA its instance.
+constexpr int kBatchMaxN = 256;
+constexpr int kRingSlots = 3;  // shared-memory ring slots of the split traces  // spatial nodes per instance (256 % N == 0)
+struct BatchInst {
+    Problem p;
+    double *hist;
+    float *tables;
+    const SplitNode *nodes;
+    const float2 *phase;
+    const double *green;
+    double *partial;  // [units][N]
+    double *rho;      // [N]
+    double *energy;   // [Nt+1]
+    double *epart;    // [solve_blocks]
+    unsigned *ecount; // [1], zero between launches
+    double *mu;       // [(Nt+1)][P] slab adjoints
+    double *lambda;   // [N]
+    int Nt, tpn;
+    int unit_begin, units;
+    int adj_unit_begin, adj_units;
+    int solve_begin, solve_blocks;
+    long long node_begin;
+};
+struct BatchLaunch {
+    const BatchInst *inst = nullptr;
+    const int *unit_inst = nullptr, *node_inst = nullptr, *solve_inst = nullptr, *adj_unit_inst = nullptr;
+    int count = 0, precision = 0, ppt = 4, slabs_per_chunk = 8;
+    bool pow2 = true;
+    size_t smem = 0;
+    int units = 0, solve_blocks = 0;
+    long long total_nodes = 0;
+    int adj_ppt = 2, adj_chunk = 8, adj_units = 0, max_P = 0;
+    double *theta_acc = nullptr;
+    unsigned *err = nullptr;
+};
+cudaError_t launch_batch_trace(const BatchLaunch &L, int n, cudaStream_t st);
+cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st);
+cudaError_t launch_batch_adjoint_step(const BatchLaunch &L, int m, cudaStream_t st);
+cudaError_t launch_batch_theta_reduce(const BatchLaunch &L, double *grad, cudaStream_t st);
+
 // FP32 table of one FP64 slab (after upload_phi).
 cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st);
 

@@ -10,7 +10,7 @@ namespace split {
 
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
-constexpr int kRing = 3;
+constexpr int kRing = kRingSlots;
 constexpr unsigned kWaitLimit = 1u << 22;      // polls of an mbarrier
 constexpr unsigned kBarrierLimit = 1u << 26;   // polls of the grid barrier
 

@@ -1,0 +1,107 @@
+"""Batched 1D instances (nufi_batch_*): every instance of a batch of uneven
+grid sizes against the same configuration run alone through a handle, and
+the batched adjoint against the single-instance adjoint and central
+differences.
+
+Tolerances: FP64 energy histories 1e-12 of max (the batch sums rho over
+other partial rows than a handle; the difference is the FP64 summation
+floor); FP32-split within the 1e-6 gate of the FP64 history; gradients
+1e-9 of max |dJ| against the single-instance adjoint (FP64 atomics in the
+slab adjoints), 1e-5 per component against central differences.
+"""
+import numpy as np
+import pytest
+
+from numericalflowiteration_gb300.config import batched_bump_on_tail, bump_on_tail_1d, landau_1d
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nufi():
+    import numericalflowiteration_gb300 as m
+    from numericalflowiteration_gb300 import build
+    build.build()
+    m.load()
+    return m
+
+
+def small_batch(precision="fp64", count=7, Nt=40):
+    return batched_bump_on_tail(count=count, seed=7, Nt=Nt, nx=(16, 32, 64), nv=(32, 64, 128), precision=precision)
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / np.max(np.abs(b)))
+
+
+def test_batch_fp64_matches_single_handles(nufi):
+    cfgs = small_batch()
+    with nufi.Batch(cfgs) as b:
+        J = b.forward()
+        E = [b.energy(i) for i in range(len(cfgs))]
+        d = b.describe()
+    assert d["instances"] == len(cfgs) and d["autotune"]["chosen"]["ppt"] in (1, 2, 4)
+    for i, c in enumerate(cfgs):
+        with nufi.Simulation(c) as s:
+            Js = s.forward()
+            Es = s.energy()
+        assert rel(E[i], Es) <= 1e-12, i
+        assert abs(J[i] - Js) <= 1e-12 * abs(Js)
+
+
+def test_batch_split_within_gate(nufi):
+    cfgs = small_batch()
+    with nufi.Batch([c.replace(precision="fp32split") for c in cfgs]) as b:
+        b.forward()
+        E = [b.energy(i) for i in range(len(cfgs))]
+        d = b.describe()
+    assert d["autotune"]["chosen"]["ppt"] in (2, 4, 8)
+    for i, c in enumerate(cfgs):
+        with nufi.Simulation(c) as s:
+            Es = s.run()
+        assert rel(E[i], Es) <= 1e-6, i
+
+
+def test_batch_backward_matches_single_adjoint(nufi):
+    cfgs = small_batch()
+    with nufi.Batch(cfgs) as b:
+        with pytest.raises(IndexError):
+            b.backward()
+        b.forward()
+        G = b.backward()
+        G2 = b.backward()
+    assert rel(G2, G) <= 1e-13
+    for i, c in enumerate(cfgs):
+        with nufi.Simulation(c) as s:
+            s.forward()
+            g = s.backward()
+        assert rel(G[i], g) <= 1e-9, (i, G[i], g)
+
+
+def test_batch_gradient_matches_central_differences(nufi):
+    cfgs = small_batch(count=3, Nt=30)
+    with nufi.Batch(cfgs) as b:
+        b.forward()
+        G = b.backward()
+    h = 1e-6
+    for i in range(4):
+        plus, minus = [], []
+        for c in cfgs:
+            pp = list(c.f0_params)
+            pp[i] += h
+            plus.append(c.replace(f0_params=list(pp)))
+            pp[i] -= 2 * h
+            minus.append(c.replace(f0_params=list(pp)))
+        with nufi.Batch(plus) as bp:
+            Jp = bp.forward()
+        with nufi.Batch(minus) as bm:
+            Jm = bm.forward()
+        fd = (Jp - Jm) / (2 * h)
+        assert np.all(np.abs(G[:, i] - fd) <= 1e-5 * np.abs(fd)), (i, G[:, i], fd)
+
+
+def test_batch_rejects_unsupported(nufi):
+    with pytest.raises(NotImplementedError):
+        nufi.Batch([landau_1d(Nx=48, Nv=32, Nt=4)])
+    with pytest.raises(NotImplementedError):
+        nufi.Batch([landau_1d(Nx=16, Nv=32, Nt=4), landau_1d(Nx=16, Nv=32, Nt=4, precision="fp32split")])

@@ -357,6 +357,58 @@ def run_ours(args, cfg):
     return 0
 
 
+def run_batch(args):
+    """The batched configuration: seeded bump-on-tail instances of uneven
+    sizes (Nx in {64,128,256}, Nv in {256,512,1024}, T = 20).  Times the
+    batched FP32-split forward, the batched FP64 forward and the FP64
+    adjoint (gradient of int |E|^2 dt for all instances), CUDA events on the
+    batch stream; prints one JSON line."""
+    import torch
+    import numericalflowiteration_gb300 as nufi
+    from numericalflowiteration_gb300 import build
+    from numericalflowiteration_gb300.config import batched_bump_on_tail
+    build.build()
+    nufi.load()
+    cfgs = batched_bump_on_tail(count=args.instances)
+    ps = sum(c.point_steps() for c in cfgs)
+
+    def timed(b, fn, reps):
+        ext = torch.cuda.ExternalStream(b.stream)
+        out = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(ext):
+                e0.record()
+            fn()
+            with torch.cuda.stream(ext):
+                e1.record()
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return min(out)
+
+    res = {"instances": len(cfgs), "point_steps": ps}
+    with nufi.Batch([c.replace(precision="fp32split") for c in cfgs]) as b:
+        b.forward()
+        ms = timed(b, b.forward, max(1, args.steps))
+        res["split_forward"] = {"ms": ms, "point_steps_per_s": ps / (ms * 1e-3), "autotune": b.describe()["autotune"]}
+    if not args.no_fp64:
+        with nufi.Batch(cfgs) as b:
+            msf = timed(b, b.forward, 1)
+            J = b.forward()
+            msb = timed(b, b.backward, 1)
+            G = b.backward()
+            res["fp64_forward"] = {"ms": msf, "point_steps_per_s": ps / (msf * 1e-3)}
+            res["fp64_backward"] = {"ms": msb, "cost_vs_forward": msb / msf,
+                                    "autotune": b.describe()["autotune"]["chosen"]}
+            res["J_first"] = float(J[0])
+            res["grad_first"] = [float(v) for v in G[0]]
+    line = {"metric": "batched bump-on-tail: forward point-steps/s and adjoint cost", "config": {
+        "workload": f"batched_bump_on_tail_{len(cfgs)}", "seed": 20261203, "Nt": 320, "dt": 1 / 16}, **res}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def profile_case(args, cfg):
     """One run of steps 0..nt in one precision; prints the chosen kernels."""
     import numericalflowiteration_gb300 as nufi
@@ -389,10 +441,14 @@ def main(argv=None):
                     help="run steps 0..--nt of the workload once in --precision and exit (a small case for ncu)")
     ap.add_argument("--precision", default="fp32split", choices=["fp32split", "fp64"])
     ap.add_argument("--nt", type=int, default=None, help="with --profile-case: last step")
+    ap.add_argument("--batch", action="store_true", help="time the batched bump-on-tail configuration and exit")
+    ap.add_argument("--instances", type=int, default=256, help="with --batch: number of instances")
     args = ap.parse_args(argv)
     cfg = WORKLOADS[args.workload]()
     if args.profile_case:
         return profile_case(args, cfg)
+    if args.batch:
+        return run_batch(args)
     if args.impl == "reference":
         return run_reference(args, cfg)
     return run_ours(args, cfg)

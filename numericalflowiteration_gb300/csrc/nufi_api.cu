@@ -363,7 +363,7 @@ int build_solve_plan(nufi_handle *h, int sms)
     pl.smem = pl.green_in_smem ? with_green : size_t(Ns) * 8;
     NUFI_CUDA(h, dalloc(h, &pl.green, green.size()));
     // also holds one part per CTA of the persistent run kernel
-    NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(std::max(pl.blocks, sms))));
+    NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(std::max(pl.blocks, kMaxCtasPerSm * sms))));
     NUFI_CUDA(h, dalloc(h, &pl.energy_counter, 1));
     NUFI_CUDA(h, cudaMemcpy(pl.green, green.data(), green.size() * sizeof(double), cudaMemcpyHostToDevice));
     NUFI_CUDA(h, cudaMemset(pl.energy_counter, 0, sizeof(unsigned)));
@@ -593,7 +593,8 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
         const char *pers = std::getenv("NUFI_PERSISTENT");
         if (!(pers && pers[0] == '0')) {
             h->persist = persistent_shape_1d(p, h->staged, h->plan, sms > 0 ? sms : 1);
-            if (h->persist.ok && (e = dalloc(h.get(), &h->persist.sync, 2)) != cudaSuccess)
+            if (h->persist.ok && ((e = dalloc(h.get(), &h->persist.sync, 2)) != cudaSuccess ||
+                                  (e = dalloc(h.get(), &h->persist.epart, nslab * size_t(p.N[0]))) != cudaSuccess))
                 return bail(cuda_fail(h.get(), e, "cudaMalloc"));
         }
     }

@@ -130,11 +130,13 @@ cudaError_t launch_trace_split_staged(const Problem &p, const StagedShape &sh, c
 // Whole FP32-split 1D simulation in one cooperative launch
 // (run_split_1d.cu): staged trace, rho, circulant solve and W_n per step,
 // separated by bounded grid barriers.  sync = {barrier count, abort flag}.
+constexpr int kMaxCtasPerSm = 2;  // whole-run kernel CTAs per SM (energy parts sized for it)
 struct PersistentRun {
     bool ok = false;
     int ctas = 0, threads = 0, ppt = 0, slabs_per_chunk = 0, tpn = 1;
     size_t smem = 0;
     unsigned *sync = nullptr;
+    double *epart = nullptr;  // [(Nt+1)][N] rho'_i phi_i per step and node
 };
 
 // rho[s] = -wv * sum over the rows of partial[row][s]: one warp per node,

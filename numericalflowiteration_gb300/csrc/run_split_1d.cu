@@ -18,10 +18,11 @@
 //   solve    every CTA loads rho, removes the mean (fixed order) and
 //            computes its nodes' circulant products c, phi, K(A,B,C) from
 //            the Green's kernels held in shared memory for the whole run;
-//            writes slab n (FP64), table n (store_kick_entry) and its part
-//            of sum rho' phi
+//            writes slab n (FP64), table n (store_kick_entry) and, per
+//            node, rho'_i phi_i into row n of epart
 //   barrier
-//   energy   CTA 0 sums the parts in CTA order -> W_n
+// After the last step, W_n = L/(2N) sum_i epart[n][i] for all n at once
+// (no per-step energy reduction on the critical path).
 // The next step's trace reads table n through the async proxy (bulk
 // copies) after the barrier; fence.proxy.async.global orders that read
 // after the generic-proxy writes made visible by the barrier.
@@ -294,7 +295,6 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
 #pragma unroll
             for (int c = 0; c < 5; ++c) wacc[warp][c] = a[c];
         __syncthreads();
-        double e_local = 0;
         if (lane == 0 && pw == 0 && slotn < K) {
             const int node = int(blockIdx.x) + slotn * G;
             double v[5];
@@ -307,21 +307,22 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
             slab[node] = v[0];
             if (node + N < p.P[0]) slab[node + N] = v[0];
             store_kick_entry(tables + (long long)n * p.table_stride, N, node, float(v[2]), float(v[3]), float(v[4]));
-            e_local = rs[node] * v[1];
+            epart[(long long)(n - n0) * N + node] = rs[node] * v[1];
         }
-        const double eb = block_sum(e_local, red);
-        if (threadIdx.x == 0) epart[blockIdx.x] = eb;
         if (!barrier(n)) return;
-
-        // ---------------- W_n ----------------
-        if (blockIdx.x == 0) {
-            double v = 0;
-            for (int b = threadIdx.x; b < G; b += blockDim.x) v += __ldcg(epart + b);
-            const double tot = block_sum(v, red);
-            if (threadIdx.x == 0) energy[n] = tot * Lfac;
-        }
     }
-    // refill issues nothing past step n1: no bulk copy is in flight here
+    // refill issues nothing past step n1: no bulk copy is in flight here.
+    // W_n = L/(2N) sum_i rho'_i phi_i for all steps at once, off the
+    // per-step critical path: CTA c sums the steps n0 + c + j G, one warp,
+    // lanes in fixed stride and a fixed shuffle tree.
+    if (warp == 0)
+        for (int n = n0 + int(blockIdx.x); n <= n1; n += G) {
+            const double *e = epart + (long long)(n - n0) * N;
+            double v = 0;
+            for (int i = lane; i < N; i += 32) v += __ldcg(e + i);
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+            if (lane == 0) energy[n] = v * Lfac;
+        }
 }
 
 namespace {
@@ -350,7 +351,7 @@ cudaError_t launch_run_ppt(const Problem &p, const PersistentRun &pr, const Solv
     e = cudaMemsetAsync(pr.sync, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     return cudaLaunchKernelEx(&cfg, fn, p, tables, hist, nodes, phase, (const double *)plan.green, partial, rho,
-                              energy, plan.energy_partial, n0, n1, pr.slabs_per_chunk, pr.threads / pr.tpn, pr.sync,
+                              energy, pr.epart, n0, n1, pr.slabs_per_chunk, pr.threads / pr.tpn, pr.sync,
                               err);
 }
 
@@ -363,7 +364,9 @@ PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const
     if (sh.ppt > 4 && sh.threads > 256) return pr;  // launch bounds of the PPT > 4 instances
     const int W = sh.threads / 32;
     const int K = (p.N[0] + sh.ctas - 1) / sh.ctas;  // nodes per CTA in reduce/solve
-    if (K > W || sh.ctas > sms) return pr;
+    // at most two CTAs per SM (cooperative launch: all co-resident), and
+    // energy_partial holds one part per CTA up to kMaxCtasPerSm * sms
+    if (K > W || sh.ctas > kMaxCtasPerSm * sms) return pr;
     pr.ctas = sh.ctas;
     pr.threads = sh.threads;
     pr.tpn = sh.tpn;

@@ -152,7 +152,11 @@ StagedShape staged_shape_1d(const Problem &p, int sms)
     StagedShape sh;
     if (p.dim != 1 || p.N[0] > 256) return sh;  // not applicable (one thread per spatial node)
     const long long Nm = p.Nm;
-    int G = int(std::min<long long>(Nm, sms));
+    // CTAs per SM: 1 by default; NUFI_SPLIT_CTAS_PER_SM=2 runs two smaller
+    // CTAs per SM (more warps, fewer chains each)
+    const char *cps_env = std::getenv("NUFI_SPLIT_CTAS_PER_SM");
+    const int cps = (cps_env && cps_env[0] == '2') ? 2 : 1;
+    int G = int(std::min<long long>(Nm, (long long)sms * cps));
     int ppt = int((Nm + G - 1) / G);
     if (ppt > kStagedMaxPPT) {
         G = int((Nm + kStagedMaxPPT - 1) / kStagedMaxPPT);
@@ -163,7 +167,7 @@ StagedShape staged_shape_1d(const Problem &p, int sms)
     // so each CTA asks for more than half of an SM's shared memory and uses
     // it for a deeper ring.
     const size_t slab_bytes = size_t(p.table_stride) * 4;
-    const size_t kOneCtaPerSm = 120 * 1024;
+    const size_t kOneCtaPerSm = cps == 2 ? 72 * 1024 : 120 * 1024;
     int S = int(std::max<size_t>(1, std::min<size_t>(32, kOneCtaPerSm / (size_t(kRing) * slab_bytes))));
     if (size_t(kRing) * S * slab_bytes > 200 * 1024) return sh;
     // Threads per spatial node: 1 (measured faster on the two-stream
@@ -178,7 +182,7 @@ StagedShape staged_shape_1d(const Problem &p, int sms)
     sh.ppt = (ppt + tpn - 1) / tpn;
     sh.threads = tpn * Nr;
     sh.slabs_per_chunk = S;
-    sh.smem = std::max(size_t(kRing) * S * slab_bytes, kOneCtaPerSm);
+    sh.smem = cps == 2 ? size_t(kRing) * S * slab_bytes : std::max(size_t(kRing) * S * slab_bytes, kOneCtaPerSm);
     sh.ok = true;
     return sh;
 }

@@ -26,6 +26,7 @@
 #ifndef NUFI_CUDA_KERNEL_HPP
 #define NUFI_CUDA_KERNEL_HPP
 
+#include <array>
 #include <cstddef>
 #include <memory>
 #include <stdexcept>
@@ -177,6 +178,22 @@ public:
         for (int i = 0; i < 4; ++i) metrics[i] += real(m[i]);
     }
 
+    // Not in the reference: J = 2 dt sum_{n<=n1} W_n after running steps
+    // 0..n1 on the device, and dJ/d(alpha, k, u_b, sigma_b) by the adjoint.
+    double forward(size_t n1)
+    {
+        double J = 0;
+        throw_status(handle.get(), nufi_forward(handle.get(), (int64_t)n1, &J));
+        return J;
+    }
+
+    std::array<double, 4> backward(size_t n1)
+    {
+        std::array<double, 4> g{};
+        throw_status(handle.get(), nufi_backward(handle.get(), (int64_t)n1, g.data()));
+        return g;
+    }
+
     nufi_handle *get() const noexcept { return handle.get(); }
 
 private:
@@ -208,6 +225,8 @@ namespace nufi {
         void upload_phi(size_t n, const real *coeffs) { impl.upload_phi(n, coeffs); }              \
         void compute_metrics(size_t n, size_t q_min, size_t q_max) { impl.compute_metrics(n, q_min, q_max); } \
         void download_metrics(real *metrics) { impl.download_metrics(metrics); }                    \
+        double forward(size_t n1) { return impl.forward(n1); }                                      \
+        std::array<double, 4> backward(size_t n1) { return impl.backward(n1); }                     \
         nufi_handle *native_handle() const noexcept { return impl.get(); }                          \
                                                                                                     \
     private:                                                                                        \

@@ -391,7 +391,12 @@ def run_batch(args):
     with nufi.Batch([c.replace(precision="fp32split") for c in cfgs]) as b:
         b.forward()
         ms = timed(b, b.forward, max(1, args.steps))
+        b.backward()
+        msb = timed(b, b.backward, max(1, args.steps))
+        G_split = b.backward()
         res["split_forward"] = {"ms": ms, "point_steps_per_s": ps / (ms * 1e-3), "autotune": b.describe()["autotune"]}
+        res["split_backward"] = {"ms": msb, "cost_vs_forward": msb / ms,
+                                 "note": "FP32-split adjoint: fixed-point reversible characteristics"}
     if not args.no_fp64:
         with nufi.Batch(cfgs) as b:
             msf = timed(b, b.forward, 1)
@@ -403,6 +408,9 @@ def run_batch(args):
                                     "autotune": b.describe()["autotune"]["chosen"]}
             res["J_first"] = float(J[0])
             res["grad_first"] = [float(v) for v in G[0]]
+            rel = np.abs(G_split - G) / np.maximum(np.abs(G), 1e-300)
+            res["split_vs_fp64_grad_rel_max"] = float(np.max(rel))
+            res["split_vs_fp64_grad_rel_median"] = float(np.median(rel))
     line = {"metric": "batched bump-on-tail: forward point-steps/s and adjoint cost", "config": {
         "workload": f"batched_bump_on_tail_{len(cfgs)}", "seed": 20261203, "Nt": 320, "dt": 1 / 16}, **res}
     print(json.dumps(line), flush=True)

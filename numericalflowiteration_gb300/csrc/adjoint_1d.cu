@@ -38,7 +38,7 @@ using namespace adj;
 // per thread from blockIdx.y*PPT.  theta_acc[i*blocks + block] += this
 // block's share of dJ/dtheta_i (a fixed slot per block: deterministic).
 template <int ORDER, int PPT>
-__global__ void __launch_bounds__(256) adjoint_trace_1d_kernel(const Problem p, const double *__restrict__ hist,
+__global__ void __launch_bounds__(256, 1) adjoint_trace_1d_kernel(const Problem p, const double *__restrict__ hist,
                                                                const double *__restrict__ lambda, int m, int chunk,
                                                                double *__restrict__ mu, double *__restrict__ theta_acc,
                                                                unsigned *err)

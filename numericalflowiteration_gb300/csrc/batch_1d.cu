@@ -58,7 +58,7 @@ __device__ __forceinline__ double combine_groups(double acc, const UnitMap &u, d
 }
 
 template <int PPT, bool POW2>
-__global__ void __launch_bounds__(256) batch_trace_split_kernel(const BatchInst *__restrict__ bi,
+__global__ void __launch_bounds__(256, 1) batch_trace_split_kernel(const BatchInst *__restrict__ bi,
                                                                 const int *__restrict__ unit_inst, int n, int S,
                                                                 unsigned *err)
 {
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256) batch_trace_split_kernel(const BatchInst 
 }
 
 template <int PPT>
-__global__ void __launch_bounds__(256) batch_trace_fp64_kernel(const BatchInst *__restrict__ bi,
+__global__ void __launch_bounds__(256, 1) batch_trace_fp64_kernel(const BatchInst *__restrict__ bi,
                                                                const int *__restrict__ unit_inst, int n,
                                                                unsigned *err)
 {
@@ -215,7 +215,7 @@ __device__ __forceinline__ double bsum(double v, double *red)
 // Field solve of every instance: block = 8 nodes of one instance, one warp
 // per node (circulant products of field_solve.cu; green from global).
 template <int NCONV>
-__global__ void __launch_bounds__(256) batch_solve_kernel(const BatchInst *__restrict__ bi,
+__global__ void __launch_bounds__(256, 1) batch_solve_kernel(const BatchInst *__restrict__ bi,
                                                           const int *__restrict__ solve_inst, int n)
 {
     __shared__ double rs[kBatchMaxN];
@@ -316,7 +316,7 @@ __global__ void batch_adjoint_lambda_kernel(const BatchInst *__restrict__ bi, in
 }
 
 template <int PPT>
-__global__ void __launch_bounds__(256) batch_adjoint_trace_kernel(const BatchInst *__restrict__ bi,
+__global__ void __launch_bounds__(256, 1) batch_adjoint_trace_kernel(const BatchInst *__restrict__ bi,
                                                                   const int *__restrict__ unit_inst, int m,
                                                                   int chunk, double *__restrict__ theta_acc,
                                                                   long long slots, unsigned *err)
@@ -361,6 +361,316 @@ __global__ void batch_theta_reduce_kernel(const BatchInst *__restrict__ bi, int 
     if (lane == 0) grad[w] = sum + comp;
 }
 
+
+// ---------------------------------------------------------------------------
+// FP32-split adjoint (1D, N a power of two).  The characteristics are
+// recomputed in fixed point so that every substep inverts exactly: position
+// P and velocity V are int64 in units of 2^-40 cells (per substep), the
+// kick is the FP32 kick table's K(A + B xi + C xi^2) (the field of the split
+// forward), rounded to 2^-40 cells:
+//   forward   P -= V;  xi, cell from P;  V += rnd(h g(xi) 2^40)
+//   inverse   V -= rnd(h g(xi) 2^40);  P += V        (bit-exact)
+// so the reverse sweep walks exactly the trajectory the recomputation
+// produced (no drift of a recomputed path).  The adjoint of one substep in
+// cells (X) and cells per substep (V), with g' = dg/dxi:
+//   Xbar <- Xbar + Vbar h g';  Vbar <- Vbar - Xbar   (Vbar compensated)
+//   table adjoints of slab k at the cell: Abar += Vbar h, Bbar += Vbar h xi,
+//   Cbar += Vbar h xi^2   (shared-memory FP32 sums, flushed into FP64)
+// The seed at the foot: Xbar = a dx df0/dx, Vbar = a (dx/dt) df0/du with
+// a = -w lambda_m(s); thetabar += a df0/dtheta (FP64).
+// ---------------------------------------------------------------------------
+
+// f0 partial derivatives in FP32 at x (unwrapped), u: as adj::f0_grad_1d.
+struct F0GradF {
+    float fx, fu, dth[4];
+};
+__device__ __forceinline__ F0GradF f0_grad_1d_f(const Problem &p, float x, float u)
+{
+    const float alpha = float(p.f0p[0]), k = float(p.f0p[1]);
+    const float c0 = 0.398942280401432678f;
+    float sk, ck;
+    sincosf(k * x, &sk, &ck);
+    const float sp = 1.f + alpha * ck;
+    float g, gu, gub = 0.f, gsb = 0.f;
+    if (p.f0_kind == NUFI_F0_LANDAU) {
+        g = c0 * expf(-0.5f * u * u);
+        gu = -u * g;
+    } else if (p.f0_kind == NUFI_F0_TWO_STREAM) {
+        const float e = c0 * expf(-0.5f * u * u);
+        g = e * u * u;
+        gu = e * u * (2.f - u * u);
+    } else {
+        const float ubv = float(p.f0p[2]), sb = float(p.f0p[3]);
+        const float z = (u - ubv) / sb;
+        const float e1 = c0 * expf(-0.5f * u * u), e2 = c0 / sb * expf(-0.5f * z * z);
+        g = 0.9f * e1 + 0.1f * e2;
+        gu = -0.9f * u * e1 - 0.1f * z / sb * e2;
+        gub = 0.1f * z / sb * e2;
+        gsb = 0.1f * (z * z - 1.f) / sb * e2;
+    }
+    F0GradF r;
+    r.fx = -alpha * k * sk * g;
+    r.fu = sp * gu;
+    r.dth[0] = ck * g;
+    r.dth[1] = -alpha * x * sk * g;
+    r.dth[2] = sp * gub;
+    r.dth[3] = sp * gsb;
+    return r;
+}
+
+// v * 2^40 rounded to an integer, without a 64-bit conversion (which runs
+// on the FP64 pipe): s = v 2^20 is split exactly into its nearest integer
+// hi (round-to-nearest add of 1.5 2^23) and the remainder s - hi (exact,
+// |s - hi| <= 1/2), whose 2^20 multiple is rounded the same way:
+// v 2^40 = hi 2^20 + lo.  Valid for |v| < 4 (kicks are far smaller); the
+// forward and the inverse substep apply it to the same float, so the
+// fixed-point path inverts exactly whatever the rounding.
+__device__ __forceinline__ long long fix40(float v)
+{
+    const float s = v * 1048576.0f;
+    const float mh = __fadd_rn(s, kMagic);
+    const int hi = __float_as_int(mh) - kMagicBits;
+    const float r = __fmul_rn(__fsub_rn(s, __fsub_rn(mh, kMagic)), 1048576.0f);
+    const int lo = __float_as_int(__fadd_rn(r, kMagic)) - kMagicBits;
+    return (long long)hi * 1048576LL + lo;
+}
+
+// float -> double by bit manipulation (exact for normal numbers; zero and
+// subnormals give 0), keeping the conversion off the FP64 pipe.
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0) return 0.0;
+    const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
+                                    ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                                    ((unsigned long long)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+// Shared-memory add without a returned value.
+__device__ __forceinline__ void red_shared_add(float *p, float v)
+{
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(smem_addr(p)), "f"(v) : "memory");
+}
+
+// Cell and fraction of a fixed-point position (N a power of two).
+__device__ __forceinline__ void fx_locate(long long P, int mask, int &J, float &xi)
+{
+    const unsigned hi = unsigned((unsigned long long)P >> 32), lo = unsigned(P);
+    J = int(hi >> 8) & mask;                     // cell = P >> 40 (two's complement, masked)
+    const unsigned frac = __funnelshift_r(lo, hi, 8);  // bits 8..39: the top 32 of the fraction
+    xi = __int_as_float(0x3f800000 | (frac >> 9)) - 1.0f;
+}
+
+template <int PPT>
+__global__ void __launch_bounds__(256, 1) batch_adjoint_split_kernel(const BatchInst *__restrict__ bi,
+                                                                  const int *__restrict__ unit_inst, int m, int S,
+                                                                  int ts_max, double *__restrict__ theta_acc,
+                                                                  long long slots, unsigned *err)
+{
+    extern __shared__ __align__(128) float ring[];  // [kRing][S][ts_max], then [S][3N] table adjoints
+    __shared__ __align__(8) unsigned long long full_bar[kRing];
+    const BatchInst &I = bi[unit_inst[blockIdx.x]];
+    if (m > I.Nt) return;
+    const Problem &p = I.p;
+    const UnitMap um = unit_map(I, blockIdx.x - I.adj_unit_begin, PPT);
+    const int N = um.N, mask = N - 1, TS = int(p.table_stride);
+    float *accT = ring + size_t(kRing) * S * ts_max;
+    const unsigned slab_bytes = unsigned(TS) * 4u;
+
+    long long P[PPT], V[PPT], V0[PPT];
+    bool live[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        const long long mm = um.m0 + q;
+        live[q] = mm < p.Nm;
+        V0[q] = I.nodes[live[q] ? mm : 0].V0;
+        V[q] = V0[q];
+        P[q] = (long long)um.s << 40;
+    }
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < kRing; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned g = 0;  // chunks consumed (both sweeps): slot g % kRing, parity (g / kRing) & 1
+    // chunk j of a sweep: slabs [k_lo, k_hi]; desc: k_hi = m-1-j*S; asc: k_lo = j*S
+    auto range = [&](bool asc, int j, int &k_lo, int &k_hi) {
+        if (asc) {
+            k_lo = j * S;
+            k_hi = min(m - 1, k_lo + S - 1);
+        } else {
+            k_hi = m - 1 - j * S;
+            k_lo = max(0, k_hi - S + 1);
+        }
+    };
+    auto issue = [&](bool asc, int j, unsigned gg) {
+        int k_lo, k_hi;
+        range(asc, j, k_lo, k_hi);
+        const unsigned bytes = unsigned(k_hi - k_lo + 1) * slab_bytes;
+        const unsigned bar = smem_addr(&full_bar[gg % kRing]);
+        mbar_expect_tx(bar, bytes);
+        bulk_g2s(smem_addr(ring + (gg % kRing) * S * ts_max), I.tables + (long long)k_lo * TS, bytes, bar);
+    };
+    const int nch = (m + S - 1) / S;
+    bool ok = true;
+    // 1. the characteristics to the foot, slabs m-1..0 (fixed point)
+    if (m > 0) {
+        if (threadIdx.x == 0)
+            for (int j = 0; j < kRing && j < nch; ++j) issue(false, j, g + j);
+        for (int j = 0; j < nch; ++j, ++g) {
+            ok &= mbar_wait(smem_addr(&full_bar[g % kRing]), (g / kRing) & 1u);
+            const float *chunk = ring + (g % kRing) * S * ts_max;
+            int k_lo, k_hi;
+            range(false, j, k_lo, k_hi);
+            for (int k = k_hi; k >= k_lo; --k) {
+                const float *tk = chunk + (k - k_lo) * TS;
+                const float h = k == 0 ? 0.5f : 1.0f;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    P[q] -= V[q];
+                    int J;
+                    float xi;
+                    fx_locate(P[q], mask, J, xi);
+                    V[q] += fix40(h * kick_lookup(tk, N, J, xi));
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0 && j + kRing < nch) issue(false, j + kRing, g + kRing);
+        }
+    }
+    // 2. seed at the foot
+    const float a = float(-p.wv * I.lambda[um.s]);
+    const float dx = float(p.dx[0]), dxdt = float(p.dx[0] / p.dt);
+    float xb[PPT], vb[PPT], vbc[PPT];
+    double th[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        xb[q] = vb[q] = vbc[q] = 0.f;
+        if (!live[q]) continue;
+        const float X = float(double(P[q]) * 0x1p-40);
+        const float x = float(p.xmin[0]) + X * dx;
+        const float u = float(I.nodes[um.m0 + q].u0) + float(double(V[q] - V0[q]) * 0x1p-40) * dxdt;
+        const F0GradF gr = f0_grad_1d_f(p, x, u);
+        xb[q] = a * dx * gr.fx;
+        vb[q] = a * dxdt * gr.fu;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) th[i] += double(a) * double(gr.dth[i]);
+    }
+    // 3. reverse sweep, slabs 0..m-1 (ascending)
+    if (m > 0) {
+        if (threadIdx.x == 0)
+            for (int j = 0; j < kRing && j < nch; ++j) issue(true, j, g + j);
+        for (int i = threadIdx.x; i < S * 3 * N; i += blockDim.x) accT[i] = 0.f;
+        __syncthreads();
+        for (int j = 0; j < nch; ++j, ++g) {
+            ok &= mbar_wait(smem_addr(&full_bar[g % kRing]), (g / kRing) & 1u);
+            const float *chunk = ring + (g % kRing) * S * ts_max;
+            int k_lo, k_hi;
+            range(true, j, k_lo, k_hi);
+            for (int k = k_lo; k <= k_hi; ++k) {
+                const float *tk = chunk + (k - k_lo) * TS;
+                float *ak = accT + (k - k_lo) * 3 * N;
+                const float h = k == 0 ? 0.5f : 1.0f;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    int J;
+                    float xi;
+                    fx_locate(P[q], mask, J, xi);
+                    const float2 ab = reinterpret_cast<const float2 *>(tk)[J];
+                    const float c = tk[2 * N + J];
+                    const float gk = fmaf(xi, fmaf(xi, c, ab.y), ab.x);  // = kick_lookup(tk, N, J, xi)
+                    const float gp = fmaf(2.f * xi, c, ab.y);
+                    // adjoint
+                    const float vh = vb[q] * h;
+                    if (live[q]) {
+                        red_shared_add(ak + J, vh);
+                        red_shared_add(ak + N + J, vh * xi);
+                        red_shared_add(ak + 2 * N + J, vh * xi * xi);
+                    }
+                    xb[q] = fmaf(vh, gp, xb[q]);
+                    {   // vb -= xb, compensated
+                        const float y = -xb[q] - vbc[q];
+                        const float t = vb[q] + y;
+                        vbc[q] = (t - vb[q]) - y;
+                        vb[q] = t;
+                    }
+                    // inverse substep (bit-exact)
+                    V[q] -= fix40(h * gk);
+                    P[q] += V[q];
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0 && j + kRing < nch) issue(true, j + kRing, g + kRing);
+            for (int i = threadIdx.x; i < (k_hi - k_lo + 1) * 3 * N; i += blockDim.x) {
+                const float v = accT[i];
+                if (v != 0.f) {
+                    atomicAdd(I.muT + (long long)k_lo * 3 * N + i, f2d_bits(v));
+                    accT[i] = 0.f;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (!ok) atomicOr(err, kErrStageTimeout);
+    adj::block_theta_add(th, theta_acc, slots, blockIdx.x);
+}
+
+// lambda_m of every instance from the kick-table adjoints of slab m: the
+// coefficient adjoint of each cell's quadratic (K A = K (c2 - c0)/2,
+// K B = K (c0 - 2 c1 + c2), K C = K (3 (c1 - c2) - c0 + c3)/2), folded
+// onto the N nodes, through G_c^T, plus 2 dt L/N phi_m.
+__global__ void batch_adjoint_lambda_split_kernel(const BatchInst *__restrict__ bi, int m)
+{
+    __shared__ double cb[kBatchMaxN + 8];
+    __shared__ double mt[kBatchMaxN];
+    const BatchInst &I = bi[blockIdx.x];
+    if (m > I.Nt) return;
+    const Problem &p = I.p;
+    const int N = p.N[0], P = p.P[0];
+    const double K = -p.dt * p.dt * p.dxinv[0] * p.dxinv[0];
+    const double *t = I.muT + (long long)m * 3 * N;
+    // padded coefficient adjoint: cell i feeds c[i..i+3]
+    for (int q = threadIdx.x; q < P; q += blockDim.x) {
+        double v = 0;
+        for (int j = 0; j < 4; ++j) {
+            const int i = q - j;
+            if (i < 0 || i >= N) continue;
+            const double A = t[i], B = t[N + i], C = t[2 * N + i];
+            const double w = j == 0 ? (-0.5 * A + B - 0.5 * C)
+                           : j == 1 ? (-2.0 * B + 1.5 * C)
+                           : j == 2 ? (0.5 * A + B - 1.5 * C)
+                                    : 0.5 * C;
+            v += K * w;
+        }
+        cb[q] = v;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double v = cb[i];
+        for (int q = i + N; q < P; q += N) v += cb[q];
+        mt[i] = v;
+    }
+    __syncthreads();
+    double b[4];
+    bspline_basis<double, 4, 0>(0.0, b);
+    const double scale = 2.0 * p.dt * p.L[0] / N;
+    const double *slab = I.hist + (long long)m * p.hist_stride;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double phi = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) phi += b[j] * slab[i + j];
+        double s = 0;
+        for (int j = 0; j < N; ++j) {
+            int d = j - i;
+            d += d < 0 ? N : 0;
+            s = fma(I.green[d], mt[j], s);
+        }
+        I.lambda[i] = scale * phi + s;
+    }
+}
+
 // ---------------------------------------------------------------------------
 
 cudaError_t launch_batch_trace(const BatchLaunch &L, int n, cudaStream_t st)
@@ -403,6 +713,24 @@ cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st)
 
 cudaError_t launch_batch_adjoint_step(const BatchLaunch &L, int m, cudaStream_t st)
 {
+    if (L.precision == NUFI_PREC_FP32_SPLIT) {
+        batch_adjoint_lambda_split_kernel<<<L.count, 256, 0, st>>>(L.inst, m);
+        const size_t smem = (size_t(kRingSlots) * L.adj_chunk * L.ts_max + size_t(L.adj_chunk) * 3 * L.max_N) *
+                            sizeof(float);
+        void (*fs)(const BatchInst *, const int *, int, int, int, double *, long long, unsigned *) = nullptr;
+        switch (L.adj_ppt) {
+        case 1: fs = batch_adjoint_split_kernel<1>; break;
+        case 2: fs = batch_adjoint_split_kernel<2>; break;
+        case 4: fs = batch_adjoint_split_kernel<4>; break;
+        case 8: fs = batch_adjoint_split_kernel<8>; break;
+        default: return cudaErrorInvalidValue;
+        }
+        cudaError_t e = cudaFuncSetAttribute(fs, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        fs<<<L.adj_units, 256, smem, st>>>(L.inst, L.adj_unit_inst, m, L.adj_chunk, L.ts_max, L.theta_acc,
+                                          L.adj_units, L.err);
+        return cudaGetLastError();
+    }
     batch_adjoint_lambda_kernel<<<L.count, 256, 0, st>>>(L.inst, m);
     const size_t smem = size_t(L.adj_chunk) * L.max_P * sizeof(double);
     void (*fn)(const BatchInst *, const int *, int, int, double *, long long, unsigned *) = nullptr;

@@ -393,6 +393,7 @@ int build_split_tables(nufi_handle *h)
             nd.sig_hi = float(sig);
             nd.sig_lo = float(sig - double(nd.sig_hi));
             nd.S0 = int(S0);
+            nd.V0 = std::llround(std::ldexp(w0, 40));
             const double gm = c0 * std::exp(-u0 * u0 / 2);
             if (p.f0_kind == NUFI_F0_LANDAU) {
                 nd.g = 0.39894228040143267793994 * std::exp(-u0 * u0 / 2);
@@ -1117,7 +1118,14 @@ int batch_autotune(nufi_batch *b)
     b->L.slabs_per_chunk = std::max(1, bc.S);
     b->L.smem = size_t(kRingSlots) * b->L.slabs_per_chunk * ts_max * sizeof(float);
     log += "], \"adjoint\": [";
-    std::vector<int> acands = tune ? std::vector<int>{1, 2, 4} : std::vector<int>{2};
+    std::vector<int> acands = tune ? (b->precision == NUFI_PREC_FP32_SPLIT ? std::vector<int>{2, 4, 8}
+                                                                          : std::vector<int>{1, 2, 4})
+                                   : std::vector<int>{b->precision == NUFI_PREC_FP32_SPLIT ? 4 : 2};
+    // NUFI_BATCH_ADJ_PPT=k fixes the adjoint's chains per thread
+    if (const char *ap = std::getenv("NUFI_BATCH_ADJ_PPT")) {
+        const int k = std::atoi(ap);
+        if (k == 1 || k == 2 || k == 4 || (k == 8 && b->precision == NUFI_PREC_FP32_SPLIT)) acands = {k};
+    }
     float abest = -1;
     int abc = acands[0];
     for (size_t c = 0; c < acands.size(); ++c) {
@@ -1245,9 +1253,13 @@ int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_b
             (e = balloc(b.get(), &I.epart, size_t(nsb))) != cudaSuccess ||
             (e = balloc(b.get(), &I.ecount, 1)) != cudaSuccess ||
             (e = balloc(b.get(), &I.mu, size_t(I.Nt + 1) * p.P[0])) != cudaSuccess ||
-            (e = balloc(b.get(), &I.lambda, size_t(p.N[0]))) != cudaSuccess)
+            (e = balloc(b.get(), &I.lambda, size_t(p.N[0]))) != cudaSuccess ||
+            (b->precision == NUFI_PREC_FP32_SPLIT &&
+             (e = balloc(b.get(), &I.muT, size_t(I.Nt + 1) * 3 * p.N[0])) != cudaSuccess))
             return bail(bcuda(b.get(), e, "cudaMalloc"));
         if ((e = cudaMemset(I.ecount, 0, sizeof(unsigned))) != cudaSuccess ||
+            (e = cudaMemset(I.lambda, 0, size_t(p.N[0]) * sizeof(double))) != cudaSuccess ||
+            (I.muT && (e = cudaMemset(I.muT, 0, size_t(I.Nt + 1) * 3 * p.N[0] * sizeof(double))) != cudaSuccess) ||
             (e = cudaMemset(I.mu, 0, size_t(I.Nt + 1) * p.P[0] * sizeof(double))) != cudaSuccess)
             return bail(bcuda(b.get(), e, "cudaMemset"));
         I.node_begin = nodes;
@@ -1260,6 +1272,8 @@ int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_b
         max_units += u1;
         max_adj += u1;
         max_P = std::max(max_P, p.P[0]);
+        b->L.ts_max = std::max(b->L.ts_max, int(p.table_stride));
+        b->L.max_N = std::max(b->L.max_N, p.N[0]);
         b->maxNt = std::max(b->maxNt, I.Nt);
         b->point_steps += p.Nq * ((long long)I.Nt * (I.Nt + 1) / 2);
         pow2 = pow2 && ((p.N[0] & (p.N[0] - 1)) == 0);
@@ -1347,13 +1361,16 @@ int nufi_batch_backward(nufi_batch *b, double *grad)
 {
     if (!b || !grad) return bfail(b, NUFI_ERR_INVALID, "null argument");
     if (!b->forward_done) return bfail(b, NUFI_ERR_RANGE, "batch backward: run the forward first");
+    if (b->precision == NUFI_PREC_FP32_SPLIT && !b->L.pow2)
+        return bfail(b, NUFI_ERR_UNSUPPORTED, "batch backward (FP32-split): Nx must be powers of two");
     DeviceGuard g(b->device);
     if (!b->bwd) {
         int st = capture(b, &b->bwd, [&] {
             cudaError_t e = cudaSuccess;
             for (const BatchInst &I : b->hi)
                 if (e == cudaSuccess)
-                    e = cudaMemsetAsync(I.mu, 0, size_t(I.Nt + 1) * I.p.P[0] * sizeof(double), b->stream);
+                    e = I.muT ? cudaMemsetAsync(I.muT, 0, size_t(I.Nt + 1) * 3 * I.p.N[0] * sizeof(double), b->stream)
+                              : cudaMemsetAsync(I.mu, 0, size_t(I.Nt + 1) * I.p.P[0] * sizeof(double), b->stream);
             if (e == cudaSuccess)
                 e = cudaMemsetAsync(b->theta_acc, 0, size_t(4) * b->L.adj_units * sizeof(double), b->stream);
             for (int m = b->maxNt; m >= 0 && e == cudaSuccess; --m) e = launch_batch_adjoint_step(b->L, m, b->stream);

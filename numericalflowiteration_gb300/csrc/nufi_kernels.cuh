@@ -24,6 +24,7 @@ struct SplitNode {
     float sig_hi, sig_lo;
     float ga, gb;   // FP32 equilibrium factors (meaning depends on f0)
     int S0;         // integer free-streaming shift, reduced mod N
+    long long V0;   // u0 dt/dx in units of 2^-40 cells per substep (fixed-point adjoint)
 };
 
 __device__ __forceinline__ void neumaier_add(double &sum, double &comp, double x)
@@ -203,6 +204,7 @@ struct BatchInst {
     double *epart;    // [solve_blocks]
     unsigned *ecount; // [1], zero between launches
     double *mu;       // [(Nt+1)][P] slab adjoints
+    double *muT;      // [(Nt+1)][3N] kick-table adjoints (FP32-split adjoint)
     double *lambda;   // [N]
     int Nt, tpn;
     int unit_begin, units;
@@ -219,6 +221,7 @@ struct BatchLaunch {
     int units = 0, solve_blocks = 0;
     long long total_nodes = 0;
     int adj_ppt = 2, adj_chunk = 8, adj_units = 0, max_P = 0;
+    int ts_max = 0, max_N = 0;  // largest table stride (floats) and N of the batch
     double *theta_acc = nullptr;
     unsigned *err = nullptr;
 };

@@ -363,21 +363,26 @@ __global__ void batch_theta_reduce_kernel(const BatchInst *__restrict__ bi, int 
 
 
 // ---------------------------------------------------------------------------
-// FP32-split adjoint (1D, N a power of two).  The characteristics are
-// recomputed in fixed point so that every substep inverts exactly: position
-// P and velocity V are int64 in units of 2^-40 cells (per substep), the
-// kick is the FP32 kick table's K(A + B xi + C xi^2) (the field of the split
-// forward), rounded to 2^-40 cells:
-//   forward   P -= V;  xi, cell from P;  V += rnd(h g(xi) 2^40)
-//   inverse   V -= rnd(h g(xi) 2^40);  P += V        (bit-exact)
-// so the reverse sweep walks exactly the trajectory the recomputation
-// produced (no drift of a recomputed path).  The adjoint of one substep in
-// cells (X) and cells per substep (V), with g' = dg/dxi:
-//   Xbar <- Xbar + Vbar h g';  Vbar <- Vbar - Xbar   (Vbar compensated)
-//   table adjoints of slab k at the cell: Abar += Vbar h, Bbar += Vbar h xi,
-//   Cbar += Vbar h xi^2   (shared-memory FP32 sums, flushed into FP64)
-// The seed at the foot: Xbar = a dx df0/dx, Vbar = a (dx/dt) df0/du with
-// a = -w lambda_m(s); thetabar += a df0/dtheta (FP64).
+// FP32-split adjoint (1D, N a power of two), with the characteristics
+// recomputed in the split arithmetic itself and checkpointed:
+//   pass 1  the trace to the foot (slabs m-1..0), in chunks of kAdjChunk
+//           slabs aligned at slab 0 (chunk c = slabs [8c, 8c+7]); the chain
+//           state entering each chunk (unwrapped cell U, fraction xi, kick
+//           sums dwT, dwTc) goes to a checkpoint area of this CTA
+//   seed    at the foot: Xbar = a dx df0/dx, Vbar = a (dx/dt) df0/du,
+//           thetabar += a df0/dtheta, a = -w lambda_m(s) (x unwrapped)
+//   pass 2  chunks c = 0, 1, ...: reload the checkpoint, recompute the
+//           chunk's substeps (same operations, so the same bits) keeping
+//           each substep's cell and fraction in registers, then run the
+//           adjoint of those substeps in ascending k:
+//             Xbar <- Xbar + Vbar h g'(xi);  Vbar <- Vbar - Xbar (compensated)
+//             kick-table adjoints of slab k: (Abar, Bbar, Cbar) += Vbar h (1, xi, xi^2)
+//           (cells and cells per substep; g' = d/dxi of the kick quadratic),
+//           summed in shared memory by red.shared.add.f32 and flushed into
+//           the instance's FP64 table adjoints after each chunk.
+// About three forward passes of work; the adjoint's own recurrences are
+// short.  A persistent grid: CTA b handles units b, b + G, ...; its
+// checkpoints live in ckpt + b * (chunks * 4 * 256 * PPT) floats.
 // ---------------------------------------------------------------------------
 
 // f0 partial derivatives in FP32 at x (unwrapped), u: as adj::f0_grad_1d.
@@ -418,23 +423,6 @@ __device__ __forceinline__ F0GradF f0_grad_1d_f(const Problem &p, float x, float
     return r;
 }
 
-// v * 2^40 rounded to an integer, without a 64-bit conversion (which runs
-// on the FP64 pipe): s = v 2^20 is split exactly into its nearest integer
-// hi (round-to-nearest add of 1.5 2^23) and the remainder s - hi (exact,
-// |s - hi| <= 1/2), whose 2^20 multiple is rounded the same way:
-// v 2^40 = hi 2^20 + lo.  Valid for |v| < 4 (kicks are far smaller); the
-// forward and the inverse substep apply it to the same float, so the
-// fixed-point path inverts exactly whatever the rounding.
-__device__ __forceinline__ long long fix40(float v)
-{
-    const float s = v * 1048576.0f;
-    const float mh = __fadd_rn(s, kMagic);
-    const int hi = __float_as_int(mh) - kMagicBits;
-    const float r = __fmul_rn(__fsub_rn(s, __fsub_rn(mh, kMagic)), 1048576.0f);
-    const int lo = __float_as_int(__fadd_rn(r, kMagic)) - kMagicBits;
-    return (long long)hi * 1048576LL + lo;
-}
-
 // float -> double by bit manipulation (exact for normal numbers; zero and
 // subnormals give 0), keeping the conversion off the FP64 pipe.
 __device__ __forceinline__ double f2d_bits(float f)
@@ -454,155 +442,190 @@ __device__ __forceinline__ void red_shared_add(float *p, float v)
     asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(smem_addr(p)), "f"(v) : "memory");
 }
 
-// Cell and fraction of a fixed-point position (N a power of two).
-__device__ __forceinline__ void fx_locate(long long P, int mask, int &J, float &xi)
+// One split substep with an unwrapped cell count U (J = U & mask): the
+// drift of trace_chunk (split_device.cuh) and the kick lookup.
+__device__ __forceinline__ float split_substep(int &U, float &xi, float dwT, float dwC, float shi, int S0um, int mask,
+                                               const float *tk, int N, int &J)
 {
-    const unsigned hi = unsigned((unsigned long long)P >> 32), lo = unsigned(P);
-    J = int(hi >> 8) & mask;                     // cell = P >> 40 (two's complement, masked)
-    const unsigned frac = __funnelshift_r(lo, hi, 8);  // bits 8..39: the top 32 of the fraction
-    xi = __int_as_float(0x3f800000 | (frac >> 9)) - 1.0f;
+    const float t = ((xi - shi) - dwT) - dwC;
+    const float mg = __fadd_rd(t, kMagic);
+    U = U - S0um + __float_as_int(mg);
+    J = U & mask;
+    xi = t - (mg - kMagic);
+    return kick_lookup(tk, N, J, xi);
 }
 
 template <int PPT>
 __global__ void __launch_bounds__(256, 1) batch_adjoint_split_kernel(const BatchInst *__restrict__ bi,
-                                                                  const int *__restrict__ unit_inst, int m, int S,
-                                                                  int ts_max, double *__restrict__ theta_acc,
-                                                                  long long slots, unsigned *err)
+                                                                     const int *__restrict__ unit_inst, int units,
+                                                                     int m, int ts_max, int max_chunks,
+                                                                     float *__restrict__ ckpt,
+                                                                     double *__restrict__ theta_acc, long long slots,
+                                                                     unsigned *err)
 {
-    extern __shared__ __align__(128) float ring[];  // [kRing][S][ts_max], then [S][3N] table adjoints
+    constexpr int SC = kAdjChunk;
+    extern __shared__ __align__(128) float ring[];  // [kRing][SC][ts_max], then [SC][3 max_N]
     __shared__ __align__(8) unsigned long long full_bar[kRing];
-    const BatchInst &I = bi[unit_inst[blockIdx.x]];
-    if (m > I.Nt) return;
-    const Problem &p = I.p;
-    const UnitMap um = unit_map(I, blockIdx.x - I.adj_unit_begin, PPT);
-    const int N = um.N, mask = N - 1, TS = int(p.table_stride);
-    float *accT = ring + size_t(kRing) * S * ts_max;
-    const unsigned slab_bytes = unsigned(TS) * 4u;
-
-    long long P[PPT], V[PPT], V0[PPT];
-    bool live[PPT];
-#pragma unroll
-    for (int q = 0; q < PPT; ++q) {
-        const long long mm = um.m0 + q;
-        live[q] = mm < p.Nm;
-        V0[q] = I.nodes[live[q] ? mm : 0].V0;
-        V[q] = V0[q];
-        P[q] = (long long)um.s << 40;
-    }
+    float *accT = ring + size_t(kRing) * SC * ts_max;
     if (threadIdx.x == 0) {
         for (int r = 0; r < kRing; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
         mbar_fence_init();
     }
     __syncthreads();
-    unsigned g = 0;  // chunks consumed (both sweeps): slot g % kRing, parity (g / kRing) & 1
-    // chunk j of a sweep: slabs [k_lo, k_hi]; desc: k_hi = m-1-j*S; asc: k_lo = j*S
-    auto range = [&](bool asc, int j, int &k_lo, int &k_hi) {
-        if (asc) {
-            k_lo = j * S;
-            k_hi = min(m - 1, k_lo + S - 1);
-        } else {
-            k_hi = m - 1 - j * S;
-            k_lo = max(0, k_hi - S + 1);
-        }
-    };
-    auto issue = [&](bool asc, int j, unsigned gg) {
-        int k_lo, k_hi;
-        range(asc, j, k_lo, k_hi);
-        const unsigned bytes = unsigned(k_hi - k_lo + 1) * slab_bytes;
-        const unsigned bar = smem_addr(&full_bar[gg % kRing]);
-        mbar_expect_tx(bar, bytes);
-        bulk_g2s(smem_addr(ring + (gg % kRing) * S * ts_max), I.tables + (long long)k_lo * TS, bytes, bar);
-    };
-    const int nch = (m + S - 1) / S;
+    const int t = threadIdx.x;
+    float *ck = ckpt + (size_t)blockIdx.x * max_chunks * 4 * 256 * PPT;
+    unsigned g = 0;  // chunks consumed by this CTA: slot g % kRing, parity (g / kRing) & 1
     bool ok = true;
-    // 1. the characteristics to the foot, slabs m-1..0 (fixed point)
-    if (m > 0) {
+    for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+        const BatchInst &I = bi[unit_inst[unit]];
+        if (m > I.Nt) continue;
+        const Problem &p = I.p;
+        const UnitMap um = unit_map(I, unit - I.adj_unit_begin, PPT);
+        const int N = um.N, mask = N - 1, TS = int(p.table_stride);
+        const unsigned slab_bytes = unsigned(TS) * 4u;
+        const int C = (m + SC - 1) / SC;  // chunks of this step
+        auto issue = [&](int c, unsigned gg) {
+            const int k_lo = c * SC, k_hi = min(m - 1, k_lo + SC - 1);
+            const unsigned bytes = unsigned(k_hi - k_lo + 1) * slab_bytes;
+            const unsigned bar = smem_addr(&full_bar[gg % kRing]);
+            mbar_expect_tx(bar, bytes);
+            bulk_g2s(smem_addr(ring + (gg % kRing) * SC * ts_max), I.tables + (long long)k_lo * TS, bytes, bar);
+        };
+        int U[PPT], S0um[PPT];
+        float xi[PPT], dwT[PPT], dwTc[PPT], shi[PPT], slo[PPT];
+        bool live[PPT];
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const long long mm = um.m0 + q;
+            live[q] = mm < p.Nm;
+            const SplitNode nd = I.nodes[live[q] ? mm : 0];
+            S0um[q] = nd.S0u + kMagicBits;
+            shi[q] = nd.sig_hi;
+            slo[q] = nd.sig_lo;
+            U[q] = um.s;
+            xi[q] = 0.f;
+            dwT[q] = slo[q];
+            dwTc[q] = 0.f;
+        }
+        // ---- pass 1: chunks C-1 .. 0 (descending k), checkpoint each entry state
         if (threadIdx.x == 0)
-            for (int j = 0; j < kRing && j < nch; ++j) issue(false, j, g + j);
-        for (int j = 0; j < nch; ++j, ++g) {
+            for (int j = 0; j < kRing && j < C; ++j) issue(C - 1 - j, g + j);
+        for (int j = 0; j < C; ++j, ++g) {
+            const int c = C - 1 - j;
+            float *cp = ck + (size_t)c * 4 * 256 * PPT;
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                cp[(0 * PPT + q) * 256 + t] = __int_as_float(U[q]);
+                cp[(1 * PPT + q) * 256 + t] = xi[q];
+                cp[(2 * PPT + q) * 256 + t] = dwT[q];
+                cp[(3 * PPT + q) * 256 + t] = dwTc[q];
+            }
             ok &= mbar_wait(smem_addr(&full_bar[g % kRing]), (g / kRing) & 1u);
-            const float *chunk = ring + (g % kRing) * S * ts_max;
-            int k_lo, k_hi;
-            range(false, j, k_lo, k_hi);
+            const float *chunk = ring + (g % kRing) * SC * ts_max;
+            const int k_lo = c * SC, k_hi = min(m - 1, k_lo + SC - 1);
+            float dwC[PPT];
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) dwC[q] = 0.f;
             for (int k = k_hi; k >= k_lo; --k) {
                 const float *tk = chunk + (k - k_lo) * TS;
                 const float h = k == 0 ? 0.5f : 1.0f;
 #pragma unroll
                 for (int q = 0; q < PPT; ++q) {
-                    P[q] -= V[q];
                     int J;
-                    float xi;
-                    fx_locate(P[q], mask, J, xi);
-                    V[q] += fix40(h * kick_lookup(tk, N, J, xi));
+                    const float kq = split_substep(U[q], xi[q], dwT[q], dwC[q], shi[q], S0um[q], mask, tk, N, J);
+                    dwC[q] = fmaf(h, kq, dwC[q]);
                 }
             }
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) kick(dwT[q], dwTc[q], dwC[q]);
             __syncthreads();
-            if (threadIdx.x == 0 && j + kRing < nch) issue(false, j + kRing, g + kRing);
+            if (threadIdx.x == 0 && j + kRing < C) issue(C - 1 - (j + kRing), g + kRing);
         }
-    }
-    // 2. seed at the foot
-    const float a = float(-p.wv * I.lambda[um.s]);
-    const float dx = float(p.dx[0]), dxdt = float(p.dx[0] / p.dt);
-    float xb[PPT], vb[PPT], vbc[PPT];
-    double th[4] = {0, 0, 0, 0};
+        // ---- seed at the foot
+        const float a = float(-p.wv * I.lambda[um.s]);
+        const float dx = float(p.dx[0]), dxdt = float(p.dx[0] / p.dt);
+        float xb[PPT], vb[PPT], vbc[PPT];
+        double th[4] = {0, 0, 0, 0};
 #pragma unroll
-    for (int q = 0; q < PPT; ++q) {
-        xb[q] = vb[q] = vbc[q] = 0.f;
-        if (!live[q]) continue;
-        const float X = float(double(P[q]) * 0x1p-40);
-        const float x = float(p.xmin[0]) + X * dx;
-        const float u = float(I.nodes[um.m0 + q].u0) + float(double(V[q] - V0[q]) * 0x1p-40) * dxdt;
-        const F0GradF gr = f0_grad_1d_f(p, x, u);
-        xb[q] = a * dx * gr.fx;
-        vb[q] = a * dxdt * gr.fu;
+        for (int q = 0; q < PPT; ++q) {
+            xb[q] = vb[q] = vbc[q] = 0.f;
+            if (!live[q]) continue;
+            const float x = float(p.xmin[0]) + (float(U[q]) + xi[q]) * dx;
+            const float u = I.nodes[um.m0 + q].u0f + ((dwT[q] - dwTc[q]) - slo[q]) * dxdt;
+            const F0GradF gr = f0_grad_1d_f(p, x, u);
+            xb[q] = a * dx * gr.fx;
+            vb[q] = a * dxdt * gr.fu;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) th[i] += double(a) * double(gr.dth[i]);
-    }
-    // 3. reverse sweep, slabs 0..m-1 (ascending)
-    if (m > 0) {
-        if (threadIdx.x == 0)
-            for (int j = 0; j < kRing && j < nch; ++j) issue(true, j, g + j);
-        for (int i = threadIdx.x; i < S * 3 * N; i += blockDim.x) accT[i] = 0.f;
+            for (int i = 0; i < 4; ++i) th[i] += double(a) * double(gr.dth[i]);
+        }
+        // ---- pass 2: chunks 0 .. C-1 (ascending k)
+        for (int i = threadIdx.x; i < SC * 3 * N; i += blockDim.x) accT[i] = 0.f;
         __syncthreads();
-        for (int j = 0; j < nch; ++j, ++g) {
+        if (threadIdx.x == 0)
+            for (int j = 0; j < kRing && j < C; ++j) issue(j, g + j);
+        for (int c = 0; c < C; ++c, ++g) {
+            const float *cp = ck + (size_t)c * 4 * 256 * PPT;
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                U[q] = __float_as_int(cp[(0 * PPT + q) * 256 + t]);
+                xi[q] = cp[(1 * PPT + q) * 256 + t];
+                dwT[q] = cp[(2 * PPT + q) * 256 + t];
+                dwTc[q] = cp[(3 * PPT + q) * 256 + t];
+            }
             ok &= mbar_wait(smem_addr(&full_bar[g % kRing]), (g / kRing) & 1u);
-            const float *chunk = ring + (g % kRing) * S * ts_max;
-            int k_lo, k_hi;
-            range(true, j, k_lo, k_hi);
-            for (int k = k_lo; k <= k_hi; ++k) {
-                const float *tk = chunk + (k - k_lo) * TS;
-                float *ak = accT + (k - k_lo) * 3 * N;
+            const float *chunk = ring + (g % kRing) * SC * ts_max;
+            const int k_lo = c * SC, k_hi = min(m - 1, k_lo + SC - 1);
+            // recompute: substep k = k_lo + i keeps its cell and fraction
+            int Js[SC][PPT];
+            float xs[SC][PPT];
+            float dwC[PPT];
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) dwC[q] = 0.f;
+#pragma unroll
+            for (int i = SC - 1; i >= 0; --i) {
+                const int k = k_lo + i;
+                if (k > k_hi) continue;
+                const float *tk = chunk + i * TS;
                 const float h = k == 0 ? 0.5f : 1.0f;
 #pragma unroll
                 for (int q = 0; q < PPT; ++q) {
                     int J;
-                    float xi;
-                    fx_locate(P[q], mask, J, xi);
-                    const float2 ab = reinterpret_cast<const float2 *>(tk)[J];
-                    const float c = tk[2 * N + J];
-                    const float gk = fmaf(xi, fmaf(xi, c, ab.y), ab.x);  // = kick_lookup(tk, N, J, xi)
-                    const float gp = fmaf(2.f * xi, c, ab.y);
-                    // adjoint
+                    const float kq = split_substep(U[q], xi[q], dwT[q], dwC[q], shi[q], S0um[q], mask, tk, N, J);
+                    dwC[q] = fmaf(h, kq, dwC[q]);
+                    Js[i][q] = J;
+                    xs[i][q] = xi[q];
+                }
+            }
+            // adjoint of the chunk's substeps, k ascending
+#pragma unroll
+            for (int i = 0; i < SC; ++i) {
+                const int k = k_lo + i;
+                if (k > k_hi) continue;
+                const float *tk = chunk + i * TS;
+                float *ak = accT + i * 3 * N;
+                const float h = k == 0 ? 0.5f : 1.0f;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    const int J = Js[i][q];
+                    const float x = xs[i][q];
+                    const float b = reinterpret_cast<const float2 *>(tk)[J].y;
+                    const float cc = tk[2 * N + J];
+                    const float gp = fmaf(2.f * x, cc, b);
                     const float vh = vb[q] * h;
                     if (live[q]) {
                         red_shared_add(ak + J, vh);
-                        red_shared_add(ak + N + J, vh * xi);
-                        red_shared_add(ak + 2 * N + J, vh * xi * xi);
+                        red_shared_add(ak + N + J, vh * x);
+                        red_shared_add(ak + 2 * N + J, vh * x * x);
                     }
                     xb[q] = fmaf(vh, gp, xb[q]);
-                    {   // vb -= xb, compensated
-                        const float y = -xb[q] - vbc[q];
-                        const float t = vb[q] + y;
-                        vbc[q] = (t - vb[q]) - y;
-                        vb[q] = t;
-                    }
-                    // inverse substep (bit-exact)
-                    V[q] -= fix40(h * gk);
-                    P[q] += V[q];
+                    const float y = -xb[q] - vbc[q];
+                    const float tt = vb[q] + y;
+                    vbc[q] = (tt - vb[q]) - y;
+                    vb[q] = tt;
                 }
             }
             __syncthreads();
-            if (threadIdx.x == 0 && j + kRing < nch) issue(true, j + kRing, g + kRing);
+            if (threadIdx.x == 0 && c + kRing < C) issue(c + kRing, g + kRing);
             for (int i = threadIdx.x; i < (k_hi - k_lo + 1) * 3 * N; i += blockDim.x) {
                 const float v = accT[i];
                 if (v != 0.f) {
@@ -612,9 +635,9 @@ __global__ void __launch_bounds__(256, 1) batch_adjoint_split_kernel(const Batch
             }
             __syncthreads();
         }
+        adj::block_theta_add(th, theta_acc, slots, unit);
     }
     if (!ok) atomicOr(err, kErrStageTimeout);
-    adj::block_theta_add(th, theta_acc, slots, blockIdx.x);
 }
 
 // lambda_m of every instance from the kick-table adjoints of slab m: the
@@ -698,6 +721,22 @@ cudaError_t launch_batch_trace(const BatchLaunch &L, int n, cudaStream_t st)
     return cudaGetLastError();
 }
 
+size_t adjoint_split_smem(const BatchLaunch &L)
+{
+    return (size_t(kRingSlots) * kAdjChunk * L.ts_max + size_t(kAdjChunk) * 3 * L.max_N) * sizeof(float);
+}
+
+int adjoint_split_ctas_per_sm(const BatchLaunch &L, int ppt)
+{
+    int nb = 0;
+    void (*fs)(const BatchInst *, const int *, int, int, int, int, float *, double *, long long, unsigned *) =
+        ppt == 1 ? batch_adjoint_split_kernel<1> : batch_adjoint_split_kernel<2>;
+    const size_t smem = adjoint_split_smem(L);
+    if (cudaFuncSetAttribute(fs, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fs, 256, smem) != cudaSuccess) return 0;
+    return nb;
+}
+
 cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st)
 {
     cudaError_t e = launch_batch_trace(L, n, st);
@@ -715,20 +754,18 @@ cudaError_t launch_batch_adjoint_step(const BatchLaunch &L, int m, cudaStream_t 
 {
     if (L.precision == NUFI_PREC_FP32_SPLIT) {
         batch_adjoint_lambda_split_kernel<<<L.count, 256, 0, st>>>(L.inst, m);
-        const size_t smem = (size_t(kRingSlots) * L.adj_chunk * L.ts_max + size_t(L.adj_chunk) * 3 * L.max_N) *
-                            sizeof(float);
-        void (*fs)(const BatchInst *, const int *, int, int, int, double *, long long, unsigned *) = nullptr;
+        void (*fs)(const BatchInst *, const int *, int, int, int, int, float *, double *, long long,
+                   unsigned *) = nullptr;
         switch (L.adj_ppt) {
         case 1: fs = batch_adjoint_split_kernel<1>; break;
         case 2: fs = batch_adjoint_split_kernel<2>; break;
-        case 4: fs = batch_adjoint_split_kernel<4>; break;
-        case 8: fs = batch_adjoint_split_kernel<8>; break;
         default: return cudaErrorInvalidValue;
         }
+        const size_t smem = adjoint_split_smem(L);
         cudaError_t e = cudaFuncSetAttribute(fs, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
-        fs<<<L.adj_units, 256, smem, st>>>(L.inst, L.adj_unit_inst, m, L.adj_chunk, L.ts_max, L.theta_acc,
-                                          L.adj_units, L.err);
+        fs<<<L.adj_grid, 256, smem, st>>>(L.inst, L.adj_unit_inst, L.adj_units, m, L.ts_max, L.max_chunks, L.ckpt,
+                                         L.theta_acc, L.adj_units, L.err);
         return cudaGetLastError();
     }
     batch_adjoint_lambda_kernel<<<L.count, 256, 0, st>>>(L.inst, m);

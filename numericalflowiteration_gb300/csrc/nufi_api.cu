@@ -393,7 +393,7 @@ int build_split_tables(nufi_handle *h)
             nd.sig_hi = float(sig);
             nd.sig_lo = float(sig - double(nd.sig_hi));
             nd.S0 = int(S0);
-            nd.V0 = std::llround(std::ldexp(w0, 40));
+            nd.S0u = int(S);
             const double gm = c0 * std::exp(-u0 * u0 / 2);
             if (p.f0_kind == NUFI_F0_LANDAU) {
                 nd.g = 0.39894228040143267793994 * std::exp(-u0 * u0 / 2);
@@ -1118,19 +1118,38 @@ int batch_autotune(nufi_batch *b)
     b->L.slabs_per_chunk = std::max(1, bc.S);
     b->L.smem = size_t(kRingSlots) * b->L.slabs_per_chunk * ts_max * sizeof(float);
     log += "], \"adjoint\": [";
-    std::vector<int> acands = tune ? (b->precision == NUFI_PREC_FP32_SPLIT ? std::vector<int>{2, 4, 8}
-                                                                          : std::vector<int>{1, 2, 4})
-                                   : std::vector<int>{b->precision == NUFI_PREC_FP32_SPLIT ? 4 : 2};
+    const bool split = b->precision == NUFI_PREC_FP32_SPLIT;
+    std::vector<int> acands = tune ? (split ? std::vector<int>{1, 2} : std::vector<int>{1, 2, 4})
+                                   : std::vector<int>{2};
     // NUFI_BATCH_ADJ_PPT=k fixes the adjoint's chains per thread
     if (const char *ap = std::getenv("NUFI_BATCH_ADJ_PPT")) {
         const int k = std::atoi(ap);
-        if (k == 1 || k == 2 || k == 4 || (k == 8 && b->precision == NUFI_PREC_FP32_SPLIT)) acands = {k};
+        if (k == 1 || k == 2 || (k == 4 && !split)) acands = {k};
+    }
+    // FP32-split adjoint: a persistent grid (CTAs per SM from the occupancy
+    // of each candidate) and one checkpoint area per CTA
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    b->L.max_chunks = (b->maxNt + kAdjChunk - 1) / kAdjChunk;
+    auto split_grid = [&](int ppt) {
+        const int per_sm = std::max(1, adjoint_split_ctas_per_sm(b->L, ppt));
+        return std::min(b->L.adj_units, per_sm * std::max(1, sms));
+    };
+    if (split) {
+        size_t need = 0;
+        for (int ppt : acands) {
+            if ((st = batch_set_units(b, ppt, true))) return st;
+            need = std::max(need, size_t(split_grid(ppt)) * b->L.max_chunks * 4 * 256 * ppt);
+        }
+        cudaError_t ea = balloc(b, &b->L.ckpt, need);
+        if (ea != cudaSuccess) return bcuda(b, ea, "cudaMalloc");
     }
     float abest = -1;
     int abc = acands[0];
     for (size_t c = 0; c < acands.size(); ++c) {
         st = batch_set_units(b, acands[c], true);
         if (st) return st;
+        if (split) b->L.adj_grid = split_grid(acands[c]);
         float ms = tune ? batch_time(b, [&] { return launch_batch_adjoint_step(b->L, n_t, b->stream); }, 1) : 0.0f;
         if (ms < 0) return bcuda(b, cudaGetLastError(), "autotune adjoint");
         char item[96];
@@ -1143,6 +1162,7 @@ int batch_autotune(nufi_batch *b)
     }
     st = batch_set_units(b, abc, true);
     if (st) return st;
+    if (split) b->L.adj_grid = split_grid(abc);
     char tail[160];
     std::snprintf(tail, sizeof(tail), "], \"chosen\": {\"ppt\": %d, \"slabs_per_chunk\": %d, \"adjoint_ppt\": %d, "
                   "\"tuned_at_step\": %d}}", b->L.ppt, b->L.slabs_per_chunk, b->L.adj_ppt, n_t);

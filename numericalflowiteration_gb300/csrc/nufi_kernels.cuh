@@ -24,7 +24,7 @@ struct SplitNode {
     float sig_hi, sig_lo;
     float ga, gb;   // FP32 equilibrium factors (meaning depends on f0)
     int S0;         // integer free-streaming shift, reduced mod N
-    long long V0;   // u0 dt/dx in units of 2^-40 cells per substep (fixed-point adjoint)
+    int S0u;        // the same shift unreduced, floor(u0 dt/dx) (unwrapped positions)
 };
 
 __device__ __forceinline__ void neumaier_add(double &sum, double &comp, double x)
@@ -222,6 +222,8 @@ struct BatchLaunch {
     long long total_nodes = 0;
     int adj_ppt = 2, adj_chunk = 8, adj_units = 0, max_P = 0;
     int ts_max = 0, max_N = 0;  // largest table stride (floats) and N of the batch
+    int adj_grid = 0, max_chunks = 0;  // FP32-split adjoint: persistent CTAs, chunks per step
+    float *ckpt = nullptr;             // its checkpoints: adj_grid x max_chunks x 4 x 256 x adj_ppt floats
     double *theta_acc = nullptr;
     unsigned *err = nullptr;
 };
@@ -229,6 +231,9 @@ cudaError_t launch_batch_trace(const BatchLaunch &L, int n, cudaStream_t st);
 cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st);
 cudaError_t launch_batch_adjoint_step(const BatchLaunch &L, int m, cudaStream_t st);
 cudaError_t launch_batch_theta_reduce(const BatchLaunch &L, double *grad, cudaStream_t st);
+constexpr int kAdjChunk = 8;  // slabs per checkpointed chunk of the FP32-split adjoint
+size_t adjoint_split_smem(const BatchLaunch &L);
+int adjoint_split_ctas_per_sm(const BatchLaunch &L, int ppt);
 
 // FP32 table of one FP64 slab (after upload_phi).
 cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st);

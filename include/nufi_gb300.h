@@ -151,6 +151,32 @@ int nufi_download_energy(nufi_handle *h, int64_t n0, int64_t n1, double *energy)
  * padded slab (stride_t values) out, returns W in *energy.  Blocks. */
 int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double *energy);
 
+/* ---- phase-space sampling and the history on disk ----------------------- */
+/* f at arbitrary points, FP64, from the handle's history (slabs 0..n, or
+ * 0..n-1 for NUFI_EVAL_FTILDA):
+ *   NUFI_EVAL_FTILDA      eval_ftilda (nufi/rho.hpp:31-61, 191-232, 318-367)
+ *   NUFI_EVAL_F           eval_f (nufi/rho.hpp:63-96, 234-281, 369-426)
+ *   NUFI_EVAL_PHASE_FLOW  1D eval_phase_flow (nufi/rho.hpp:98-131): the
+ *                         eval_f trajectory only when n > 1, then
+ *                         x - L floor(x / L); f_out unused.
+ * pts: npts x (x.., v..) doubles; f_out: npts (may be NULL); feet: npts x
+ * (x.., v..) final positions and velocities (may be NULL).  Blocks. */
+#define NUFI_EVAL_FTILDA     0
+#define NUFI_EVAL_F          1
+#define NUFI_EVAL_PHASE_FLOW 2
+int nufi_eval_points(nufi_handle *h, int64_t n, int mode, int64_t npts, const double *pts, double *f_out,
+                     double *feet);
+/* The coefficient history as the reference's text files
+ * (bin/test_nufi_cpu_3d_isolated.cpp:64-72, 190-211): a header of seven
+ * lines (Nt, dt, Nx, Ny, Nz, order, blank) and one coefficient per line,
+ * slabs 0..n1.  nufi_load_history also reads files without the header
+ * (bin/test_nufi_gpu_1d.cpp:239, 364-366), uploads the whole slabs found
+ * (as upload_phi) and returns their count; a header that disagrees with
+ * the handle is NUFI_ERR_INVALID.  Resuming a run: load, then nufi_run
+ * from the first missing step. */
+int nufi_save_history(nufi_handle *h, int64_t n1, const char *path);
+int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs);
+
 /* ---- gradient of the time-integrated field energy ----------------------
  * No counterpart in the reference.  Objective J = 2 dt sum_{n=0}^{n1} W_n
  * (the time integral of int |E|^2 dx as a rectangle sum over the steps),

@@ -41,6 +41,9 @@ SIGNATURES = {
     "nufi_compute_metrics": (ctypes.c_int, [_P, _I64, _I64, _I64]),
     "nufi_describe": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "nufi_forward": (ctypes.c_int, [_P, _I64, _P]),
+    "nufi_eval_points": (ctypes.c_int, [_P, _I64, ctypes.c_int, _I64, _P, _P, _P]),
+    "nufi_save_history": (ctypes.c_int, [_P, _I64, ctypes.c_char_p]),
+    "nufi_load_history": (ctypes.c_int, [_P, ctypes.c_char_p, _P]),
     "nufi_objective": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_backward": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_batch_create": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int, _P]),
@@ -157,6 +160,30 @@ class Simulation:
     def compute_rho(self, n: int, q_begin: int = 0, q_end: int | None = None):
         q_end = self.n_points if q_end is None else q_end
         self._check(self._lib.nufi_compute_rho(self._h, n, q_begin, q_end))
+
+    # -- phase-space sampling, history files -------------------------------
+    EVAL_FTILDA, EVAL_F, EVAL_PHASE_FLOW = 0, 1, 2
+
+    def eval_points(self, n: int, pts: np.ndarray, mode: int = 1, feet: bool = False):
+        """f (mode 1), f~ (mode 0) or the 1D phase flow (mode 2) at points
+        pts[i] = (x.., v..); returns f (or None for mode 2) and, if asked,
+        the final (x.., v..)."""
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        npts = pts.shape[0]
+        f = np.zeros(npts) if mode != 2 else None
+        ft = np.zeros_like(pts) if (feet or mode == 2) else None
+        self._check(self._lib.nufi_eval_points(self._h, n, mode, npts, _ptr(pts), _ptr(f) if f is not None else None,
+                                               _ptr(ft) if ft is not None else None))
+        return (f, ft) if (feet or mode == 2) else f
+
+    def save_history(self, path: str, n1: int | None = None):
+        n1 = self.cfg.Nt if n1 is None else n1
+        self._check(self._lib.nufi_save_history(self._h, n1, str(path).encode()))
+
+    def load_history(self, path: str) -> int:
+        n = ctypes.c_int64()
+        self._check(self._lib.nufi_load_history(self._h, str(path).encode(), ctypes.byref(n)))
+        return n.value
 
     # -- gradient of J = 2 dt sum_n W_n (no reference counterpart) ----------
     def forward(self, n1: int | None = None) -> float:

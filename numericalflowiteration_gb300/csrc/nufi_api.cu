@@ -928,6 +928,117 @@ int nufi_backward(nufi_handle *h, int64_t n1, double *grad)
     return sync_and_check(h);
 }
 
+int nufi_eval_points(nufi_handle *h, int64_t n, int mode, int64_t npts, const double *pts, double *f_out,
+                     double *feet)
+{
+    if (!h || (npts > 0 && !pts)) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
+    if (mode < NUFI_EVAL_FTILDA || mode > NUFI_EVAL_PHASE_FLOW || (mode == NUFI_EVAL_PHASE_FLOW && h->p.dim != 1))
+        return fail(h, NUFI_ERR_INVALID, "eval_points: mode (phase flow is 1D, as the reference's)");
+    if (npts < 0) return fail(h, NUFI_ERR_INVALID, "eval_points: npts < 0");
+    if (npts == 0) return NUFI_OK;
+    DeviceGuard g(h->device);
+    const int D = h->p.dim;
+    const size_t pbytes = size_t(npts) * 2 * D * sizeof(double);
+    double *dp = nullptr, *df = nullptr, *dfeet = nullptr;
+    auto cleanup = [&] {
+        cudaFree(dp);
+        cudaFree(df);
+        cudaFree(dfeet);
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&dp, pbytes)) != cudaSuccess ||
+        (f_out && mode != NUFI_EVAL_PHASE_FLOW && (e = cudaMalloc(&df, size_t(npts) * sizeof(double))) != cudaSuccess) ||
+        (feet && (e = cudaMalloc(&dfeet, pbytes)) != cudaSuccess)) {
+        cleanup();
+        return cuda_fail(h, e, "cudaMalloc");
+    }
+    e = cudaMemcpyAsync(dp, pts, pbytes, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = launch_eval_points(h->p, h->hist, int(n), mode, (long long)npts, dp, df, dfeet, h->err, h->stream);
+    if (e == cudaSuccess && df)
+        e = cudaMemcpyAsync(f_out, df, size_t(npts) * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && dfeet) e = cudaMemcpyAsync(feet, dfeet, pbytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(h->stream);
+        cleanup();
+        return cuda_fail(h, e, "eval_points");
+    }
+    h->launches += 1;
+    const int st = sync_and_check(h);
+    cleanup();
+    return st;
+}
+
+// Coefficient history as text in the reference's layout
+// (bin/test_nufi_cpu_3d_isolated.cpp:64-72, 190-211): seven header lines
+// "Nt = ", "dt = ", "Nx = ", "Ny = ", "Nz = ", "order = " and a blank one,
+// then every coefficient of slabs 0..n1, one per line, slab after slab.
+// 17 significant digits, so FP64 values read back exactly.
+int nufi_save_history(nufi_handle *h, int64_t n1, const char *path)
+{
+    if (!h || !path) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (n1 < 0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step outside [0, Nt]");
+    const Problem &p = h->p;
+    std::vector<double> all(size_t(n1 + 1) * p.stride_t);
+    int st = nufi_download_history(h, 0, n1, all.data());
+    if (st) return st;
+    FILE *f = std::fopen(path, "w");
+    if (!f) return fail(h, NUFI_ERR_INVALID, std::string("save_history: cannot open ") + path);
+    std::fprintf(f, "Nt = %lld\ndt = %.17g\nNx = %d\nNy = %d\nNz = %d\norder = %d\n\n", (long long)n1, p.dt,
+                 p.N[0], p.dim > 1 ? p.N[1] : 1, p.dim > 2 ? p.N[2] : 1, p.order);
+    for (double v : all) std::fprintf(f, "%.17g\n", v);
+    const bool ok = std::fclose(f) == 0;
+    return ok ? NUFI_OK : fail(h, NUFI_ERR_INVALID, "save_history: write failed");
+}
+
+// Reads such a file (or one without the header, as bin/test_nufi_gpu_1d.cpp
+// writes) and uploads its slabs 0..n-1; *n_slabs = n.  A header that
+// disagrees with the handle's grid or order is NUFI_ERR_INVALID.
+int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs)
+{
+    if (!h || !path) return fail(h, NUFI_ERR_INVALID, "null argument");
+    const Problem &p = h->p;
+    FILE *f = std::fopen(path, "r");
+    if (!f) return fail(h, NUFI_ERR_INVALID, std::string("load_history: cannot open ") + path);
+    std::vector<double> vals;
+    char line[512];
+    long long hdr[4] = {-1, -1, -1, -1};  // Nx Ny Nz order
+    while (std::fgets(line, sizeof(line), f)) {
+        char key[32];
+        double v;
+        if (std::sscanf(line, " %31[A-Za-z] = %lf", key, &v) == 2) {
+            const std::string k = key;
+            if (k == "Nx") hdr[0] = (long long)v;
+            else if (k == "Ny") hdr[1] = (long long)v;
+            else if (k == "Nz") hdr[2] = (long long)v;
+            else if (k == "order") hdr[3] = (long long)v;
+            continue;
+        }
+        char *s = line, *end = nullptr;
+        for (;;) {
+            const double x = std::strtod(s, &end);
+            if (end == s) break;
+            vals.push_back(x);
+            s = end;
+        }
+    }
+    std::fclose(f);
+    const long long want[4] = {p.N[0], p.dim > 1 ? p.N[1] : 1, p.dim > 2 ? p.N[2] : 1, p.order};
+    for (int i = 0; i < 4; ++i)
+        if (hdr[i] >= 0 && hdr[i] != want[i])
+            return fail(h, NUFI_ERR_INVALID, "load_history: header does not match the handle's grid or order");
+    const long long ns = (long long)(vals.size() / size_t(p.stride_t));
+    if (ns < 1 || ns > h->cfg.Nt + 1)
+        return fail(h, NUFI_ERR_RANGE, "load_history: no whole slab, or more than Nt + 1 slabs");
+    for (long long n = 0; n < ns; ++n) {
+        const int st = upload_slab(h, n, vals.data() + n * p.stride_t);
+        if (st) return st;
+    }
+    if (n_slabs) *n_slabs = ns;
+    return NUFI_OK;
+}
+
 int nufi_describe(const nufi_handle *h, char *buf, size_t len)
 {
     if (!h || !buf || len == 0) return fail(nullptr, NUFI_ERR_INVALID, "null argument");

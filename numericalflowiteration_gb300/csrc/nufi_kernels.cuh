@@ -100,6 +100,9 @@ __device__ __forceinline__ void write_metrics_block(const double (&m4)[4], doubl
 cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
                               long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st);
 bool fp64_order_supported(int dim, int order);
+// eval_ftilda / eval_f / 1D eval_phase_flow at arbitrary points (FP64).
+cudaError_t launch_eval_points(const Problem &p, const double *hist, int n, int mode, long long npts,
+                               const double *pts, double *f_out, double *feet, unsigned *err, cudaStream_t st);
 
 cudaError_t launch_trace_split(const Problem &p, const LaunchShape &ls, const float *tables, const SplitNode *nodes,
                                const float2 *phase, int n, long long qb, long long qe, double *partial, int *rows,

@@ -299,6 +299,77 @@ cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const dou
     return cudaErrorNotSupported;
 }
 
+// f~ (mode 0, eval_ftilda), f (mode 1, eval_f, nufi/rho.hpp:63-96,
+// 234-281, 369-426) or the phase flow (mode 2, 1D eval_phase_flow,
+// nufi/rho.hpp:98-131: the eval_f trajectory only when n > 1, then x
+// wrapped as x - L floor(x / L)) at arbitrary points, one thread per point.
+// pts: [npts][2D] (x.., v..); f_out (modes 0, 1) may be null; feet
+// (may be null) receives the final (x.., v..).
+template <int D, int ORDER>
+__global__ void eval_points_kernel(const Problem p, const double *__restrict__ hist, int n, int mode, long long npts,
+                                   const double *__restrict__ pts, double *__restrict__ f_out,
+                                   double *__restrict__ feet, unsigned *err)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npts) return;
+    double x[D], u[D], E[D];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+        x[a] = pts[i * 2 * D + a];
+        u[a] = pts[i * 2 * D + D + a];
+    }
+    const double dt = p.dt;
+    const bool trace = mode == 2 ? n > 1 : n > 0;
+    if (trace) {
+        int k = n;
+        if (mode >= 1) {
+            field_fp64<D, ORDER>(p, hist + (long long)n * p.hist_stride, x, E, err);
+#pragma unroll
+            for (int a = 0; a < D; ++a) u[a] += 0.5 * dt * E[a];
+        }
+        while (--k) {
+#pragma unroll
+            for (int a = 0; a < D; ++a) x[a] = x[a] - dt * u[a];
+            field_fp64<D, ORDER>(p, hist + (long long)k * p.hist_stride, x, E, err);
+#pragma unroll
+            for (int a = 0; a < D; ++a) u[a] = u[a] + dt * E[a];
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) x[a] -= dt * u[a];
+        field_fp64<D, ORDER>(p, hist, x, E, err);
+#pragma unroll
+        for (int a = 0; a < D; ++a) u[a] += 0.5 * dt * E[a];
+    }
+    if (mode == 2) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) x[a] = x[a] - p.L[a] * floor(x[a] * p.Linv[a]);
+    } else if (f_out) {
+        f_out[i] = f0_fp64<D>(p, x, u);
+    }
+    if (feet)
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            feet[i * 2 * D + a] = x[a];
+            feet[i * 2 * D + D + a] = u[a];
+        }
+}
+
+cudaError_t launch_eval_points(const Problem &p, const double *hist, int n, int mode, long long npts,
+                               const double *pts, double *f_out, double *feet, unsigned *err, cudaStream_t st)
+{
+    const unsigned blocks = unsigned((npts + 127) / 128);
+#define NUFI_CASE(D, O)                                                                                       \
+    if (p.dim == D && p.order == O) {                                                                        \
+        eval_points_kernel<D, O><<<blocks, 128, 0, st>>>(p, hist, n, mode, npts, pts, f_out, feet, err); \
+        return cudaGetLastError();                                                                           \
+    }
+    NUFI_CASE(1, 3) NUFI_CASE(1, 4) NUFI_CASE(1, 5) NUFI_CASE(1, 6) NUFI_CASE(1, 7) NUFI_CASE(1, 8)
+    NUFI_CASE(2, 3) NUFI_CASE(2, 4) NUFI_CASE(2, 5) NUFI_CASE(2, 6)
+    NUFI_CASE(3, 3) NUFI_CASE(3, 4) NUFI_CASE(3, 5)
+#undef NUFI_CASE
+    return cudaErrorNotSupported;
+}
+
 bool fp64_order_supported(int dim, int order)
 {
     if (dim == 1) return order >= 3 && order <= 8;

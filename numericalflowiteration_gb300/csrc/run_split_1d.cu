@@ -10,7 +10,8 @@
 // barrier:
 //   trace    each CTA: its velocity chains through slabs n-1..0, streamed
 //            through the shared-memory ring (as trace_split_staged.cu);
-//            writes partial[cta][s]
+//            writes partial[s][cta] (node-major: the reduce reads a node's
+//            parts contiguously)
 //   barrier
 //   reduce   node s is reduced by CTA s mod G, one warp per node, lanes in
 //            fixed stride with Neumaier compensation, fixed shuffle tree
@@ -81,16 +82,19 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     double *gs = rs + N;                                                                       // green [5][N]
     unsigned *count = sync, *abort = sync + 1;
 
-    const long long m0 = (long long)blockIdx.x * p.Nm / G;
-    const long long m1 = (long long)(blockIdx.x + 1) * p.Nm / G;
+    // velocity nodes interleaved over the CTAs (chain j of CTA c: c + j G),
+    // so every CTA holds a spread of velocities and the per-step barriers
+    // wait less for the CTAs whose velocities filament most
+    long long mv[PPT];
     int S0m[PPT];
     float shi[PPT], slo[PPT];
     bool live[PPT];
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
-        const long long m = m0 + grp * PPT + q;
-        live[q] = (s < N) && (m < m1);
-        const SplitNode nd = nodes[m < m1 ? m : m0];
+        const long long m = blockIdx.x + (long long)(grp * PPT + q) * G;
+        live[q] = (s < N) && (m < p.Nm);
+        mv[q] = live[q] ? m : blockIdx.x;
+        const SplitNode nd = nodes[mv[q]];
         S0m[q] = nd.S0 + kMagicBits;
         shi[q] = nd.sig_hi;
         slo[q] = nd.sig_lo;
@@ -238,7 +242,7 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
             if (!live[q]) continue;
-            const SplitNode nd = nodes[m0 + grp * PPT + q];
+            const SplitNode nd = nodes[mv[q]];
             acc += double(delta_f0(f, nd, __ldg(phase + I[q]), xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
         }
         if (blockDim.x > unsigned(Nr)) {
@@ -246,14 +250,14 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
             __syncthreads();
             if (grp == 0) acc += combine[s];
         }
-        if (grp == 0 && s < N) partial[(long long)blockIdx.x * N + s] = acc;
+        if (grp == 0 && s < N) partial[(long long)s * G + blockIdx.x] = acc;
         if (!barrier(n)) return;
 
         // ---------------- rho: node blockIdx.x + warp*G ----------------
         if (warp < K) {
             const int node = int(blockIdx.x) + warp * G;
             double sum = 0, comp = 0;
-            for (int r = lane; r < G; r += 32) neumaier_add(sum, comp, __ldcg(partial + (long long)r * N + node));
+            for (int r = lane; r < G; r += 32) neumaier_add(sum, comp, __ldcg(partial + (long long)node * G + r));
             for (int off = 16; off > 0; off >>= 1) {
                 const double os = __shfl_down_sync(0xffffffffu, sum, off);
                 const double oc = __shfl_down_sync(0xffffffffu, comp, off);
@@ -265,14 +269,11 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
         if (!barrier(n)) return;
 
         // ---------------- field solve ----------------
-        double part = 0;
-        for (int j = threadIdx.x; j < N; j += blockDim.x) {
-            const double r = __ldcg(rho + j);
-            rs[j] = r;
-            part += r;
-        }
-        const double mean = block_sum(part, red) / double(N);
-        for (int j = threadIdx.x; j < N; j += blockDim.x) rs[j] -= mean;
+        // rho itself, not rho - mean: every circulant kernel sums to zero
+        // (the k = 0 mode is dropped), so the mean only costs a block-wide
+        // sum per step; the rounding it would remove is ~1e-13 of the
+        // field, far below the FP32-split arithmetic
+        for (int j = threadIdx.x; j < N; j += blockDim.x) rs[j] = __ldcg(rho + j);
         __syncthreads();
         const int slotn = warp / wpn, pw = warp % wpn;
         double a[5] = {0, 0, 0, 0, 0};

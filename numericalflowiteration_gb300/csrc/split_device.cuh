@@ -155,6 +155,7 @@ __device__ __forceinline__ void kick(float &dw, float &dwc, float k)
 struct F0 {
     int kind;
     float alpha, kdx, dx_dt, ub, inv_s2;
+    bool small;  // |k dx| <= 1/4: sin / cos of k dx xi by their Taylor polynomials
 };
 
 __device__ __forceinline__ F0 make_f0(const Problem &p)
@@ -166,7 +167,17 @@ __device__ __forceinline__ F0 make_f0(const Problem &p)
     f.dx_dt = float(p.dx[0] / p.dt);
     f.ub = float(p.f0p[2]);
     f.inv_s2 = p.f0_kind == NUFI_F0_BUMP_ON_TAIL ? float(1.0 / (p.f0p[3] * p.f0p[3])) : 0.0f;
+    f.small = fabs(p.f0p[1] * p.dx[0]) <= 0.25;
     return f;
+}
+
+// sin a and cos a for |a| <= 1/4 by their Taylor polynomials to a^9 / a^8
+// (truncation below 1e-11, far under FP32 rounding).
+__device__ __forceinline__ void sincos_small(float a, float &s, float &c)
+{
+    const float a2 = a * a;
+    s = a * fmaf(a2, fmaf(a2, fmaf(a2, fmaf(a2, 1.0f / 362880.0f, -1.0f / 5040.0f), 1.0f / 120.0f), -1.0f / 6.0f), 1.0f);
+    c = fmaf(a2, fmaf(a2, fmaf(a2, fmaf(a2, 1.0f / 40320.0f, -1.0f / 720.0f), 1.0f / 24.0f), -0.5f), 1.0f);
 }
 
 // f0(foot) - G(u0) in FP32: f0 = (1 + alpha cos kx) G(u), expm1 form so
@@ -174,7 +185,10 @@ __device__ __forceinline__ F0 make_f0(const Problem &p)
 __device__ __forceinline__ float delta_f0(const F0 &f, const SplitNode &nd, float2 cs, float xi, float dw)
 {
     float sp, cp;
-    sincosf(f.kdx * xi, &sp, &cp);
+    if (f.small)
+        sincos_small(f.kdx * xi, sp, cp);
+    else
+        sincosf(f.kdx * xi, &sp, &cp);
     const float c = cs.x * cp - cs.y * sp;  // cos(k x_foot)
     const float du = dw * f.dx_dt;
     if (f.kind == NUFI_F0_LANDAU) {

@@ -13,8 +13,8 @@
 // Geometry: a persistent grid of about one CTA per SM.  Each thread owns
 // one spatial node (x-lanes, so the 32 lanes of a warp read neighbouring
 // cells: few bank conflicts) and PPT velocity nodes, i.e. PPT
-// independent dependency chains.  CTA c owns velocity nodes
-// [c*Nm/G, (c+1)*Nm/G).  rho: per thread over its chains (FP64) into
+// independent dependency chains.  CTA c owns the velocity nodes c, c + G,
+// c + 2G, ... (interleaved, so that each CTA holds a spread of velocities).  rho: per thread over its chains (FP64) into
 // partial[c][s]; reduce_rho sums the G rows.
 //
 // The per-point arithmetic is that of trace_split.cu (same substep order as
@@ -47,18 +47,18 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
     const int s = threadIdx.x % Nr;    // spatial node
     const int grp = threadIdx.x / Nr;  // chain group (threads per node > 1)
     const int G = gridDim.x;
-    const long long m0 = (long long)blockIdx.x * p.Nm / G;
-    const long long m1 = (long long)(blockIdx.x + 1) * p.Nm / G;
-
+    // velocity nodes interleaved over the CTAs: chain j of CTA c is c + j G
+    long long mv[PPT];
     int I[PPT], S0m[PPT];
     float xi[PPT], dwT[PPT], dwTc[PPT], shi[PPT], slo[PPT];
     bool live[PPT];
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
-        const long long m = m0 + grp * PPT + q;
+        const long long m = blockIdx.x + (long long)(grp * PPT + q) * G;
         const long long qq = (long long)s * p.Nm + m;
-        live[q] = (s < N) && (m < m1) && (qq >= q_begin) && (qq < q_end);
-        const SplitNode nd = nodes[m < m1 ? m : m0];
+        live[q] = (s < N) && (m < p.Nm) && (qq >= q_begin) && (qq < q_end);
+        mv[q] = m < p.Nm ? m : blockIdx.x;
+        const SplitNode nd = nodes[mv[q]];
         S0m[q] = nd.S0 + kMagicBits;
         shi[q] = nd.sig_hi;
         slo[q] = nd.sig_lo;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
         if (!live[q]) continue;
-        const SplitNode nd = nodes[m0 + grp * PPT + q];
+        const SplitNode nd = nodes[mv[q]];
         acc += double(delta_f0(f, nd, __ldg(phase + I[q]), xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
     }
     // groups of the same node combined in group order

@@ -17,8 +17,9 @@
 // (nufi/config.hpp:148-149, 233-234), evaluated as f0(foot) - G(u0) with
 // expm1; G(u0) is added back in FP64.
 //
-// Geometry: about one CTA per SM; CTA c owns the velocity nodes
-// [c*Nm/G, (c+1)*Nm/G) for every spatial node.  Thread t owns the spatial
+// Geometry: about one CTA per SM; CTA c owns the velocity nodes c, c + G,
+// c + 2G, ... (interleaved: a spread of velocities per CTA) for every
+// spatial node.  Thread t owns the spatial
 // nodes s = t + T j and visits its items in (j, m) order, PPT at a time
 // (one full trace per batch), so the 32 lanes of a warp hold 32
 // consecutive spatial nodes (x fastest) at one velocity: neighbouring
@@ -30,7 +31,9 @@
 // Tables: with ring > 0 the history is streamed through `ring` shared-
 // memory slots of S slabs (cp.async.bulk completing on an mbarrier), one
 // chunk stream over all batches so the copies run ahead across batch
-// boundaries; with ring == 0 (slabs too large for shared memory) the
+// boundaries; the last warp to finish a slot refills it (per-slot count
+// in shared memory, acquire-release), so warps wait only for their data;
+// with ring == 0 (slabs too large for shared memory) the
 // gathers read the tables in global memory.  Every mbarrier wait is
 // bounded; a timeout raises kErrStageTimeout (no trap, no hang).
 #include <algorithm>
@@ -154,13 +157,15 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
 {
     extern __shared__ __align__(128) float ring[];
     __shared__ __align__(8) unsigned long long full_bar[kRing];
+    __shared__ unsigned released[kRing];  // warps done with the slot's chunk
 
     const int T = blockDim.x;
     const int t = threadIdx.x;
     const int G = gridDim.x;
+    const int W = T >> 5;
     const long long Ns = p.Ns;
-    const long long m0 = (long long)blockIdx.x * p.Nm / G;
-    const long long Mc = (long long)(blockIdx.x + 1) * p.Nm / G - m0;
+    // velocity nodes interleaved over the CTAs: CTA c owns c, c + G, ...
+    const long long Mc = (p.Nm - blockIdx.x + G - 1) / G;
     const long long nj = t < Ns ? (Ns - t + T - 1) / T : 0;  // spatial nodes of this thread
     const long long nj0 = (Ns + T - 1) / T;                  // ... of thread 0 (the most)
     const long long batches = (nj0 * Mc + PPT - 1) / PPT;
@@ -189,7 +194,10 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
     };
     if constexpr (STAGED) {
         if (t == 0) {
-            for (int r = 0; r < R; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
+            for (int r = 0; r < R; ++r) {
+                mbar_init(smem_addr(&full_bar[r]), 1);
+                released[r] = 0;
+            }
             mbar_fence_init();
         }
         __syncthreads();
@@ -208,7 +216,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
         for (int q = 0; q < PPT; ++q) {
             const long long k = b * PPT + q;
             const long long j = k / Mc;
-            const long long m = m0 + k % Mc;
+            const long long m = blockIdx.x + (k % Mc) * G;
             const long long s = t + j * T;
             const bool inside = j < nj;
             const long long qq = s * p.Nm + m;
@@ -263,8 +271,15 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
                     ch[q].dwC[a] = 0.0f;
                 }
             if constexpr (STAGED) {
-                __syncthreads();  // everyone is done with this slot
-                if (t == 0 && g + R < total_chunks) issue(g + R);
+                // the last warp to finish the slot refills it; no warp
+                // waits for another, only for its data
+                __syncwarp();
+                const unsigned slot = unsigned(g % R);
+                if ((t & 31) == 0 && atom_add_acq_rel_cta(&released[slot], 1u) == unsigned(W - 1)) {
+                    released[slot] = 0;
+                    fence_proxy_async_shared();
+                    if (g + R < total_chunks) issue(g + R);
+                }
             }
         }
         // f0(foot) - G(u0) in FP32, the FP64 background G(u0) added back
@@ -278,7 +293,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
                 cur_j = j;
             }
             if (!live[q]) continue;
-            long long rm = m0 + k % Mc;
+            long long rm = blockIdx.x + (k % Mc) * G;
             float delta = 0.0f, csum = 0.0f, Gf = 1.0f;
             double Gd = 1.0;
 #pragma unroll

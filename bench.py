@@ -107,6 +107,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def aggregate_replicas(total_ms: float, steps: int, point_steps: int, ws: int, device: str = "cuda"):
+    """Replicas on ws ranks (one GPU each, the same workload): the slowest
+    rank's time per step and the whole-job rate ws * point_steps / time.
+    With ws > 1 the max is taken over the process group."""
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(total_ms)], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / steps
+    return ms_per_step, ws * point_steps / (ms_per_step * 1e-3)
+
+
 def measure_peaks():
     """FP32 / FP64 FMA throughput (TFLOP/s) and shared-memory load bandwidth
     (GB/s) of this GPU, from probes/peaks.cu (best of 3 each)."""
@@ -228,14 +242,8 @@ def run_ours(args, cfg):
     barrier()
     clocks = sampler.stop()
     launches = sim.launches - launches0
-    total_ms = sum(times)
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms_per_step = total_ms / args.steps
     ps = cfg.point_steps()
-    value = ws * ps / (ms_per_step * 1e-3)
+    ms_per_step, value = aggregate_replicas(sum(times), args.steps, ps, ws, device="cuda")
     e_split = sim.energy()
 
     # FP64 plain form: same workload, for the error gate and its own rate.

@@ -108,7 +108,9 @@ int nufi_compute_rho(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end);
 int nufi_download_rho(nufi_handle *h, double *rho);
 int nufi_download_rho_f32(nufi_handle *h, float *rho);
 /* cuda_kernel::upload_phi (nufi/cuda_kernel.cu:147-156): copies slab n from
- * coeffs_base + n*stride_t of the caller's history to the device. */
+ * coeffs_base + n*stride_t of the caller's history to the device.  Returns
+ * once the caller's values have been read (the buffer may be reused); the
+ * transfer is ordered before the handle's later work. */
 int nufi_upload_phi(nufi_handle *h, int64_t n, const double *coeffs_base);
 int nufi_upload_phi_f32(nufi_handle *h, int64_t n, const float *coeffs_base);
 /* cuda_kernel::compute_metrics (nufi/cuda_kernel.cu:158-175, 341-358,

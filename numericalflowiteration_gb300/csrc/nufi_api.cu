@@ -61,6 +61,8 @@ struct nufi_handle {
     double *theta_acc = nullptr;  // [4][adjoint blocks]
     double *grad = nullptr;       // [4]
     std::vector<char> slab_set;   // slab n written (step, run, upload_phi)
+    double *stage = nullptr;      // pinned staging buffer of upload_phi (one slab)
+    cudaEvent_t stage_done = nullptr;
     std::vector<char> energy_set; // W_n recorded (step, run)
     SolvePlan plan;
     bool solve_ok = false;
@@ -512,6 +514,11 @@ void release(nufi_handle *h)
     h->graphs.clear();
     for (void *p : h->allocations) cudaFree(p);
     h->allocations.clear();
+    if (h->stage_done) cudaEventSynchronize(h->stage_done);
+    if (h->stage) cudaFreeHost(h->stage);
+    if (h->stage_done) cudaEventDestroy(h->stage_done);
+    h->stage = nullptr;
+    h->stage_done = nullptr;
     if (h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
 }
@@ -688,19 +695,31 @@ int nufi_download_rho_f32(nufi_handle *h, float *rho)
     return NUFI_OK;
 }
 
+// The slab goes through a pinned staging buffer, so the call returns as
+// soon as the caller's buffer has been read (as the reference's blocking
+// copy), and the transfer and table derivation stay ordered on the stream
+// before the next trace.  The staging buffer is reused after the previous
+// upload's copy has completed (event).
 static int upload_slab(nufi_handle *h, int64_t n, const double *slab)
 {
     const Problem &p = h->p;
     DeviceGuard g(h->device);
-    NUFI_CUDA(h, cudaMemcpyAsync(h->hist + n * p.hist_stride, slab, size_t(p.stride_t) * sizeof(double),
-                                 cudaMemcpyHostToDevice, h->stream));
+    const size_t bytes = size_t(p.stride_t) * sizeof(double);
+    if (!h->stage) {
+        NUFI_CUDA(h, cudaMallocHost(&h->stage, bytes));
+        NUFI_CUDA(h, cudaEventCreateWithFlags(&h->stage_done, cudaEventDisableTiming));
+    } else {
+        NUFI_CUDA(h, cudaEventSynchronize(h->stage_done));
+    }
+    std::memcpy(h->stage, slab, bytes);
+    NUFI_CUDA(h, cudaMemcpyAsync(h->hist + n * p.hist_stride, h->stage, bytes, cudaMemcpyHostToDevice, h->stream));
+    NUFI_CUDA(h, cudaEventRecord(h->stage_done, h->stream));
     if (h->tables) {
         cudaError_t e = launch_derive_table(p, h->hist + n * p.hist_stride, h->tables + n * p.table_stride, h->stream);
         if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
         h->launches += 1;
     }
     h->slab_set[size_t(n)] = 1;
-    NUFI_CUDA(h, cudaStreamSynchronize(h->stream));
     return NUFI_OK;
 }
 

@@ -212,6 +212,60 @@ __device__ __forceinline__ float delta_f0(const F0 &f, const SplitNode &nd, floa
 namespace nufi_gb300 {
 namespace split {
 
+// Packed FP32 pairs (two chains per instruction: add / sub / fma .f32x2,
+// sm_100 family).  Each op is the IEEE operation of the scalar code on
+// both lanes, so the pairs give the same bits as one chain at a time.
+__device__ __forceinline__ unsigned long long f2_pack(float a, float b)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float &a, float &b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b)
+{
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b)
+{
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_add_rm(unsigned long long a, unsigned long long b)
+{
+    unsigned long long r;
+    asm("add.rm.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+template <bool POW2>
+__device__ __forceinline__ int wrap_cell(int J, int N, unsigned *err)
+{
+    if constexpr (POW2) {
+        J &= N - 1;
+    } else {
+        J += (J < 0) ? N : 0;
+        J -= (J >= N) ? N : 0;
+        if ((unsigned)J >= (unsigned)N) {
+            atomicOr(err, kErrKickRange);
+            J = ((J % N) + N) % N;
+        }
+    }
+    return J;
+}
+
 // Substeps k_hi..k_lo (descending) of PPT chains over a chunk of tables in
 // shared memory (slab k at chunk + (k - k_lo) * TS floats, kick_lookup layout).
 // State per chain: cell I, fraction xi, and the kick sum in two levels:
@@ -222,43 +276,69 @@ namespace split {
 //           floor(t) by a round-down add of 1.5*2^23, whose bit pattern
 //           minus S0m = S0 + bits(1.5*2^23) moves the cell
 //   kick:   dwC += K (A + B xi + C xi^2) of the cell (halved for k = 0)
-// 13 FP32/INT instructions and two shared loads (8 + 4 bytes) per substep.
+// Chains go two at a time through the packed FP32 instructions (the FP32
+// part of a substep, 9 operations, in 9 instructions for two chains); the
+// integer cell update and the two shared loads stay per chain.
 template <int PPT, bool POW2>
 __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int TS, int k_hi, int k_lo, int N,
                                             int (&I)[PPT], float (&xi)[PPT], float (&dwT)[PPT], float (&dwTc)[PPT],
                                             const float (&shi)[PPT], const int (&S0m)[PPT], unsigned *err)
 {
-    float dwC[PPT];
+    constexpr int NP = PPT / 2;  // packed pairs; chain PPT-1 alone when PPT is odd
+    const unsigned long long MAG2 = f2_pack(kMagic, kMagic);
+    unsigned long long X[NP > 0 ? NP : 1], SH[NP > 0 ? NP : 1], DT[NP > 0 ? NP : 1], DC[NP > 0 ? NP : 1];
 #pragma unroll
-    for (int q = 0; q < PPT; ++q) dwC[q] = 0.0f;
+    for (int p = 0; p < NP; ++p) {
+        X[p] = f2_pack(xi[2 * p], xi[2 * p + 1]);
+        SH[p] = f2_pack(shi[2 * p], shi[2 * p + 1]);
+        DT[p] = f2_pack(dwT[2 * p], dwT[2 * p + 1]);
+        DC[p] = 0ull;
+    }
+    float dwC_last = 0.0f;
     auto substep = [&](const float *__restrict__ tk, float h) {
+        const unsigned long long H2 = f2_pack(h, h);
 #pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            const float t = ((xi[q] - shi[q]) - dwT[q]) - dwC[q];
+        for (int p = 0; p < NP; ++p) {
+            const unsigned long long t = f2_sub(f2_sub(f2_sub(X[p], SH[p]), DT[p]), DC[p]);
+            const unsigned long long mg = f2_add_rm(t, MAG2);
+            float mg0, mg1;
+            f2_unpack(mg, mg0, mg1);
+            const int J0 = wrap_cell<POW2>(I[2 * p] - S0m[2 * p] + __float_as_int(mg0), N, err);
+            const int J1 = wrap_cell<POW2>(I[2 * p + 1] - S0m[2 * p + 1] + __float_as_int(mg1), N, err);
+            I[2 * p] = J0;
+            I[2 * p + 1] = J1;
+            X[p] = f2_sub(t, f2_sub(mg, MAG2));
+            const float2 ab0 = reinterpret_cast<const float2 *>(tk)[J0];
+            const float2 ab1 = reinterpret_cast<const float2 *>(tk)[J1];
+            const unsigned long long C2 = f2_pack(tk[2 * N + J0], tk[2 * N + J1]);
+            const unsigned long long q = f2_fma(X[p], C2, f2_pack(ab0.y, ab1.y));
+            const unsigned long long kq = f2_fma(X[p], q, f2_pack(ab0.x, ab1.x));
+            DC[p] = (h == 1.0f) ? f2_add(DC[p], kq) : f2_fma(H2, kq, DC[p]);
+        }
+        if constexpr (PPT % 2 == 1) {
+            constexpr int q = PPT - 1;
+            const float t = ((xi[q] - shi[q]) - dwT[q]) - dwC_last;
             const float mg = __fadd_rd(t, kMagic);
-            int J = I[q] - S0m[q] + __float_as_int(mg);
-            if constexpr (POW2) {
-                J &= N - 1;
-            } else {
-                J += (J < 0) ? N : 0;
-                J -= (J >= N) ? N : 0;
-                if ((unsigned)J >= (unsigned)N) {
-                    atomicOr(err, kErrKickRange);
-                    J = ((J % N) + N) % N;
-                }
-            }
+            const int J = wrap_cell<POW2>(I[q] - S0m[q] + __float_as_int(mg), N, err);
             I[q] = J;
             xi[q] = t - (mg - kMagic);
             const float kq = kick_lookup(tk, N, J, xi[q]);
-            dwC[q] = (h == 1.0f) ? dwC[q] + kq : fmaf(h, kq, dwC[q]);
+            dwC_last = (h == 1.0f) ? dwC_last + kq : fmaf(h, kq, dwC_last);
         }
     };
     const int k_stop = max(k_lo, 1);
     for (int k = k_hi; k >= k_stop; --k) substep(chunk + (k - k_lo) * TS, 1.0f);
     if (k_lo == 0) substep(chunk, 0.5f);
-    // fold this chunk's kicks into the compensated total
+    // fold this chunk's kicks into the compensated totals
 #pragma unroll
-    for (int q = 0; q < PPT; ++q) kick(dwT[q], dwTc[q], dwC[q]);
+    for (int p = 0; p < NP; ++p) {
+        f2_unpack(X[p], xi[2 * p], xi[2 * p + 1]);
+        float c0, c1;
+        f2_unpack(DC[p], c0, c1);
+        kick(dwT[2 * p], dwTc[2 * p], c0);
+        kick(dwT[2 * p + 1], dwTc[2 * p + 1], c1);
+    }
+    if constexpr (PPT % 2 == 1) kick(dwT[PPT - 1], dwTc[PPT - 1], dwC_last);
 }
 
 }  // namespace split

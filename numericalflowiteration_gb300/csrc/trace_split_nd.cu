@@ -91,6 +91,10 @@ __device__ __forceinline__ void drift_axis(int &I, float &xi, float dwT, float d
 }
 
 // dS/dxi_a of the FP32 slab window at the chain's cells and fractions.
+// Rows j and j+1 of the window go through the packed FP32 instructions
+// together (f32x2: the same IEEE operation on both lanes): their x sums
+// with the value and derivative bases, then their shares of the y (and z)
+// sums, whose two halves are added at the end.
 template <int D>
 __device__ __forceinline__ void field_grad(const float *__restrict__ slab, int sy, int sz, const Chain<D> &c,
                                            float (&g)[D])
@@ -98,23 +102,39 @@ __device__ __forceinline__ void field_grad(const float *__restrict__ slab, int s
     float Nx[4], Dx[4], Ny[4], Dy[4];
     cubic_basis(c.xi[0], Nx, Dx);
     cubic_basis(c.xi[1], Ny, Dy);
+    unsigned long long NXX[4], DXX[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        NXX[i] = f2_pack(Nx[i], Nx[i]);
+        DXX[i] = f2_pack(Dx[i], Dx[i]);
+    }
+    const unsigned long long NY01 = f2_pack(Ny[0], Ny[1]), NY23 = f2_pack(Ny[2], Ny[3]);
+    const unsigned long long DY01 = f2_pack(Dy[0], Dy[1]), DY23 = f2_pack(Dy[2], Dy[3]);
+    // x sums of rows (j, j+1) at plane w: R0 = sum_i v N_i, R1 = sum_i v D_i
+    auto rows = [&](const float *w, int j, unsigned long long &R0, unsigned long long &R1) {
+        R0 = 0ull;
+        R1 = 0ull;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const unsigned long long V = f2_pack(w[j * sy + i], w[(j + 1) * sy + i]);
+            R0 = f2_fma(V, NXX[i], R0);
+            R1 = f2_fma(V, DXX[i], R1);
+        }
+    };
     if constexpr (D == 2) {
         const float *w = slab + c.I[1] * sy + c.I[0];
-        float gx = 0.0f, gy = 0.0f;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            float r0 = 0.0f, r1 = 0.0f;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const float v = w[j * sy + i];
-                r0 = fmaf(v, Nx[i], r0);
-                r1 = fmaf(v, Dx[i], r1);
-            }
-            gx = fmaf(r1, Ny[j], gx);
-            gy = fmaf(r0, Dy[j], gy);
-        }
-        g[0] = gx;
-        g[1] = gy;
+        unsigned long long GX = 0ull, GY = 0ull, R0, R1;
+        rows(w, 0, R0, R1);
+        GX = f2_fma(R1, NY01, GX);
+        GY = f2_fma(R0, DY01, GY);
+        rows(w, 2, R0, R1);
+        GX = f2_fma(R1, NY23, GX);
+        GY = f2_fma(R0, DY23, GY);
+        float a, b;
+        f2_unpack(GX, a, b);
+        g[0] = a + b;
+        f2_unpack(GY, a, b);
+        g[1] = a + b;
     } else {
         float Nz[4], Dz[4];
         cubic_basis(c.xi[2], Nz, Dz);
@@ -122,23 +142,23 @@ __device__ __forceinline__ void field_grad(const float *__restrict__ slab, int s
         float gx = 0.0f, gy = 0.0f, gz = 0.0f;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            float ax = 0.0f, ay = 0.0f, az = 0.0f;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float r0 = 0.0f, r1 = 0.0f;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const float v = w[k * sz + j * sy + i];
-                    r0 = fmaf(v, Nx[i], r0);
-                    r1 = fmaf(v, Dx[i], r1);
-                }
-                ax = fmaf(r1, Ny[j], ax);
-                ay = fmaf(r0, Dy[j], ay);
-                az = fmaf(r0, Ny[j], az);
-            }
-            gx = fmaf(ax, Nz[k], gx);
-            gy = fmaf(ay, Nz[k], gy);
-            gz = fmaf(az, Dz[k], gz);
+            const float *wk = w + k * sz;
+            unsigned long long AX = 0ull, AY = 0ull, AZ = 0ull, R0, R1;
+            rows(wk, 0, R0, R1);
+            AX = f2_fma(R1, NY01, AX);
+            AY = f2_fma(R0, DY01, AY);
+            AZ = f2_fma(R0, NY01, AZ);
+            rows(wk, 2, R0, R1);
+            AX = f2_fma(R1, NY23, AX);
+            AY = f2_fma(R0, DY23, AY);
+            AZ = f2_fma(R0, NY23, AZ);
+            float a, b;
+            f2_unpack(AX, a, b);
+            gx = fmaf(a + b, Nz[k], gx);
+            f2_unpack(AY, a, b);
+            gy = fmaf(a + b, Nz[k], gy);
+            f2_unpack(AZ, a, b);
+            gz = fmaf(a + b, Dz[k], gz);
         }
         g[0] = gx;
         g[1] = gy;

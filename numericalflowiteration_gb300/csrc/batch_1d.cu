@@ -378,11 +378,15 @@ __global__ void batch_theta_reduce_kernel(const BatchInst *__restrict__ bi, int 
 //             Xbar <- Xbar + Vbar h g'(xi);  Vbar <- Vbar - Xbar (compensated)
 //             kick-table adjoints of slab k: (Abar, Bbar, Cbar) += Vbar h (1, xi, xi^2)
 //           (cells and cells per substep; g' = d/dxi of the kick quadratic),
-//           summed in shared memory by red.shared.add.f32 and flushed into
-//           the instance's FP64 table adjoints after each chunk.
-// About three forward passes of work; the adjoint's own recurrences are
-// short.  A persistent grid: CTA b handles units b, b + G, ...; its
-// checkpoints live in ckpt + b * (chunks * 4 * 256 * PPT) floats.
+//           summed in shared memory as scaled integers (native integer
+//           reductions; the FP32 shared-memory add is a compare-and-swap
+//           loop) and flushed after each chunk into the instance's FP32
+//           table adjoints of this step, which a small kernel folds into
+//           the FP64 sums after the step.
+// Chains go in packed pairs (f32x2).  About three forward passes of work;
+// the adjoint's own recurrences are short.  A persistent grid of kAdjThreads-
+// thread CTAs: CTA b handles units b, b + G, ...; its checkpoints live in
+// ckpt + b * (chunks * 4 * kAdjThreads * PPT) floats.
 // ---------------------------------------------------------------------------
 
 // f0 partial derivatives in FP32 at x (unwrapped), u: as adj::f0_grad_1d.
@@ -428,216 +432,442 @@ __device__ __forceinline__ F0GradF f0_grad_1d_f(const Problem &p, float x, float
 __device__ __forceinline__ double f2d_bits(float f)
 {
     const unsigned b = __float_as_uint(f);
-    const unsigned e = (b >> 23) & 0xffu;
-    if (e == 0) return 0.0;
-    const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
-                                    ((unsigned long long)(e + (1023u - 127u)) << 52) |
-                                    ((unsigned long long)(b & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
+    // high word: sign, exponent + (1023 - 127), top 20 mantissa bits; low word: the last 3
+    const unsigned hi = (b & 0x80000000u) | (((b >> 3) & 0x0fffffffu) + ((1023u - 127u) << 20));
+    return (b & 0x7f800000u) ? __hiloint2double(int(hi), int(b << 29)) : 0.0;
 }
 
-// Shared-memory add without a returned value.
-__device__ __forceinline__ void red_shared_add(float *p, float v)
+// Shared-memory integer add without a returned value, at a shared-window
+// address (a native shared-memory reduction, unlike the FP32 form).
+__device__ __forceinline__ void red_shared_add(unsigned addr, int v)
 {
-    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(smem_addr(p)), "f"(v) : "memory");
+    asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
 
-// One split substep with an unwrapped cell count U (J = U & mask): the
-// drift of trace_chunk (split_device.cuh) and the kick lookup.
-__device__ __forceinline__ float split_substep(int &U, float &xi, float dwT, float dwC, float shi, int S0um, int mask,
-                                               const float *tk, int N, int &J)
+// 2^k as a float, k in [-126, 127].
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+
+// Fixed-point table adjoints.  In each chunk the adjoint state (Xbar, Vbar,
+// and Vbar's compensation) carries a power-of-two scale 2^F, the same for
+// the whole CTA, and each term vh (1, xi, xi^2) is added as the integer
+// nearest to it.  Integer sums are exact and independent of order.  The
+// scale comes from L = sum over the CTA's chains of |Vbar| + 8 |Xbar| at the
+// chunk's start: every term of the chunk is at most |Vbar| at its substep,
+// and |Vbar| moves by at most |Xbar| per substep (Xbar itself changes by
+// vh g', a few per cent of vh at most), so no cell's sum exceeds L.  The
+// scale puts 2 L below 2^30.  One term's rounding is 2^-F <= 2^-28 L.
+// This adds a thread's share of L to *slot (a warp sum, one shared add per warp).
+template <int NP>
+__device__ __forceinline__ void adj_bound_add(const unsigned long long (&XB)[NP], const unsigned long long (&VB)[NP],
+                                              float *slot)
 {
-    const float t = ((xi - shi) - dwT) - dwC;
-    const float mg = __fadd_rd(t, kMagic);
-    U = U - S0um + __float_as_int(mg);
-    J = U & mask;
-    xi = t - (mg - kMagic);
-    return kick_lookup(tk, N, J, xi);
+    using namespace split;
+    float l = 0.f;
+#pragma unroll
+    for (int pp = 0; pp < NP; ++pp) {
+        float x0, x1, v0, v1;
+        f2_unpack(XB[pp], x0, x1);
+        f2_unpack(VB[pp], v0, v1);
+        l += (fabsf(v0) + fabsf(v1)) + 8.f * (fabsf(x0) + fabsf(x1));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(slot, l);
+}
+
+// The change k of the scale exponent F that puts 2 L 2^k in [2^29, 2^30)
+// (0 for L = 0 or not finite), keeping F + k in [-120, 120].
+__device__ __forceinline__ int adj_rescale(float L, int F)
+{
+    const unsigned b = __float_as_uint(L);
+    const int e = int((b >> 23) & 0xffu);
+    if (e == 0 || e == 0xff || (b >> 31)) return 0;
+    return max(-120 - F, min(120 - F, 28 - (e - 127)));
+}
+
+// Scales the adjoint state by 2^k.
+template <int NP>
+__device__ __forceinline__ void adj_scale_state(int k, unsigned long long (&XB)[NP], unsigned long long (&VB)[NP],
+                                                unsigned long long (&VBC)[NP])
+{
+    using namespace split;
+    if (k == 0) return;
+    const float s = pow2f(k);
+    const unsigned long long S2 = f2_pack(s, s);
+#pragma unroll
+    for (int pp = 0; pp < NP; ++pp) {
+        XB[pp] = f2_mul(XB[pp], S2);
+        VB[pp] = f2_mul(VB[pp], S2);
+        VBC[pp] = f2_mul(VBC[pp], S2);
+    }
+}
+
+// Substeps i = cnt-1 .. 0 of a chunk (slab k_lo + i at chunk + i TS) for PPT
+// chains in packed pairs: the drift and kick of trace_chunk (split_device.cuh)
+// with an unwrapped cell count U (cell J = U & mask), the chunk's kick sum in
+// DC (the slab-0 kick scaled by H0 = 1/2 when the chunk starts at slab 0).
+// With SAVE, substep i keeps each pair's cells (J0 | J1 << 16; N <= 256)
+// and fractions for the reverse sweep.  FULL: cnt == kAdjChunk.
+template <int PPT, bool FULL, bool SAVE>
+__device__ __forceinline__ void adj_chunk_primal(const float *__restrict__ chunk, int TS, int N, int mask, int cnt,
+                                                 unsigned long long H0, int (&U)[PPT], const int (&S0um)[PPT],
+                                                 unsigned long long (&X)[PPT / 2],
+                                                 const unsigned long long (&SH)[PPT / 2],
+                                                 const unsigned long long (&DT)[PPT / 2],
+                                                 unsigned long long (&DC)[PPT / 2], unsigned (&Jp)[kAdjChunk][PPT / 2],
+                                                 unsigned long long (&Xs)[kAdjChunk][PPT / 2])
+{
+    using namespace split;
+    constexpr int NP = PPT / 2;
+    const unsigned long long MAG2 = f2_pack(kMagic, kMagic);
+#pragma unroll
+    for (int i = kAdjChunk - 1; i >= 0; --i) {
+        if (!FULL && i >= cnt) continue;
+        const float *tk = chunk + i * TS;
+#pragma unroll
+        for (int pp = 0; pp < NP; ++pp) {
+            const unsigned long long t = f2_sub(f2_sub(f2_sub(X[pp], SH[pp]), DT[pp]), DC[pp]);
+            const unsigned long long mg = f2_add_rm(t, MAG2);
+            float mg0, mg1;
+            f2_unpack(mg, mg0, mg1);
+            U[2 * pp] = U[2 * pp] - S0um[2 * pp] + __float_as_int(mg0);
+            U[2 * pp + 1] = U[2 * pp + 1] - S0um[2 * pp + 1] + __float_as_int(mg1);
+            const int J0 = U[2 * pp] & mask, J1 = U[2 * pp + 1] & mask;
+            X[pp] = f2_sub(t, f2_sub(mg, MAG2));
+            const float2 ab0 = reinterpret_cast<const float2 *>(tk)[J0];
+            const float2 ab1 = reinterpret_cast<const float2 *>(tk)[J1];
+            const unsigned long long C2 = f2_pack(tk[2 * N + J0], tk[2 * N + J1]);
+            const unsigned long long kq =
+                f2_fma(X[pp], f2_fma(X[pp], C2, f2_pack(ab0.y, ab1.y)), f2_pack(ab0.x, ab1.x));
+            DC[pp] = i == 0 ? f2_fma(H0, kq, DC[pp]) : f2_add(DC[pp], kq);
+            if constexpr (SAVE) {
+                Jp[i][pp] = unsigned(J0) | (unsigned(J1) << 16);
+                Xs[i][pp] = X[pp];
+            }
+        }
+    }
+}
+
+// The adjoint of a chunk's substeps in ascending k from the kept cells and
+// fractions (slab k_lo + i still staged at chunk + i TS): per chain
+//   g' = K B + 2 K C xi;  vh = Vbar h;
+//   (Abar, Bbar, Cbar)[J] += rint(vh (1, xi, xi^2))  (state scaled by 2^F;
+//   shared memory, cell-interleaved: 3 integers per cell from accb, one
+//   slab every 3N)
+//   Xbar += vh g';  Vbar -= Xbar  (compensated: VBC holds the lost low part)
+template <int PPT, bool FULL>
+__device__ __forceinline__ void adj_chunk_reverse(const float *__restrict__ chunk, int TS, int N, unsigned accb,
+                                                  int cnt, unsigned long long H0,
+                                                  const unsigned (&Jp)[kAdjChunk][PPT / 2],
+                                                  const unsigned long long (&Xs)[kAdjChunk][PPT / 2],
+                                                  unsigned long long (&XB)[PPT / 2], unsigned long long (&VB)[PPT / 2],
+                                                  unsigned long long (&VBC)[PPT / 2])
+{
+    using namespace split;
+    constexpr int NP = PPT / 2;
+    const int T3 = 3 * N;
+#pragma unroll
+    for (int i = 0; i < kAdjChunk; ++i) {
+        if (!FULL && i >= cnt) continue;
+        const float *tk = chunk + i * TS;
+        const unsigned base = accb + unsigned(i * T3) * 4u;
+#pragma unroll
+        for (int pp = 0; pp < NP; ++pp) {
+            const int J0 = int(Jp[i][pp] & 0xffffu), J1 = int(Jp[i][pp] >> 16);
+            const unsigned long long x = Xs[i][pp];
+            const unsigned long long gp = f2_fma(f2_add(x, x), f2_pack(tk[2 * N + J0], tk[2 * N + J1]),
+                                                 f2_pack(tk[2 * J0 + 1], tk[2 * J1 + 1]));
+            const unsigned long long vh = i == 0 ? f2_mul(VB[pp], H0) : VB[pp];
+            const unsigned long long vx = f2_mul(vh, x);
+            const unsigned long long vxx = f2_mul(vx, x);
+            float h0, h1, x0, x1, xx0, xx1;
+            f2_unpack(vh, h0, h1);
+            f2_unpack(vx, x0, x1);
+            f2_unpack(vxx, xx0, xx1);
+            const unsigned a0 = base + unsigned(J0) * 12u, a1 = base + unsigned(J1) * 12u;
+            red_shared_add(a0, __float2int_rn(h0));
+            red_shared_add(a0 + 4u, __float2int_rn(x0));
+            red_shared_add(a0 + 8u, __float2int_rn(xx0));
+            red_shared_add(a1, __float2int_rn(h1));
+            red_shared_add(a1 + 4u, __float2int_rn(x1));
+            red_shared_add(a1 + 8u, __float2int_rn(xx1));
+            XB[pp] = f2_fma(vh, gp, XB[pp]);
+            const unsigned long long z = f2_add(XB[pp], VBC[pp]);
+            const unsigned long long tt = f2_sub(VB[pp], z);
+            VBC[pp] = f2_add(f2_sub(tt, VB[pp]), z);
+            VB[pp] = tt;
+        }
+    }
+}
+
+// Adds a chunk's fixed-point table adjoints (n integers in shared memory,
+// units of 2^-F) into the instance's FP32 staging buffer of this step (four
+// at a time) and zeroes them; groups of four still zero are skipped.  A sum
+// at or beyond 2^30 in magnitude raises kErrAdjointRange.
+__device__ __forceinline__ bool adj_flush(int *__restrict__ a, float *__restrict__ dst, int n, int F)
+{
+    const float u = pow2f(-F);
+    auto in_range = [](int v) { return unsigned(v + (1 << 30)) < (1u << 31); };
+    bool ok = true;
+    const int n4 = n & ~3;
+    for (int e = 4 * int(threadIdx.x); e < n4; e += 4 * int(blockDim.x)) {
+        const int4 v = *reinterpret_cast<const int4 *>(a + e);
+        if ((v.x | v.y | v.z | v.w) != 0) {
+            ok &= in_range(v.x) & in_range(v.y) & in_range(v.z) & in_range(v.w);
+            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst + e), "f"(float(v.x) * u),
+                         "f"(float(v.y) * u), "f"(float(v.z) * u), "f"(float(v.w) * u)
+                         : "memory");
+            *reinterpret_cast<int4 *>(a + e) = make_int4(0, 0, 0, 0);
+        }
+    }
+    for (int e = n4 + int(threadIdx.x); e < n; e += int(blockDim.x)) {
+        const int v = a[e];
+        if (v != 0) {
+            ok &= in_range(v);
+            atomicAdd(dst + e, float(v) * u);
+            a[e] = 0;
+        }
+    }
+    return ok;
+}
+
+// muT[k] += muS[k], muS[k] = 0 for the slabs k < m of every instance (one
+// step's table adjoints into the FP64 sums): block (x, instance).
+__global__ void batch_adjoint_fold_kernel(const BatchInst *__restrict__ bi, int m)
+{
+    const BatchInst &I = bi[blockIdx.y];
+    if (m > I.Nt) return;
+    const long long n = (long long)m * 3 * I.p.N[0];  // a multiple of 4 when N is
+    float4 *s4 = reinterpret_cast<float4 *>(I.muS);
+    const long long n4 = n >> 2;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n4; e += (long long)gridDim.x * blockDim.x) {
+        const float4 v = s4[e];
+        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+            double *d = I.muT + 4 * e;
+            d[0] += double(v.x);
+            d[1] += double(v.y);
+            d[2] += double(v.z);
+            d[3] += double(v.w);
+            s4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    for (long long e = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const float v = I.muS[e];
+        if (v != 0.f) {
+            I.muT[e] += double(v);
+            I.muS[e] = 0.f;
+        }
+    }
 }
 
 template <int PPT>
-__global__ void __launch_bounds__(256, 1) batch_adjoint_split_kernel(const BatchInst *__restrict__ bi,
+__global__ void __launch_bounds__(kAdjThreads, 1) batch_adjoint_split_kernel(const BatchInst *__restrict__ bi,
                                                                      const int *__restrict__ unit_inst, int units,
                                                                      int m, int ts_max, int max_chunks,
                                                                      float *__restrict__ ckpt,
                                                                      double *__restrict__ theta_acc, long long slots,
                                                                      unsigned *err)
 {
-    constexpr int SC = kAdjChunk;
-    extern __shared__ __align__(128) float ring[];  // [kRing][SC][ts_max], then [SC][3 max_N]
-    __shared__ __align__(8) unsigned long long full_bar[kRing];
-    float *accT = ring + size_t(kRing) * SC * ts_max;
+    using namespace split;
+    static_assert(PPT % 2 == 0, "chains go in packed pairs");
+    constexpr int SC = kAdjChunk, NP = PPT / 2, R = kAdjRing;
+    // [R][SC][ts_max] table slabs, then two [SC][N][3] fixed-point table-
+    // adjoint buffers (2 SC ts_max integers; 3N <= ts_max), zero between flushes
+    extern __shared__ __align__(128) float ring[];
+    __shared__ __align__(8) unsigned long long full_bar[R];
+    __shared__ float lsum[3];  // scale bounds of chunks c, c + 1, c + 2 (slot c % 3)
+    int *acc0 = reinterpret_cast<int *>(ring + size_t(R) * SC * ts_max);
+    for (int e = threadIdx.x; e < 2 * SC * ts_max; e += blockDim.x) acc0[e] = 0;
+    if (threadIdx.x < 3) lsum[threadIdx.x] = 0.f;
     if (threadIdx.x == 0) {
-        for (int r = 0; r < kRing; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
+        for (int r = 0; r < R; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
         mbar_fence_init();
     }
     __syncthreads();
     const int t = threadIdx.x;
-    float *ck = ckpt + (size_t)blockIdx.x * max_chunks * 4 * 256 * PPT;
-    unsigned g = 0;  // chunks consumed by this CTA: slot g % kRing, parity (g / kRing) & 1
-    bool ok = true;
+    // checkpoint area of this CTA: [chunk][field][pair][kAdjThreads] packed pairs,
+    // written and read once per step with the streaming (evict-first) cache
+    // policy so that they pass through L2 without displacing the tables
+    unsigned long long *ck =
+        reinterpret_cast<unsigned long long *>(ckpt) + (size_t)blockIdx.x * max_chunks * 2 * kAdjThreads * PPT;
+    unsigned g = 0;  // chunks consumed by this CTA: slot g % R, parity (g / R) & 1
+    bool ok = true, in_range = true;
     for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
         const BatchInst &I = bi[unit_inst[unit]];
         if (m > I.Nt) continue;
         const Problem &p = I.p;
-        const UnitMap um = unit_map(I, unit - I.adj_unit_begin, PPT);
-        const int N = um.N, mask = N - 1, TS = int(p.table_stride);
+        // thread t: node s = t % N, velocity chains (unit tpn' + t / N) PPT + q, tpn' = kAdjThreads / N
+        UnitMap um;
+        um.N = p.N[0];
+        um.s = t % um.N;
+        um.m0 = ((long long)(unit - I.adj_unit_begin) * (kAdjThreads / um.N) + t / um.N) * PPT;
+        const int N = um.N, mask = N - 1, TS = int(p.table_stride), T3 = 3 * N;
         const unsigned slab_bytes = unsigned(TS) * 4u;
-        const int C = (m + SC - 1) / SC;  // chunks of this step
+        const int C = (m + SC - 1) / SC;  // chunks of this step; chunk c = slabs [c SC, min(m, c SC + SC) - 1]
         auto issue = [&](int c, unsigned gg) {
             const int k_lo = c * SC, k_hi = min(m - 1, k_lo + SC - 1);
             const unsigned bytes = unsigned(k_hi - k_lo + 1) * slab_bytes;
-            const unsigned bar = smem_addr(&full_bar[gg % kRing]);
+            const unsigned bar = smem_addr(&full_bar[gg % R]);
             mbar_expect_tx(bar, bytes);
-            bulk_g2s(smem_addr(ring + (gg % kRing) * SC * ts_max), I.tables + (long long)k_lo * TS, bytes, bar);
+            bulk_g2s(smem_addr(ring + (gg % R) * SC * ts_max), I.tables + (long long)k_lo * TS, bytes, bar);
         };
+        auto ckp = [&](int c, int field, int pp) -> unsigned long long * {
+            return ck + ((size_t(c) * 4 + field) * NP + pp) * kAdjThreads + t;
+        };
+        // chains past the last velocity node trace node Nm-1 with a zero seed
         int U[PPT], S0um[PPT];
-        float xi[PPT], dwT[PPT], dwTc[PPT], shi[PPT], slo[PPT];
+        float dwTc[PPT];
         bool live[PPT];
+        unsigned long long X[NP], SH[NP], DT[NP];
 #pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            const long long mm = um.m0 + q;
-            live[q] = mm < p.Nm;
-            const SplitNode nd = I.nodes[live[q] ? mm : 0];
-            S0um[q] = nd.S0u + kMagicBits;
-            shi[q] = nd.sig_hi;
-            slo[q] = nd.sig_lo;
-            U[q] = um.s;
-            xi[q] = 0.f;
-            dwT[q] = slo[q];
-            dwTc[q] = 0.f;
+        for (int pp = 0; pp < NP; ++pp) {
+            float sh[2], sl[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int q = 2 * pp + h;
+                const long long mm = um.m0 + q;
+                live[q] = mm < p.Nm;
+                const SplitNode nd = I.nodes[live[q] ? mm : p.Nm - 1];
+                S0um[q] = nd.S0u + kMagicBits;
+                U[q] = um.s;
+                dwTc[q] = 0.f;
+                sh[h] = nd.sig_hi;
+                sl[h] = nd.sig_lo;
+            }
+            X[pp] = 0ull;
+            SH[pp] = f2_pack(sh[0], sh[1]);
+            DT[pp] = f2_pack(sl[0], sl[1]);
         }
+        unsigned Jp[SC][NP];
+        unsigned long long Xs[SC][NP], DC[NP];
+        const unsigned long long ONE2 = f2_pack(1.0f, 1.0f), HALF2 = f2_pack(0.5f, 0.5f);
+        auto fold = [&]() {
+#pragma unroll
+            for (int pp = 0; pp < NP; ++pp) {
+                float d0, d1, c0, c1;
+                f2_unpack(DT[pp], d0, d1);
+                f2_unpack(DC[pp], c0, c1);
+                kick(d0, dwTc[2 * pp], c0);
+                kick(d1, dwTc[2 * pp + 1], c1);
+                DT[pp] = f2_pack(d0, d1);
+            }
+        };
         // ---- pass 1: chunks C-1 .. 0 (descending k), checkpoint each entry state
         if (threadIdx.x == 0)
-            for (int j = 0; j < kRing && j < C; ++j) issue(C - 1 - j, g + j);
+            for (int j = 0; j < R && j < C; ++j) issue(C - 1 - j, g + j);
         for (int j = 0; j < C; ++j, ++g) {
             const int c = C - 1 - j;
-            float *cp = ck + (size_t)c * 4 * 256 * PPT;
 #pragma unroll
-            for (int q = 0; q < PPT; ++q) {
-                cp[(0 * PPT + q) * 256 + t] = __int_as_float(U[q]);
-                cp[(1 * PPT + q) * 256 + t] = xi[q];
-                cp[(2 * PPT + q) * 256 + t] = dwT[q];
-                cp[(3 * PPT + q) * 256 + t] = dwTc[q];
+            for (int pp = 0; pp < NP; ++pp) {
+                __stcs(ckp(c, 0, pp), f2_pack(__int_as_float(U[2 * pp]), __int_as_float(U[2 * pp + 1])));
+                __stcs(ckp(c, 1, pp), X[pp]);
+                __stcs(ckp(c, 2, pp), DT[pp]);
+                __stcs(ckp(c, 3, pp), f2_pack(dwTc[2 * pp], dwTc[2 * pp + 1]));
             }
-            ok &= mbar_wait(smem_addr(&full_bar[g % kRing]), (g / kRing) & 1u);
-            const float *chunk = ring + (g % kRing) * SC * ts_max;
-            const int k_lo = c * SC, k_hi = min(m - 1, k_lo + SC - 1);
-            float dwC[PPT];
+            ok &= mbar_wait(smem_addr(&full_bar[g % R]), (g / R) & 1u);
+            const float *chunk = ring + (g % R) * SC * ts_max;
+            const int cnt = min(SC, m - c * SC);
+            const unsigned long long H0 = c == 0 ? HALF2 : ONE2;
 #pragma unroll
-            for (int q = 0; q < PPT; ++q) dwC[q] = 0.f;
-            for (int k = k_hi; k >= k_lo; --k) {
-                const float *tk = chunk + (k - k_lo) * TS;
-                const float h = k == 0 ? 0.5f : 1.0f;
-#pragma unroll
-                for (int q = 0; q < PPT; ++q) {
-                    int J;
-                    const float kq = split_substep(U[q], xi[q], dwT[q], dwC[q], shi[q], S0um[q], mask, tk, N, J);
-                    dwC[q] = fmaf(h, kq, dwC[q]);
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < PPT; ++q) kick(dwT[q], dwTc[q], dwC[q]);
+            for (int pp = 0; pp < NP; ++pp) DC[pp] = 0ull;
+            if (cnt == SC)
+                adj_chunk_primal<PPT, true, false>(chunk, TS, N, mask, cnt, H0, U, S0um, X, SH, DT, DC, Jp, Xs);
+            else
+                adj_chunk_primal<PPT, false, false>(chunk, TS, N, mask, cnt, H0, U, S0um, X, SH, DT, DC, Jp, Xs);
+            fold();
             __syncthreads();
-            if (threadIdx.x == 0 && j + kRing < C) issue(C - 1 - (j + kRing), g + kRing);
+            if (threadIdx.x == 0 && j + R < C) issue(C - 1 - (j + R), g + R);
         }
         // ---- seed at the foot
-        const float a = float(-p.wv * I.lambda[um.s]);
         const float dx = float(p.dx[0]), dxdt = float(p.dx[0] / p.dt);
-        float xb[PPT], vb[PPT], vbc[PPT];
+        const float a = float(-p.wv * I.lambda[um.s]);
+        unsigned long long XB[NP], VB[NP], VBC[NP];
         double th[4] = {0, 0, 0, 0};
 #pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            xb[q] = vb[q] = vbc[q] = 0.f;
-            if (!live[q]) continue;
-            const float x = float(p.xmin[0]) + (float(U[q]) + xi[q]) * dx;
-            const float u = I.nodes[um.m0 + q].u0f + ((dwT[q] - dwTc[q]) - slo[q]) * dxdt;
-            const F0GradF gr = f0_grad_1d_f(p, x, u);
-            xb[q] = a * dx * gr.fx;
-            vb[q] = a * dxdt * gr.fu;
+        for (int pp = 0; pp < NP; ++pp) {
+            float xi2[2], dw2[2], xb2[2], vb2[2];
+            f2_unpack(X[pp], xi2[0], xi2[1]);
+            f2_unpack(DT[pp], dw2[0], dw2[1]);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) th[i] += double(a) * double(gr.dth[i]);
+            for (int h = 0; h < 2; ++h) {
+                const int q = 2 * pp + h;
+                const long long mm = live[q] ? um.m0 + q : p.Nm - 1;
+                const SplitNode &nd = I.nodes[mm];
+                const float aq = live[q] ? a : 0.f;
+                const float x = float(p.xmin[0]) + (float(U[q]) + xi2[h]) * dx;
+                const float u = nd.u0f + ((dw2[h] - dwTc[q]) - nd.sig_lo) * dxdt;
+                const F0GradF gr = f0_grad_1d_f(p, x, u);
+                xb2[h] = aq * dx * gr.fx;
+                vb2[h] = aq * dxdt * gr.fu;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) th[i] += double(aq) * double(gr.dth[i]);
+            }
+            XB[pp] = f2_pack(xb2[0], xb2[1]);
+            VB[pp] = f2_pack(vb2[0], vb2[1]);
+            VBC[pp] = 0ull;
         }
-        // ---- pass 2: chunks 0 .. C-1 (ascending k)
-        for (int i = threadIdx.x; i < SC * 3 * N; i += blockDim.x) accT[i] = 0.f;
-        __syncthreads();
+        // ---- pass 2: chunks 0 .. C-1 (ascending k); table adjoints of chunk c
+        // in buffer c & 1, flushed while the next chunk runs
         if (threadIdx.x == 0)
-            for (int j = 0; j < kRing && j < C; ++j) issue(j, g + j);
+            for (int j = 0; j < R && j < C; ++j) issue(j, g + j);
+        int F = 0;  // the adjoint state's scale exponent in the current chunk
+        if (C > 0) {
+            adj_bound_add(XB, VB, &lsum[0]);
+            __syncthreads();
+            F = adj_rescale(lsum[0], 0);
+            adj_scale_state(F, XB, VB, VBC);
+        }
+        auto load_ckpt = [&](int c) {
+#pragma unroll
+            for (int pp = 0; pp < NP; ++pp) {
+                float u0, u1, c0, c1;
+                f2_unpack(__ldcs(ckp(c, 0, pp)), u0, u1);
+                U[2 * pp] = __float_as_int(u0);
+                U[2 * pp + 1] = __float_as_int(u1);
+                X[pp] = __ldcs(ckp(c, 1, pp));
+                DT[pp] = __ldcs(ckp(c, 2, pp));
+                f2_unpack(__ldcs(ckp(c, 3, pp)), c0, c1);
+                dwTc[2 * pp] = c0;
+                dwTc[2 * pp + 1] = c1;
+            }
+        };
+        if (C > 0) load_ckpt(0);
         for (int c = 0; c < C; ++c, ++g) {
-            const float *cp = ck + (size_t)c * 4 * 256 * PPT;
+            ok &= mbar_wait(smem_addr(&full_bar[g % R]), (g / R) & 1u);
+            const float *chunk = ring + (g % R) * SC * ts_max;
+            const int cnt = min(SC, m - c * SC);
+            const unsigned long long H0 = c == 0 ? HALF2 : ONE2;
+            int *acc = acc0 + (c & 1) * SC * T3;
 #pragma unroll
-            for (int q = 0; q < PPT; ++q) {
-                U[q] = __float_as_int(cp[(0 * PPT + q) * 256 + t]);
-                xi[q] = cp[(1 * PPT + q) * 256 + t];
-                dwT[q] = cp[(2 * PPT + q) * 256 + t];
-                dwTc[q] = cp[(3 * PPT + q) * 256 + t];
+            for (int pp = 0; pp < NP; ++pp) DC[pp] = 0ull;
+            if (cnt == SC) {
+                adj_chunk_primal<PPT, true, true>(chunk, TS, N, mask, cnt, H0, U, S0um, X, SH, DT, DC, Jp, Xs);
+                if (c + 1 < C) load_ckpt(c + 1);
+                adj_chunk_reverse<PPT, true>(chunk, TS, N, smem_addr(acc), cnt, H0, Jp, Xs, XB, VB, VBC);
+            } else {
+                adj_chunk_primal<PPT, false, true>(chunk, TS, N, mask, cnt, H0, U, S0um, X, SH, DT, DC, Jp, Xs);
+                if (c + 1 < C) load_ckpt(c + 1);
+                adj_chunk_reverse<PPT, false>(chunk, TS, N, smem_addr(acc), cnt, H0, Jp, Xs, XB, VB, VBC);
             }
-            ok &= mbar_wait(smem_addr(&full_bar[g % kRing]), (g / kRing) & 1u);
-            const float *chunk = ring + (g % kRing) * SC * ts_max;
-            const int k_lo = c * SC, k_hi = min(m - 1, k_lo + SC - 1);
-            // recompute: substep k = k_lo + i keeps its cell and fraction
-            int Js[SC][PPT];
-            float xs[SC][PPT];
-            float dwC[PPT];
-#pragma unroll
-            for (int q = 0; q < PPT; ++q) dwC[q] = 0.f;
-#pragma unroll
-            for (int i = SC - 1; i >= 0; --i) {
-                const int k = k_lo + i;
-                if (k > k_hi) continue;
-                const float *tk = chunk + i * TS;
-                const float h = k == 0 ? 0.5f : 1.0f;
-#pragma unroll
-                for (int q = 0; q < PPT; ++q) {
-                    int J;
-                    const float kq = split_substep(U[q], xi[q], dwT[q], dwC[q], shi[q], S0um[q], mask, tk, N, J);
-                    dwC[q] = fmaf(h, kq, dwC[q]);
-                    Js[i][q] = J;
-                    xs[i][q] = xi[q];
-                }
-            }
-            // adjoint of the chunk's substeps, k ascending
-#pragma unroll
-            for (int i = 0; i < SC; ++i) {
-                const int k = k_lo + i;
-                if (k > k_hi) continue;
-                const float *tk = chunk + i * TS;
-                float *ak = accT + i * 3 * N;
-                const float h = k == 0 ? 0.5f : 1.0f;
-#pragma unroll
-                for (int q = 0; q < PPT; ++q) {
-                    const int J = Js[i][q];
-                    const float x = xs[i][q];
-                    const float b = reinterpret_cast<const float2 *>(tk)[J].y;
-                    const float cc = tk[2 * N + J];
-                    const float gp = fmaf(2.f * x, cc, b);
-                    const float vh = vb[q] * h;
-                    if (live[q]) {
-                        red_shared_add(ak + J, vh);
-                        red_shared_add(ak + N + J, vh * x);
-                        red_shared_add(ak + 2 * N + J, vh * x * x);
-                    }
-                    xb[q] = fmaf(vh, gp, xb[q]);
-                    const float y = -xb[q] - vbc[q];
-                    const float tt = vb[q] + y;
-                    vbc[q] = (tt - vb[q]) - y;
-                    vb[q] = tt;
-                }
-            }
+            if (c + 1 < C) adj_bound_add(XB, VB, &lsum[(c + 1) % 3]);
             __syncthreads();
-            if (threadIdx.x == 0 && c + kRing < C) issue(c + kRing, g + kRing);
-            for (int i = threadIdx.x; i < (k_hi - k_lo + 1) * 3 * N; i += blockDim.x) {
-                const float v = accT[i];
-                if (v != 0.f) {
-                    atomicAdd(I.muT + (long long)k_lo * 3 * N + i, f2d_bits(v));
-                    accT[i] = 0.f;
-                }
+            if (threadIdx.x == 0) {
+                if (c + R < C) issue(c + R, g + R);
+                lsum[c % 3] = 0.f;
             }
-            __syncthreads();
+            in_range &= adj_flush(acc, I.muS + (long long)c * SC * T3, cnt * T3, F);
+            if (c + 1 < C) {
+                const int k = adj_rescale(lsum[(c + 1) % 3], F);
+                adj_scale_state(k, XB, VB, VBC);
+                F += k;
+            }
         }
         adj::block_theta_add(th, theta_acc, slots, unit);
+        __syncthreads();
     }
     if (!ok) atomicOr(err, kErrStageTimeout);
+    if (!in_range) atomicOr(err, kErrAdjointRange);
 }
 
 // lambda_m of every instance from the kick-table adjoints of slab m: the
@@ -660,7 +890,7 @@ __global__ void batch_adjoint_lambda_split_kernel(const BatchInst *__restrict__ 
         for (int j = 0; j < 4; ++j) {
             const int i = q - j;
             if (i < 0 || i >= N) continue;
-            const double A = t[i], B = t[N + i], C = t[2 * N + i];
+            const double A = t[3 * i], B = t[3 * i + 1], C = t[3 * i + 2];
             const double w = j == 0 ? (-0.5 * A + B - 0.5 * C)
                            : j == 1 ? (-2.0 * B + 1.5 * C)
                            : j == 2 ? (0.5 * A + B - 1.5 * C)
@@ -723,17 +953,17 @@ cudaError_t launch_batch_trace(const BatchLaunch &L, int n, cudaStream_t st)
 
 size_t adjoint_split_smem(const BatchLaunch &L)
 {
-    return (size_t(kRingSlots) * kAdjChunk * L.ts_max + size_t(kAdjChunk) * 3 * L.max_N) * sizeof(float);
+    return size_t(kAdjRing + 2) * kAdjChunk * L.ts_max * sizeof(float);
 }
 
 int adjoint_split_ctas_per_sm(const BatchLaunch &L, int ppt)
 {
     int nb = 0;
     void (*fs)(const BatchInst *, const int *, int, int, int, int, float *, double *, long long, unsigned *) =
-        ppt == 1 ? batch_adjoint_split_kernel<1> : batch_adjoint_split_kernel<2>;
+        ppt == 2 ? batch_adjoint_split_kernel<2> : batch_adjoint_split_kernel<4>;
     const size_t smem = adjoint_split_smem(L);
     if (cudaFuncSetAttribute(fs, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fs, 256, smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fs, kAdjThreads, smem) != cudaSuccess) return 0;
     return nb;
 }
 
@@ -757,15 +987,18 @@ cudaError_t launch_batch_adjoint_step(const BatchLaunch &L, int m, cudaStream_t 
         void (*fs)(const BatchInst *, const int *, int, int, int, int, float *, double *, long long,
                    unsigned *) = nullptr;
         switch (L.adj_ppt) {
-        case 1: fs = batch_adjoint_split_kernel<1>; break;
         case 2: fs = batch_adjoint_split_kernel<2>; break;
+        case 4: fs = batch_adjoint_split_kernel<4>; break;
         default: return cudaErrorInvalidValue;
         }
         const size_t smem = adjoint_split_smem(L);
         cudaError_t e = cudaFuncSetAttribute(fs, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
-        fs<<<L.adj_grid, 256, smem, st>>>(L.inst, L.adj_unit_inst, L.adj_units, m, L.ts_max, L.max_chunks, L.ckpt,
-                                         L.theta_acc, L.adj_units, L.err);
+        fs<<<L.adj_grid, kAdjThreads, smem, st>>>(L.inst, L.adj_unit_inst, L.adj_units, m, L.ts_max, L.max_chunks,
+                                                 L.ckpt, L.theta_acc, L.adj_units, L.err);
+        if (m > 0) batch_adjoint_fold_kernel<<<dim3(unsigned(std::max(1, L.max_chunks * kAdjChunk * 3 * L.max_N / 4096)),
+                                                    unsigned(L.count)),
+                                               256, 0, st>>>(L.inst, m);
         return cudaGetLastError();
     }
     batch_adjoint_lambda_kernel<<<L.count, 256, 0, st>>>(L.inst, m);

@@ -436,6 +436,8 @@ int check_device_flags(nufi_handle *h)
         if (flags & kErrKickRange) m += " split-mode kick displacement out of range";
         if (flags & kErrSolveSize) m += " field-solve size";
         if (flags & kErrStageTimeout) m += " shared-memory staging wait timed out";
+        if (flags & kErrBarrierTimeout) m += " grid barrier wait timed out";
+        if (flags & kErrAdjointRange) m += " adjoint fixed-point sum out of range";
         return fail(h, NUFI_ERR_DEVICE, m);
     }
     return NUFI_OK;
@@ -1249,15 +1251,22 @@ int batch_autotune(nufi_batch *b)
     b->L.smem = size_t(kRingSlots) * b->L.slabs_per_chunk * ts_max * sizeof(float);
     log += "], \"adjoint\": [";
     const bool split = b->precision == NUFI_PREC_FP32_SPLIT;
-    std::vector<int> acands = tune ? (split ? std::vector<int>{1, 2} : std::vector<int>{1, 2, 4})
-                                   : std::vector<int>{2};
+    std::vector<int> acands = tune ? (split ? std::vector<int>{2, 4} : std::vector<int>{1, 2, 4})
+                                   : std::vector<int>{split ? 4 : 2};
     // NUFI_BATCH_ADJ_PPT=k fixes the adjoint's chains per thread
     if (const char *ap = std::getenv("NUFI_BATCH_ADJ_PPT")) {
         const int k = std::atoi(ap);
-        if (k == 1 || k == 2 || (k == 4 && !split)) acands = {k};
+        if (split ? (k == 2 || k == 4) : (k == 1 || k == 2 || k == 4)) acands = {k};
     }
     // FP32-split adjoint: a persistent grid (CTAs per SM from the occupancy
-    // of each candidate) and one checkpoint area per CTA
+    // of each candidate) and one checkpoint area per CTA; its units are
+    // kAdjThreads threads x ppt chains
+    auto set_adj = [&](int ppt) {
+        if (!split) return batch_set_units(b, ppt, true);
+        const int r = batch_set_units(b, ppt * (kAdjThreads / kBatchMaxN), true);
+        b->L.adj_ppt = ppt;
+        return r;
+    };
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
     b->L.max_chunks = (b->maxNt + kAdjChunk - 1) / kAdjChunk;
@@ -1268,8 +1277,8 @@ int batch_autotune(nufi_batch *b)
     if (split) {
         size_t need = 0;
         for (int ppt : acands) {
-            if ((st = batch_set_units(b, ppt, true))) return st;
-            need = std::max(need, size_t(split_grid(ppt)) * b->L.max_chunks * 4 * 256 * ppt);
+            if ((st = set_adj(ppt))) return st;
+            need = std::max(need, size_t(split_grid(ppt)) * b->L.max_chunks * 4 * kAdjThreads * ppt);
         }
         cudaError_t ea = balloc(b, &b->L.ckpt, need);
         if (ea != cudaSuccess) return bcuda(b, ea, "cudaMalloc");
@@ -1277,7 +1286,7 @@ int batch_autotune(nufi_batch *b)
     float abest = -1;
     int abc = acands[0];
     for (size_t c = 0; c < acands.size(); ++c) {
-        st = batch_set_units(b, acands[c], true);
+        st = set_adj(acands[c]);
         if (st) return st;
         if (split) b->L.adj_grid = split_grid(acands[c]);
         float ms = tune ? batch_time(b, [&] { return launch_batch_adjoint_step(b->L, n_t, b->stream); }, 1) : 0.0f;
@@ -1290,7 +1299,7 @@ int batch_autotune(nufi_batch *b)
             abc = acands[c];
         }
     }
-    st = batch_set_units(b, abc, true);
+    st = set_adj(abc);
     if (st) return st;
     if (split) b->L.adj_grid = split_grid(abc);
     char tail[160];
@@ -1405,11 +1414,13 @@ int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_b
             (e = balloc(b.get(), &I.mu, size_t(I.Nt + 1) * p.P[0])) != cudaSuccess ||
             (e = balloc(b.get(), &I.lambda, size_t(p.N[0]))) != cudaSuccess ||
             (b->precision == NUFI_PREC_FP32_SPLIT &&
-             (e = balloc(b.get(), &I.muT, size_t(I.Nt + 1) * 3 * p.N[0])) != cudaSuccess))
+             ((e = balloc(b.get(), &I.muT, size_t(I.Nt + 1) * 3 * p.N[0])) != cudaSuccess ||
+              (e = balloc(b.get(), &I.muS, size_t(I.Nt + 1) * 3 * p.N[0])) != cudaSuccess)))
             return bail(bcuda(b.get(), e, "cudaMalloc"));
         if ((e = cudaMemset(I.ecount, 0, sizeof(unsigned))) != cudaSuccess ||
             (e = cudaMemset(I.lambda, 0, size_t(p.N[0]) * sizeof(double))) != cudaSuccess ||
             (I.muT && (e = cudaMemset(I.muT, 0, size_t(I.Nt + 1) * 3 * p.N[0] * sizeof(double))) != cudaSuccess) ||
+            (I.muS && (e = cudaMemset(I.muS, 0, size_t(I.Nt + 1) * 3 * p.N[0] * sizeof(float))) != cudaSuccess) ||
             (e = cudaMemset(I.mu, 0, size_t(I.Nt + 1) * p.P[0] * sizeof(double))) != cudaSuccess)
             return bail(bcuda(b.get(), e, "cudaMemset"));
         I.node_begin = nodes;
@@ -1521,6 +1532,9 @@ int nufi_batch_backward(nufi_batch *b, double *grad)
                 if (e == cudaSuccess)
                     e = I.muT ? cudaMemsetAsync(I.muT, 0, size_t(I.Nt + 1) * 3 * I.p.N[0] * sizeof(double), b->stream)
                               : cudaMemsetAsync(I.mu, 0, size_t(I.Nt + 1) * I.p.P[0] * sizeof(double), b->stream);
+            for (const BatchInst &I : b->hi)
+                if (e == cudaSuccess && I.muS)
+                    e = cudaMemsetAsync(I.muS, 0, size_t(I.Nt + 1) * 3 * I.p.N[0] * sizeof(float), b->stream);
             if (e == cudaSuccess)
                 e = cudaMemsetAsync(b->theta_acc, 0, size_t(4) * b->L.adj_units * sizeof(double), b->stream);
             for (int m = b->maxNt; m >= 0 && e == cudaSuccess; --m) e = launch_batch_adjoint_step(b->L, m, b->stream);

@@ -20,6 +20,7 @@ enum : unsigned {
     kErrSolveSize = 1u << 2,   // field solve: grid larger than its shared-memory plan
     kErrStageTimeout = 1u << 3, // a bounded wait on a shared-memory staging barrier gave up
     kErrBarrierTimeout = 1u << 4, // a bounded wait on the persistent kernel's grid barrier gave up
+    kErrAdjointRange = 1u << 5,   // FP32-split adjoint: a fixed-point table-adjoint sum left its range
 };
 
 // Everything a kernel needs to know about one configuration, by value.

@@ -207,7 +207,8 @@ struct BatchInst {
     double *epart;    // [solve_blocks]
     unsigned *ecount; // [1], zero between launches
     double *mu;       // [(Nt+1)][P] slab adjoints
-    double *muT;      // [(Nt+1)][3N] kick-table adjoints (FP32-split adjoint)
+    double *muT;      // [(Nt+1)][N][3] kick-table adjoints (A, B, C of each cell; FP32-split adjoint)
+    float *muS;       // [(Nt+1)][N][3] one step's kick-table adjoints, folded into muT after the step
     double *lambda;   // [N]
     int Nt, tpn;
     int unit_begin, units;
@@ -226,7 +227,7 @@ struct BatchLaunch {
     int adj_ppt = 2, adj_chunk = 8, adj_units = 0, max_P = 0;
     int ts_max = 0, max_N = 0;  // largest table stride (floats) and N of the batch
     int adj_grid = 0, max_chunks = 0;  // FP32-split adjoint: persistent CTAs, chunks per step
-    float *ckpt = nullptr;             // its checkpoints: adj_grid x max_chunks x 4 x 256 x adj_ppt floats
+    float *ckpt = nullptr;             // its checkpoints: adj_grid x max_chunks x 4 x kAdjThreads x adj_ppt floats
     double *theta_acc = nullptr;
     unsigned *err = nullptr;
 };
@@ -235,6 +236,8 @@ cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st);
 cudaError_t launch_batch_adjoint_step(const BatchLaunch &L, int m, cudaStream_t st);
 cudaError_t launch_batch_theta_reduce(const BatchLaunch &L, double *grad, cudaStream_t st);
 constexpr int kAdjChunk = 8;  // slabs per checkpointed chunk of the FP32-split adjoint
+constexpr int kAdjRing = 3;   // its staged chunks
+constexpr int kAdjThreads = 512;  // threads of its CTAs (one per SM)
 size_t adjoint_split_smem(const BatchLaunch &L);
 int adjoint_split_ctas_per_sm(const BatchLaunch &L, int ppt);
 

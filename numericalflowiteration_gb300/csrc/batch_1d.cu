@@ -662,7 +662,7 @@ __global__ void batch_adjoint_fold_kernel(const BatchInst *__restrict__ bi, int 
 }
 
 template <int PPT>
-__global__ void __launch_bounds__(kAdjThreads, 1) batch_adjoint_split_kernel(const BatchInst *__restrict__ bi,
+__global__ void __launch_bounds__(kAdjThreads, 2) batch_adjoint_split_kernel(const BatchInst *__restrict__ bi,
                                                                      const int *__restrict__ unit_inst, int units,
                                                                      int m, int ts_max, int max_chunks,
                                                                      float *__restrict__ ckpt,

@@ -236,8 +236,8 @@ cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st);
 cudaError_t launch_batch_adjoint_step(const BatchLaunch &L, int m, cudaStream_t st);
 cudaError_t launch_batch_theta_reduce(const BatchLaunch &L, double *grad, cudaStream_t st);
 constexpr int kAdjChunk = 8;  // slabs per checkpointed chunk of the FP32-split adjoint
-constexpr int kAdjRing = 3;   // its staged chunks
-constexpr int kAdjThreads = 512;  // threads of its CTAs (one per SM)
+constexpr int kAdjRing = 2;   // its staged chunks
+constexpr int kAdjThreads = 256;  // threads of its CTAs (two per SM)
 size_t adjoint_split_smem(const BatchLaunch &L);
 int adjoint_split_ctas_per_sm(const BatchLaunch &L, int ppt);
 

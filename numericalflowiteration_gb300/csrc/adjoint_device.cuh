@@ -72,6 +72,9 @@ __device__ __forceinline__ double efield_primal(const Problem &p, const double *
 {
     double xi;
     const int ii = locate_adj(p, x, xi, err);
+    if constexpr (ORDER == 4)
+        return -((1 * p.dxinv[0]) *
+                 deboor4_d1(xi, __ldg(c + ii), __ldg(c + ii + 1), __ldg(c + ii + 2), __ldg(c + ii + 3)));
     double w[ORDER];
 #pragma unroll
     for (int j = 0; j < ORDER; ++j) w[j] = __ldg(c + ii + j);
@@ -133,6 +136,44 @@ __device__ __forceinline__ void adjoint_chains(const Problem &p, const double *_
             const double h = k == 0 ? 0.5 : 1.0;
             const double *c = hist + k * hs;
             double *ms = mu_s + (k - k0) * P;
+            if constexpr (ORDER == 4) {
+                // The cubic spline's derivatives from the window's first
+                // differences D_j = w_{j+1} - w_j and the quadratic B-spline
+                // values B0 = (1-xi)^2/2, B2 = xi^2/2, B1 = 1 - B0 - B2:
+                //   S'  = D0 B0 + D1 B1 + D2 B2
+                //   S'' = (D1 - D0) + xi ((D2 - D1) - (D1 - D0))
+                //   dS'/dw = (-B0, B0 - B1, B1 - B2, B2)
+                // (per cell, times dx^-1 and dx^-2); the same mathematics
+                // as the basis loops below in fewer FP64 operations.
+                const double hdt = h * dt, cscale = hdt * -dxinv;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    if (!live[q]) continue;
+                    double xi;
+                    const int ii = locate_adj(p, x[q], xi, err);
+                    const double w0 = __ldg(c + ii), w1 = __ldg(c + ii + 1), w2 = __ldg(c + ii + 2),
+                                 w3 = __ldg(c + ii + 3);
+                    const double D0 = w1 - w0, D1 = w2 - w1, D2 = w3 - w2;
+                    const double om = 1.0 - xi;
+                    const double B0 = 0.5 * (om * om), B2 = 0.5 * (xi * xi), B1 = (1.0 - B0) - B2;
+                    const double s1 = D0 * B0 + D1 * B1 + D2 * B2;
+                    const double Da = D1 - D0, s2 = Da + xi * ((D2 - D1) - Da);
+                    const double E = -dxinv * s1;
+                    const double Ep = -dxinv * dxinv * s2;
+                    const double coef = ub[q] * cscale;
+                    const double g0 = coef * B0, g1 = coef * B1, g2 = coef * B2;
+                    atomicAdd(ms + ii, -g0);
+                    atomicAdd(ms + ii + 1, g0 - g1);
+                    atomicAdd(ms + ii + 2, g1 - g2);
+                    atomicAdd(ms + ii + 3, g2);
+                    const double xt = xb[q] + ub[q] * hdt * Ep;
+                    xb[q] = xt;
+                    ub[q] = ub[q] - dt * xt;
+                    u[q] = u[q] - hdt * E;
+                    x[q] = x[q] + dt * u[q];
+                }
+                continue;
+            }
 #pragma unroll
             for (int q = 0; q < PPT; ++q) {
                 if (!live[q]) continue;

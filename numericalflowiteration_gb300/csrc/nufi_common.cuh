@@ -80,7 +80,12 @@ __host__ __device__ __forceinline__ void bspline_basis(real x, real *result)
 }
 
 // splines1d::eval<real,order,derivative> (nufi/splines.hpp:81-110) on a
-// window already gathered into c[0..ORDER) (destroyed).
+// window already gathered into c[0..ORDER) (destroyed), x the local
+// coordinate in [0, 1] (to a rounding).  The first factor of each de Boor
+// update is ((x + n) - d - 1 - i) there, four adds in that order; with x in
+// [0, 1] every subtraction after the first add is exact, so x + n rounded
+// once and then minus the integer d + 1 + i gives the same bits with one
+// add per update (the FP64 trace is bound by the FP64 pipe).
 template <typename real, int ORDER, int DERIV>
 __host__ __device__ __forceinline__ real deboor(real x, real *c)
 {
@@ -90,12 +95,27 @@ __host__ __device__ __forceinline__ real deboor(real x, real *c)
     for (int j = 1; j <= d; ++j)
 #pragma unroll
         for (int i = n - 1; i >= j; --i) c[i] = c[i] - c[i - 1];
+    const real y = x + real(n);
 #pragma unroll
     for (int j = 1; j < n - d; ++j)
 #pragma unroll
         for (int i = n - d - 1; i >= j; --i)
-            c[d + i] = (x + n - d - 1 - i) * c[d + i] + (i - j + 1 - x) * c[d + i - 1];
+            c[d + i] = (y - real(d + 1 + i)) * c[d + i] + (i - j + 1 - x) * c[d + i - 1];
     return (real(1) / real(faculty(ORDER - DERIV - 1))) * c[n - 1];
+}
+
+// deboor<double, 4, 1> on the window c0..c3 held in registers: the same
+// operations in the same order (the differences, then the three de Boor
+// updates), written out.  On the FP64 pipe this form compiles to about six
+// fewer FP64 instructions per evaluation than the array loop.
+__host__ __device__ __forceinline__ double deboor4_d1(double x, double c0, double c1, double c2, double c3)
+{
+    const double d3 = c3 - c2, d2 = c2 - c1, d1 = c1 - c0;
+    const double y = x + 4.0;
+    const double a4 = y - 4.0, a3 = y - 3.0, b2 = 2.0 - x, b1 = 1.0 - x;
+    const double e3 = a4 * d3 + b2 * d2;
+    const double e2 = a3 * d2 + b1 * d1;
+    return 0.5 * (a4 * e3 + b1 * e2);
 }
 
 // Initial conditions in FP64, same expressions as the oracle's and the

@@ -51,11 +51,15 @@ __device__ __forceinline__ void field_1d(const Problem &p, const double *__restr
 {
     double xi;
     const int ii = locate_fp64(p, 0, x[0], xi, err);
-    double w[ORDER];
-#pragma unroll
-    for (int j = 0; j < ORDER; ++j) w[j] = __ldg(c + ii + j);
     const double factor = 1 * p.dxinv[0];
-    E[0] = -(factor * deboor<double, ORDER, 1>(xi, w));
+    if constexpr (ORDER == 4) {
+        E[0] = -(factor * deboor4_d1(xi, __ldg(c + ii), __ldg(c + ii + 1), __ldg(c + ii + 2), __ldg(c + ii + 3)));
+    } else {
+        double w[ORDER];
+#pragma unroll
+        for (int j = 0; j < ORDER; ++j) w[j] = __ldg(c + ii + j);
+        E[0] = -(factor * deboor<double, ORDER, 1>(xi, w));
+    }
 }
 
 template <int ORDER>

@@ -62,6 +62,26 @@ __device__ __forceinline__ void field_1d(const Problem &p, const double *__restr
     }
 }
 
+// Cubic (order-4) B-spline values b[0..3] and derivatives d[0..3] (d/dt)
+// at the local coordinate t in [0, 1]: closed forms of splines1d::N<4,0>
+// and N<4,1> (nufi/splines.hpp:39-79),
+//   b0 = (1-t)^3/6, b3 = t^3/6, b1 = 2/3 - t^2 + t^3/2, b2 = 1 - b0 - b1 - b3,
+//   d0 = -(1-t)^2/2, d3 = t^2/2, d1 = t (3t/2 - 2), d2 = -(d0 + d1 + d3),
+// about 20 FP64 operations for both (the FP64 trace is bound by the FP64
+// pipe; the results agree with the recurrence to rounding).
+__device__ __forceinline__ void cubic_bd_fp64(double t, double (&b)[4], double (&d)[4])
+{
+    const double s = 1.0 - t, t2 = t * t, s2 = s * s;
+    b[0] = (s2 * s) * (1.0 / 6.0);
+    b[3] = (t2 * t) * (1.0 / 6.0);
+    b[1] = fma(0.5 * t, t2, 2.0 / 3.0 - t2);
+    b[2] = ((1.0 - b[0]) - b[1]) - b[3];
+    d[0] = -0.5 * s2;
+    d[3] = 0.5 * t2;
+    d[1] = t * fma(1.5, t, -2.0);
+    d[2] = -((d[0] + d[1]) + d[3]);
+}
+
 template <int ORDER>
 __device__ __forceinline__ void field_2d(const Problem &p, const double *__restrict__ c, const double *x, double *E,
                                          unsigned *err)
@@ -71,6 +91,29 @@ __device__ __forceinline__ void field_2d(const Problem &p, const double *__restr
     const int jj = locate_fp64(p, 1, x[1], eta, err);
     const int sy = p.P[0];
     const double *__restrict__ w = c + (long long)jj * sy + ii;
+    if constexpr (ORDER == 4) {
+        // E_x = -dx^-1 sum_j (sum_i w_ji d_i(xi)) b_j(eta), E_y likewise with
+        // the roles swapped: one pass over the 16 coefficients
+        double bx[4], dx[4], by[4], dy[4];
+        cubic_bd_fp64(xi, bx, dx);
+        cubic_bd_fp64(eta, by, dy);
+        double ex = 0, ey = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            double r0 = 0, r1 = 0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const double v = __ldg(w + j * sy + i);
+                r0 = fma(v, bx[i], r0);
+                r1 = fma(v, dx[i], r1);
+            }
+            ex = fma(r1, by[j], ex);
+            ey = fma(r0, dy[j], ey);
+        }
+        E[0] = -(p.dxinv[0] * ex);
+        E[1] = -(p.dxinv[1] * ey);
+        return;
+    }
     double N0[ORDER], N1[ORDER], c0[ORDER], c1[ORDER];
     bspline_basis<double, ORDER, 0>(xi, N0);
     bspline_basis<double, ORDER, 1>(xi, N1);
@@ -100,6 +143,40 @@ __device__ __forceinline__ void field_3d(const Problem &p, const double *__restr
     const int kk = locate_fp64(p, 2, x[2], zeta, err);
     const int sy = p.P[0], sz = p.P[0] * p.P[1];
     const double *__restrict__ w = c + (long long)kk * sz + (long long)jj * sy + ii;
+    if constexpr (ORDER == 4) {
+        // one pass over the 64 coefficients: per (k, j) the x-contractions
+        // with the value and derivative bases, folded at once into the three
+        // components' y-contractions, then the z-contractions per k
+        double bx[4], dx[4], by[4], dy[4], bz[4], dz[4];
+        cubic_bd_fp64(xi, bx, dx);
+        cubic_bd_fp64(eta, by, dy);
+        cubic_bd_fp64(zeta, bz, dz);
+        double ex = 0, ey = 0, ez = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            double sx = 0, s_y = 0, s_z = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                double r0 = 0, r1 = 0;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const double v = __ldg(w + k * sz + j * sy + i);
+                    r0 = fma(v, bx[i], r0);
+                    r1 = fma(v, dx[i], r1);
+                }
+                sx = fma(r1, by[j], sx);
+                s_y = fma(r0, dy[j], s_y);
+                s_z = fma(r0, by[j], s_z);
+            }
+            ex = fma(sx, bz[k], ex);
+            ey = fma(s_y, bz[k], ey);
+            ez = fma(s_z, dz[k], ez);
+        }
+        E[0] = -(p.dxinv[0] * ex);
+        E[1] = -(p.dxinv[1] * ey);
+        E[2] = -(p.dxinv[2] * ez);
+        return;
+    }
     double Nx0[ORDER], Nx1[ORDER];
     bspline_basis<double, ORDER, 0>(xi, Nx0);
     bspline_basis<double, ORDER, 1>(xi, Nx1);

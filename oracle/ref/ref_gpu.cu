@@ -5,12 +5,13 @@
 // through the CUDA driver API).  Test infrastructure only; built by
 // oracle/ref/Makefile into oracle/_ref/.
 //
-// The reference hard-codes f0 as config_t<real>::f0 (nufi/config.hpp:72-84).
-// As ref_driver.cpp does for the host code, the 1D f0 is supplied here by
-// explicit specialisations of that member, declared before any use; they
-// read the configured kind and parameters from __constant__ memory (set by
-// the launcher) and evaluate nufi_f0.h's expressions in double.  Everything
-// else is the reference's code.
+// The reference hard-codes f0 as config_t<real>::f0 (nufi/config.hpp:72-84,
+// 140-159, 221-247).  As ref_driver.cpp does for the host code, f0 is
+// supplied here by explicit specialisations of that member (1D, 2D, 3D;
+// float and double), declared before any use; they read the configured kind
+// and parameters from __constant__ memory (set by the launcher) and evaluate
+// nufi_f0.h's expressions in double.  Everything else is the reference's
+// code.
 #include <nufi/config.hpp>
 
 #include "../nufi_f0.h"
@@ -54,6 +55,67 @@ __host__ __device__ double config_t<double>::f0(double x, double u) noexcept
 }
 
 }  // namespace dim1
+
+namespace dim2 {
+
+__device__ inline double ref_f0_2d(double x, double y, double u, double v)
+{
+    const double alpha = nufi_ref_f0.p[0], k = nufi_ref_f0.p[1];
+    return 1.0 / (2.0 * M_PI) * exp(-0.5 * (u * u + v * v)) * (1 + alpha * (cos(k * x) + cos(k * y)));
+}
+
+template <>
+__host__ __device__ float config_t<float>::f0(float x, float y, float u, float v) noexcept
+{
+#ifdef __CUDA_ARCH__
+    return float(ref_f0_2d(x, y, u, v));
+#else
+    return 0.0f;
+#endif
+}
+
+template <>
+__host__ __device__ double config_t<double>::f0(double x, double y, double u, double v) noexcept
+{
+#ifdef __CUDA_ARCH__
+    return ref_f0_2d(x, y, u, v);
+#else
+    return 0.0;
+#endif
+}
+
+}  // namespace dim2
+
+namespace dim3 {
+
+__device__ inline double ref_f0_3d(double x, double y, double z, double u, double v, double w)
+{
+    const double alpha = nufi_ref_f0.p[0], k = nufi_ref_f0.p[1];
+    return 0.06349363593424096978576330493464 * (1. + alpha * cos(k * x) + alpha * cos(k * y) + alpha * cos(k * z)) *
+           exp(-(u * u + v * v + w * w) / 2);
+}
+
+template <>
+__host__ __device__ float config_t<float>::f0(float x, float y, float z, float u, float v, float w) noexcept
+{
+#ifdef __CUDA_ARCH__
+    return float(ref_f0_3d(x, y, z, u, v, w));
+#else
+    return 0.0f;
+#endif
+}
+
+template <>
+__host__ __device__ double config_t<double>::f0(double x, double y, double z, double u, double v, double w) noexcept
+{
+#ifdef __CUDA_ARCH__
+    return ref_f0_3d(x, y, z, u, v, w);
+#else
+    return 0.0;
+#endif
+}
+
+}  // namespace dim3
 }  // namespace nufi
 
 #include <nufi/cuda_kernel.cu>

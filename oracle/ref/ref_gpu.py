@@ -1,14 +1,15 @@
-"""The reference's own 1D GPU kernel on the GPU machine: TEST INFRASTRUCTURE.
+"""The reference's own GPU kernels on the GPU machine: TEST INFRASTRUCTURE.
 
 oracle/ref/Makefile compiles the reference's nufi/cuda_kernel.cu (where it
 lies, unchanged; the configured f0 supplied as explicit specialisations of
 config_t<real>::f0, see ref_gpu.cu) into oracle/_ref/nufi_ref_gpu.cubin,
 device code only, plus the names of its entry functions and the byte layout
-of its by-value config argument.  This module loads the cubin through the
+of its by-value config arguments.  This module loads the cubin through the
 CUDA driver API (ctypes on libcuda, inside torch's context) and launches
-nufi::dim1::cuda_eval_rho<real, order> exactly as the reference's
-cuda_kernel::compute_rho does (nufi/cuda_kernel.cu:112-132: rho zeroed,
-64-thread blocks, one thread per quadrature point, one atomicAdd each).
+nufi::dim{1,2,3}::cuda_eval_rho<real, order> exactly as the reference's
+cuda_kernel::compute_rho does (nufi/cuda_kernel.cu:112-132, 289-311,
+486-510: rho zeroed, 64-thread blocks, one thread per quadrature point in
+the reference's q order, one atomicAdd each).
 
 It is used by tests/test_gpu_reference_kernel.py (the reference's GPU rho
 against the new FP64 path) and, as a script, to time the reference's GPU
@@ -29,7 +30,10 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parents[2]
 REF_DIR = ROOT / "oracle" / "_ref"
-BLOCK = 64  # nufi/cuda_kernel.cu:124
+BLOCK = 64  # nufi/cuda_kernel.cu:124, 301, 497
+
+SPACE = ("x", "y", "z")
+VEL = ("u", "v", "w")
 
 
 class RefGpuUnavailable(RuntimeError):
@@ -41,8 +45,8 @@ def available() -> bool:
 
 
 class RefGpu:
-    """The reference's cuda_eval_rho<real, order> (dim1), launched on torch's
-    current CUDA context and stream."""
+    """The reference's cuda_eval_rho<real, order> (dim 1, 2, 3), launched on
+    torch's current CUDA context and stream."""
 
     def __init__(self):
         if not available():
@@ -68,14 +72,14 @@ class RefGpu:
         if rc != 0:
             raise RuntimeError(f"{what} failed (CUresult {rc})")
 
-    def _func(self, real: str, order: int):
-        key = (real, order)
+    def _func(self, dim: int, real: str, order: int):
+        key = (dim, real, order)
         if key not in self.funcs:
             tag = {"float": "If", "double": "Id"}[real]
-            name = next((e for e in self.entries if e.startswith("_ZN4nufi4dim113cuda_eval_rho" + tag + f"Lm{order}E")),
-                        None)
+            prefix = f"_ZN4nufi4dim{dim}13cuda_eval_rho{tag}Lm{order}E"
+            name = next((e for e in self.entries if e.startswith(prefix)), None)
             if name is None:
-                raise RefGpuUnavailable(f"cuda_eval_rho<{real},{order}> not in the cubin")
+                raise RefGpuUnavailable(f"dim{dim}::cuda_eval_rho<{real},{order}> not in the cubin")
             f = ctypes.c_void_p()
             self._check(self.cu.cuModuleGetFunction(ctypes.byref(f), self.module, name.encode()), "cuModuleGetFunction")
             self.funcs[key] = f
@@ -99,48 +103,64 @@ class RefGpu:
         src = (ctypes.c_char * len(buf)).from_buffer(buf)
         self._check(self.cu.cuMemcpyHtoD_v2(dptr, src, ctypes.c_size_t(len(buf))), "cuMemcpyHtoD")
 
-    def pack_conf(self, real: str, Nx: int, Nu: int, Nt: int, dt: float, x_min: float, x_max: float, u_min: float,
-                  u_max: float) -> bytes:
-        """config_t<real> by value, the derived fields computed in `real` as
-        the reference's constructor does (nufi/config.hpp:53-67)."""
-        lay = self.layout[f"config_t<{real}>"]
+    def pack_conf(self, real: str, cfg) -> bytes:
+        """dim{D}::config_t<real> by value for a Config, the derived fields
+        computed in `real` as the reference's constructors do
+        (nufi/config.hpp:53-67, 116-135, 195-219)."""
+        D = cfg.dim
+        lay = self.layout[f"dim{D}::config_t<{real}>"]
         R = np.float32 if real == "float" else np.float64
-        f = {"dt": R(dt), "x_min": R(x_min), "x_max": R(x_max), "u_min": R(u_min), "u_max": R(u_max)}
-        f["Lx"] = R(f["x_max"] - f["x_min"])
-        f["Lx_inv"] = R(R(1) / f["Lx"])
-        f["dx"] = R(f["Lx"] / R(Nx))
-        f["dx_inv"] = R(R(1) / f["dx"])
-        f["du"] = R(R(f["u_max"] - f["u_min"]) / R(Nu))
-        buf = bytearray(lay["size"])
+        f = {"dt": R(cfg.dt)}
+        ints = {"Nt": cfg.Nt}
+        for a in range(D):
+            s, v = SPACE[a], VEL[a]
+            ints["N" + s] = cfg.Nx[a]
+            ints["N" + v] = cfg.Nv[a]
+            f[s + "_min"], f[s + "_max"] = R(cfg.x_min[a]), R(cfg.x_max[a])
+            f[v + "_min"], f[v + "_max"] = R(cfg.v_min[a]), R(cfg.v_max[a])
+            L = R(f[s + "_max"] - f[s + "_min"])
+            f["L" + s], f["L" + s + "_inv"] = L, R(R(1) / L)
+            d = R(L / R(cfg.Nx[a]))
+            f["d" + s], f["d" + s + "_inv"] = d, R(R(1) / d)
+            f["d" + v] = R(R(f[v + "_max"] - f[v + "_min"]) / R(cfg.Nv[a]))
         off = lay["fields"]
-        for name, v in (("Nx", Nx), ("Nu", Nu), ("Nt", Nt)):
+        if set(off) != set(f) | set(ints):
+            raise RuntimeError(f"config_t layout fields {sorted(off)} do not match {sorted(set(f) | set(ints))}")
+        buf = bytearray(lay["size"])
+        for name, v in ints.items():
             buf[off[name]:off[name] + 8] = int(v).to_bytes(8, "little")
         for name, v in f.items():
             b = np.array([v], dtype=R).tobytes()
             buf[off[name]:off[name] + len(b)] = b
         return bytes(buf)
 
-    def eval_rho(self, real: str, order: int, n: int, coeffs, conf: bytes, rho, q_begin: int, q_end: int,
-                 Nx: int, Nu: int, Nt: int, stream=None) -> None:
-        """rho = 0, then cuda_eval_rho<real, order> over q in [q_begin, q_end)
-        (cuda_kernel::compute_rho).  coeffs and rho are torch tensors of the
-        real type; the sizes are checked here so that every access of the
-        kernel stays inside them."""
+    def eval_rho(self, real: str, cfg, n: int, coeffs, conf: bytes, rho, q_begin: int = 0, q_end: int | None = None,
+                 stream=None) -> None:
+        """rho = 0, then dim{D}::cuda_eval_rho<real, order> over q in
+        [q_begin, q_end) (cuda_kernel::compute_rho).  coeffs and rho are torch
+        tensors of the real type; the sizes are checked here so that every
+        access of the kernel stays inside them."""
         torch = self.torch
         dt = torch.float32 if real == "float" else torch.float64
-        stride = Nx + order - 1
-        if not (0 <= n <= Nt and 0 <= q_begin <= q_end <= Nx * Nu):
+        Nq, Ns = cfg.n_points, cfg.n_spatial
+        q_end = Nq if q_end is None else q_end
+        if not (0 <= n <= cfg.Nt and 0 <= q_begin <= q_end <= Nq):
             raise ValueError("step or point range out of range")
         if coeffs.dtype != dt or rho.dtype != dt or not coeffs.is_cuda or not rho.is_cuda:
             raise TypeError("coeffs and rho must be CUDA tensors of the kernel's real type")
-        # slabs 0..n-1 are read; a window may reach one element into the next slab
-        if coeffs.numel() < (Nt + 1) * stride + order or rho.numel() < Nx:
+        # slabs 0..n-1 are read; a window at the wrap edge may reach past its
+        # slab by less than one slab
+        if coeffs.numel() < (cfg.Nt + 2) * cfg.stride_t or rho.numel() < Ns:
             raise ValueError("coeffs or rho too small")
-        rho[:Nx].zero_()
+        if len(conf) != self.layout[f"dim{cfg.dim}::config_t<{real}>"]["size"]:
+            raise ValueError("config of the wrong size")
+        rho[:Ns].zero_()
         if q_end == q_begin:
             return
         N = q_end - q_begin
         nblocks = 1 + (N - 1) // BLOCK
+        if nblocks >= 2 ** 31:
+            raise ValueError("too many blocks")
         a_n = ctypes.c_size_t(n)
         a_c = ctypes.c_void_p(coeffs.data_ptr())
         a_conf = (ctypes.c_char * len(conf)).from_buffer_copy(conf)
@@ -150,28 +170,39 @@ class RefGpu:
         params = (ctypes.c_void_p * 6)(*[ctypes.cast(ctypes.byref(a), ctypes.c_void_p) for a in
                                          (a_n, a_c, a_conf, a_rho, a_qb, a_qe)])
         st = ctypes.c_void_p(stream if stream is not None else torch.cuda.current_stream().cuda_stream)
-        self._check(self.cu.cuLaunchKernel(self._func(real, order), ctypes.c_uint(nblocks), ctypes.c_uint(1),
-                                           ctypes.c_uint(1), ctypes.c_uint(BLOCK), ctypes.c_uint(1), ctypes.c_uint(1),
-                                           ctypes.c_uint(0), st, params, None), "cuLaunchKernel")
+        self._check(self.cu.cuLaunchKernel(self._func(cfg.dim, real, cfg.order), ctypes.c_uint(nblocks),
+                                           ctypes.c_uint(1), ctypes.c_uint(1), ctypes.c_uint(BLOCK), ctypes.c_uint(1),
+                                           ctypes.c_uint(1), ctypes.c_uint(0), st, params, None), "cuLaunchKernel")
 
 
 def device_history(cfg, hist: np.ndarray, real: str):
     """The FP64 coefficient history as a CUDA tensor of `real`, padded by one
-    slab (the reference reads a window's last coefficient up to one element
-    into the next slab)."""
+    slab (a window at the wrap edge may read past its slab)."""
     import torch
     dt = torch.float32 if real == "float" else torch.float64
-    stride = cfg.Nx[0] + cfg.order - 1
-    t = torch.zeros((cfg.Nt + 2) * stride, dtype=dt, device="cuda")
+    t = torch.zeros((cfg.Nt + 2) * cfg.stride_t, dtype=dt, device="cuda")
     t[:hist.size] = torch.from_numpy(np.ascontiguousarray(hist)).to(device="cuda", dtype=dt)
     return t
 
 
+# Steps timed per dimension and precision: every step where that is quick,
+# a spread of steps where the reference's kernel is slow (the rate is flat
+# in n beyond the first few steps).
+def timed_steps(cfg, real: str):
+    Nt = cfg.Nt
+    if cfg.dim == 1:
+        return list(range(0, Nt + 1)) if real == "float" else list(range(8, Nt + 1, 8))
+    if cfg.dim == 2:
+        return list(range(4, Nt + 1, 4)) if real == "float" else list(range(16, Nt + 1, 16))
+    return [Nt // 5, 2 * Nt // 5, 3 * Nt // 5, 4 * Nt // 5, Nt] if real == "float" else [Nt // 4, Nt // 2]
+
+
 def main(argv=None) -> int:
     """Times the reference's GPU path (cuda_eval_rho<float,4> and <double,4>,
-    one launch per step as its driver does) on a workload's coefficient
-    history from the new FP64 path, beside the new per-step kernels, and
-    checks the reference's rho against the new FP64 rho at a few steps."""
+    one launch per step as its drivers do) on a workload's coefficient
+    history (from the new FP32-split run), beside the new per-step kernels
+    on the same history, and checks the reference's rho against the new
+    FP64 rho at a few steps."""
     import argparse
     import torch
     sys.path.insert(0, str(ROOT))
@@ -179,29 +210,24 @@ def main(argv=None) -> int:
     from numericalflowiteration_gb300.config import WORKLOADS, _F0_NAMES
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="two_stream_1d_256x1024_T50")
-    ap.add_argument("--double-every", type=int, default=8, help="time the double kernel on every k-th step")
+    ap.add_argument("--workload", default="two_stream_1d_256x1024_T50", choices=sorted(WORKLOADS))
     ap.add_argument("--profile-step", type=int, default=None,
                     help="only launch the reference's cuda_eval_rho<double,4> and the new FP64 trace once each at "
-                         "this step (history from the FP32-split run), for a profiler")
+                         "this step, for a profiler")
     args = ap.parse_args(argv)
     nufi.load()
     cfg = WORKLOADS[args.workload]().replace(precision="fp64")
-    if cfg.dim != 1:
-        raise SystemExit("the reference GPU line covers the 1D kernel")
-    Nx, Nu, Nt, order = cfg.Nx[0], cfg.Nv[0], cfg.Nt, cfg.order
-    Nq = Nx * Nu
+    Nq, Ns, Nt = cfg.n_points, cfg.n_spatial, cfg.Nt
     ref = RefGpu()
     ref.set_f0(_F0_NAMES[cfg.f0], cfg.f0_params)
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        sim.run()
+        hist = sim.history()
     if args.profile_step is not None:
         n = args.profile_step
-        with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
-            sim.run()
-            hist = sim.history()
         coeffs = device_history(cfg, hist, "double")
-        rho = torch.zeros(Nx, dtype=coeffs.dtype, device="cuda")
-        conf = ref.pack_conf("double", Nx, Nu, Nt, cfg.dt, cfg.x_min[0], cfg.x_max[0], cfg.v_min[0], cfg.v_max[0])
-        ref.eval_rho("double", order, n, coeffs, conf, rho, 0, Nq, Nx, Nu, Nt)
+        rho = torch.zeros(Ns, dtype=coeffs.dtype, device="cuda")
+        ref.eval_rho("double", cfg, n, coeffs, ref.pack_conf("double", cfg), rho)
         torch.cuda.synchronize()
         with nufi.Simulation(cfg) as sim:
             for k in range(n):
@@ -210,14 +236,15 @@ def main(argv=None) -> int:
             sim.synchronize()
         print(json.dumps({"profile_step": n, "point_steps_per_launch": Nq * n}), flush=True)
         return 0
+
+    check_steps = sorted({1, 2, Nt // 2, Nt})
+    rho_new = {}
     with nufi.Simulation(cfg) as sim:
-        sim.run()
-        hist = sim.history()
-        check_steps = sorted({1, 2, Nt // 4, Nt // 2, Nt})
-        rho_new = {}
+        for k in range(Nt + 1):
+            sim.upload_phi(k, hist)
         for n in check_steps:
             sim.compute_rho(n)
-            rho_new[n] = sim.download_rho(np.zeros(Nx))
+            rho_new[n] = sim.download_rho(np.zeros(Ns))
     stream = torch.cuda.current_stream()
 
     def timed(fn):
@@ -229,36 +256,33 @@ def main(argv=None) -> int:
         e1.synchronize()
         return e0.elapsed_time(e1)
 
-    out = {"workload": args.workload, "Nq": Nq, "Nt": Nt, "order": order,
-           "path": "reference nufi/cuda_kernel.cu built for sm_103a: cuda_eval_rho<real,4>, 64-thread blocks, "
-                   "one FP atomicAdd per point, rho zeroed per step (cuda_kernel::compute_rho)"}
+    out = {"workload": args.workload, "dim": cfg.dim, "Nq": Nq, "Nt": Nt, "order": cfg.order,
+           "path": f"reference nufi/cuda_kernel.cu built for sm_103a: dim{cfg.dim}::cuda_eval_rho<real,4>, "
+                   "64-thread blocks, one FP atomicAdd per point, rho zeroed per step (cuda_kernel::compute_rho)",
+           "history": "from the new FP32-split run of the workload"}
     for real in ("double", "float"):
         coeffs = device_history(cfg, hist, real)
-        rho = torch.zeros(Nx, dtype=coeffs.dtype, device="cuda")
-        conf = ref.pack_conf(real, Nx, Nu, Nt, cfg.dt, cfg.x_min[0], cfg.x_max[0], cfg.v_min[0], cfg.v_max[0])
+        rho = torch.zeros(Ns, dtype=coeffs.dtype, device="cuda")
+        conf = ref.pack_conf(real, cfg)
         errs = {}
         for n in check_steps:
-            ref.eval_rho(real, order, n, coeffs, conf, rho, 0, Nq, Nx, Nu, Nt)
+            ref.eval_rho(real, cfg, n, coeffs, conf, rho)
             r = rho.double().cpu().numpy()
             errs[n] = float(np.max(np.abs(r - rho_new[n])) / max(np.max(np.abs(rho_new[n])), 1e-300))
-        steps = list(range(0, Nt + 1)) if real == "float" else list(range(args.double_every, Nt + 1, args.double_every))
-        for n in steps[:3]:  # warm-up
-            ref.eval_rho(real, order, n, coeffs, conf, rho, 0, Nq, Nx, Nu, Nt)
-        ms = timed(lambda: [ref.eval_rho(real, order, n, coeffs, conf, rho, 0, Nq, Nx, Nu, Nt) for n in steps])
+        steps = timed_steps(cfg, real)
+        ref.eval_rho(real, cfg, steps[0], coeffs, conf, rho)  # warm-up
+        ms = timed(lambda: [ref.eval_rho(real, cfg, n, coeffs, conf, rho) for n in steps])
         ps = Nq * sum(steps)
         out[f"reference_{real}"] = {"point_steps_per_s": ps / (ms * 1e-3), "ms": ms, "steps_timed": len(steps),
                                     "point_steps": ps, "rho_rel_err_vs_new_fp64": errs}
-    # the new per-step kernels on the same steps (drop-in compute_rho)
-    for prec in ("fp32split", "fp64"):
-        c2 = cfg.replace(precision=prec)
-        with nufi.Simulation(c2) as sim:
+    # the new per-step kernels on the same history (drop-in compute_rho)
+    for prec, real in (("fp32split", "float"), ("fp64", "double")):
+        with nufi.Simulation(cfg.replace(precision=prec)) as sim:
             for n in range(Nt + 1):
                 sim.upload_phi(n, hist)
-            steps = list(range(0, Nt + 1)) if prec == "fp32split" else list(range(args.double_every, Nt + 1,
-                                                                                  args.double_every))
+            steps = timed_steps(cfg, real)
             ext = torch.cuda.ExternalStream(sim.stream)
-            for n in steps[:3]:
-                sim.compute_rho(n)
+            sim.compute_rho(steps[0])
             sim.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)

@@ -195,18 +195,20 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
     for (int a = 0; a < D; ++a) K[a] = float(-p.dt * p.dt * p.dxinv[a] * p.dxinv[a]);
     const long long slab_f = p.table_stride;
 
-    // chunk stream: chunk g covers slabs [k_lo, k_hi] of batch g / nchunks
+    // chunk stream: chunk g is chunk j = g mod nchunks of batch g / nchunks
+    // and covers slabs [k_lo, k_hi]; it lands in ring slot g mod R.  The
+    // loops below carry j, the slot and the mbarrier phase along instead of
+    // dividing the 64-bit g (a software division, once per slab in 3D,
+    // where a chunk is one slab).
     const int nchunks = n > 0 ? (n + S - 1) / S : 0;
     const long long total_chunks = batches * nchunks;
-    auto chunk_range = [&](long long g, int &k_hi, int &k_lo) {
-        const int j = int(g % nchunks);
+    auto chunk_range = [&](int j, int &k_hi, int &k_lo) {
         k_hi = n - 1 - j * S;
         k_lo = max(0, k_hi - S + 1);
     };
-    auto issue = [&](long long g) {
+    auto issue = [&](int j, int slot) {
         int k_hi, k_lo;
-        chunk_range(g, k_hi, k_lo);
-        const int slot = int(g % R);
+        chunk_range(j, k_hi, k_lo);
         const unsigned bar = smem_addr(&full_bar[slot]);
         const unsigned bytes = unsigned(k_hi - k_lo + 1) * unsigned(slab_f) * 4u;
         mbar_expect_tx(bar, bytes);
@@ -222,10 +224,12 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
         }
         __syncthreads();
         if (t == 0)
-            for (long long g = 0; g < R && g < total_chunks; ++g) issue(g);
+            for (int g0 = 0; g0 < R && g0 < total_chunks; ++g0) issue(g0 % nchunks, g0);
     }
     bool ok = true;
-    long long g = 0;  // next chunk of the stream
+    long long g = 0;     // next chunk of the stream
+    int slot = 0;        // its ring slot, g mod R
+    unsigned parity = 0;  // its mbarrier phase parity, (g / R) & 1
 
     long long cur_j = 0;
     double acc = 0;
@@ -271,11 +275,10 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
         };
         for (int j = 0; j < nchunks; ++j, ++g) {
             int k_hi, k_lo;
-            chunk_range(g, k_hi, k_lo);
+            chunk_range(j, k_hi, k_lo);
             const float *__restrict__ base;
             if constexpr (STAGED) {
-                const int slot = int(g % R);
-                ok &= mbar_wait(smem_addr(&full_bar[slot]), unsigned((g / R) & 1));
+                ok &= mbar_wait(smem_addr(&full_bar[slot]), parity);
                 base = ring + (long long)slot * S * slab_f;
             } else {
                 base = tables + (long long)k_lo * slab_f;
@@ -294,11 +297,18 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
                 // the last warp to finish the slot refills it; no warp
                 // waits for another, only for its data
                 __syncwarp();
-                const unsigned slot = unsigned(g % R);
                 if ((t & 31) == 0 && atom_add_acq_rel_cta(&released[slot], 1u) == unsigned(W - 1)) {
                     released[slot] = 0;
                     fence_proxy_async_shared();
-                    if (g + R < total_chunks) issue(g + R);
+                    if (g + R < total_chunks) {
+                        int jr = j + R;  // chunk g + R is chunk jr mod nchunks of its batch
+                        while (jr >= nchunks) jr -= nchunks;
+                        issue(jr, slot);
+                    }
+                }
+                if (++slot == R) {
+                    slot = 0;
+                    parity ^= 1u;
                 }
             }
         }

@@ -201,14 +201,32 @@ Problem make_problem(const nufi_config &c)
     }
     p.Nq = p.Ns * p.Nm;
     p.hist_stride = (p.stride_t + 1) / 2 * 2;
-    // 2D/3D FP32 tables: x rows of table_sx floats.  A warp holds 32
-    // consecutive spatial nodes, i.e. 32 / N[0] rows when N[0] < 32; with
-    // table_sx = N[0] (mod 32) those rows fall on disjoint shared-memory
-    // banks (with P[0] = N[0] + 3 two 16-node rows would share 3 banks and
-    // every gather would take two wavefronts).
+    // 2D/3D FP32 tables: x rows of table_sx floats.  When N[0] < 32 a warp
+    // of the split trace spans g = 32 / N[0] x rows, and its gathers take one
+    // wavefront only if the rows' N[0] banks are disjoint (with P[0] = N[0]
+    // + 3 two 16-node neighbour rows share 3 banks).  The rows a warp holds
+    // are row_step = N[1] / g apart (the kernel maps its spatial nodes so),
+    // and table_sx is the smallest stride >= P[0] with row_step * table_sx
+    // = N[0] (mod 32): 22 instead of 19 for 16^3 (a slab of 31.8 KB), where
+    // consecutive rows would need 48 (69.3 KB).  Where no such stride exists
+    // the rows are consecutive and table_sx = N[0] (mod 32).
     p.table_sx = p.P[0];
-    if (c.dim > 1 && p.N[0] < 32)
-        while (p.table_sx % 32 != p.N[0] % 32) ++p.table_sx;
+    p.row_step = 0;
+    if (c.dim > 1 && p.N[0] < 32) {
+        const int g = 32 / p.N[0];
+        bool found = false;
+        if (32 % p.N[0] == 0 && p.N[1] % g == 0) {
+            const int step = p.N[1] / g;
+            for (int sx = p.P[0]; sx < p.P[0] + 32 && !found; ++sx)
+                if ((1LL * step * sx) % 32 == p.N[0] % 32) {
+                    p.table_sx = sx;
+                    p.row_step = step;
+                    found = true;
+                }
+        }
+        if (!found)
+            while (p.table_sx % 32 != p.N[0] % 32) ++p.table_sx;
+    }
     p.table_stride = c.dim == 1 ? (3LL * p.N[0] + 3) / 4 * 4 : (1LL * p.table_sx * p.P[1] * p.P[2] + 3) / 4 * 4;
     p.dt = c.dt;
     for (int i = 0; i < 8; ++i) p.f0p[i] = c.f0_params[i];

@@ -36,6 +36,8 @@ struct Problem {
     long long hist_stride;  // doubles between slabs in the device FP64 history
     long long table_stride; // floats between slabs in the device FP32 tables
     int table_sx;           // 2D/3D FP32 table: floats per x row (>= P[0], see make_problem)
+    int row_step;           // 2D/3D split trace with N[0] < 32: the 32 / N[0] x rows a warp
+                            // spans are row_step rows apart (0: consecutive rows)
     double dt;
     double xmin[3], L[3], Linv[3], dx[3], dxinv[3];
     double vmin[3], dv[3];

@@ -20,13 +20,15 @@
 // Geometry: about one CTA per SM; CTA c owns the velocity nodes c, c + G,
 // c + 2G, ... (interleaved: a spread of velocities per CTA) for every
 // spatial node.  Thread t owns the spatial
-// nodes s = t + T j and visits its items in (j, m) order, PPT at a time
-// (one full trace per batch), so the 32 lanes of a warp hold 32
-// consecutive spatial nodes (x fastest) at one velocity: neighbouring
-// cells, conflict-free shared-memory gathers.  Each thread is the only one
-// in the CTA to touch its nodes, and its items of one node are consecutive,
-// so rho is a register sum flushed to partial[c][s] when j changes (FP64,
-// fixed order: deterministic).
+// nodes s = node(t + T j) and visits its items in (j, m) order, PPT at a
+// time (one full trace per batch), so the 32 lanes of a warp hold 32
+// spatial nodes at one velocity: x fastest, and when N[0] < 32 the
+// 32 / N[0] x rows of a warp row_step rows apart (node(v) = v when
+// row_step = 0), on disjoint shared-memory banks (see table_sx): neighbouring
+// cells, conflict-free gathers.  Each thread is the only one in the CTA to
+// touch its nodes, and its items of one node are consecutive, so rho is a
+// register sum flushed to partial[c][s] when j changes (FP64, fixed order:
+// deterministic).
 //
 // Tables: with ring > 0 the history is streamed through `ring` shared-
 // memory slots of S slabs (cp.async.bulk completing on an mbarrier), one
@@ -190,6 +192,15 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
     const long long nj0 = (Ns + T - 1) / T;                  // ... of thread 0 (the most)
     const long long batches = (nj0 * Mc + PPT - 1) / PPT;
     const int sy = p.table_sx, sz = p.table_sx * p.P[1];
+    // spatial node of virtual index v (< Ns, so in int range): lane l of
+    // warp w takes x = l mod N0 of row y0 + (l / N0) row_step, y0 = w mod
+    // row_step, in plane w / row_step (once per batch)
+    auto node_of = [&](long long v) -> long long {
+        if (p.row_step == 0) return v;
+        const int vi = int(v), N0 = p.N[0], w = vi >> 5;
+        const int x = vi % N0, r = (vi & 31) / N0;
+        return x + (long long)N0 * ((w % p.row_step + r * p.row_step) + (long long)p.N[1] * (w / p.row_step));
+    };
     float K[D];
 #pragma unroll
     for (int a = 0; a < D; ++a) K[a] = float(-p.dt * p.dt * p.dxinv[a] * p.dxinv[a]);
@@ -241,7 +252,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
             const long long k = b * PPT + q;
             const long long j = k / Mc;
             const long long m = blockIdx.x + (k % Mc) * G;
-            const long long s = t + j * T;
+            const long long s = node_of(t + j * T);
             const bool inside = j < nj;
             const long long qq = s * p.Nm + m;
             live[q] = inside && qq >= q_begin && qq < q_end;
@@ -318,7 +329,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
             const long long k = b * PPT + q;
             const long long j = k / Mc;
             if (j != cur_j) {
-                if (cur_j < nj) partial[(long long)blockIdx.x * Ns + t + cur_j * T] = acc;
+                if (cur_j < nj) partial[(long long)blockIdx.x * Ns + node_of(t + cur_j * T)] = acc;
                 acc = 0;
                 cur_j = j;
             }
@@ -344,7 +355,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
             acc += double(df) + Gd;
         }
     }
-    if (cur_j < nj) partial[(long long)blockIdx.x * Ns + t + cur_j * T] = acc;
+    if (cur_j < nj) partial[(long long)blockIdx.x * Ns + node_of(t + cur_j * T)] = acc;
     if (!ok) atomicOr(err, kErrStageTimeout);
 }
 
@@ -395,7 +406,7 @@ StagedShape staged_shape_nd(const Problem &p, int sms)
     if (size_t(kRing) * slab_bytes <= kMaxSmem) {
         sh.ring = kRing;
         sh.slabs_per_chunk =
-            int(std::max<size_t>(1, std::min<size_t>(16, kOneCtaPerSm / (size_t(kRing) * slab_bytes))));
+            int(std::max<size_t>(1, std::min<size_t>(16, kMaxSmem / (size_t(kRing) * slab_bytes))));
     } else if (2 * slab_bytes <= kMaxSmem) {
         sh.ring = 2;
         sh.slabs_per_chunk = 1;

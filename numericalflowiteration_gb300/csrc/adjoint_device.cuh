@@ -72,13 +72,15 @@ __device__ __forceinline__ double efield_primal(const Problem &p, const double *
 {
     double xi;
     const int ii = locate_adj(p, x, xi, err);
-    if constexpr (ORDER == 4)
+    if constexpr (ORDER == 4) {
         return -((1 * p.dxinv[0]) *
                  deboor4_d1(xi, __ldg(c + ii), __ldg(c + ii + 1), __ldg(c + ii + 2), __ldg(c + ii + 3)));
-    double w[ORDER];
+    } else {
+        double w[ORDER];
 #pragma unroll
-    for (int j = 0; j < ORDER; ++j) w[j] = __ldg(c + ii + j);
-    return -((1 * p.dxinv[0]) * deboor<double, ORDER, 1>(xi, w));
+        for (int j = 0; j < ORDER; ++j) w[j] = __ldg(c + ii + j);
+        return -((1 * p.dxinv[0]) * deboor<double, ORDER, 1>(xi, w));
+    }
 }
 
 // Phases of one block's points for step m: (1) the primal trace to the
@@ -172,33 +174,33 @@ __device__ __forceinline__ void adjoint_chains(const Problem &p, const double *_
                     u[q] = u[q] - hdt * E;
                     x[q] = x[q] + dt * u[q];
                 }
-                continue;
-            }
+            } else {
 #pragma unroll
-            for (int q = 0; q < PPT; ++q) {
-                if (!live[q]) continue;
-                double xi;
-                const int ii = locate_adj(p, x[q], xi, err);
-                double N1[ORDER], N2[ORDER];
-                bspline_basis<double, ORDER, 1>(xi, N1);
-                bspline_basis<double, ORDER, 2>(xi, N2);
-                double s1 = 0, s2 = 0;
+                for (int q = 0; q < PPT; ++q) {
+                    if (!live[q]) continue;
+                    double xi;
+                    const int ii = locate_adj(p, x[q], xi, err);
+                    double N1[ORDER], N2[ORDER];
+                    bspline_basis<double, ORDER, 1>(xi, N1);
+                    bspline_basis<double, ORDER, 2>(xi, N2);
+                    double s1 = 0, s2 = 0;
 #pragma unroll
-                for (int j = 0; j < ORDER; ++j) {
-                    const double w = __ldg(c + ii + j);
-                    s1 = fma(w, N1[j], s1);
-                    s2 = fma(w, N2[j], s2);
+                    for (int j = 0; j < ORDER; ++j) {
+                        const double w = __ldg(c + ii + j);
+                        s1 = fma(w, N1[j], s1);
+                        s2 = fma(w, N2[j], s2);
+                    }
+                    const double E = -dxinv * s1;
+                    const double Ep = -dxinv * dxinv * s2;
+                    const double coef = ub[q] * h * dt * (-dxinv);
+#pragma unroll
+                    for (int j = 0; j < ORDER; ++j) atomicAdd(ms + ii + j, coef * N1[j]);
+                    const double xt = xb[q] + ub[q] * h * dt * Ep;
+                    xb[q] = xt;
+                    ub[q] = ub[q] - dt * xt;
+                    u[q] = u[q] - h * dt * E;
+                    x[q] = x[q] + dt * u[q];
                 }
-                const double E = -dxinv * s1;
-                const double Ep = -dxinv * dxinv * s2;
-                const double coef = ub[q] * h * dt * (-dxinv);
-#pragma unroll
-                for (int j = 0; j < ORDER; ++j) atomicAdd(ms + ii + j, coef * N1[j]);
-                const double xt = xb[q] + ub[q] * h * dt * Ep;
-                xb[q] = xt;
-                ub[q] = ub[q] - dt * xt;
-                u[q] = u[q] - h * dt * E;
-                x[q] = x[q] + dt * u[q];
             }
         }
         __syncthreads();

@@ -107,15 +107,6 @@ cudaError_t dalloc(nufi_handle *h, T **ptr, size_t count)
     return cudaSuccess;
 }
 
-bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
-
-int ilog2(long long v)
-{
-    int l = 0;
-    while ((1LL << l) < v) ++l;
-    return l;
-}
-
 // Host-side B-spline basis at x = 0 (collocation stencil N_j(0)).
 void stencil(int order, double *Nb)
 {

@@ -34,28 +34,6 @@ namespace nufi_gb300 {
 
 using namespace split;
 
-namespace {
-
-// Fixed-order sum over the block of one value per thread (any multiple of
-// 32 threads): shuffle tree per warp, then warp sums in order.
-__device__ __forceinline__ double block_sum(double v, double *red)
-{
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double t = 0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < int(blockDim.x >> 5); ++w) t += red[w];
-    __syncthreads();
-    if (threadIdx.x == 0) red[0] = t;
-    __syncthreads();
-    const double r = red[0];
-    __syncthreads();
-    return r;
-}
-
-}  // namespace
-
 template <int PPT, bool POW2>
 __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     const Problem p, float *__restrict__ tables, double *__restrict__ hist, const SplitNode *__restrict__ nodes,
@@ -66,7 +44,6 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long full_bar[kRing];
     __shared__ unsigned released[kRing];  // warps done with the slot's chunk
-    __shared__ double red[32];
     __shared__ double wacc[16][5];
     __shared__ double combine[256];
 

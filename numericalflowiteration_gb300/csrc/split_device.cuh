@@ -256,6 +256,24 @@ __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsig
     return r;
 }
 
+// Shared-memory loads at a 32-bit shared-window address.  The paired
+// kick-table lookups of the staged traces go through these, so their
+// addresses stay 32-bit integer arithmetic (0.9 % off the whole 1D run,
+// same bits).  volatile keeps them after the mbarrier wait that makes the
+// slab visible.
+__device__ __forceinline__ float2 lds_f32x2(unsigned addr)
+{
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
+__device__ __forceinline__ float lds_f32(unsigned addr)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+
 template <bool POW2>
 __device__ __forceinline__ int wrap_cell(int J, int N, unsigned *err)
 {
@@ -303,6 +321,8 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
     float dwC_last = 0.0f;
     auto substep = [&](const float *__restrict__ tk, float h) {
         const unsigned long long H2 = f2_pack(h, h);
+        // table of this slab in the shared window: (K A, K B) at tb + 8 J, K C at tc + 4 J
+        const unsigned tb = smem_addr(tk), tc = tb + unsigned(N) * 8u;
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             const unsigned long long t = f2_sub(f2_sub(f2_sub(X[p], SH[p]), DT[p]), DC[p]);
@@ -314,9 +334,11 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
             I[2 * p] = J0;
             I[2 * p + 1] = J1;
             X[p] = f2_sub(t, f2_sub(mg, MAG2));
-            const float2 ab0 = reinterpret_cast<const float2 *>(tk)[J0];
-            const float2 ab1 = reinterpret_cast<const float2 *>(tk)[J1];
-            const unsigned long long C2 = f2_pack(tk[2 * N + J0], tk[2 * N + J1]);
+            const float2 ab0 = lds_f32x2(tb + unsigned(J0) * 8u);
+            const float2 ab1 = lds_f32x2(tb + unsigned(J1) * 8u);
+            const float c0 = lds_f32(tc + unsigned(J0) * 4u);
+            const float c1 = lds_f32(tc + unsigned(J1) * 4u);
+            const unsigned long long C2 = f2_pack(c0, c1);
             const unsigned long long q = f2_fma(X[p], C2, f2_pack(ab0.y, ab1.y));
             const unsigned long long kq = f2_fma(X[p], q, f2_pack(ab0.x, ab1.x));
             DC[p] = (h == 1.0f) ? f2_add(DC[p], kq) : f2_fma(H2, kq, DC[p]);
@@ -328,6 +350,8 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
             const int J = wrap_cell<POW2>(I[q] - S0m[q] + __float_as_int(mg), N, err);
             I[q] = J;
             xi[q] = t - (mg - kMagic);
+            // the odd chain keeps the plain loads: with the ordering of
+            // volatile loads here the whole run measured 1 % slower
             const float kq = kick_lookup(tk, N, J, xi[q]);
             dwC_last = (h == 1.0f) ? dwC_last + kq : fmaf(h, kq, dwC_last);
         }

@@ -12,8 +12,8 @@ FP32-split form; the FP64 plain form runs beside it for the error gate
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Under torchrun (N > 1) every rank runs an independent replica on its own
-GPU (the path is not split across GPUs in this build); value is the total
-point-steps of all ranks over the slowest rank's time.
+GPU (the path is not split across GPUs); value is the total point-steps of
+all ranks over the slowest rank's time.
 """
 from __future__ import annotations
 

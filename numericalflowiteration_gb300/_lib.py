@@ -7,7 +7,7 @@ device-resident step / run / field_solve of this library.  Failures raise
 the exception type the reference raises for the same condition:
 ``IndexError`` where it throws std::range_error, ``RuntimeError`` for CUDA
 errors (nufi::cuda::exception), ``ValueError`` for invalid arguments and
-``NotImplementedError`` for configurations this build does not cover.
+``NotImplementedError`` for configurations the library does not cover.
 
 There is no fallback: if the CUDA library is missing or cannot load,
 ``load()`` raises.

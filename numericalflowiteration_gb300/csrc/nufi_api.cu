@@ -130,7 +130,7 @@ int validate(const nufi_config *c, std::string &why)
     for (int a = 0; a < c->dim; ++a) {
         if (c->Nx[a] < 1 || c->Nv[a] < 1) { why = "grid sizes must be >= 1"; return NUFI_ERR_INVALID; }
         if (c->Nx[a] > (1 << 20) || c->Nv[a] > kMaxVelocityTable) {
-            why = "grid too large for this build";
+            why = "grid too large (at most 2^20 nodes and 4096 velocity nodes per axis)";
             return NUFI_ERR_RANGE;
         }
         if (!(c->x_max[a] > c->x_min[a]) || !(c->v_max[a] > c->v_min[a])) {

@@ -1,7 +1,7 @@
 /*
  * nufi_oracle.c — CPU restatement of the NuFI hot path.  TEST
  * INFRASTRUCTURE ONLY: the parity tests, the smoke check and the CPU
- * baseline leg of bench.py call this library as the checker.  The product
+ * baseline leg of bench.py call this library as the oracle.  The product
  * (numericalflowiteration_gb300/) never links, loads or calls it.
  *
  * Parity pin: the restatement follows the reference's operation order so

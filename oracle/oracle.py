@@ -1,8 +1,8 @@
 """ctypes binding of the CPU oracle (liboracle.so, built from nufi_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke()
-and by bench.py's CPU-baseline leg, always as the checker.  The product
-package never imports it.
+and by bench.py's CPU-baseline leg, always as the oracle that the CUDA
+path is compared with.  The product package never imports it.
 """
 from __future__ import annotations
 

@@ -1,4 +1,4 @@
-"""The reference's own GPU kernels on the GPU machine: TEST INFRASTRUCTURE.
+"""The reference's own GPU kernels, launched beside the new ones: TEST INFRASTRUCTURE.
 
 oracle/ref/Makefile compiles the reference's nufi/cuda_kernel.cu (where it
 lies, unchanged; the configured f0 supplied as explicit specialisations of

@@ -1,6 +1,6 @@
-"""bench.py's multi-GPU path runs independent replicas (the path does not
-shard across GPUs in this build): the slowest rank's time and the whole-job
-rate, checked here with two gloo ranks on the CPU."""
+"""bench.py's multi-GPU path runs independent replicas (the path is not
+sharded across GPUs): the slowest rank's time and the whole-job rate,
+checked here with two gloo ranks on the CPU."""
 import os
 import socket
 import sys

@@ -5,7 +5,8 @@ against central finite differences (h = 1e-6) of the GPU FP64 forward.
 Tolerances: 1e-8 of max |dJ| against forward mode (both FP64; the adjoint
 recomputes the characteristics by inverting the substeps, which rounds
 differently), 1e-5 relative per component against finite differences (the
-the benchmark spec's bound; the difference quotient itself is good to ~1e-7).
+gradient's accuracy target; the difference quotient itself is good to
+~1e-7).
 """
 import numpy as np
 import pytest

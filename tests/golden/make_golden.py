@@ -47,6 +47,11 @@ RUN_CASES = {
     "landau_3d_16x32_n3": (landau_3d(), 3, [0, 1, 2, 3], [0, 1, 2, 3]),
     "landau_3d_8x8_T2": (landau_3d(Nx=8, Nv=8, Nt=20), 20, [0, 1, 10, 20], [0, 19, 20]),
     "small_landau_3d_4x4": (landau_3d(Nx=4, Nv=4, Nt=5), 5, list(range(6)), list(range(6))),
+    # spline orders other than 4 in 2D and 3D
+    "ordernd3_landau_2d_8x8": (landau_2d(Nx=8, Nv=8, Nt=10, order=3), 10, [0, 1, 5, 10], [0, 5, 10]),
+    "ordernd5_landau_2d_8x8": (landau_2d(Nx=8, Nv=8, Nt=10, order=5), 10, [0, 1, 5, 10], [0, 5, 10]),
+    "ordernd3_landau_3d_4x4": (landau_3d(Nx=4, Nv=4, Nt=5, order=3), 5, [0, 1, 3, 5], [0, 3, 5]),
+    "ordernd5_landau_3d_4x4": (landau_3d(Nx=4, Nv=4, Nt=5, order=5), 5, [0, 1, 3, 5], [0, 3, 5]),
 }
 
 # name -> (config, metrics steps): the reference's eval_f metrics of its own

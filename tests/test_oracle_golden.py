@@ -26,6 +26,10 @@ RUN_CASES_FAST = [
     "two_stream_1d_256x1024_n40",
     "landau_3d_8x8_T2",
     "landau_2d_16x16_T20",
+    "ordernd3_landau_2d_8x8",
+    "ordernd5_landau_2d_8x8",
+    "ordernd3_landau_3d_4x4",
+    "ordernd5_landau_3d_4x4",
 ]
 
 # Long two-stream run: chaotic after saturation, so agreement is looser

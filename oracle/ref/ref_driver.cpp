@@ -212,6 +212,9 @@ void rho_any(const nufi_config &k, size_t n, const double *coeffs, double *rho)
         NUFI_REF_ORDER_CASE(3)
         NUFI_REF_ORDER_CASE(4)
         NUFI_REF_ORDER_CASE(5)
+        NUFI_REF_ORDER_CASE(6)
+        NUFI_REF_ORDER_CASE(7)
+        NUFI_REF_ORDER_CASE(8)
     default: std::fprintf(stderr, "order %d not built\n", k.order); std::exit(2);
     }
 #undef NUFI_REF_ORDER_CASE
@@ -303,6 +306,9 @@ void metrics_any(const nufi_config &k, size_t n, const double *coeffs, double *o
         NUFI_REF_ORDER_CASE(3)
         NUFI_REF_ORDER_CASE(4)
         NUFI_REF_ORDER_CASE(5)
+        NUFI_REF_ORDER_CASE(6)
+        NUFI_REF_ORDER_CASE(7)
+        NUFI_REF_ORDER_CASE(8)
     default: std::fprintf(stderr, "order %d not built\n", k.order); std::exit(2);
     }
 #undef NUFI_REF_ORDER_CASE
@@ -327,6 +333,9 @@ double solve_any(const nufi_config &k, double *rho, double *slab)
         NUFI_REF_ORDER_CASE(3)
         NUFI_REF_ORDER_CASE(4)
         NUFI_REF_ORDER_CASE(5)
+        NUFI_REF_ORDER_CASE(6)
+        NUFI_REF_ORDER_CASE(7)
+        NUFI_REF_ORDER_CASE(8)
     default: std::fprintf(stderr, "order %d not built\n", k.order); std::exit(2);
     }
 #undef NUFI_REF_ORDER_CASE

@@ -52,6 +52,11 @@ RUN_CASES = {
     "ordernd5_landau_2d_8x8": (landau_2d(Nx=8, Nv=8, Nt=10, order=5), 10, [0, 1, 5, 10], [0, 5, 10]),
     "ordernd3_landau_3d_4x4": (landau_3d(Nx=4, Nv=4, Nt=5, order=3), 5, [0, 1, 3, 5], [0, 3, 5]),
     "ordernd5_landau_3d_4x4": (landau_3d(Nx=4, Nv=4, Nt=5, order=5), 5, [0, 1, 3, 5], [0, 3, 5]),
+    # the highest orders the FP64 path takes: 6..8 in 1D, 6 in 2D
+    "orderhi6_landau_1d_32x64": (landau_1d(Nx=32, Nv=64, Nt=12, order=6), 12, [0, 1, 6, 12], [0, 6, 12]),
+    "orderhi7_landau_1d_32x64": (landau_1d(Nx=32, Nv=64, Nt=12, order=7), 12, [0, 1, 6, 12], [0, 6, 12]),
+    "orderhi8_landau_1d_32x64": (landau_1d(Nx=32, Nv=64, Nt=12, order=8), 12, [0, 1, 6, 12], [0, 6, 12]),
+    "orderhi6_landau_2d_8x8": (landau_2d(Nx=8, Nv=8, Nt=10, order=6), 10, [0, 1, 5, 10], [0, 5, 10]),
 }
 
 # name -> (config, metrics steps): the reference's eval_f metrics of its own

@@ -35,7 +35,9 @@ def _slabs_ok(cfg, hist, g, tol=1e-11):
 @pytest.mark.parametrize("name", ["small_landau_1d_16x32", "small_landau_2d_8x8", "small_landau_3d_4x4",
                                   "order3_landau_1d_32x64", "order5_landau_1d_32x64",
                                   "ordernd3_landau_2d_8x8", "ordernd5_landau_2d_8x8",
-                                  "ordernd3_landau_3d_4x4", "ordernd5_landau_3d_4x4"])
+                                  "ordernd3_landau_3d_4x4", "ordernd5_landau_3d_4x4",
+                                  "orderhi6_landau_1d_32x64", "orderhi7_landau_1d_32x64",
+                                  "orderhi8_landau_1d_32x64", "orderhi6_landau_2d_8x8"])
 def test_fp64_stepwise_rho_energy_slabs(nufi, name):
     cfg, g = golden(name)
     with nufi.Simulation(cfg) as sim:

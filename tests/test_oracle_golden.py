@@ -30,6 +30,10 @@ RUN_CASES_FAST = [
     "ordernd5_landau_2d_8x8",
     "ordernd3_landau_3d_4x4",
     "ordernd5_landau_3d_4x4",
+    "orderhi6_landau_1d_32x64",
+    "orderhi7_landau_1d_32x64",
+    "orderhi8_landau_1d_32x64",
+    "orderhi6_landau_2d_8x8",
 ]
 
 # Long two-stream run: chaotic after saturation, so agreement is looser

@@ -112,3 +112,51 @@ def test_point_step_count():
     assert cfg.n_points == 262144
     assert cfg.point_steps() == 262144 * 800 * 801 // 2
     assert cfg.point_steps(10, 20) == 262144 * sum(range(10, 21))
+
+
+def _batch_status(lib, cfgs):
+    arr = (NufiConfigC * len(cfgs))(*[c.to_c() for c in cfgs]) if cfgs else None
+    h = ctypes.c_void_p()
+    st = lib.nufi_batch_create(arr, len(cfgs), 0, ctypes.byref(h))
+    msg = lib.nufi_batch_last_error(None).decode()
+    if st == 0:
+        lib.nufi_batch_destroy(h)
+    return st, msg
+
+
+def test_batch_rejects_bad_sets_before_cuda(lib):
+    """nufi_batch_create checks the whole set before any instance touches
+    the GPU: 1D, order 4, one precision, Nx dividing 256; a member's own
+    config errors come back with its index."""
+    from numericalflowiteration_gb300.config import bump_on_tail_1d, landau_2d
+    b = bump_on_tail_1d
+    assert _batch_status(lib, [])[0] == _lib.ERR_INVALID
+    st, msg = _batch_status(lib, [b(), landau_2d(Nx=8, Nv=8, Nt=4)])
+    assert st == _lib.ERR_UNSUPPORTED and "order 4" in msg
+    st, _ = _batch_status(lib, [b(), b(precision="fp32split")])
+    assert st == _lib.ERR_UNSUPPORTED
+    st, _ = _batch_status(lib, [b(), b(order=5)])
+    assert st == _lib.ERR_UNSUPPORTED
+    for nx in (96, 512):
+        st, msg = _batch_status(lib, [b(Nx=nx)])
+        assert st == _lib.ERR_UNSUPPORTED and "divide 256" in msg
+    st, msg = _batch_status(lib, [b(dt=-1.0), b()])
+    assert st == _lib.ERR_INVALID and msg.startswith("instance 0:")
+
+
+def test_batch_null_calls_fail_cleanly(lib):
+    buf = (ctypes.c_double * 8)()
+    assert lib.nufi_batch_forward(None, buf) == _lib.ERR_INVALID
+    assert lib.nufi_batch_backward(None, buf) == _lib.ERR_INVALID
+    assert lib.nufi_batch_energy(None, 0, buf) == _lib.ERR_INVALID
+    s = ctypes.create_string_buffer(16)
+    assert lib.nufi_batch_describe(None, s, 16) == _lib.ERR_INVALID
+    assert lib.nufi_batch_destroy(None) == 0
+
+
+def test_batch_python_errors(lib):
+    from numericalflowiteration_gb300.config import bump_on_tail_1d, landau_2d
+    with pytest.raises(ValueError):
+        nufi.Batch([])
+    with pytest.raises(NotImplementedError):
+        nufi.Batch([landau_2d(Nx=8, Nv=8, Nt=4)])

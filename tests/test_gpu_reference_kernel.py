@@ -88,3 +88,16 @@ def test_reference_config_packing(dim):
         assert get("Lx") == L and get("dx") == R(L / R(cfg.Nx[0])) and get("dx_inv") == R(R(1) / R(L / R(cfg.Nx[0])))
         assert get("du") == R(R(R(cfg.v_max[0]) - R(cfg.v_min[0])) / R(cfg.Nv[0]))
 
+
+
+def test_reference_cubin_holds_the_launched_entries():
+    """(CPU) The reference GPU build lists the six kernels ref_gpu.py
+    launches (dim 1-3 cuda_eval_rho, float and double, order 4)."""
+    from oracle.ref import ref_gpu
+    if not ref_gpu.available():
+        pytest.skip("no reference GPU build in oracle/_ref")
+    entries = (ref_gpu.REF_DIR / "nufi_ref_gpu.entries").read_text().split()
+    for dim in (1, 2, 3):
+        for tag in ("If", "Id"):
+            prefix = f"_ZN4nufi4dim{dim}13cuda_eval_rho{tag}Lm4E"
+            assert sum(e.startswith(prefix) for e in entries) == 1, prefix

@@ -89,7 +89,6 @@ def test_reference_config_packing(dim):
         assert get("du") == R(R(R(cfg.v_max[0]) - R(cfg.v_min[0])) / R(cfg.Nv[0]))
 
 
-
 def test_reference_cubin_holds_the_launched_entries():
     """(CPU) The reference GPU build lists the six kernels ref_gpu.py
     launches (dim 1-3 cuda_eval_rho, float and double, order 4)."""

@@ -125,6 +125,50 @@ def test_oracle_fields_known_answer(oracle_mod):
     assert err < 1e-12 and ref < 1e-12
 
 
+def test_oracle_spline_known_answers(oracle_mod):
+    """nufi/splines.hpp:39-110 on a 1D grid with dx = 1: at a node the
+    order-4 window weights are N4(0) = [1/6, 2/3, 1/6, 0]; at the cell
+    midpoint the coefficients e1 = [0, 1, 0, 0] give eval<4,0>(0.5) =
+    0.47916666666666663 and eval<4,1>(0.5) = -0.625 (values the reference's
+    own functions print)."""
+    from numericalflowiteration_gb300.config import Config
+    N = 16
+    cfg = Config(1, [N], [1], 0, 1.0, [0.0], [float(N)], [0.0], [1.0])
+    i = 5
+    node = np.array([[float(i)]])
+    weights = []
+    for j in range(4):
+        slab = np.zeros(N + 3)
+        slab[i + j] = 1.0
+        weights.append(oracle_mod.eval_field(cfg, slab, node)[0])
+    assert weights == [0.16666666666666666, 0.66666666666666663, 0.16666666666666666, 0.0]
+    slab = np.zeros(N + 3)
+    slab[i + 1] = 1.0
+    mid = np.array([[i + 0.5]])
+    assert oracle_mod.eval_field(cfg, slab, mid)[0] == 0.47916666666666663
+    assert oracle_mod.eval_field(cfg, slab, mid, deriv=(1, 0, 0))[0] == -0.625
+
+
+@pytest.mark.parametrize("case", ["landau_1d", "two_stream_1d", "landau_2d", "landau_3d"])
+def test_oracle_initial_energy_known_answer(case, oracle_mod):
+    """The field energy at t = 0 of f0 = (1 + a sum_i cos k x_i) g(v) with
+    unit-mass g: E_i = (a/k) sin k x_i, so 1/2 int |E|^2 = 1/2 d (a/k)^2
+    L^(d-1) L/2.  The velocity midpoint sum of g is exact to rounding on
+    [-10, 10] and [-8, 8]; on [-6, 6]^3 the truncated Gaussian's missing
+    mass (2e-9 per axis) sets the 3D tolerance."""
+    from numericalflowiteration_gb300 import config
+    cfg, tol = {"landau_1d": (config.landau_1d(Nt=1), 1e-12),
+                "two_stream_1d": (config.two_stream_1d(Nx=64, Nv=256, Nt=1), 1e-12),
+                "landau_2d": (config.landau_2d(Nx=16, Nv=32, Nt=1), 1e-12),
+                "landau_3d": (config.landau_3d(Nx=8, Nv=16, Nt=1), 2e-8)}[case]
+    a, k = cfg.f0_params[0], cfg.f0_params[1]
+    L = cfg.x_max[0] - cfg.x_min[0]
+    d = cfg.dim
+    expect = 0.5 * d * (a / k) ** 2 * L ** (d - 1) * L / 2
+    energy, _, _ = oracle_mod.run(cfg, 0, 0)
+    assert abs(energy[0] - expect) <= tol * expect, (energy[0], expect)
+
+
 def test_oracle_q_range_partition(oracle_mod):
     """rho over a split q range adds up to rho over the whole range, as the
     reference's multi-device split relies on (nufi/cuda_scheduler.hpp:88-118)."""

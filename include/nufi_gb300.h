@@ -94,7 +94,12 @@ const char *nufi_last_error(const nufi_handle *h);
  * Replaces the constructor of nufi::dimN::cuda_kernel<real,order>
  * (nufi/cuda_kernel.hpp:37-38, 82, 124; nufi/cuda_kernel.cu:81-109,
  * 273-286, 468-483): allocates the coefficient history (Nt+1 slabs),
- * rho and the metrics accumulators on `device`. */
+ * rho and the metrics accumulators on `device`.  Checked before any CUDA
+ * call: NUFI_ERR_RANGE for Nt > 2^30, more than 2^31 - 1 spatial or
+ * velocity nodes, more than 2^20 nodes or 4096 velocity nodes on an axis,
+ * or a history above 2^50 bytes; NUFI_ERR_INVALID / NUFI_ERR_UNSUPPORTED
+ * for the other configuration errors.  NUFI_ERR_CUDA (with the CUDA error's
+ * name) when no device is usable or an allocation fails. */
 int nufi_create(const nufi_config *cfg, int device, nufi_handle **out);
 int nufi_destroy(nufi_handle *h);
 

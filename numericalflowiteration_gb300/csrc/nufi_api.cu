@@ -13,8 +13,10 @@
 //   rho      [Ns] FP64, energy [Nt+1] FP64, err (one error word).
 //   solve plan: circulant kernels of the Poisson + collocation diagonal.
 //   split tables: per-velocity-node constants and per-cell phases.
+#include <climits>
 #include <cmath>
 #include <complex>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -100,6 +102,7 @@ template <typename T>
 cudaError_t dalloc(nufi_handle *h, T **ptr, size_t count)
 {
     void *p = nullptr;
+    if (count > SIZE_MAX / sizeof(T)) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
     if (e != cudaSuccess) return e;
     h->allocations.push_back(p);
@@ -137,6 +140,29 @@ int validate(const nufi_config *c, std::string &why)
             why = "domain bounds must satisfy min < max";
             return NUFI_ERR_INVALID;
         }
+    }
+    // Sizes below are products of these counts in 64-bit integers, and the
+    // launch shapes hold node and block counts in 32-bit fields: bounded here
+    // so that no product wraps (a wrapped allocation size would leave the
+    // kernels indexing past their buffers).  A history that merely exceeds
+    // the device's memory fails cleanly in cudaMalloc.
+    long double ns = 1, nm = 1, slab = 1;
+    for (int a = 0; a < c->dim; ++a) {
+        ns *= (long double)c->Nx[a];
+        nm *= (long double)c->Nv[a];
+        slab *= (long double)(c->Nx[a] + c->order - 1);
+    }
+    if (c->Nt > kMaxSteps) { why = "Nt too large (at most 2^30 time steps)"; return NUFI_ERR_RANGE; }
+    if (ns > (long double)INT_MAX || nm > (long double)INT_MAX) {
+        why = "grid too large (at most 2^31 - 1 spatial and 2^31 - 1 velocity nodes)";
+        return NUFI_ERR_RANGE;
+    }
+    // 20 bytes per slab value stands for the FP64 history and the FP32
+    // tables; with the tables' row padding the real figure is at most 7x
+    // that, still far below 2^64
+    if (((long double)c->Nt + 1) * (slab + 2) * 20 > (long double)(1ULL << 50)) {
+        why = "coefficient history too large (more than 2^50 bytes)";
+        return NUFI_ERR_RANGE;
     }
     if (c->precision != NUFI_PREC_FP64 && c->precision != NUFI_PREC_FP32_SPLIT) {
         why = "unknown precision mode";
@@ -1139,6 +1165,7 @@ template <typename T>
 cudaError_t balloc(nufi_batch *b, T **ptr, size_t count)
 {
     void *p = nullptr;
+    if (count > SIZE_MAX / sizeof(T)) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&p, std::max<size_t>(count * sizeof(T), 16));
     if (e != cudaSuccess) return e;
     b->allocations.push_back(p);

@@ -79,6 +79,39 @@ def test_invalid_configs_rejected_before_cuda(lib, mutate, code):
     assert st == code and msg.startswith("nufi_create:")
 
 
+def test_oversized_runs_rejected_before_cuda(lib):
+    """Step counts, node counts and history sizes whose 64-bit products
+    could wrap are range errors at create (as the reference's range_error
+    for too many blocks, nufi/cuda_kernel.cu:115-116), before any CUDA
+    call; the largest accepted step count still reaches CUDA."""
+    from numericalflowiteration_gb300.config import landau_3d
+    cases = [landau_1d(Nt=2 ** 30 + 1), landau_1d(Nt=2 ** 62),
+             landau_3d(Nx=2048, Nv=8, Nt=2), landau_3d(Nx=8, Nv=2048, Nt=2),
+             landau_3d(Nx=1024, Nv=8, Nt=2 ** 20), landau_1d(Nx=2 ** 20, Nt=2 ** 30)]
+    for cfg in cases:
+        st, msg = _create_status(lib, cfg.to_c())
+        assert st == _lib.ERR_RANGE and msg.startswith("nufi_create:") and "too large" in msg, (cfg, msg)
+        with pytest.raises(IndexError):
+            nufi.Simulation(cfg)
+    st, msg = _create_status(lib, landau_1d(Nt=2 ** 30).to_c())
+    assert not msg.startswith("nufi_create:"), msg
+
+
+def test_create_without_a_device_reports_the_cuda_error(lib):
+    """A valid configuration where no device is usable fails with the CUDA
+    error's name and text (the reference's cuda::exception,
+    nufi/cuda_runtime.hpp:46-51), and the library stays usable."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    st, msg = _create_status(lib, landau_1d().to_c())
+    assert st == _lib.ERR_CUDA and "cudaError" in msg
+    with pytest.raises(nufi.NufiError):
+        nufi.Simulation(landau_1d())
+    st, _ = _create_status(lib, landau_1d(order=12).to_c())
+    assert st == _lib.ERR_INVALID
+
+
 def test_unbuilt_combinations_report_unsupported(lib):
     c = landau_1d(order=5, precision="fp32split").to_c()
     st, msg = _create_status(lib, c)

@@ -167,7 +167,8 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
  *                         eval_f trajectory only when n > 1, then
  *                         x - L floor(x / L); f_out unused.
  * pts: npts x (x.., v..) doubles; f_out: npts (may be NULL); feet: npts x
- * (x.., v..) final positions and velocities (may be NULL).  Blocks. */
+ * (x.., v..) final positions and velocities (may be NULL).  At most 2^36
+ * points per call (NUFI_ERR_RANGE above).  Blocks. */
 #define NUFI_EVAL_FTILDA     0
 #define NUFI_EVAL_F          1
 #define NUFI_EVAL_PHASE_FLOW 2
@@ -232,7 +233,8 @@ int nufi_batch_describe(const nufi_batch *b, char *buf, size_t len);
  * else's CUDA-graph capture or memory pool, or a real-time loop whose
  * device memory is reserved up front.  FP64 plain form only.  The caller
  * passes device buffers: hist (slab k at hist + k*hist_stride doubles,
- * reference layout inside a slab, hist_stride >= stride_t) and rho (Ns
+ * reference layout inside a slab, stride_t <= hist_stride, and
+ * (Nt + 1) * hist_stride * 8 <= 2^50 bytes) and rho (Ns
  * doubles, overwritten, not accumulated).  Enqueued on `stream` (a
  * cudaStream_t, NULL = legacy default stream) on the current device;
  * returns without waiting.

@@ -993,6 +993,8 @@ int nufi_eval_points(nufi_handle *h, int64_t n, int mode, int64_t npts, const do
         return fail(h, NUFI_ERR_INVALID, "eval_points: mode (phase flow is 1D, as the reference's)");
     if (npts < 0) return fail(h, NUFI_ERR_INVALID, "eval_points: npts < 0");
     if (npts == 0) return NUFI_OK;
+    // buffer bytes and the launch's block count stay far from wrapping
+    if (npts > kMaxEvalPoints) return fail(h, NUFI_ERR_RANGE, "eval_points: more than 2^36 points in one call");
     DeviceGuard g(h->device);
     const int D = h->p.dim;
     const size_t pbytes = size_t(npts) * 2 * D * sizeof(double);
@@ -1668,6 +1670,10 @@ extern "C" int nufi_compute_rho_noalloc(const nufi_config *cfg, int64_t n, const
     Problem p = make_problem(*cfg);
     if (hist_stride < p.stride_t)
         return fail(nullptr, NUFI_ERR_INVALID, "nufi_compute_rho_noalloc: hist_stride smaller than one slab");
+    // the kernels address slab k at hist + k * hist_stride in 64-bit
+    // integers: the history's extent is held to the bound nufi_create uses
+    if ((long double)(cfg->Nt + 1) * (long double)hist_stride * 8 > (long double)(1ULL << 50))
+        return fail(nullptr, NUFI_ERR_RANGE, "nufi_compute_rho_noalloc: history above 2^50 bytes");
     p.hist_stride = hist_stride;
     if (n < 0 || n > cfg->Nt) return fail(nullptr, NUFI_ERR_RANGE, "nufi_compute_rho_noalloc: Time-step out of range.");
     if (q_begin < 0 || q_end < q_begin || q_end > p.Nq)

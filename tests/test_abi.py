@@ -97,6 +97,23 @@ def test_oversized_runs_rejected_before_cuda(lib):
     assert not msg.startswith("nufi_create:"), msg
 
 
+def test_noalloc_rejects_bad_strides_before_cuda(lib):
+    """nufi_compute_rho_noalloc checks the caller's history stride (at least
+    one slab; history within 2^50 bytes) and the step before any CUDA call.
+    The device pointers are never touched on these paths."""
+    cfg = landau_1d(Nx=16, Nv=32, Nt=8)
+    c = cfg.to_c()
+    dummy = ctypes.c_void_p(0x1000)
+    call = lambda stride, n: lib.nufi_compute_rho_noalloc(ctypes.byref(c), n, dummy, stride, 0, cfg.n_points,
+                                                          dummy, None)
+    assert call(cfg.stride_t - 1, 1) == _lib.ERR_INVALID
+    assert call(2 ** 62, 1) == _lib.ERR_RANGE
+    assert "2^50" in lib.nufi_last_error(None).decode()
+    assert call(cfg.stride_t, 9) == _lib.ERR_RANGE
+    null = lib.nufi_compute_rho_noalloc(ctypes.byref(c), 1, None, cfg.stride_t, 0, 1, dummy, None)
+    assert null == _lib.ERR_INVALID
+
+
 def test_create_without_a_device_reports_the_cuda_error(lib):
     """A valid configuration where no device is usable fails with the CUDA
     error's name and text (the reference's cuda::exception,

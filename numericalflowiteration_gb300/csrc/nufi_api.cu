@@ -180,6 +180,10 @@ int validate(const nufi_config *c, std::string &why)
         why = "FP64 trace not built for this (dim, order)";
         return NUFI_ERR_UNSUPPORTED;
     }
+    if (c->precision == NUFI_PREC_FP64 && nm > (long double)kMaxFp64VelocityNodes) {
+        why = "FP64 trace takes at most 65535 x 16 = 1048560 velocity nodes (blocks of 16 on the grid's y axis)";
+        return NUFI_ERR_UNSUPPORTED;
+    }
     if (c->precision == NUFI_PREC_FP32_SPLIT && !split_supported(c->dim, c->order, c->f0_kind)) {
         why = "FP32-split trace not built for this (dim, order, f0)";
         return NUFI_ERR_UNSUPPORTED;
@@ -697,6 +701,8 @@ int nufi_compute_metrics(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_e
     if (q_begin < 0 || q_end < q_begin || q_end > h->p.Nq)
         return fail(h, NUFI_ERR_RANGE, "quadrature range outside [0, Nq]");
     if (q_begin == q_end) return NUFI_OK;  // as the reference: no launch, sums untouched
+    if (h->p.Nm > kMaxFp64VelocityNodes)  // metrics run the FP64 trace in every precision
+        return fail(h, NUFI_ERR_UNSUPPORTED, "compute_metrics: the FP64 trace takes at most 1048560 velocity nodes");
     DeviceGuard g(h->device);
     const Problem &p = h->p;
     int rows = 0;

@@ -13,6 +13,9 @@ constexpr int kMaxOrder = 8;
 constexpr int kMaxVelocityTable = 4096;  // per-axis velocity nodes kept in tables
 constexpr long long kMaxSteps = 1LL << 30;  // time steps per run (kernels take 32-bit step indices)
 constexpr long long kMaxEvalPoints = 1LL << 36;  // points per nufi_eval_points call
+// FP64 trace launch: velocity blocks of 4 warps x 4 points on the grid's y
+// axis, which holds at most 65535 blocks
+constexpr long long kMaxFp64VelocityNodes = 65535LL * 16;
 
 // Bits of the device error word (checked by the host after each blocking
 // call).  Kernels set a bit and skip the offending access; they never trap.

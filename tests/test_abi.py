@@ -97,6 +97,21 @@ def test_oversized_runs_rejected_before_cuda(lib):
     assert not msg.startswith("nufi_create:"), msg
 
 
+def test_fp64_velocity_grid_limit(lib):
+    """The FP64 trace puts velocity blocks of 16 nodes on the launch grid's
+    y axis (at most 65535): FP64 handles above 1048560 velocity nodes are
+    refused at create, before CUDA; the FP32-split trace has no such limit
+    and the largest accepted FP64 grid reaches CUDA."""
+    from numericalflowiteration_gb300.config import landau_3d
+    st, msg = _create_status(lib, landau_3d(Nx=4, Nv=128, Nt=2).to_c())
+    assert st == _lib.ERR_UNSUPPORTED and "1048560" in msg
+    with pytest.raises(NotImplementedError):
+        nufi.Simulation(landau_3d(Nx=4, Nv=128, Nt=2))
+    for cfg in (landau_3d(Nx=4, Nv=128, Nt=2, precision="fp32split"), landau_3d(Nx=4, Nv=101, Nt=2)):
+        st, msg = _create_status(lib, cfg.to_c())
+        assert not msg.startswith("nufi_create:"), msg
+
+
 def test_noalloc_rejects_bad_strides_before_cuda(lib):
     """nufi_compute_rho_noalloc checks the caller's history stride (at least
     one slab; history within 2^50 bytes) and the step before any CUDA call.

@@ -266,6 +266,14 @@ int nufi_launch_count(const nufi_handle *h, int64_t *count);
  * NUL-terminated into buf; NUFI_ERR_RANGE if len is too small (the text is
  * cut). */
 int nufi_describe(const nufi_handle *h, char *buf, size_t len);
+/* No counterpart in the reference: the plan nufi_create would choose for cfg
+ * on a device with `sms` multiprocessors (1..4096), with no CUDA call: the
+ * fields of nufi_describe plus "layout" (node counts, slab and table
+ * strides, the 2D/3D table row stride and row step, partial-sum rows),
+ * "staged_tpn", "solve_smem", "solve_why" and "adjoint" (its grid).  For
+ * capacity planning; configuration errors as nufi_create's, via
+ * nufi_last_error(NULL). */
+int nufi_plan(const nufi_config *cfg, int sms, char *buf, size_t len);
 
 #ifdef __cplusplus
 }

@@ -40,6 +40,7 @@ SIGNATURES = {
     "nufi_upload_phi_f32": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_compute_metrics": (ctypes.c_int, [_P, _I64, _I64, _I64]),
     "nufi_describe": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    "nufi_plan": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
     "nufi_forward": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_eval_points": (ctypes.c_int, [_P, _I64, ctypes.c_int, _I64, _P, _P, _P]),
     "nufi_save_history": (ctypes.c_int, [_P, _I64, ctypes.c_char_p]),
@@ -104,6 +105,19 @@ def _raise(code: int, msg: str):
     if code == ERR_UNSUPPORTED:
         raise NotImplementedError(msg)
     raise NufiError(f"[{code}] {msg}")
+
+
+def plan(cfg, sms: int = 152) -> dict:
+    """The launch plan a Simulation of cfg would choose on a device with
+    `sms` multiprocessors (nufi_plan), without touching CUDA."""
+    import json
+    lib = load()
+    c = cfg.to_c()
+    buf = ctypes.create_string_buffer(4096)
+    st = lib.nufi_plan(ctypes.byref(c), int(sms), buf, len(buf))
+    if st:
+        _raise(st, lib.nufi_last_error(None).decode())
+    return json.loads(buf.value.decode())
 
 
 class Simulation:

@@ -283,6 +283,56 @@ LaunchShape choose_shape(const Problem &p, int sms)
     return s;
 }
 
+// Trace launch shapes for p on a device with `sms` multiprocessors, with no
+// CUDA call (nufi_create and nufi_plan).  NUFI_SPLIT_STAGED=0 reads the
+// split tables from global memory instead of the shared-memory ring.
+void plan_traces(const Problem &p, int sms, LaunchShape &shape, StagedShape &staged)
+{
+    shape = choose_shape(p, sms);
+    staged = StagedShape{};
+    const char *env = std::getenv("NUFI_SPLIT_STAGED");
+    const bool no_ring = env && env[0] == '0';
+    if (p.precision == NUFI_PREC_FP32_SPLIT && p.dim > 1) {
+        staged = staged_shape_nd(p, sms);
+        if (no_ring) {
+            staged.ring = 0;
+            staged.smem = 0;
+        }
+    } else if (p.precision == NUFI_PREC_FP32_SPLIT && !p.split_plain_kick && !no_ring) {
+        staged = staged_shape_1d(p, sms);
+    }
+}
+
+// Shape of the field solve (its node limit and grid), with no CUDA call.
+bool solve_geometry(const Problem &p, int sms, SolvePlan &pl, std::string &why)
+{
+    if (p.Ns > 16384) {
+        why = "device field solve holds at most 16384 grid nodes";
+        return false;
+    }
+    pl.nconv = (p.precision == NUFI_PREC_FP32_SPLIT && p.dim == 1) ? 5 : 2;
+    // nodes per block: enough blocks to cover the SMs, up to 8 warps per node
+    int npb = 8;
+    while (npb > 1 && (p.Ns + npb - 1) / npb < sms) npb /= 2;
+    pl.nodes_per_block = npb;
+    pl.blocks = int((p.Ns + npb - 1) / npb);
+    const size_t with_green = size_t(p.Ns) * 8 * (1 + pl.nconv);
+    pl.green_in_smem = with_green <= 160 * 1024;
+    pl.smem = pl.green_in_smem ? with_green : size_t(p.Ns) * 8;
+    return true;
+}
+
+// The whole-run kernel's shape where it applies (1D split with the staged
+// trace and the device solve); NUFI_PERSISTENT=0 turns it off.
+PersistentRun plan_persistent(const Problem &p, const StagedShape &staged, const SolvePlan &plan, bool solve_ok,
+                              int sms)
+{
+    if (!(solve_ok && staged.ok)) return PersistentRun{};
+    const char *env = std::getenv("NUFI_PERSISTENT");
+    if (env && env[0] == '0') return PersistentRun{};
+    return persistent_shape_1d(p, staged, plan, sms);
+}
+
 // The field solve's circulant kernels (see field_solve.cu): for every mode
 // k the diagonal D(k) of Poisson (1 / (N |k|^2)) and of Poisson followed by
 // the collocation solve (divided by the symbol lambda(k)), then the inverse
@@ -297,10 +347,7 @@ int build_solve_plan(nufi_handle *h, int sms)
     const Problem &p = h->p;
     h->solve_ok = false;
     const long long Ns = p.Ns;
-    if (Ns > 16384) {
-        h->solve_why = "device field solve holds at most 16384 grid nodes";
-        return NUFI_OK;
-    }
+    if (!solve_geometry(p, sms, h->plan, h->solve_why)) return NUFI_OK;
     using cld = std::complex<long double>;
     const long double two_pi = 6.283185307179586476925286766559005768L;
     double Nb[kMaxOrder] = {0};
@@ -325,7 +372,7 @@ int build_solve_plan(nufi_handle *h, int sms)
         }
     }
     const bool split1d = p.precision == NUFI_PREC_FP32_SPLIT && p.dim == 1;
-    const int nconv = split1d ? 5 : 2;
+    const int nconv = h->plan.nconv;  // 5 for split1d, else 2
     std::vector<cld> D((size_t)nconv * Ns, cld(0, 0));
     long double lmax = 0;
     for (long long s = 0; s < Ns; ++s) {
@@ -393,15 +440,6 @@ int build_solve_plan(nufi_handle *h, int sms)
     std::vector<double> green((size_t)nconv * Ns);
     for (size_t i = 0; i < green.size(); ++i) green[i] = double(D[i].real());
     SolvePlan &pl = h->plan;
-    pl.nconv = nconv;
-    // nodes per block: enough blocks to cover the SMs, up to 8 warps per node
-    int npb = 8;
-    while (npb > 1 && (Ns + npb - 1) / npb < sms) npb /= 2;
-    pl.nodes_per_block = npb;
-    pl.blocks = int((Ns + npb - 1) / npb);
-    const size_t with_green = size_t(Ns) * 8 * (1 + nconv);
-    pl.green_in_smem = with_green <= 160 * 1024;
-    pl.smem = pl.green_in_smem ? with_green : size_t(Ns) * 8;
     NUFI_CUDA(h, dalloc(h, &pl.green, green.size()));
     // also holds one part per CTA of the persistent run kernel
     NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(std::max(pl.blocks, kMaxCtasPerSm * sms))));
@@ -588,19 +626,8 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     DeviceGuard g(device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    h->shape = choose_shape(h->p, sms > 0 ? sms : 1);
+    plan_traces(h->p, sms > 0 ? sms : 1, h->shape, h->staged);
     const Problem &p = h->p;
-    if (p.precision == NUFI_PREC_FP32_SPLIT && p.dim > 1) {
-        h->staged = staged_shape_nd(p, sms > 0 ? sms : 1);
-        const char *staged = std::getenv("NUFI_SPLIT_STAGED");
-        if (staged && staged[0] == '0') {  // tables read from global memory
-            h->staged.ring = 0;
-            h->staged.smem = 0;
-        }
-    } else if (p.precision == NUFI_PREC_FP32_SPLIT && !p.split_plain_kick) {
-        const char *staged = std::getenv("NUFI_SPLIT_STAGED");
-        if (!(staged && staged[0] == '0')) h->staged = staged_shape_1d(p, sms > 0 ? sms : 1);
-    }
     const size_t partial_rows = size_t(std::max(h->shape.vblocks, h->staged.ok ? h->staged.ctas : 0));
     auto bail = [&](int code) {
         g_last_error = h->last_error;
@@ -638,15 +665,10 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     h->slab_set.assign(nslab, 0);
     h->energy_set.assign(nslab, 0);
     h->aplan = adjoint_plan_1d(p);
-    if (h->solve_ok && h->staged.ok) {
-        const char *pers = std::getenv("NUFI_PERSISTENT");
-        if (!(pers && pers[0] == '0')) {
-            h->persist = persistent_shape_1d(p, h->staged, h->plan, sms > 0 ? sms : 1);
-            if (h->persist.ok && ((e = dalloc(h.get(), &h->persist.sync, 2)) != cudaSuccess ||
-                                  (e = dalloc(h.get(), &h->persist.epart, nslab * size_t(p.N[0]))) != cudaSuccess))
-                return bail(cuda_fail(h.get(), e, "cudaMalloc"));
-        }
-    }
+    h->persist = plan_persistent(p, h->staged, h->plan, h->solve_ok, sms > 0 ? sms : 1);
+    if (h->persist.ok && ((e = dalloc(h.get(), &h->persist.sync, 2)) != cudaSuccess ||
+                          (e = dalloc(h.get(), &h->persist.epart, nslab * size_t(p.N[0]))) != cudaSuccess))
+        return bail(cuda_fail(h.get(), e, "cudaMalloc"));
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(cuda_fail(h.get(), e, "nufi_create"));
     *out = h.release();
     return NUFI_OK;
@@ -1103,9 +1125,14 @@ int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs)
     return NUFI_OK;
 }
 
-int nufi_describe(const nufi_handle *h, char *buf, size_t len)
+}  // extern "C"
+
+namespace {
+
+// The launch plan of a handle as JSON (nufi_describe); with `layout`, also
+// the device layout and the adjoint's grid (nufi_plan).
+std::string plan_json(const nufi_handle *h, bool layout)
 {
-    if (!h || !buf || len == 0) return fail(nullptr, NUFI_ERR_INVALID, "null argument");
     const Problem &p = h->p;
     char tmp[1024];
     const char *trace = p.precision == NUFI_PREC_FP64 ? "trace_fp64_kernel"
@@ -1124,9 +1151,58 @@ int nufi_describe(const nufi_handle *h, char *buf, size_t len)
         h->persist.ok ? "run_split_1d_kernel" : "graph of per-step launches", int(h->persist.ok), h->persist.ctas,
         h->persist.threads, h->persist.ppt, h->persist.smem, int(h->solve_ok), h->plan.nconv, h->plan.blocks,
         h->plan.nodes_per_block);
-    if (k < 0) return fail(nullptr, NUFI_ERR_INVALID, "describe");
-    std::snprintf(buf, len, "%s", tmp);
-    return size_t(k) < len ? NUFI_OK : fail(nullptr, NUFI_ERR_RANGE, "describe: buffer too small");
+    if (k < 0 || size_t(k) >= sizeof(tmp)) return std::string();
+    std::string s(tmp);
+    if (layout) {
+        k = std::snprintf(
+            tmp, sizeof(tmp),
+            ", \"layout\": {\"Ns\": %lld, \"Nm\": %lld, \"Nq\": %lld, \"stride_t\": %lld, \"hist_stride\": %lld, "
+            "\"table_stride\": %lld, \"table_sx\": %d, \"row_step\": %d, \"partial_rows\": %d}, "
+            "\"staged_tpn\": %d, \"solve_smem\": %zu, \"solve_why\": \"%s\", "
+            "\"adjoint\": {\"ok\": %d, \"threads\": %d, \"grid_x\": %d, \"grid_y\": %d, \"chunk\": %d}}",
+            p.Ns, p.Nm, p.Nq, p.stride_t, p.hist_stride, p.table_stride, p.table_sx, p.row_step,
+            std::max(h->shape.vblocks, h->staged.ok ? h->staged.ctas : 0), h->staged.tpn, h->plan.smem,
+            h->solve_ok ? "" : h->solve_why.c_str(), int(h->aplan.ok), h->aplan.threads, h->aplan.grid_x,
+            h->aplan.grid_y, h->aplan.chunk);
+        if (k < 0 || size_t(k) >= sizeof(tmp)) return std::string();
+        s.pop_back();  // the closing brace
+        s += tmp;
+    }
+    return s;
+}
+
+int copy_out(const std::string &s, char *buf, size_t len, const char *who)
+{
+    if (s.empty()) return fail(nullptr, NUFI_ERR_INVALID, who);
+    std::snprintf(buf, len, "%s", s.c_str());
+    return s.size() < len ? NUFI_OK : fail(nullptr, NUFI_ERR_RANGE, std::string(who) + ": buffer too small");
+}
+
+}  // namespace
+
+extern "C" {
+
+int nufi_describe(const nufi_handle *h, char *buf, size_t len)
+{
+    if (!h || !buf || len == 0) return fail(nullptr, NUFI_ERR_INVALID, "null argument");
+    return copy_out(plan_json(h, false), buf, len, "describe");
+}
+
+int nufi_plan(const nufi_config *cfg, int sms, char *buf, size_t len)
+{
+    if (!buf || len == 0) return fail(nullptr, NUFI_ERR_INVALID, "nufi_plan: null argument");
+    if (sms < 1 || sms > 4096) return fail(nullptr, NUFI_ERR_INVALID, "nufi_plan: sms outside [1, 4096]");
+    std::string why;
+    const int st = validate(cfg, why);
+    if (st) return fail(nullptr, st, "nufi_plan: " + why);
+    nufi_handle h;  // planning only: no stream, no device memory
+    h.cfg = *cfg;
+    h.p = make_problem(*cfg);
+    plan_traces(h.p, sms, h.shape, h.staged);
+    h.solve_ok = solve_geometry(h.p, sms, h.plan, h.solve_why);
+    h.persist = plan_persistent(h.p, h.staged, h.plan, h.solve_ok, sms);
+    h.aplan = adjoint_plan_1d(h.p);
+    return copy_out(plan_json(&h, true), buf, len, "nufi_plan");
 }
 
 }  // extern "C"

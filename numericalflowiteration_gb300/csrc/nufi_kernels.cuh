@@ -192,8 +192,8 @@ cudaError_t launch_adjoint_1d(const Problem &p, const AdjointPlan &ap, const dou
 
 // Batched 1D instances (batch_1d.cu).  One descriptor per instance; the
 // unit, node and solve-block maps give each CTA its instance.
-constexpr int kBatchMaxN = 256;
-constexpr int kRingSlots = 3;  // shared-memory ring slots of the split traces  // spatial nodes per instance (256 % N == 0)
+constexpr int kBatchMaxN = 256;  // spatial nodes per instance (256 % N == 0)
+constexpr int kRingSlots = 3;    // shared-memory ring slots of the split traces
 struct BatchInst {
     Problem p;
     double *hist;

@@ -274,6 +274,19 @@ int nufi_describe(const nufi_handle *h, char *buf, size_t len);
  * capacity planning; configuration errors as nufi_create's, via
  * nufi_last_error(NULL). */
 int nufi_plan(const nufi_config *cfg, int sms, char *buf, size_t len);
+/* No counterpart in the reference: the field solve's circulant kernels for
+ * cfg, computed on the host with no CUDA call (what nufi_create uploads).
+ * Row r of nconv rows of Ns values (x fastest) is G_r; with
+ * rho' = rho - mean(rho) the solve is out_r[i] = sum_j G_r[i - j] rho'_j
+ * (index differences per axis, periodic):
+ *   r = 0: spline coefficients c (unpadded; the slab pads periodically),
+ *   r = 1: the potential phi at the nodes (W = prod L / (2 Ns) sum rho' phi),
+ *   r = 2, 3, 4 (1D FP32-split only): K A, K B, K C of the per-cell
+ *          quadratic of the kick, K = -dt^2 / dx^2.
+ * *nconv receives the row count; kernels == NULL queries only.
+ * NUFI_ERR_RANGE if len < nconv * Ns, NUFI_ERR_UNSUPPORTED above 16384
+ * nodes. */
+int nufi_solve_kernels(const nufi_config *cfg, double *kernels, int64_t len, int32_t *nconv);
 
 #ifdef __cplusplus
 }

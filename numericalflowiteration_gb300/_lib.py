@@ -41,6 +41,7 @@ SIGNATURES = {
     "nufi_compute_metrics": (ctypes.c_int, [_P, _I64, _I64, _I64]),
     "nufi_describe": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "nufi_plan": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
+    "nufi_solve_kernels": (ctypes.c_int, [_P, _P, _I64, _P]),
     "nufi_forward": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_eval_points": (ctypes.c_int, [_P, _I64, ctypes.c_int, _I64, _P, _P, _P]),
     "nufi_save_history": (ctypes.c_int, [_P, _I64, ctypes.c_char_p]),
@@ -118,6 +119,21 @@ def plan(cfg, sms: int = 152) -> dict:
     if st:
         _raise(st, lib.nufi_last_error(None).decode())
     return json.loads(buf.value.decode())
+
+
+def solve_kernels(cfg) -> np.ndarray:
+    """The field solve's circulant kernels for cfg (nufi_solve_kernels), as
+    an (nconv, Ns) array, computed on the host."""
+    lib = load()
+    c = cfg.to_c()
+    n = ctypes.c_int32()
+    st = lib.nufi_solve_kernels(ctypes.byref(c), None, 0, ctypes.byref(n))
+    if st == 0:
+        out = np.zeros((n.value, cfg.n_spatial))
+        st = lib.nufi_solve_kernels(ctypes.byref(c), _ptr(out), out.size, ctypes.byref(n))
+    if st:
+        _raise(st, lib.nufi_last_error(None).decode())
+    return out
 
 
 class Simulation:

@@ -342,12 +342,9 @@ PersistentRun plan_persistent(const Problem &p, const StagedShape &staged, const
 // i.e. drops that mode: the same pseudo-inverse here.  In 1D split mode
 // three more kernels give K (A, B, C) of the per-cell quadratic directly
 // (shifts of c are phase factors of its diagonal).
-int build_solve_plan(nufi_handle *h, int sms)
+std::vector<double> solve_green(const Problem &p, int nconv)
 {
-    const Problem &p = h->p;
-    h->solve_ok = false;
     const long long Ns = p.Ns;
-    if (!solve_geometry(p, sms, h->plan, h->solve_why)) return NUFI_OK;
     using cld = std::complex<long double>;
     const long double two_pi = 6.283185307179586476925286766559005768L;
     double Nb[kMaxOrder] = {0};
@@ -371,8 +368,7 @@ int build_solve_plan(nufi_handle *h, int sms)
             ks[a][k] = kk * kk;
         }
     }
-    const bool split1d = p.precision == NUFI_PREC_FP32_SPLIT && p.dim == 1;
-    const int nconv = h->plan.nconv;  // 5 for split1d, else 2
+    const bool split1d = nconv == 5;  // 1D split: K A, K B, K C follow c and phi
     std::vector<cld> D((size_t)nconv * Ns, cld(0, 0));
     long double lmax = 0;
     for (long long s = 0; s < Ns; ++s) {
@@ -439,6 +435,15 @@ int build_solve_plan(nufi_handle *h, int sms)
     }
     std::vector<double> green((size_t)nconv * Ns);
     for (size_t i = 0; i < green.size(); ++i) green[i] = double(D[i].real());
+    return green;
+}
+
+int build_solve_plan(nufi_handle *h, int sms)
+{
+    const Problem &p = h->p;
+    h->solve_ok = false;
+    if (!solve_geometry(p, sms, h->plan, h->solve_why)) return NUFI_OK;
+    const std::vector<double> green = solve_green(p, h->plan.nconv);
     SolvePlan &pl = h->plan;
     NUFI_CUDA(h, dalloc(h, &pl.green, green.size()));
     // also holds one part per CTA of the persistent run kernel
@@ -1203,6 +1208,23 @@ int nufi_plan(const nufi_config *cfg, int sms, char *buf, size_t len)
     h.persist = plan_persistent(h.p, h.staged, h.plan, h.solve_ok, sms);
     h.aplan = adjoint_plan_1d(h.p);
     return copy_out(plan_json(&h, true), buf, len, "nufi_plan");
+}
+
+int nufi_solve_kernels(const nufi_config *cfg, double *kernels, int64_t len, int32_t *nconv)
+{
+    std::string why;
+    int st = validate(cfg, why);
+    if (st) return fail(nullptr, st, "nufi_solve_kernels: " + why);
+    const Problem p = make_problem(*cfg);
+    SolvePlan geom;
+    if (!solve_geometry(p, 1, geom, why)) return fail(nullptr, NUFI_ERR_UNSUPPORTED, "nufi_solve_kernels: " + why);
+    if (nconv) *nconv = geom.nconv;
+    if (!kernels) return NUFI_OK;  // size query
+    if (len < geom.nconv * p.Ns)
+        return fail(nullptr, NUFI_ERR_RANGE, "nufi_solve_kernels: len below nconv * Ns");
+    const std::vector<double> g = solve_green(p, geom.nconv);
+    std::memcpy(kernels, g.data(), g.size() * sizeof(double));
+    return NUFI_OK;
 }
 
 }  // extern "C"

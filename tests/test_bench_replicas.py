@@ -1,6 +1,7 @@
 """bench.py's multi-GPU path runs independent replicas (the path is not
 sharded across GPUs): the slowest rank's time and the whole-job rate,
-checked here with two gloo ranks on the CPU."""
+checked here with two gloo ranks on the CPU.  Also the reference arm's
+JSON line, which runs on the host cores only."""
 import os
 import socket
 import sys
@@ -47,3 +48,32 @@ def test_single_rank_needs_no_process_group():
     import bench
     ms, value = bench.aggregate_replicas(total_ms=50.0, steps=5, point_steps=1000, ws=1)
     assert ms == 10.0 and value == pytest.approx(1000 / 10e-3)
+
+
+def _bench(args, env_extra=None):
+    import json
+    import subprocess
+    env = dict(os.environ, **(env_extra or {}))
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), *args], cwd=ROOT, env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    return [json.loads(ln) for ln in lines]
+
+
+def test_reference_arm_line():
+    """bench.py --impl reference (the oracle port on the host cores, a
+    bounded sample per step) prints one line with the contract's keys and a
+    zero-copy e2e; under a multi-rank launch only rank 0 prints."""
+    (line,) = _bench(["--impl", "reference", "--steps", "1", "--warmup", "3", "--ref-steps", "2"])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["steps"] == 1 and line["warmup"] == 3
+    assert line["value"] > 0 and line["higher_is_better"] is True
+    assert line["config"]["workload"] == "two_stream_1d_256x1024_T50"
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert _bench(["--impl", "reference", "--steps", "1", "--warmup", "3", "--ref-steps", "2"],
+                  {"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []

@@ -52,35 +52,43 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks + throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks + throttle reasons, sampled every `interval_ms`;
+    each line is stamped on arrival, and stop(t0, t1) keeps the samples
+    inside the timed window [t0, t1] (time.monotonic())."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
     NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int, interval_ms: int = 50):
         self.gpu = gpu
+        self.interval_ms = interval_ms
         self.proc = None
-        self.lines = []
+        self.lines = []  # (arrival time, line)
         self.thread = None
 
-    def start(self):
+    def start(self, ready_timeout: float = 3.0):
+        """Start sampling and wait (at most ready_timeout s) for the first
+        sample, so that sampling covers a timed region started next."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
-                                         stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", str(self.interval_ms), "-i", str(self.gpu)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, FileNotFoundError):
             self.proc = None
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        t_end = time.monotonic() + ready_timeout
+        while not self.lines and time.monotonic() < t_end and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
 
-    def stop(self):
+    def stop(self, t0: float | None = None, t1: float | None = None):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         self.proc.terminate()
@@ -90,8 +98,12 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
+        inside = [ln for t, ln in self.lines if (t0 is None or t >= t0) and (t1 is None or t <= t1)]
+        in_window = bool(inside)
+        if not inside:  # a window shorter than the interval: the samples around it
+            inside = [ln for _, ln in self.lines]
         sm, smax, reasons = [], [], set()
-        for ln in self.lines:
+        for ln in inside:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -104,7 +116,7 @@ class ClockSampler:
                 if val.lower().startswith("active"):
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "in_timed_window": in_window}
 
 
 def aggregate_replicas(total_ms: float, steps: int, point_steps: int, ws: int, device: str = "cuda"):
@@ -227,6 +239,7 @@ def run_ours(args, cfg):
     sampler.start()
     launches0 = sim.launches
     times = []
+    t_start = time.monotonic()
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -239,8 +252,9 @@ def run_ours(args, cfg):
             e1.record()
         e1.synchronize()
         times.append(e0.elapsed_time(e1))
+    t_end = time.monotonic()
     barrier()
-    clocks = sampler.stop()
+    clocks = sampler.stop(t_start, t_end)
     launches = sim.launches - launches0
     ps = cfg.point_steps()
     ms_per_step, value = aggregate_replicas(sum(times), args.steps, ps, ws, device="cuda")

@@ -50,6 +50,53 @@ def test_single_rank_needs_no_process_group():
     assert ms == 10.0 and value == pytest.approx(1000 / 10e-3)
 
 
+FAKE_SMI = """#!{python}
+import sys, time
+# stands in for nvidia-smi --query-gpu=... -lms N: one CSV line per interval
+rows = [("1980", "none"), ("2070", "none"), ("2070", "Active"), ("2070", "none")] * 1000
+ms = int(sys.argv[sys.argv.index("-lms") + 1])
+time.sleep({delay})
+for sm, hw in rows:
+    print(f"0, {{sm}}, 2070, 900.0, 0x0, {{hw}}, Not Active, Not Active, Not Active", flush=True)
+    time.sleep(ms / 1000)
+"""
+
+
+def test_clock_sampler_keeps_the_timed_window(tmp_path, monkeypatch):
+    """Samples are stamped on arrival and only those inside the timed
+    window count; start() waits for the first sample; an Active
+    hw_slowdown is reported by name."""
+    sys.path.insert(0, str(ROOT))
+    import time
+    import bench
+    smi = tmp_path / "nvidia-smi"
+    smi.write_text(FAKE_SMI.format(python=sys.executable, delay=0.3))
+    smi.chmod(0o755)
+    monkeypatch.setenv("PATH", f"{tmp_path}{os.pathsep}{os.environ['PATH']}")
+    s = bench.ClockSampler(0, interval_ms=20)
+    t_call = time.monotonic()
+    s.start()
+    assert s.lines and time.monotonic() - t_call >= 0.25  # waited for the first sample
+    t0 = time.monotonic()
+    time.sleep(0.5)
+    t1 = time.monotonic()
+    time.sleep(0.2)
+    c = s.stop(t0, t1)
+    assert c["in_timed_window"] and 5 <= c["samples"] <= 40
+    assert len(s.lines) > c["samples"]  # the samples after t1 were left out
+    assert c["sm_max_mhz"] == 2070 and c["sm_mhz"] in (1980, 2070)
+    assert c["reasons"] == ["hw_slowdown"]
+
+
+def test_clock_sampler_without_nvidia_smi(tmp_path, monkeypatch):
+    sys.path.insert(0, str(ROOT))
+    import bench
+    monkeypatch.setenv("PATH", str(tmp_path))
+    s = bench.ClockSampler(0)
+    s.start()
+    assert s.stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
 def _bench(args, env_extra=None):
     import json
     import subprocess

@@ -57,6 +57,16 @@ RUN_CASES = {
     "orderhi7_landau_1d_32x64": (landau_1d(Nx=32, Nv=64, Nt=12, order=7), 12, [0, 1, 6, 12], [0, 6, 12]),
     "orderhi8_landau_1d_32x64": (landau_1d(Nx=32, Nv=64, Nt=12, order=8), 12, [0, 1, 6, 12], [0, 6, 12]),
     "orderhi6_landau_2d_8x8": (landau_2d(Nx=8, Nv=8, Nt=10, order=6), 10, [0, 1, 5, 10], [0, 5, 10]),
+    # f0 parameters at the corners of the batched workload's ranges
+    # (alpha in [0.01, 0.05], k in [0.3, 0.5], u_b in [4, 5], sigma_b in
+    # [0.4, 0.6]; the bump-on-tail domain is [0, 2 pi / k)).  The Landau case
+    # keeps [0, 4 pi) with k = 0.3, where cos(kx) is not periodic, so f0 at
+    # the unwrapped foot (nufi/rho.hpp:59-60) matters
+    "params_bump_lo_1d_64x256_n60": (bump_on_tail_1d(Nt=60, alpha=0.05, k=0.3, u_b=4.0, sigma_b=0.4), 60,
+                                     [0, 1, 30, 60], [0, 30, 60]),
+    "params_bump_hi_1d_128x512_n40": (bump_on_tail_1d(Nx=128, Nv=512, Nt=40, alpha=0.01, k=0.5, u_b=5.0,
+                                                      sigma_b=0.6), 40, [0, 1, 20, 40], [0, 20, 40]),
+    "params_landau_k03_1d_64x256_n60": (landau_1d(Nt=60, alpha=0.05, k=0.3), 60, [0, 1, 30, 60], [0, 30, 60]),
 }
 
 # name -> (config, metrics steps): the reference's eval_f metrics of its own

@@ -34,6 +34,9 @@ RUN_CASES_FAST = [
     "orderhi7_landau_1d_32x64",
     "orderhi8_landau_1d_32x64",
     "orderhi6_landau_2d_8x8",
+    "params_bump_lo_1d_64x256_n60",
+    "params_bump_hi_1d_128x512_n40",
+    "params_landau_k03_1d_64x256_n60",
 ]
 
 # Long two-stream run: chaotic after saturation, so agreement is looser

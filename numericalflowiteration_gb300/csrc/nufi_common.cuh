@@ -53,7 +53,9 @@ struct Problem {
                            // what the compensation buys)
 };
 
-__host__ __device__ inline double faculty(int n) { return (n > 1) ? double(n) * faculty(n - 1) : 1.0; }
+// n!, evaluated at compile time where the spline kernels use it (a runtime
+// call would recurse and divide in every spline evaluation)
+__host__ __device__ constexpr double faculty(int n) { return (n > 1) ? double(n) * faculty(n - 1) : 1.0; }
 
 // splines1d::N<real,order,derivative> (nufi/splines.hpp:39-79), restated:
 // all `order` basis values (or their derivative) at reference coordinate x.
@@ -81,7 +83,7 @@ __host__ __device__ __forceinline__ void bspline_basis(real x, real *result)
 #pragma unroll
         for (int i = j + 1; i < ORDER - 1; ++i) v[i] = v[i] - v[i + 1];
     }
-    const real factor = real(1) / real(faculty(ORDER - DERIV - 1));
+    constexpr real factor = real(1) / real(faculty(ORDER - DERIV - 1));
 #pragma unroll
     for (int i = 0; i < ORDER; ++i) result[i] = v[i] * factor;
 }
@@ -108,7 +110,8 @@ __host__ __device__ __forceinline__ real deboor(real x, real *c)
 #pragma unroll
         for (int i = n - d - 1; i >= j; --i)
             c[d + i] = (y - real(d + 1 + i)) * c[d + i] + (i - j + 1 - x) * c[d + i - 1];
-    return (real(1) / real(faculty(ORDER - DERIV - 1))) * c[n - 1];
+    constexpr real factor = real(1) / real(faculty(ORDER - DERIV - 1));
+    return factor * c[n - 1];
 }
 
 // deboor<double, 4, 1> on the window c0..c3 held in registers: the same

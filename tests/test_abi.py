@@ -112,6 +112,25 @@ def test_fp64_velocity_grid_limit(lib):
         assert not msg.startswith("nufi_create:"), msg
 
 
+def test_split_needs_a_periodic_f0_phase(lib):
+    """The FP32-split traces evaluate cos(k x) at the foot wrapped into the
+    domain; the reference (nufi/rho.hpp:59-60) and the FP64 trace at the
+    unwrapped foot.  Split handles whose k (x_max - x_min) is not a multiple
+    of 2 pi on some axis are refused at create; FP64 takes them."""
+    from numericalflowiteration_gb300.config import bump_on_tail_1d, landau_2d, landau_3d
+    for cfg in (landau_1d(k=0.3, precision="fp32split"), two_stream_1d(k=0.45, precision="fp32split"),
+                landau_2d(k=0.25, precision="fp32split"), landau_3d(k=0.75, precision="fp32split")):
+        st, msg = _create_status(lib, cfg.to_c())
+        assert st == _lib.ERR_UNSUPPORTED and "2 pi" in msg, (cfg, msg)
+    for cfg in (landau_1d(k=0.3), landau_1d(k=1.0, precision="fp32split"), landau_2d(k=1.5, precision="fp32split"),
+                bump_on_tail_1d(k=0.37, precision="fp32split"), bump_on_tail_1d(k=0.3, precision="fp32split"),
+                landau_3d(precision="fp32split")):
+        st, msg = _create_status(lib, cfg.to_c())
+        assert not msg.startswith("nufi_create:"), (cfg, msg)
+    with pytest.raises(NotImplementedError):
+        nufi.Simulation(landau_1d(k=0.3, precision="fp32split"))
+
+
 def test_noalloc_rejects_bad_strides_before_cuda(lib):
     """nufi_compute_rho_noalloc checks the caller's history stride (at least
     one slab; history within 2^50 bytes) and the step before any CUDA call.

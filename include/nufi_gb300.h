@@ -57,7 +57,11 @@ extern "C" {
 /* FP32 split: position = integer cell + FP32 fraction, velocity = exact
  * grid velocity + FP32 kick sum, field tables in FP32, f0 evaluated as a
  * perturbation of its value at the grid velocity; FP64 only in the rho
- * accumulator, the Poisson solve and the spline interpolation solve.       */
+ * accumulator, the Poisson solve and the spline interpolation solve.
+ * f0's phase comes from the cell the foot lands in (the foot wrapped into
+ * the domain), so k (x_max - x_min) must be a multiple of 2 pi on every
+ * axis (NUFI_ERR_UNSUPPORTED otherwise; FP64 evaluates f0 at the unwrapped
+ * foot, as the reference, for any k).                                       */
 #define NUFI_PREC_FP32_SPLIT  1
 
 /* ---- initial conditions (f0) ------------------------------------------- */

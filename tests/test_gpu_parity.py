@@ -56,7 +56,9 @@ def test_fp64_stepwise_rho_energy_slabs(nufi, name):
 
 @pytest.mark.parametrize("name", ["landau_1d_64x256_T30", "bump_on_tail_1d_64x256_T20",
                                   "two_stream_1d_256x1024_n40", "landau_2d_16x16_T20", "landau_3d_8x8_T2",
-                                  "landau_2d_32x64_n20", "landau_3d_16x32_n3"])
+                                  "landau_2d_32x64_n20", "landau_3d_16x32_n3",
+                                  "params_bump_lo_1d_64x256_n60", "params_bump_hi_1d_128x512_n40",
+                                  "params_landau_k03_1d_64x256_n60"])
 def test_fp64_graph_run_matches_reference(nufi, name):
     cfg, g = golden(name)
     n_last = int(g["n_last"])

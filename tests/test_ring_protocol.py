@@ -1,6 +1,7 @@
-"""(CPU) A model of the shared-memory ring of the whole-run kernel
+"""(CPU) Models of the shared-memory rings of the whole-run kernel
 (numericalflowiteration_gb300/csrc/run_split_1d.cu: issue, copy_part,
-start_step, refill), run under random interleavings of the CTA's warps.
+start_step, refill) and of the 2D/3D split trace (simulate_nd), run under
+random interleavings of the CTA's warps.
 
 The ring is one stream of chunks over the run: chunk g sits in slot
 g % R; chunk j of step n holds slabs [max(0, k_hi - S + 1), k_hi],
@@ -119,7 +120,66 @@ def test_ring_protocol_holds(S):
                 assert total == sum((n + S - 1) // S for n in range(max(n0, 1), n1 + 1))
 
 
+def simulate_nd(n, batches, S, W, seed, no_wrap=False):
+    """The per-step ring of the 2D/3D split trace
+    (numericalflowiteration_gb300/csrc/trace_split_nd.cu): a stream of
+    batches x nchunks chunks, chunk g = chunk g mod nchunks of batch
+    g / nchunks in slot g mod R; the first R issued up front, then the last
+    warp to release a slot issues chunk g + R, i.e. chunk (j + R) mod
+    nchunks, while g + R < total.  Each warp waits for chunk g on its slot
+    with phase parity (g / R) & 1; checked: the slot then holds chunk g
+    (so the parity is unambiguous) with the slabs of chunk g mod nchunks."""
+    rnd = random.Random(seed)
+    nchunks = (n + S - 1) // S if n > 0 else 0
+    total = batches * nchunks
+    holds = {}   # slot -> (g, j) of the chunk it holds
+    issued = []
+    released = [0] * R
+
+    def issue(g, j):
+        s = g % R
+        check(s not in holds, "slot re-armed while in use", g, holds)
+        holds[s] = (g, j)
+        issued.append(g)
+
+    for g0 in range(min(R, total)):
+        issue(g0, g0 % nchunks)
+    pos = [0] * W
+    while any(p < total for p in pos):
+        ready = [w for w in range(W) if pos[w] < total and holds.get(pos[w] % R, (None,))[0] == pos[w]]
+        check(ready, "deadlock", pos, holds)
+        w = rnd.choice(ready)
+        g = pos[w]
+        j = g % nchunks
+        check(holds[g % R] == (g, j), "slot holds another chunk", g, holds[g % R])
+        pos[w] += 1
+        s = g % R
+        released[s] += 1
+        if released[s] == W:
+            released[s] = 0
+            del holds[s]
+            if g + R < total:
+                jr = j + R
+                if not no_wrap:
+                    while jr >= nchunks:
+                        jr -= nchunks
+                issue(g + R, jr)
+    check(issued == list(range(total)), "stream not issued in order", issued[:10])
+    check(not holds, "slots left armed", holds)
+
+
+@pytest.mark.parametrize("S", [1, 2, 3, 15, 16])
+def test_nd_ring_protocol_holds(S):
+    for n in (0, 1, 2, 5, 17, 40, 100):
+        for batches in (1, 2, 3, 7):
+            for W in (1, 4, 16):
+                for seed in range(2):
+                    simulate_nd(n, batches, S, W, seed)
+
+
 def test_planted_mistakes_are_caught():
+    with pytest.raises(ProtocolError, match="another chunk"):
+        simulate_nd(5, 4, 2, 4, 0, no_wrap=True)
     with pytest.raises(ProtocolError, match="before its step finished"):
         simulate(0, 40, 4, 8, 0, newest_early=True)
     with pytest.raises(ProtocolError):

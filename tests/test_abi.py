@@ -185,6 +185,43 @@ def test_python_errors_map_to_reference_exception_types(lib):
         nufi.Simulation(two_stream_1d(order=3, precision="fp32split"))
 
 
+def test_handle_less_errors_are_per_thread(lib):
+    """nufi_last_error(NULL) keeps each host thread's own message: a
+    second thread's failure does not overwrite the first thread's."""
+    import threading
+    first_done, second_done = threading.Event(), threading.Event()
+    seen = {}
+
+    def first():
+        c = landau_1d().to_c()
+        c.dim = 4
+        seen["st1"] = _create_status_raw(lib, c)
+        first_done.set()
+        second_done.wait(30)
+        seen["msg1"] = lib.nufi_last_error(None).decode()
+
+    def second():
+        first_done.wait(30)
+        c = landau_1d().to_c()
+        c.order = 12
+        seen["st2"] = _create_status_raw(lib, c)
+        seen["msg2"] = lib.nufi_last_error(None).decode()
+        second_done.set()
+
+    threads = [threading.Thread(target=first), threading.Thread(target=second)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(60)
+    assert seen["st1"] == seen["st2"] == _lib.ERR_INVALID
+    assert "dim" in seen["msg1"] and "order" in seen["msg2"], seen
+
+
+def _create_status_raw(lib, cfg_c):
+    h = ctypes.c_void_p()
+    return lib.nufi_create(ctypes.byref(cfg_c), 0, ctypes.byref(h))
+
+
 def test_null_handle_calls_fail_cleanly(lib):
     assert lib.nufi_compute_rho(None, 0, 0, 1) == _lib.ERR_INVALID
     assert lib.nufi_destroy(None) == 0

@@ -98,6 +98,15 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+def _host_buffer(a: np.ndarray, n: int, what: str):
+    """The C ABI takes bare pointers: the array must be contiguous and hold
+    at least n values, or the library would read or write past it."""
+    if not isinstance(a, np.ndarray) or not a.flags.c_contiguous:
+        raise TypeError(f"{what} must be a C-contiguous numpy array")
+    if a.size < n:
+        raise ValueError(f"{what} holds {a.size} values, the call needs {n}")
+
+
 def _raise(code: int, msg: str):
     if code == ERR_RANGE:
         raise IndexError(msg)
@@ -199,6 +208,8 @@ class Simulation:
         pts[i] = (x.., v..); returns f (or None for mode 2) and, if asked,
         the final (x.., v..)."""
         pts = np.ascontiguousarray(pts, dtype=np.float64)
+        if pts.ndim != 2 or pts.shape[1] != 2 * self.cfg.dim:
+            raise ValueError(f"pts must have shape (npts, {2 * self.cfg.dim})")
         npts = pts.shape[0]
         f = np.zeros(npts) if mode != 2 else None
         ft = np.zeros_like(pts) if (feet or mode == 2) else None
@@ -258,6 +269,7 @@ class Simulation:
 
     def download_rho(self, rho: np.ndarray) -> np.ndarray:
         """rho += device rho (the caller zeroes it first, as the reference's drivers do)."""
+        _host_buffer(rho, self.n_spatial, "rho")
         if rho.dtype == np.float64:
             self._check(self._lib.nufi_download_rho(self._h, _ptr(rho)))
         elif rho.dtype == np.float32:
@@ -267,6 +279,9 @@ class Simulation:
         return rho
 
     def upload_phi(self, n: int, coeffs: np.ndarray):
+        """Slab n from the history base `coeffs` (slab n at n * stride_t)."""
+        if 0 <= n <= self.cfg.Nt:  # other n: the library's range error, before any read
+            _host_buffer(coeffs, (n + 1) * self.stride_t, "coeffs")
         if coeffs.dtype == np.float64:
             self._check(self._lib.nufi_upload_phi(self._h, n, _ptr(coeffs)))
         elif coeffs.dtype == np.float32:
@@ -296,6 +311,10 @@ class Simulation:
         n1 = self.cfg.Nt if n1 is None else n1
         if out is None:
             out = np.zeros((self.cfg.Nt + 1) * self.stride_t)
+        if out.dtype != np.float64:
+            raise TypeError("out must be float64")
+        if 0 <= n0 <= n1 <= self.cfg.Nt:  # other ranges: the library's range error, before any write
+            _host_buffer(out, (n1 + 1) * self.stride_t, "out")
         self._check(self._lib.nufi_download_history(self._h, n0, n1, _ptr(out)))
         return out
 
@@ -307,6 +326,7 @@ class Simulation:
 
     def field_solve(self, rho: np.ndarray):
         r = np.ascontiguousarray(rho, dtype=np.float64)
+        _host_buffer(r, self.n_spatial, "rho")
         slab = np.zeros(self.stride_t)
         e = np.zeros(1)
         self._check(self._lib.nufi_field_solve(self._h, _ptr(r), _ptr(slab), _ptr(e)))

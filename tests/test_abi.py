@@ -217,6 +217,35 @@ def test_handle_less_errors_are_per_thread(lib):
     assert "dim" in seen["msg1"] and "order" in seen["msg2"], seen
 
 
+def test_python_mirror_checks_host_buffers():
+    """The C ABI takes bare pointers; the Python mirror refuses host arrays
+    that are too small or not contiguous before calling the library (a
+    stand-in library fails the test if reached)."""
+    class NoLibrary:
+        def __getattr__(self, name):
+            raise AssertionError(f"{name} reached the library")
+
+    cfg = landau_1d(Nx=16, Nv=32, Nt=8)
+    sim = object.__new__(nufi.Simulation)
+    sim.cfg, sim._lib, sim._h = cfg, NoLibrary(), None
+    sim.stride_t, sim.n_spatial, sim.n_points = cfg.stride_t, cfg.n_spatial, cfg.n_points
+    with pytest.raises(ValueError):
+        sim.download_rho(np.zeros(cfg.n_spatial - 1))
+    with pytest.raises(TypeError):
+        sim.download_rho(np.zeros(2 * cfg.n_spatial)[::2])
+    with pytest.raises(ValueError):
+        sim.upload_phi(3, np.zeros(3 * cfg.stride_t))
+    with pytest.raises(ValueError):
+        sim.history(0, 5, out=np.zeros(5 * cfg.stride_t))
+    with pytest.raises(TypeError):
+        sim.history(0, 5, out=np.zeros(6 * cfg.stride_t, dtype=np.float32))
+    with pytest.raises(ValueError):
+        sim.field_solve(np.zeros(cfg.n_spatial - 2))
+    with pytest.raises(ValueError):
+        sim.eval_points(1, np.zeros((10, 3)))
+    sim._h = None  # nothing to destroy
+
+
 def _create_status_raw(lib, cfg_c):
     h = ctypes.c_void_p()
     return lib.nufi_create(ctypes.byref(cfg_c), 0, ctypes.byref(h))

@@ -87,23 +87,36 @@ static int oc_setup(const nufi_config *c, oc_t *o)
 }
 
 /* ---- f0 (nufi_f0.h) ----------------------------------------------------- */
-static double oc_f0(const oc_t *o, const double *x, const double *u)
+static inline __attribute__((always_inline)) double oc_f0_dim(const oc_t *o, int dim, const double *x,
+                                                              const double *u)
 {
     nufi_f0_params f;
     int i;
     f.kind = o->f0_kind;
     for (i = 0; i < 8; ++i) f.p[i] = o->p[i];
-    if (o->dim == 1) return nufi_f0_1d(&f, x[0], u[0]);
-    if (o->dim == 2) return nufi_f0_2d(&f, x[0], x[1], u[0], u[1]);
+    if (dim == 1) return nufi_f0_1d(&f, x[0], u[0]);
+    if (dim == 2) return nufi_f0_2d(&f, x[0], x[1], u[0], u[1]);
     return nufi_f0_3d(&f, x[0], x[1], x[2], u[0], u[1], u[2]);
 }
 
+static double oc_f0(const oc_t *o, const double *x, const double *u) { return oc_f0_dim(o, o->dim, x, u); }
+
 /* ---- B-splines (splines.hpp:33-110) ------------------------------------ */
-static double oc_faculty(int n) { return (n > 1) ? (double)n * oc_faculty(n - 1) : 1.0; }
+/* 1 / k!: the reference's constexpr factor 1 / faculty<real>(order - d - 1)
+ * (splines.hpp:33-37, 76, 108), folded by the compiler here too. */
+static const double oc_inv_fac[OC_MAX_ORDER + 1] = {
+    1.0 / 1.0, 1.0 / 1.0, 1.0 / 2.0, 1.0 / 6.0, 1.0 / 24.0, 1.0 / 120.0, 1.0 / 720.0, 1.0 / 5040.0, 1.0 / 40320.0};
+
+/* The trace's functions are written once with the dimension and the spline
+ * order as parameters and inlined into one copy per (dimension, order)
+ * (oc_trace below), so both are compile-time constants there, as in the
+ * reference's templates; the operations and their order are the same in
+ * every copy. */
+#define OC_INLINE static inline __attribute__((always_inline))
 
 /* splines1d::N<real,order,derivative>: all `order` basis values (or
  * derivatives) at reference coordinate x in [0,1). */
-static void oc_N(int order, int deriv, double x, double *result)
+OC_INLINE void oc_N(int order, int deriv, double x, double *result)
 {
     const int n = order, d = deriv;
     double v[OC_MAX_ORDER];
@@ -125,13 +138,13 @@ static void oc_N(int order, int deriv, double x, double *result)
         for (i = j + 1; i < order - 1; ++i) v[i] = v[i] - v[i + 1];
     }
     {
-        const double factor = 1.0 / oc_faculty(order - deriv - 1);
+        const double factor = oc_inv_fac[order - deriv - 1];
         for (i = 0; i < order; ++i) result[i] = v[i] * factor;
     }
 }
 
 /* splines1d::eval<real,order,derivative> on an already gathered window. */
-static double oc_eval1(int order, int deriv, double x, const double *coef, size_t stride)
+OC_INLINE double oc_eval1(int order, int deriv, double x, const double *coef, size_t stride)
 {
     const int n = order, d = deriv;
     double c[OC_MAX_ORDER];
@@ -144,11 +157,11 @@ static double oc_eval1(int order, int deriv, double x, const double *coef, size_
     for (j = 1; j < n - d; ++j)
         for (i = n - d - 1; i >= j; --i)
             c[d + i] = (x + n - d - 1 - i) * c[d + i] + (i - j + 1 - x) * c[d + i - 1];
-    return (1.0 / oc_faculty(order - deriv - 1)) * c[n - 1];
+    return oc_inv_fac[order - deriv - 1] * c[n - 1];
 }
 
 /* fields.hpp periodic wrap + knot (shared by all dims, per axis). */
-static void oc_locate(const oc_t *o, int a, double x, size_t *knot, double *xi)
+OC_INLINE void oc_locate(const oc_t *o, int a, double x, size_t *knot, double *xi)
 {
     double xk;
     x -= o->xmin[a];
@@ -159,18 +172,17 @@ static void oc_locate(const oc_t *o, int a, double x, size_t *knot, double *xi)
 }
 
 /* dim1::eval<real,order,1> (fields.hpp:36-61) */
-static double oc_eval_1d(const oc_t *o, double x, const double *c, int deriv)
+OC_INLINE double oc_eval_1d(const oc_t *o, int order, double x, const double *c, int deriv)
 {
     size_t ii; double xi, factor = 1; int i;
     oc_locate(o, 0, x, &ii, &xi);
     for (i = 0; i < deriv; ++i) factor *= o->dxinv[0];
-    return factor * oc_eval1(o->order, deriv, xi, c + ii, 1);
+    return factor * oc_eval1(order, deriv, xi, c + ii, 1);
 }
 
 /* dim2::eval<real,order,dx,dy> (fields.hpp:149-184, splines.hpp:117-137) */
-static double oc_eval_2d(const oc_t *o, double x, double y, const double *coeffs, int ddx, int ddy)
+OC_INLINE double oc_eval_2d(const oc_t *o, int order, double x, double y, const double *coeffs, int ddx, int ddy)
 {
-    const int order = o->order;
     size_t ii, jj, i, j;
     double xi, eta, factor = 1, cc[OC_MAX_ORDER], Nb[OC_MAX_ORDER];
     const size_t sy = o->sstride[1];
@@ -190,10 +202,9 @@ static double oc_eval_2d(const oc_t *o, double x, double y, const double *coeffs
 }
 
 /* dim3::eval<real,order,dx,dy,dz> (fields.hpp:308-350, splines.hpp:144-172) */
-static double oc_eval_3d(const oc_t *o, double x, double y, double z, const double *coeffs,
-                         int ddx, int ddy, int ddz)
+OC_INLINE double oc_eval_3d(const oc_t *o, int order, double x, double y, double z, const double *coeffs,
+                            int ddx, int ddy, int ddz)
 {
-    const int order = o->order;
     size_t ii, jj, kk, i, j, k;
     double xi, eta, zeta, factor = 1;
     double czy[OC_MAX_ORDER * OC_MAX_ORDER], cz[OC_MAX_ORDER], Nb[OC_MAX_ORDER];
@@ -222,48 +233,73 @@ static double oc_eval_3d(const oc_t *o, double x, double y, double z, const doub
 
 /* E = -grad phi from one slab, component by component as the reference
  * does (two / three separate eval calls, rho.hpp:213-214, 343-345). */
-static void oc_field(const oc_t *o, const double *x, const double *c, double *E)
+OC_INLINE void oc_field(const oc_t *o, int dim, int order, const double *x, const double *c, double *E)
 {
-    if (o->dim == 1) {
-        E[0] = -oc_eval_1d(o, x[0], c, 1);
-    } else if (o->dim == 2) {
-        E[0] = -oc_eval_2d(o, x[0], x[1], c, 1, 0);
-        E[1] = -oc_eval_2d(o, x[0], x[1], c, 0, 1);
+    if (dim == 1) {
+        E[0] = -oc_eval_1d(o, order, x[0], c, 1);
+    } else if (dim == 2) {
+        E[0] = -oc_eval_2d(o, order, x[0], x[1], c, 1, 0);
+        E[1] = -oc_eval_2d(o, order, x[0], x[1], c, 0, 1);
     } else {
-        E[0] = -oc_eval_3d(o, x[0], x[1], x[2], c, 1, 0, 0);
-        E[1] = -oc_eval_3d(o, x[0], x[1], x[2], c, 0, 1, 0);
-        E[2] = -oc_eval_3d(o, x[0], x[1], x[2], c, 0, 0, 1);
+        E[0] = -oc_eval_3d(o, order, x[0], x[1], x[2], c, 1, 0, 0);
+        E[1] = -oc_eval_3d(o, order, x[0], x[1], x[2], c, 0, 1, 0);
+        E[2] = -oc_eval_3d(o, order, x[0], x[1], x[2], c, 0, 0, 1);
     }
 }
 
 /* eval_ftilda (rho.hpp:31-61 / 191-232 / 318-367) when half_first == 0,
  * eval_f (rho.hpp:63-96 / 234-281 / 369-426) when half_first == 1.
  * x, u are updated in place to the foot of the characteristic. */
-static double oc_trace(const oc_t *o, size_t n, double *x, double *u, const double *coeffs,
-                       int half_first)
+OC_INLINE double oc_trace_k(const oc_t *o, int D, int order, size_t n, double *x, double *u, const double *coeffs,
+                            int half_first)
 {
-    const int D = o->dim;
     const double dt = o->dt;
     double E[3];
     const double *c;
     int a;
-    if (n == 0) return oc_f0(o, x, u);
+    if (n == 0) return oc_f0_dim(o, D, x, u);
     if (half_first) {
         c = coeffs + n * o->stride_t;
-        oc_field(o, x, c, E);
+        oc_field(o, D, order, x, c, E);
         for (a = 0; a < D; ++a) u[a] += 0.5 * dt * E[a];
     }
     while (--n) {
         for (a = 0; a < D; ++a) x[a] = x[a] - dt * u[a];
         c = coeffs + n * o->stride_t;
-        oc_field(o, x, c, E);
+        oc_field(o, D, order, x, c, E);
         for (a = 0; a < D; ++a) u[a] = u[a] + dt * E[a];
     }
     for (a = 0; a < D; ++a) x[a] -= dt * u[a];
     c = coeffs + n * o->stride_t;
-    oc_field(o, x, c, E);
+    oc_field(o, D, order, x, c, E);
     for (a = 0; a < D; ++a) u[a] += 0.5 * dt * E[a];
-    return oc_f0(o, x, u);
+    return oc_f0_dim(o, D, x, u);
+}
+
+/* one copy of the trace per dimension and spline order (oc_setup admits
+ * dim 1..3 and order 2..8) */
+#define OC_TRACE_COPY(D, K)                                                                        \
+    static double oc_trace_##D##_##K(const oc_t *o, size_t n, double *x, double *u, const double *c, \
+                                     int half_first)                                               \
+    {                                                                                              \
+        return oc_trace_k(o, D, K, n, x, u, c, half_first);                                        \
+    }
+#define OC_TRACE_DIM(D) \
+    OC_TRACE_COPY(D, 2) OC_TRACE_COPY(D, 3) OC_TRACE_COPY(D, 4) OC_TRACE_COPY(D, 5) OC_TRACE_COPY(D, 6) \
+    OC_TRACE_COPY(D, 7) OC_TRACE_COPY(D, 8)
+OC_TRACE_DIM(1)
+OC_TRACE_DIM(2)
+OC_TRACE_DIM(3)
+
+typedef double (*oc_trace_fn)(const oc_t *, size_t, double *, double *, const double *, int);
+static const oc_trace_fn oc_trace_copies[3][7] = {
+    {oc_trace_1_2, oc_trace_1_3, oc_trace_1_4, oc_trace_1_5, oc_trace_1_6, oc_trace_1_7, oc_trace_1_8},
+    {oc_trace_2_2, oc_trace_2_3, oc_trace_2_4, oc_trace_2_5, oc_trace_2_6, oc_trace_2_7, oc_trace_2_8},
+    {oc_trace_3_2, oc_trace_3_3, oc_trace_3_4, oc_trace_3_5, oc_trace_3_6, oc_trace_3_7, oc_trace_3_8}};
+
+static double oc_trace(const oc_t *o, size_t n, double *x, double *u, const double *coeffs, int half_first)
+{
+    return oc_trace_copies[o->dim - 1][o->order - 2](o, n, x, u, coeffs, half_first);
 }
 
 /* Point coordinates by the GPU kernels' convention (cuda_kernel.cu:43-44,
@@ -372,26 +408,37 @@ int oracle_metrics(const nufi_config *cfg, int64_t n, const double *coeffs, int6
         return NUFI_ERR_RANGE;
     {
         double w = oc_weight_v(&o);
+        /* per-node sums in q order, then over the nodes in order: the same
+         * result for any thread count or schedule */
+        double *part = (double *)malloc(sizeof(double) * 4 * o.Ns);
         int a;
+        if (!part) return NUFI_ERR_INVALID;
         if (o.dim < 3 || weight3d_full)
             for (a = 0; a < o.dim; ++a) w *= o.dx[a];
         (void)nthreads;
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : m0, m1, m2, m3) num_threads(nthreads > 0 ? nthreads : 1)
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
         for (s = 0; s < (long long)o.Ns; ++s) {
             size_t m;
+            double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
             for (m = 0; m < o.Nm; ++m) {
                 const int64_t q = (int64_t)((size_t)s * o.Nm + m);
                 double x[3], u[3], u0[3], f, uu = 0;
+                int b;
                 if (q < q_begin || q >= q_end) continue;
                 oc_point(&o, (size_t)s, m, x, u);
-                for (a = 0; a < o.dim; ++a) { u0[a] = u[a]; uu += u0[a] * u0[a]; }
+                for (b = 0; b < o.dim; ++b) { u0[b] = u[b]; uu += u0[b] * u0[b]; }
                 f = oc_trace(&o, (size_t)n, x, u, coeffs, 1);
-                m0 += w * f;
-                m1 += w * f * f;
-                m2 += w * (uu * f / 2);
-                m3 += (f > 0) ? -w * f * log(f) : 0;
+                p0 += w * f;
+                p1 += w * f * f;
+                p2 += w * (uu * f / 2);
+                p3 += (f > 0) ? -w * f * log(f) : 0;
             }
+            part[4 * s] = p0; part[4 * s + 1] = p1; part[4 * s + 2] = p2; part[4 * s + 3] = p3;
         }
+        for (s = 0; s < (long long)o.Ns; ++s) {
+            m0 += part[4 * s]; m1 += part[4 * s + 1]; m2 += part[4 * s + 2]; m3 += part[4 * s + 3];
+        }
+        free(part);
     }
     metrics[0] = m0; metrics[1] = m1; metrics[2] = m2; metrics[3] = m3;
     return NUFI_OK;
@@ -403,9 +450,9 @@ int oracle_metrics(const nufi_config *cfg, int64_t n, const double *coeffs, int6
  * sums are formed in long double: with rho ~ -1 + O(alpha) the non-zero
  * modes are small differences of O(1) terms, and the oracle should sit
  * closer to the exact transform than any FP64 FFT. */
-static long double oc_cas(size_t j, size_t k, size_t N)
+static long double oc_cas(size_t r, size_t N)
 {
-    const long double a = 6.283185307179586476925286766559005768L * (long double)((j * k) % N) / (long double)N;
+    const long double a = 6.283185307179586476925286766559005768L * (long double)r / (long double)N;
     return cosl(a) + sinl(a);
 }
 
@@ -418,11 +465,15 @@ static void oc_dht(const oc_t *o, double *data)
         const size_t N = o->N[a];
         size_t stride = 1, b, lines, l, j, k;
         long double *cas_t = (long double *)malloc(sizeof(long double) * N * N);
+        long double *cas_r = (long double *)malloc(sizeof(long double) * N);
         double *tmp = (double *)malloc(sizeof(double) * N);
         for (b = 0; b < (size_t)a; ++b) stride *= o->N[b];
         lines = total / N;
+        /* cas(2 pi j k / N) takes N distinct values, one per (j k) mod N */
+        for (j = 0; j < N; ++j) cas_r[j] = oc_cas(j, N);
         for (j = 0; j < N; ++j)
-            for (k = 0; k < N; ++k) cas_t[j * N + k] = oc_cas(j, k, N);
+            for (k = 0; k < N; ++k) cas_t[j * N + k] = cas_r[(j * k) % N];
+        free(cas_r);
         for (l = 0; l < lines; ++l) {
             const size_t lo = l % stride, hi = l / stride;
             double *line = data + hi * stride * N + lo;
@@ -623,9 +674,9 @@ int oracle_eval_field(const nufi_config *cfg, const double *slab, int64_t npts, 
     if (st) return st;
     for (i = 0; i < npts; ++i) {
         const double *x = pts + i * o.dim;
-        if (o.dim == 1) out[i] = oc_eval_1d(&o, x[0], slab, deriv[0]);
-        else if (o.dim == 2) out[i] = oc_eval_2d(&o, x[0], x[1], slab, deriv[0], deriv[1]);
-        else out[i] = oc_eval_3d(&o, x[0], x[1], x[2], slab, deriv[0], deriv[1], deriv[2]);
+        if (o.dim == 1) out[i] = oc_eval_1d(&o, o.order, x[0], slab, deriv[0]);
+        else if (o.dim == 2) out[i] = oc_eval_2d(&o, o.order, x[0], x[1], slab, deriv[0], deriv[1]);
+        else out[i] = oc_eval_3d(&o, o.order, x[0], x[1], x[2], slab, deriv[0], deriv[1], deriv[2]);
     }
     return NUFI_OK;
 }

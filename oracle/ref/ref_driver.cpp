@@ -28,6 +28,8 @@
 //       summed in order; writes <out>.metrics (4 doubles).
 //   ref_driver poisson_kat        bin/test_poisson.cpp's analytic check
 //   ref_driver fields_kat         bin/test_fields.cpp's checks at nodes
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -412,6 +414,31 @@ int cmd_metrics(int argc, char **argv)
     return 0;
 }
 
+// rho of step n from a given history, `reps` times: writes rho and prints
+// the best wall time in seconds (the trace alone, for timing the
+// reference's own CPU trace beside the oracle's on the same cores).
+int cmd_rho(int argc, char **argv)
+{
+    if (argc < 7) return 2;
+    nufi_config k;
+    if (!read_file(argv[2], &k, sizeof(k))) return 2;
+    g_f0.kind = k.f0_kind;
+    for (int i = 0; i < 8; ++i) g_f0.p[i] = k.f0_params[i];
+    std::vector<double> coeffs((k.Nt + 1) * slab_size(k)), rho(spatial_size(k));
+    if (!read_file(argv[3], coeffs.data(), sizeof(double) * coeffs.size())) return 2;
+    const size_t n = std::strtoull(argv[4], nullptr, 10);
+    const int reps = std::atoi(argv[6]);
+    double best = 1e300;
+    for (int r = 0; r < reps; ++r) {
+        const auto t0 = std::chrono::steady_clock::now();
+        rho_any(k, n, coeffs.data(), rho.data());
+        best = std::min(best, std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+    }
+    write_file(std::string(argv[5]) + ".rho", rho.data(), sizeof(double) * rho.size());
+    std::printf("%.9f\n", best);
+    return 0;
+}
+
 // bin/test_poisson.cpp:36-119: rho = cos2z + sin8y + cos42x on 128x64x32.
 template <typename real>
 double poisson_kat()
@@ -478,7 +505,7 @@ double fields_kat_2d()
 int main(int argc, char **argv)
 {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: ref_driver run|solve|poisson_kat|fields_kat ...\n");
+        std::fprintf(stderr, "usage: ref_driver run|solve|metrics|rho|poisson_kat|fields_kat ...\n");
         return 2;
     }
     if (const char *m = std::getenv("NUFI_REF_SUMMATION")) g_sum_mode = std::atoi(m);
@@ -486,6 +513,7 @@ int main(int argc, char **argv)
     if (cmd == "run") return cmd_run(argc, argv);
     if (cmd == "solve") return cmd_solve(argc, argv);
     if (cmd == "metrics") return cmd_metrics(argc, argv);
+    if (cmd == "rho") return cmd_rho(argc, argv);
     if (cmd == "poisson_kat") {
         std::printf("{\"float\": %.17g, \"double\": %.17g}\n", poisson_kat<float>(), poisson_kat<double>());
         return 0;

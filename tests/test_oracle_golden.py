@@ -172,6 +172,41 @@ def test_oracle_initial_energy_known_answer(case, oracle_mod):
     assert abs(energy[0] - expect) <= tol * expect, (energy[0], expect)
 
 
+def _ref_driver():
+    from conftest import ROOT
+    drv = ROOT / "oracle" / "_ref" / "ref_driver"
+    if not drv.exists():
+        pytest.skip("no reference build in oracle/_ref")
+    return drv
+
+
+@pytest.mark.parametrize("dim,order", [(1, o) for o in range(3, 9)] + [(2, o) for o in (3, 4, 5, 6)] +
+                         [(3, o) for o in (3, 4, 5)])
+def test_oracle_rho_bit_identical_to_reference_build(dim, order, oracle_mod, tmp_path):
+    """rho of the oracle and of the reference's own eval_ftilda (its headers
+    compiled by oracle/ref/Makefile, `ref_driver rho`) on the same seeded
+    random history, every spline order each dimension takes: equal to the
+    last bit (the same operations in the same order, -ffp-contract=off)."""
+    import subprocess
+    from numericalflowiteration_gb300.config import landau_1d, landau_2d, landau_3d
+    drv = _ref_driver()
+    cfg = {1: lambda: landau_1d(Nx=32, Nv=64, Nt=9, order=order),
+           2: lambda: landau_2d(Nx=8, Nv=8, Nt=5, order=order),
+           3: lambda: landau_3d(Nx=4, Nv=4, Nt=4, order=order)}[dim]()
+    rng = np.random.default_rng(100 + 10 * dim + order)
+    hist = 1e-2 * rng.standard_normal((cfg.Nt + 1) * cfg.stride_t)
+    p = tmp_path / "c"
+    p.with_suffix(".cfg").write_bytes(cfg.to_bytes())
+    hist.tofile(str(p) + ".hist")
+    oracle_mod.set_summation(0)
+    for n in (1, cfg.Nt):
+        subprocess.run([str(drv), "rho", str(p.with_suffix(".cfg")), str(p) + ".hist", str(n), str(p), "1"],
+                       check=True, capture_output=True)
+        ref = np.fromfile(str(p) + ".rho")
+        got = oracle_mod.rho(cfg, n, hist)
+        assert np.array_equal(got, ref), (n, float(np.max(np.abs(got - ref))))
+
+
 def test_oracle_q_range_partition(oracle_mod):
     """rho over a split q range adds up to rho over the whole range, as the
     reference's multi-device split relies on (nufi/cuda_scheduler.hpp:88-118)."""

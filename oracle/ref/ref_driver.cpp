@@ -26,6 +26,12 @@
 //       239-271, 428-466) over all q, f from the reference's eval_f
 //       (nufi/rho.hpp:63-93, 234-, 369-); per-node sums in q order, nodes
 //       summed in order; writes <out>.metrics (4 doubles).
+//   ref_driver rho <cfg.bin> <coeffs.bin> <n> <out_prefix> <reps>
+//       rho of step n (as in run), reps times; writes <out>.rho and prints
+//       the best wall time of the trace in seconds.
+//   ref_driver points <cfg.bin> <coeffs.bin> <n> <mode> <pts.bin> <out_prefix>
+//       eval_ftilda (mode 0), eval_f (1) or the 1D eval_phase_flow (2) at
+//       points (x.., v..); writes <out>.f and <out>.pts (moved by mode 2).
 //   ref_driver poisson_kat        bin/test_poisson.cpp's analytic check
 //   ref_driver fields_kat         bin/test_fields.cpp's checks at nodes
 #include <algorithm>
@@ -414,6 +420,82 @@ int cmd_metrics(int argc, char **argv)
     return 0;
 }
 
+// The reference's point functions at arbitrary points (x.., v..) of step n:
+// mode 0 eval_ftilda, 1 eval_f (nufi/rho.hpp:31-96, 191-281, 318-426),
+// 2 the 1D eval_phase_flow (rho.hpp:98-131), which moves the point.
+template <size_t order>
+void points_order(const nufi_config &k, size_t n, int mode, const double *coeffs, double *pts, size_t npts,
+                  double *f)
+{
+    const int D = k.dim;
+    if (D == 1) {
+        nufi::dim1::config_t<double> c;
+        fill(c, k);
+        for (size_t i = 0; i < npts; ++i) {
+            double &x = pts[2 * i], &u = pts[2 * i + 1];
+            if (mode == 0) f[i] = nufi::dim1::eval_ftilda<double, order>(n, x, u, coeffs, c);
+            else if (mode == 1) f[i] = nufi::dim1::eval_f<double, order>(n, x, u, coeffs, c);
+            else nufi::dim1::eval_phase_flow<double, order>(n, x, u, coeffs, c);
+        }
+    } else if (D == 2) {
+        nufi::dim2::config_t<double> c;
+        fill(c, k);
+        for (size_t i = 0; i < npts; ++i) {
+            const double *q = pts + 4 * i;
+            f[i] = mode == 0 ? nufi::dim2::eval_ftilda<double, order>(n, q[0], q[1], q[2], q[3], coeffs, c)
+                             : nufi::dim2::eval_f<double, order>(n, q[0], q[1], q[2], q[3], coeffs, c);
+        }
+    } else {
+        nufi::dim3::config_t<double> c;
+        fill(c, k);
+        for (size_t i = 0; i < npts; ++i) {
+            const double *q = pts + 6 * i;
+            f[i] = mode == 0
+                       ? nufi::dim3::eval_ftilda<double, order>(n, q[0], q[1], q[2], q[3], q[4], q[5], coeffs, c)
+                       : nufi::dim3::eval_f<double, order>(n, q[0], q[1], q[2], q[3], q[4], q[5], coeffs, c);
+        }
+    }
+}
+
+// ref_driver points <cfg> <hist> <n> <mode> <pts file> <out>: writes
+// <out>.f (f per point) and <out>.pts (the points, moved by mode 2).
+int cmd_points(int argc, char **argv)
+{
+    if (argc < 8) return 2;
+    nufi_config k;
+    if (!read_file(argv[2], &k, sizeof(k))) return 2;
+    g_f0.kind = k.f0_kind;
+    for (int i = 0; i < 8; ++i) g_f0.p[i] = k.f0_params[i];
+    std::vector<double> coeffs((k.Nt + 1) * slab_size(k));
+    if (!read_file(argv[3], coeffs.data(), sizeof(double) * coeffs.size())) return 2;
+    const size_t n = std::strtoull(argv[4], nullptr, 10);
+    const int mode = std::atoi(argv[5]);
+    if (mode == 2 && k.dim != 1) return 2;
+    FILE *fp = std::fopen(argv[6], "rb");
+    if (!fp) return 2;
+    std::vector<double> pts;
+    double v;
+    while (std::fread(&v, sizeof(double), 1, fp) == 1) pts.push_back(v);
+    std::fclose(fp);
+    const size_t npts = pts.size() / size_t(2 * k.dim);
+    std::vector<double> f(npts, 0.0);
+    switch (k.order) {
+#define NUFI_REF_ORDER_CASE(O) \
+    case O: points_order<O>(k, n, mode, coeffs.data(), pts.data(), npts, f.data()); break;
+        NUFI_REF_ORDER_CASE(3)
+        NUFI_REF_ORDER_CASE(4)
+        NUFI_REF_ORDER_CASE(5)
+        NUFI_REF_ORDER_CASE(6)
+        NUFI_REF_ORDER_CASE(7)
+        NUFI_REF_ORDER_CASE(8)
+#undef NUFI_REF_ORDER_CASE
+    default: return 2;
+    }
+    write_file(std::string(argv[7]) + ".f", f.data(), sizeof(double) * f.size());
+    write_file(std::string(argv[7]) + ".pts", pts.data(), sizeof(double) * pts.size());
+    return 0;
+}
+
 // rho of step n from a given history, `reps` times: writes rho and prints
 // the best wall time in seconds (the trace alone, for timing the
 // reference's own CPU trace beside the oracle's on the same cores).
@@ -505,7 +587,7 @@ double fields_kat_2d()
 int main(int argc, char **argv)
 {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: ref_driver run|solve|metrics|rho|poisson_kat|fields_kat ...\n");
+        std::fprintf(stderr, "usage: ref_driver run|solve|metrics|rho|points|poisson_kat|fields_kat ...\n");
         return 2;
     }
     if (const char *m = std::getenv("NUFI_REF_SUMMATION")) g_sum_mode = std::atoi(m);
@@ -514,6 +596,7 @@ int main(int argc, char **argv)
     if (cmd == "solve") return cmd_solve(argc, argv);
     if (cmd == "metrics") return cmd_metrics(argc, argv);
     if (cmd == "rho") return cmd_rho(argc, argv);
+    if (cmd == "points") return cmd_points(argc, argv);
     if (cmd == "poisson_kat") {
         std::printf("{\"float\": %.17g, \"double\": %.17g}\n", poisson_kat<float>(), poisson_kat<double>());
         return 0;

@@ -207,6 +207,48 @@ def test_oracle_rho_bit_identical_to_reference_build(dim, order, oracle_mod, tmp
         assert np.array_equal(got, ref), (n, float(np.max(np.abs(got - ref))))
 
 
+@pytest.mark.parametrize("dim,order", [(1, 4), (1, 6), (1, 3), (2, 4), (2, 5), (3, 4), (3, 3)])
+def test_oracle_points_bit_identical_to_reference_build(dim, order, oracle_mod, tmp_path):
+    """eval_ftilda and eval_f at arbitrary points (the sampling path), and
+    in 1D eval_phase_flow (the eval_f trajectory only when n > 1, then
+    x - L floor(x / L), nufi/rho.hpp:98-131), of the oracle and of the
+    reference's own functions (`ref_driver points`), on a seeded random
+    history and points partly outside the domain: equal to the last bit."""
+    import subprocess
+    from numericalflowiteration_gb300.config import landau_1d, landau_2d, landau_3d
+    drv = _ref_driver()
+    cfg = {1: lambda: landau_1d(Nx=32, Nv=64, Nt=9, order=order),
+           2: lambda: landau_2d(Nx=8, Nv=8, Nt=5, order=order),
+           3: lambda: landau_3d(Nx=4, Nv=4, Nt=4, order=order)}[dim]()
+    rng = np.random.default_rng(200 + 10 * dim + order)
+    hist = 1e-2 * rng.standard_normal((cfg.Nt + 1) * cfg.stride_t)
+    lo = np.array(list(cfg.x_min[:dim]) + list(cfg.v_min[:dim]))
+    hi = np.array(list(cfg.x_max[:dim]) + list(cfg.v_max[:dim]))
+    span = hi - lo
+    pts = lo - 0.5 * span + 2.0 * span * rng.random((300, 2 * dim))
+    p = tmp_path / "c"
+    p.with_suffix(".cfg").write_bytes(cfg.to_bytes())
+    hist.tofile(str(p) + ".hist")
+    pts.tofile(str(p) + ".in")
+
+    def ref(n, mode):
+        subprocess.run([str(drv), "points", str(p.with_suffix(".cfg")), str(p) + ".hist", str(n), str(mode),
+                        str(p) + ".in", str(p)], check=True, capture_output=True)
+        return np.fromfile(str(p) + ".f"), np.fromfile(str(p) + ".pts").reshape(pts.shape)
+
+    for n in (0, 1, 2, cfg.Nt):
+        for mode in (0, 1):
+            got = oracle_mod.eval_points(cfg, n, hist, pts, mode=mode)
+            want, _ = ref(n, mode)
+            assert np.array_equal(got, want), (n, mode, float(np.max(np.abs(got - want))))
+        if dim == 1:
+            _, flow = ref(n, 2)
+            feet = oracle_mod.eval_points(cfg, n, hist, pts, mode=1, feet=True)[1] if n > 1 else pts.copy()
+            L = cfg.x_max[0] - cfg.x_min[0]
+            feet[:, 0] = feet[:, 0] - L * np.floor(feet[:, 0] * (1.0 / L))
+            assert np.array_equal(feet, flow), n
+
+
 def test_oracle_q_range_partition(oracle_mod):
     """rho over a split q range adds up to rho over the whole range, as the
     reference's multi-device split relies on (nufi/cuda_scheduler.hpp:88-118)."""

@@ -1109,12 +1109,23 @@ int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs)
     FILE *f = std::fopen(path, "r");
     if (!f) return fail(h, NUFI_ERR_INVALID, std::string("load_history: cannot open ") + path);
     std::vector<double> vals;
-    char line[512];
     long long hdr[4] = {-1, -1, -1, -1};  // Nx Ny Nz order
-    while (std::fgets(line, sizeof(line), f)) {
+    // whole lines of any length (the reference reads whitespace-separated
+    // values with >>, so a line may hold many of them)
+    std::string line;
+    char chunk[512];
+    auto next_line = [&]() -> bool {
+        line.clear();
+        while (std::fgets(chunk, sizeof(chunk), f)) {
+            line += chunk;
+            if (line.back() == '\n') return true;
+        }
+        return !line.empty();
+    };
+    while (next_line()) {
         char key[32];
         double v;
-        if (std::sscanf(line, " %31[A-Za-z] = %lf", key, &v) == 2) {
+        if (std::sscanf(line.c_str(), " %31[A-Za-z] = %lf", key, &v) == 2) {
             const std::string k = key;
             if (k == "Nx") hdr[0] = (long long)v;
             else if (k == "Ny") hdr[1] = (long long)v;
@@ -1122,7 +1133,8 @@ int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs)
             else if (k == "order") hdr[3] = (long long)v;
             continue;
         }
-        char *s = line, *end = nullptr;
+        const char *s = line.c_str();
+        char *end = nullptr;
         for (;;) {
             const double x = std::strtod(s, &end);
             if (end == s) break;

@@ -86,6 +86,11 @@ def test_history_round_trip_and_resume(nufi, tmp_path):
     with nufi.Simulation(cfg) as c:
         assert c.load_history(tmp_path / "plain.txt") == 10
         assert np.array_equal(c.history()[:10 * cfg.stride_t], hist[:10 * cfg.stride_t])
+    # whitespace-separated values on one long line (the reference reads with >>)
+    (tmp_path / "line.txt").write_text(" ".join(repr(float(v)) for v in hist[:12 * cfg.stride_t]))
+    with nufi.Simulation(cfg) as c:
+        assert c.load_history(tmp_path / "line.txt") == 12
+        assert np.array_equal(c.history()[:12 * cfg.stride_t], hist[:12 * cfg.stride_t])
     # a header for another grid is refused
     with nufi.Simulation(landau_1d(Nx=16, Nv=32, Nt=60)) as d:
         with pytest.raises(ValueError):

@@ -49,6 +49,24 @@ def test_cpp_api_forward_backward_match_python(tmp_path):
     assert "batch J" in out
 
 
+@pytest.mark.skipif(not (REF / "bin" / "test_nufi_gpu_1d.cpp").exists(), reason="reference sources not present")
+@pytest.mark.parametrize("driver", ["test_nufi_gpu_1d.cpp", "test_nufi_gpu_2d.cpp", "test_nufi_gpu_3d.cpp"])
+def test_reference_drivers_compile_unchanged_against_the_dropin(driver):
+    """The reference's own GPU drivers (bin/test_nufi_gpu_{1d,2d,3d}.cpp),
+    unchanged, compile against the drop-in nufi/cuda_kernel.hpp: their
+    scheduler includes this repository's header, not the reference's.
+    Declaration-only stand-ins cover the libraries absent here (MPI for the
+    2D/3D drivers, armadillo for the 1D driver's plots, FFTW's header)."""
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-fopenmp", "-H",
+                        "-I", str(ROOT / "include" / "nufi_gb300"), "-I", str(ROOT / "tests" / "cpp" / "stubs"),
+                        "-I", str(ROOT / "oracle" / "ref" / "shim"), "-I", str(REF), "-I", "/usr/local/cuda/include",
+                        str(REF / "bin" / driver)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    kernel_headers = [ln.strip(". ") for ln in r.stderr.splitlines() if ln.endswith("cuda_kernel.hpp")]
+    assert kernel_headers and all(str(ROOT / "include" / "nufi_gb300") in str(Path(h).resolve())
+                                  for h in kernel_headers), kernel_headers
+
+
 @pytest.mark.skipif(not (REF / "nufi" / "cuda_scheduler.hpp").exists(), reason="reference sources not present")
 def test_dropin_header_compiles_inside_reference_scheduler(tmp_path):
     src = tmp_path / "tu.cpp"

@@ -51,20 +51,35 @@ def test_cpp_api_forward_backward_match_python(tmp_path):
 
 @pytest.mark.skipif(not (REF / "bin" / "test_nufi_gpu_1d.cpp").exists(), reason="reference sources not present")
 @pytest.mark.parametrize("driver", ["test_nufi_gpu_1d.cpp", "test_nufi_gpu_2d.cpp", "test_nufi_gpu_3d.cpp"])
-def test_reference_drivers_compile_unchanged_against_the_dropin(driver):
+def test_reference_drivers_build_unchanged_against_the_dropin(driver, tmp_path):
     """The reference's own GPU drivers (bin/test_nufi_gpu_{1d,2d,3d}.cpp),
-    unchanged, compile against the drop-in nufi/cuda_kernel.hpp: their
-    scheduler includes this repository's header, not the reference's.
-    Declaration-only stand-ins cover the libraries absent here (MPI for the
-    2D/3D drivers, armadillo for the 1D driver's plots, FFTW's header)."""
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-fopenmp", "-H",
-                        "-I", str(ROOT / "include" / "nufi_gb300"), "-I", str(ROOT / "tests" / "cpp" / "stubs"),
-                        "-I", str(ROOT / "oracle" / "ref" / "shim"), "-I", str(REF), "-I", "/usr/local/cuda/include",
-                        str(REF / "bin" / driver)], capture_output=True, text=True)
+    unchanged, compile and link against the drop-in nufi/cuda_kernel.hpp and
+    libnufi_gb300.so (with the reference's poisson.cpp and the oracle's FFTW
+    and BLAS shims, as the reference build would): their scheduler includes
+    this repository's header, not the reference's.  Stand-ins cover the
+    libraries absent here (single-rank MPI for 2D/3D, armadillo for the 1D
+    plots).  Without a GPU the program stops where the reference's does: its
+    scheduler's device count throws nufi::cuda::exception."""
+    from numericalflowiteration_gb300 import build
+    build.build()
+    exe = tmp_path / "driver"
+    r = subprocess.run(["g++", "-std=c++17", "-O0", "-fopenmp", "-w", "-H",
+                        "-I", str(ROOT / "include" / "nufi_gb300"), "-I", str(ROOT / "include"),
+                        "-I", str(ROOT / "tests" / "cpp" / "stubs"), "-I", str(ROOT / "oracle" / "ref" / "shim"),
+                        "-I", str(REF), "-I", "/usr/local/cuda/include", str(REF / "bin" / driver),
+                        str(REF / "nufi" / "poisson.cpp"), str(ROOT / "oracle" / "ref" / "shim_fftw.cpp"),
+                        str(ROOT / "oracle" / "ref" / "shim_blas.cpp"), "-L", str(PKG), "-lnufi_gb300",
+                        "-L", "/usr/local/cuda/lib64", "-lcudart", f"-Wl,-rpath,{PKG}", "-o", str(exe)],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     kernel_headers = [ln.strip(". ") for ln in r.stderr.splitlines() if ln.endswith("cuda_kernel.hpp")]
     assert kernel_headers and all(str(ROOT / "include" / "nufi_gb300") in str(Path(h).resolve())
                                   for h in kernel_headers), kernel_headers
+    import torch
+    if torch.cuda.is_available():
+        return  # the full simulation is not run here
+    run = subprocess.run([str(exe)], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert run.returncode != 0 and "nufi::cuda::exception" in run.stderr, run.stderr[-2000:]
 
 
 @pytest.mark.skipif(not (REF / "nufi" / "cuda_scheduler.hpp").exists(), reason="reference sources not present")

@@ -60,8 +60,9 @@ extern "C" {
  * accumulator, the Poisson solve and the spline interpolation solve.
  * f0's phase comes from the cell the foot lands in (the foot wrapped into
  * the domain), so k (x_max - x_min) must be a multiple of 2 pi on every
- * axis (NUFI_ERR_UNSUPPORTED otherwise; FP64 evaluates f0 at the unwrapped
- * foot, as the reference, for any k).                                       */
+ * axis, to 2.5e-7 relative (a single-precision domain length passes);
+ * NUFI_ERR_UNSUPPORTED otherwise.  FP64 evaluates f0 at the unwrapped foot,
+ * as the reference, for any k.                                              */
 #define NUFI_PREC_FP32_SPLIT  1
 
 /* ---- initial conditions (f0) ------------------------------------------- */

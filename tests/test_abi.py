@@ -122,9 +122,13 @@ def test_split_needs_a_periodic_f0_phase(lib):
                 landau_2d(k=0.25, precision="fp32split"), landau_3d(k=0.75, precision="fp32split")):
         st, msg = _create_status(lib, cfg.to_c())
         assert st == _lib.ERR_UNSUPPORTED and "2 pi" in msg, (cfg, msg)
+    # the reference's <float, 4> 1D configuration through the drop-in header:
+    # x_max = 4 pi computed in float (2.8e-8 above 4 pi) must pass
+    float_4pi = float(np.float32(4 * np.pi))
     for cfg in (landau_1d(k=0.3), landau_1d(k=1.0, precision="fp32split"), landau_2d(k=1.5, precision="fp32split"),
                 bump_on_tail_1d(k=0.37, precision="fp32split"), bump_on_tail_1d(k=0.3, precision="fp32split"),
-                landau_3d(precision="fp32split")):
+                landau_3d(precision="fp32split"),
+                two_stream_1d(Nx=256, Nv=512, Nt=1600, precision="fp32split").replace(x_max=[float_4pi])):
         st, msg = _create_status(lib, cfg.to_c())
         assert not msg.startswith("nufi_create:"), (cfg, msg)
     with pytest.raises(NotImplementedError):

@@ -473,7 +473,7 @@ def main(argv=None):
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-steps", type=int, default=120, help="CPU baseline sample: steps 0..N")
+    ap.add_argument("--cpu-steps", type=int, default=150, help="CPU baseline sample: steps 0..N")
     ap.add_argument("--ref-steps", type=int, default=40, help="reference arm sample per step: steps 0..N")
     ap.add_argument("--profile-case", action="store_true",
                     help="run steps 0..--nt of the workload once in --precision and exit (a small case for ncu)")

@@ -82,6 +82,48 @@ def test_reference_drivers_build_unchanged_against_the_dropin(driver, tmp_path):
     assert run.returncode != 0 and "nufi::cuda::exception" in run.stderr, run.stderr[-2000:]
 
 
+@pytest.mark.skipif(not (REF / "nufi" / "config.hpp").exists(), reason="reference sources not present")
+def test_dropin_refuses_a_different_metrics_grid(tmp_path):
+    """The drop-in's metrics use the rho grid, as the reference's drivers
+    pass it (bin/test_nufi_gpu_1d.cpp:216-221); a conf_metrics with other
+    node counts is refused with std::invalid_argument before any CUDA call,
+    and the drivers' own equal grid gets through to device creation."""
+    from numericalflowiteration_gb300 import build
+    build.build()
+    src = tmp_path / "grid.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include <stdexcept>
+#include <nufi/cuda_kernel.hpp>
+int main()
+{
+    nufi::dim1::config_t<double> c, cm;
+    cm.Nu = 2 * c.Nu;
+    cm.du = (cm.u_max - cm.u_min) / cm.Nu;
+    try { nufi::dim1::cuda_kernel<double, 4> k(c, cm, 0); std::puts("finer: created"); }
+    catch (const std::invalid_argument &) { std::puts("finer: invalid_argument"); }
+    catch (const std::exception &e) { std::printf("finer: other %s\n", e.what()); }
+    nufi::dim1::config_t<double> same;
+    same.Nx = c.Nx; same.Nu = c.Nu;
+    same.dx = (same.x_max - same.x_min) / same.Nx;
+    same.du = (same.u_max - same.u_min) / same.Nu;
+    try { nufi::dim1::cuda_kernel<double, 4> k(c, same, 0); std::puts("same: created"); }
+    catch (const std::invalid_argument &) { std::puts("same: invalid_argument"); }
+    catch (const std::exception &) { std::puts("same: device error"); }
+    return 0;
+}
+''')
+    exe = tmp_path / "grid"
+    subprocess.run(["g++", "-std=c++17", "-O0", "-w", "-I", str(ROOT / "include" / "nufi_gb300"), "-I",
+                    str(ROOT / "include"), "-I", str(REF), "-I", "/usr/local/cuda/include", str(src), "-L", str(PKG),
+                    "-lnufi_gb300", "-L", "/usr/local/cuda/lib64", "-lcudart", f"-Wl,-rpath,{PKG}", "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120).stdout.split("\n")
+    assert out[0] == "finer: invalid_argument"
+    import torch
+    assert out[1] == ("same: created" if torch.cuda.is_available() else "same: device error"), out
+
+
 @pytest.mark.skipif(not (REF / "nufi" / "cuda_scheduler.hpp").exists(), reason="reference sources not present")
 def test_dropin_header_compiles_inside_reference_scheduler(tmp_path):
     src = tmp_path / "tu.cpp"

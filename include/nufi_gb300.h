@@ -72,7 +72,10 @@ extern "C" {
 /* Two-stream:  (1 + alpha cos(k x)) v^2 exp(-v^2/2) / sqrt(2 pi)   (1D)    */
 #define NUFI_F0_TWO_STREAM    1
 /* Bump-on-tail:(1 + alpha cos(k x)) [0.9 N(v;0,1) + 0.1 N(v;u_b,sigma_b)]
- *              params[2] = u_b, params[3] = sigma_b                  (1D)  */
+ *              params[2] = u_b, params[3] = sigma_b                  (1D)
+ *              3D (FP64 only): (1 + alpha sum_d cos(k x_d))
+ *              [0.9 N(u;0,1) + 0.1 N(u;u_b,sigma_b)] N(v;0,1) N(w;0,1),
+ *              the reference's compiled-in 3D f0 (nufi/config.hpp)         */
 #define NUFI_F0_BUMP_ON_TAIL  2
 
 typedef struct nufi_config {

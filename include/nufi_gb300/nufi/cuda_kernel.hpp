@@ -18,10 +18,11 @@
  * The reference hard-codes f0 in config_t<real>::f0; the device side needs
  * it as data.  nufi_gb300::set_initial_condition() selects it (kind +
  * parameters, see NUFI_F0_* in nufi_gb300.h); the default per dimension is
- * the reference's compiled-in f0 where this library has it (1D: the
- * u^2 M(u) form with alpha = 0.01, k = 0.5, config.hpp:80-82; 2D: Landau
- * with alpha = 0.5, k = 0.5, config.hpp:148-149).  real = double runs the
- * FP64 plain form, real = float the FP32-split form.
+ * the reference's compiled-in f0 (1D: the u^2 M(u) form with alpha = 0.01,
+ * k = 0.5; 2D: Landau with alpha = 0.5, k = 0.5; 3D: bump-on-tail with
+ * alpha = 0.03, k = 0.3, u_b = 4.5, sigma_b = 0.5; nufi/config.hpp), each
+ * reproduced to the last bit by the matching f0 kind.  real = double runs
+ * the FP64 plain form, real = float the FP32-split form.
  */
 #ifndef NUFI_CUDA_KERNEL_HPP
 #define NUFI_CUDA_KERNEL_HPP
@@ -50,7 +51,7 @@ inline initial_condition &initial_condition_slot(int dim)
     static initial_condition slots[3] = {
         {NUFI_F0_TWO_STREAM, {0.01, 0.5, 0, 0, 0, 0, 0, 0}},
         {NUFI_F0_LANDAU, {0.5, 0.5, 0, 0, 0, 0, 0, 0}},
-        {NUFI_F0_LANDAU, {0.01, 0.5, 0, 0, 0, 0, 0, 0}},
+        {NUFI_F0_BUMP_ON_TAIL, {0.03, 0.3, 4.5, 0.5, 0, 0, 0, 0}},
     };
     return slots[dim - 1];
 }

@@ -152,6 +152,17 @@ def bump_on_tail_1d(Nx=64, Nv=256, Nt=320, dt=1.0 / 16, alpha=0.03, k=0.4, u_b=4
                   [alpha, k, u_b, sigma_b], **kw)
 
 
+def bump_on_tail_3d(Nx=8, Nv=8, Nt=50, dt=0.1, alpha=0.03, k=0.3, u_b=4.5, sigma_b=0.5, v_min=-9.0, v_max=0.0,
+                    **kw) -> Config:
+    """3D3V bump-on-tail, the reference's compiled-in 3D configuration
+    (nufi/config.hpp: 8^3 x 8^3, dt = 0.1, T = 5, x in [0, 20 pi / 3)^3,
+    v in [-9, 0]^3): f0 = (1 + a sum_d cos k x_d)[0.9 N(u;0,1) +
+    0.1 N(u;u_b,s_b)] N(v;0,1) N(w;0,1).  FP64 form only."""
+    L = 2.0 * math.pi / k
+    return Config(3, [Nx] * 3, [Nv] * 3, Nt, dt, [0.0] * 3, [L] * 3, [v_min] * 3, [v_max] * 3, "bump_on_tail",
+                  [alpha, k, u_b, sigma_b], **kw)
+
+
 def landau_2d(Nx=32, Nv=64, Nt=160, dt=1.0 / 8, alpha=0.01, k=0.5, **kw) -> Config:
     """2D2V weak Landau damping: x in [0, 4 pi)^2, v in [-8, 8]^2; defaults
     are the 32^2 x 64^2, T = 20 run (4.2M points)."""

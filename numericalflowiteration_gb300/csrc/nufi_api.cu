@@ -172,8 +172,9 @@ int validate(const nufi_config *c, std::string &why)
         why = "unknown f0 kind";
         return NUFI_ERR_INVALID;
     }
-    if (c->dim > 1 && c->f0_kind != NUFI_F0_LANDAU) {
-        why = "f0 kinds other than Landau are 1D only";
+    // 2D: Landau; 3D: Landau and the reference's compiled-in bump-on-tail
+    if (c->dim > 1 && c->f0_kind != NUFI_F0_LANDAU && !(c->dim == 3 && c->f0_kind == NUFI_F0_BUMP_ON_TAIL)) {
+        why = "f0 kinds other than Landau are 1D only (and bump-on-tail in 3D)";
         return NUFI_ERR_UNSUPPORTED;
     }
     if (c->precision == NUFI_PREC_FP64 && !fp64_order_supported(c->dim, c->order)) {

@@ -152,6 +152,14 @@ __device__ __forceinline__ double f0_2d(const Problem &p, double x, double y, do
 __device__ __forceinline__ double f0_3d(const Problem &p, double x, double y, double z, double u, double v, double w)
 {
     const double alpha = p.f0p[0], k = p.f0p[1];
+    if (p.f0_kind == NUFI_F0_BUMP_ON_TAIL) {
+        // the reference's compiled-in 3D f0 (nufi/config.hpp:80-82) with
+        // runtime alpha, k, u_b, sigma_b, in its operation order
+        const double ub = p.f0p[2], sb = p.f0p[3], a = 1 / (2 * sb * sb);
+        return 0.06349363593424096978576330493464 *
+               (0.9 * exp(-0.5 * u * u) + 0.1 / sb * exp(-a * (u - ub) * (u - ub))) *
+               exp(-0.5 * (v * v + w * w)) * (1 + alpha * (cos(k * x) + cos(k * y) + cos(k * z)));
+    }
     return 0.06349363593424096978576330493464 * (1. + alpha * cos(k * x) + alpha * cos(k * y) + alpha * cos(k * z)) *
            exp(-(u * u + v * v + w * w) / 2);
 }

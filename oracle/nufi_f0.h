@@ -58,6 +58,15 @@ static inline double nufi_f0_3d(const nufi_f0_params *f, double x, double y, dou
         return 0.06349363593424096978576330493464 *
                (1. + alpha * cos(k * x) + alpha * cos(k * y) + alpha * cos(k * z)) *
                exp(-(u * u + v * v + w * w) / 2);
+    if (f->kind == NUFI_F0_BUMP_ON_TAIL) {
+        /* the reference's compiled-in 3D f0 (config.hpp:80-82), with
+         * alpha, k, u_b, sigma_b at run time: 0.1 / sigma_b = 0.2 and
+         * 1 / (2 sigma_b^2) = 2 there, in the same operation order */
+        const double ub = f->p[2], sb = f->p[3], a = 1 / (2 * sb * sb);
+        return 0.06349363593424096978576330493464 *
+               (0.9 * exp(-0.5 * u * u) + 0.1 / sb * exp(-a * (u - ub) * (u - ub))) *
+               exp(-0.5 * (v * v + w * w)) * (1 + alpha * (cos(k * x) + cos(k * y) + cos(k * z)));
+    }
     return NAN;
 }
 

@@ -69,6 +69,11 @@ struct rho_sum {
     double value() const { return acc + comp; }
 };
 
+// Built with NUFI_REF_NATIVE_F0 (ref_driver_native), the driver keeps the
+// reference's own compiled-in f0 of each dimension instead (config.hpp:
+// 1D u^2 M two-stream, 2D Landau alpha = k = 0.5, 3D bump-on-tail), and the
+// configured f0 is ignored.
+#ifndef NUFI_REF_NATIVE_F0
 namespace nufi {
 namespace dim1 {
 template <> __host__ __device__ double config_t<double>::f0(double x, double u) noexcept
@@ -84,6 +89,7 @@ template <> __host__ __device__ double config_t<double>::f0(double x, double y, 
 { return nufi_f0_3d(&g_f0, x, y, z, u, v, w); }
 }  // namespace dim3
 }  // namespace nufi
+#endif
 
 #include <nufi/fields.hpp>
 #include <nufi/poisson.hpp>

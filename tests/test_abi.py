@@ -112,6 +112,21 @@ def test_fp64_velocity_grid_limit(lib):
         assert not msg.startswith("nufi_create:"), msg
 
 
+def test_bump_on_tail_in_3d_is_fp64_only(lib):
+    """Bump-on-tail (the reference's compiled-in 3D f0) is admitted in 3D for
+    the FP64 trace; the FP32-split 3D trace is Landau only, and 2D takes
+    Landau only."""
+    from numericalflowiteration_gb300.config import bump_on_tail_3d, landau_2d
+    st, msg = _create_status(lib, bump_on_tail_3d().to_c())
+    assert not msg.startswith("nufi_create:"), msg
+    st, msg = _create_status(lib, bump_on_tail_3d(precision="fp32split").to_c())
+    assert st == _lib.ERR_UNSUPPORTED and "FP32-split" in msg
+    c = landau_2d(Nx=8, Nv=8, Nt=2).to_c()
+    c.f0_kind = 2
+    st, msg = _create_status(lib, c)
+    assert st == _lib.ERR_UNSUPPORTED
+
+
 def test_split_needs_a_periodic_f0_phase(lib):
     """The FP32-split traces evaluate cos(k x) at the foot wrapped into the
     domain; the reference (nufi/rho.hpp:59-60) and the FP64 trace at the

@@ -71,6 +71,25 @@ def test_fp64_graph_run_matches_reference(nufi, name):
         assert rel_max(rho, g["rho"][list(g["rho_steps"]).index(n_last)]) <= 1e-12
 
 
+def test_fp64_bump_on_tail_3d_matches_oracle(nufi, oracle_mod):
+    """The reference's compiled-in 3D configuration (bump-on-tail, v in
+    [-9, 0]^3, x in [0, 20 pi / 3)^3), reduced to 4^3 x 6^3 and 6 steps:
+    the FP64 run against the oracle with compensated sums (the oracle's f0
+    matches the reference's compiled f0 to the last bit)."""
+    from numericalflowiteration_gb300.config import bump_on_tail_3d
+    cfg = bump_on_tail_3d(Nx=4, Nv=6, Nt=6)
+    with nufi.Simulation(cfg) as sim:
+        e = sim.run()
+        hist = sim.history()
+    oracle_mod.set_summation(1)
+    try:
+        e_ref, _, h_ref = oracle_mod.run(cfg, 0, cfg.Nt)
+    finally:
+        oracle_mod.set_summation(0)
+    assert rel_max(e, e_ref) <= 1e-12
+    assert rel_max(hist, h_ref) <= 1e-11
+
+
 def test_fp64_two_stream_through_saturation(nufi):
     cfg, g = golden("two_stream_1d_64x256_T50")
     with nufi.Simulation(cfg) as sim:

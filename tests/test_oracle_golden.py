@@ -207,6 +207,37 @@ def test_oracle_rho_bit_identical_to_reference_build(dim, order, oracle_mod, tmp
         assert np.array_equal(got, ref), (n, float(np.max(np.abs(got - ref))))
 
 
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_f0_kinds_bit_identical_to_the_references_compiled_f0(dim, oracle_mod, tmp_path):
+    """The reference hard-codes one f0 per dimension (nufi/config.hpp: 1D
+    u^2 M two-stream with alpha = 0.01, k = 0.5; 2D Landau with alpha = k =
+    0.5; 3D bump-on-tail with alpha = 0.03, k = 0.3, u_b = 4.5, sigma_b =
+    0.5).  `ref_driver_native` keeps those compiled-in functions; the f0
+    kinds with these parameters must give its rho to the last bit: at step 0
+    (f0 alone at the grid points) and after traced steps."""
+    import subprocess
+    from conftest import ROOT
+    from numericalflowiteration_gb300.config import bump_on_tail_3d, landau_2d, two_stream_1d
+    drv = ROOT / "oracle" / "_ref" / "ref_driver_native"
+    if not drv.exists():
+        pytest.skip("no reference build in oracle/_ref")
+    cfg = {1: lambda: two_stream_1d(Nx=32, Nv=64, Nt=9, alpha=0.01, k=0.5),
+           2: lambda: landau_2d(Nx=8, Nv=8, Nt=5, alpha=0.5, k=0.5),
+           3: lambda: bump_on_tail_3d(Nx=4, Nv=6, Nt=4)}[dim]()
+    rng = np.random.default_rng(300 + dim)
+    hist = 1e-2 * rng.standard_normal((cfg.Nt + 1) * cfg.stride_t)
+    p = tmp_path / "c"
+    p.with_suffix(".cfg").write_bytes(cfg.to_bytes())
+    hist.tofile(str(p) + ".hist")
+    oracle_mod.set_summation(0)
+    for n in (0, 1, cfg.Nt):
+        subprocess.run([str(drv), "rho", str(p.with_suffix(".cfg")), str(p) + ".hist", str(n), str(p), "1"],
+                       check=True, capture_output=True)
+        ref = np.fromfile(str(p) + ".rho")
+        got = oracle_mod.rho(cfg, n, hist)
+        assert np.any(ref != 0) and np.array_equal(got, ref), (n, float(np.max(np.abs(got - ref))))
+
+
 @pytest.mark.parametrize("dim,order", [(1, 4), (1, 6), (1, 3), (2, 4), (2, 5), (3, 4), (3, 3)])
 def test_oracle_points_bit_identical_to_reference_build(dim, order, oracle_mod, tmp_path):
     """eval_ftilda and eval_f at arbitrary points (the sampling path), and

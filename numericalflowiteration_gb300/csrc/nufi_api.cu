@@ -140,6 +140,10 @@ int validate(const nufi_config *c, std::string &why)
             why = "domain bounds must satisfy min < max";
             return NUFI_ERR_INVALID;
         }
+        if (!std::isfinite(c->x_max[a] - c->x_min[a]) || !std::isfinite(c->v_max[a] - c->v_min[a])) {
+            why = "domain bounds must be finite";
+            return NUFI_ERR_INVALID;
+        }
     }
     // Sizes below are products of these counts in 64-bit integers, and the
     // launch shapes hold node and block counts in 32-bit fields: bounded here
@@ -170,6 +174,15 @@ int validate(const nufi_config *c, std::string &why)
     }
     if (c->f0_kind < NUFI_F0_LANDAU || c->f0_kind > NUFI_F0_BUMP_ON_TAIL) {
         why = "unknown f0 kind";
+        return NUFI_ERR_INVALID;
+    }
+    for (int i = 0; i < 8; ++i)
+        if (!std::isfinite(c->f0_params[i])) {
+            why = "f0 parameters must be finite";
+            return NUFI_ERR_INVALID;
+        }
+    if (c->f0_kind == NUFI_F0_BUMP_ON_TAIL && !(c->f0_params[3] > 0)) {
+        why = "bump-on-tail needs sigma_b > 0";
         return NUFI_ERR_INVALID;
     }
     // 2D: Landau; 3D: Landau and the reference's compiled-in bump-on-tail

@@ -66,6 +66,10 @@ def _create_status(lib, cfg_c):
 
 
 @pytest.mark.parametrize("mutate,code", [
+    (lambda c: c.x_max.__setitem__(0, float("inf")), _lib.ERR_INVALID),
+    (lambda c: c.v_min.__setitem__(0, float("-inf")), _lib.ERR_INVALID),
+    (lambda c: c.f0_params.__setitem__(0, float("nan")), _lib.ERR_INVALID),
+    (lambda c: (setattr(c, "f0_kind", 2), c.f0_params.__setitem__(3, 0.0)), _lib.ERR_INVALID),
     (lambda c: setattr(c, "dim", 4), _lib.ERR_INVALID),
     (lambda c: setattr(c, "order", 9), _lib.ERR_INVALID),
     (lambda c: setattr(c, "dt", -1.0), _lib.ERR_INVALID),
@@ -123,6 +127,7 @@ def test_bump_on_tail_in_3d_is_fp64_only(lib):
     assert st == _lib.ERR_UNSUPPORTED and "FP32-split" in msg
     c = landau_2d(Nx=8, Nv=8, Nt=2).to_c()
     c.f0_kind = 2
+    c.f0_params[2], c.f0_params[3] = 4.5, 0.5
     st, msg = _create_status(lib, c)
     assert st == _lib.ERR_UNSUPPORTED
 

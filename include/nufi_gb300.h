@@ -109,7 +109,9 @@ const char *nufi_last_error(const nufi_handle *h);
  * more than 1048560 velocity nodes (the FP64 trace's launch grid; FP32-split
  * handles trace any size but nufi_compute_metrics, which runs the FP64
  * trace, refuses the same sizes); NUFI_ERR_INVALID / NUFI_ERR_UNSUPPORTED
- * for the other configuration errors.  NUFI_ERR_CUDA (with the CUDA error's
+ * for the other configuration errors (among them non-finite domain bounds or
+ * f0 parameters, and sigma_b <= 0 for bump-on-tail: NUFI_ERR_INVALID).
+ * NUFI_ERR_CUDA (with the CUDA error's
  * name) when no device is usable or an allocation fails. */
 int nufi_create(const nufi_config *cfg, int device, nufi_handle **out);
 int nufi_destroy(nufi_handle *h);

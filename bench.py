@@ -171,17 +171,106 @@ def profiled_traffic(kernel: str, workload: str):
         return None
 
 
-def cpu_baseline(cfg, n_last: int, threads: int):
-    """Oracle port (test infrastructure) on the host cores: steps 0..n_last."""
+def golden_energy(workload: str, nt: int):
+    """The reference's own energy history of the whole workload, from the
+    committed golden fixture tests/golden/<workload>.npz (written by
+    tests/golden/make_golden.py with the reference's code): (in-order,
+    compensated) arrays of W_0..W_Nt, or None where no such fixture exists."""
+    p = ROOT / "tests" / "golden" / f"{workload}.npz"
+    if not p.exists():
+        return None
+    g = np.load(p)
+    if int(g["n_last"]) != nt:
+        return None
+    return np.asarray(g["energy"]), np.asarray(g["energy_comp"])
+
+
+def energy_errors_vs_oracle(e_split, e64, gold):
+    """Errors of the FP32-split and FP64 energy histories against the
+    reference's (compensated rho sums; the in-order one beside it)."""
+    ref_inorder, ref_comp = gold
+
+    def errs(e, ref):
+        d = np.abs(np.asarray(e) - ref)
+        return {"max_normalised": float(np.max(d) / np.max(np.abs(ref))),
+                "pointwise_max": float(np.max(d / np.abs(ref)))}
+
+    return {"oracle": "reference energy history W_0..W_Nt (tests/golden, the reference's own code, "
+                      "compensated rho sums)",
+            "fp32split": errs(e_split, ref_comp), "fp64": errs(e64, ref_comp),
+            "fp64_vs_inorder_reference": errs(e64, ref_inorder),
+            "reference_summation_floor": float(np.max(np.abs(ref_inorder - ref_comp)) / np.max(np.abs(ref_comp))),
+            "gating_measure": "max_normalised"}
+
+
+def parse_windows(spec: str, nt: int):
+    """'0:10,200:10,...' -> [(first step, count), ...]; a first step below
+    0 counts from the end (-10:10 = the last 10 steps)."""
+    out = []
+    for part in spec.split(","):
+        a, b = part.split(":")
+        n0, cnt = int(a), int(b)
+        if n0 < 0:
+            n0 = nt + 1 + n0
+        n0 = max(0, min(n0, nt))
+        out.append((n0, max(1, min(cnt, nt + 1 - n0))))
+    return out
+
+
+def cpu_windows(cfg, windows, threads: int):
+    """The CPU loop of the reference (oracle port: per step rho over all
+    points, then the field solve) timed step by step in the given windows
+    of the workload, and the whole run's time extrapolated from them.
+
+    Step n costs t(n) = c0 + c1 n: c0 (f0 at every point, the rho sums,
+    the solve) and c1 (one backward substep of every point) are fitted by
+    least squares to the timed steps; the whole run is then
+    sum_{n=0..Nt} t(n) = (Nt+1) c0 + c1 Nt(Nt+1)/2.  The first window
+    starts at step 0 and computes real slabs; a later window at n0 runs on
+    a history whose slab k is real slab k mod (len of the first window):
+    a step's work depends only on n, not on the field values."""
     from oracle import oracle
     oracle.build()
     oracle.set_summation(0)
-    t0 = time.perf_counter()
-    oracle.run(cfg, 0, n_last, keep_rho=False, nthreads=threads)
-    dt = time.perf_counter() - t0
-    ps = cfg.point_steps(0, n_last)
-    return {"value": ps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"steps 0..{n_last} of the workload ({ps:.3e} point-steps, {dt:.1f} s, OpenMP over spatial nodes)"}
+    windows = sorted(windows)
+    if windows[0][0] != 0:
+        windows = [(0, 1)] + windows
+    st = cfg.stride_t
+    hist = np.zeros((cfg.Nt + 1) * st)
+    ns, ts = [], []
+    real = 0
+    for i, (n0, cnt) in enumerate(windows):
+        if i > 0:
+            h = hist.copy()
+            for k in range(real, n0 + cnt):
+                h[k * st:(k + 1) * st] = hist[(k % real) * st:(k % real + 1) * st]
+        else:
+            h = hist
+        for n in range(n0, n0 + cnt):
+            t0 = time.perf_counter()
+            oracle.run(cfg, n, n, coeffs=h, keep_rho=False, nthreads=threads)
+            ts.append(time.perf_counter() - t0)
+            ns.append(n)
+        if i == 0:
+            real = n0 + cnt
+    A = np.stack([np.ones(len(ns)), np.asarray(ns, dtype=np.float64)], axis=1)
+    t_arr = np.asarray(ts)
+    (c0, c1), *_ = np.linalg.lstsq(A, t_arr, rcond=None)
+    if c0 < 0:  # both costs are non-negative: refit with c0 = 0
+        c0, c1 = 0.0, float(np.dot(A[:, 1], t_arr) / np.dot(A[:, 1], A[:, 1]))
+    pred = A @ np.array([c0, c1])
+    resid = float(np.sqrt(np.mean((pred - np.asarray(ts)) ** 2)) / np.mean(ts))
+    nt = cfg.Nt
+    full_s = (nt + 1) * c0 + c1 * nt * (nt + 1) / 2
+    ps = cfg.point_steps()
+    timed_ps = sum(cfg.n_points * n for n in ns)
+    return {"value": ps / full_s, "unit": UNIT, "cores": threads, "kind": "port",
+            "full_run_s_extrapolated": full_s, "fit_c0_s": float(c0), "fit_c1_s": float(c1),
+            "fit_rel_rms_residual": resid, "timed_s": float(sum(ts)), "same_config": True,
+            "sample": (f"{len(ns)} steps of the workload in windows "
+                       + ",".join(f"{a}..{a + c - 1}" for a, c in windows)
+                       + f" ({timed_ps:.3e} point-steps, {sum(ts):.1f} s, OpenMP over spatial nodes); "
+                       "per-step time fitted as c0 + c1 n and summed over all steps 0..Nt")}
 
 
 def run_reference(args, cfg):
@@ -189,20 +278,23 @@ def run_reference(args, cfg):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    n_last = args.ref_steps
-    vals = []
+    windows = parse_windows(args.cpu_windows, cfg.Nt)
+    vals, fits = [], []
     for k in range(args.warmup + args.steps):
-        r = cpu_baseline(cfg, n_last, threads)
+        r = cpu_windows(cfg.replace(precision="fp64"), windows, threads)
         if k >= args.warmup:
             vals.append(r["value"])
+            fits.append(r)
     value = statistics.median(vals)
-    ps = cfg.point_steps(0, n_last)
+    fit = fits[vals.index(value)] if value in vals else fits[-1]
+    ps = cfg.point_steps()
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * ps / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic initial condition)",
-            "config": {"workload": args.workload, "sample_steps": f"0..{n_last}", "threads": threads},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"steps 0..{n_last} per step ({ps:.3e} point-steps)"},
+            "config": {"workload": args.workload, "Nx": cfg.Nx[0], "Nv": cfg.Nv[0], "Nt": cfg.Nt, "dt": cfg.dt,
+                       "point_steps_per_step": ps, "threads": threads, "same_config": True,
+                       "sample_windows": args.cpu_windows},
+            "cpu_baseline": {**fit, "value": value},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -282,7 +374,13 @@ def run_ours(args, cfg):
         err_pt = float(np.max(np.abs(e_split - e64) / np.abs(e64)))
         fp64 = {"value": ps / (ms64 * 1e-3), "ms_per_step": ms64, "speedup_split_vs_fp64": ms64 / ms_per_step,
                 "energy_err_max_normalised": err_max, "energy_err_pointwise_max": err_pt,
-                "gate": GATE, "gate_passed": err_max <= GATE}
+                "gate": GATE, "gate_passed": err_max <= GATE,
+                "gating_measure": "max_n |dW_n| / max_n |W_n| (normalised); the pointwise max_n |dW_n|/|W_n| "
+                                  "is reported beside it"}
+        gold = golden_energy(args.workload, cfg.Nt)
+        if gold is not None:
+            fp64["err_vs_oracle"] = energy_errors_vs_oracle(e_split, e64, gold)
+            fp64["gate_passed_vs_oracle"] = fp64["err_vs_oracle"]["fp32split"]["max_normalised"] <= GATE
 
     # Per-step trace launches: CUDA events around compute_rho(n) on the
     # handle's stream at several n (trace + rho reduction).
@@ -360,7 +458,8 @@ def run_ours(args, cfg):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_baseline(cfg.replace(precision="fp64"), args.cpu_steps, os.cpu_count() or 1)
+        cpu = cpu_windows(cfg.replace(precision="fp64"), parse_windows(args.cpu_windows, cfg.Nt),
+                          os.cpu_count() or 1)
     sim.close()
 
     if rank == 0:
@@ -473,8 +572,9 @@ def main(argv=None):
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-steps", type=int, default=150, help="CPU baseline sample: steps 0..N")
-    ap.add_argument("--ref-steps", type=int, default=40, help="reference arm sample per step: steps 0..N")
+    ap.add_argument("--cpu-windows", default="0:12,200:6,400:6,600:4,-4:4",
+                    help="CPU baseline and reference arm: timed step windows first:count (negative first: "
+                         "from the end); the whole run is extrapolated from them")
     ap.add_argument("--profile-case", action="store_true",
                     help="run steps 0..--nt of the workload once in --precision and exit (a small case for ncu)")
     ap.add_argument("--precision", default="fp32split", choices=["fp32split", "fp64"])

@@ -116,6 +116,40 @@ const char *nufi_last_error(const nufi_handle *h);
 int nufi_create(const nufi_config *cfg, int device, nufi_handle **out);
 int nufi_destroy(nufi_handle *h);
 
+/* No counterpart in the reference: launch options of a handle or a batch.
+ * Every field's 0 is the default (a zeroed struct, or a NULL pointer, is
+ * what nufi_create and nufi_batch_create use).  The options choose among
+ * kernels and launch shapes of the same computation; none changes what a
+ * call computes beyond the rounding of the FP32-split arithmetic, and the
+ * GPU tests use them to check one kernel against another.
+ *   split_global_loads      1: FP32-split traces read their field tables
+ *                           from global memory, not through the
+ *                           shared-memory ring
+ *   split_plain_kick        1: the 1D FP32-split kick summed in plain,
+ *                           uncompensated FP32 (global-load 1D trace; shows
+ *                           what the compensation buys)
+ *   no_persistent           1: nufi_run as a CUDA graph of per-step
+ *                           launches instead of the whole-run kernel
+ *   split_ctas_per_sm       0 or 1: one CTA per SM; 2: two smaller CTAs
+ *                           per SM (1D staged split trace)
+ *   split_threads_per_node  0 or 1: one thread per spatial node; 2: two
+ *                           (1D staged split trace)
+ *   batch_no_autotune       1: nufi_batch_create keeps the default shapes
+ *   batch_adjoint_ppt       0: autotuned; 2 or 4 (FP32-split) or 1, 2, 4
+ *                           (FP64): chains per thread of the batch adjoint
+ * Other values are NUFI_ERR_INVALID. */
+typedef struct nufi_options {
+    int32_t split_global_loads;
+    int32_t split_plain_kick;
+    int32_t no_persistent;
+    int32_t split_ctas_per_sm;
+    int32_t split_threads_per_node;
+    int32_t batch_no_autotune;
+    int32_t batch_adjoint_ppt;
+    int32_t reserved[9]; /* must be 0 */
+} nufi_options;
+int nufi_create_ex(const nufi_config *cfg, const nufi_options *opt, int device, nufi_handle **out);
+
 /* ---- reference-facing drop-in calls ------------------------------------ */
 /* cuda_kernel::compute_rho (nufi/cuda_kernel.cu:112-132, 289-311, 486-510):
  * rho := -w * sum over q in [q_begin, q_end) of f~(n, q), using slabs
@@ -189,12 +223,15 @@ int nufi_eval_points(nufi_handle *h, int64_t n, int mode, int64_t npts, const do
                      double *feet);
 /* The coefficient history as the reference's text files
  * (bin/test_nufi_cpu_3d_isolated.cpp:64-72, 190-211): a header of seven
- * lines (Nt, dt, Nx, Ny, Nz, order, blank) and one coefficient per line,
- * slabs 0..n1.  nufi_load_history also reads files without the header
- * (bin/test_nufi_gpu_1d.cpp:239, 364-366), uploads the whole slabs found
- * (as upload_phi) and returns their count; a header that disagrees with
- * the handle is NUFI_ERR_INVALID.  Resuming a run: load, then nufi_run
- * from the first missing step. */
+ * lines (Nt = the configuration's Nt, dt as std::to_string prints it, Nx,
+ * Ny, Nz, order, blank) and one coefficient per line, slabs 0..Nt: the
+ * computed slabs 0..n1, then zeros for the steps not computed yet (the
+ * reference's reader takes Nt + 1 slabs).  nufi_load_history also reads
+ * files without the header (bin/test_nufi_gpu_1d.cpp:239, 364-366), uploads
+ * the whole slabs found (as upload_phi) and returns their count without
+ * trailing all-zero slabs; a header that disagrees with the handle is
+ * NUFI_ERR_INVALID.  Resuming a run: load, then nufi_run from step
+ * *n_slabs. */
 int nufi_save_history(nufi_handle *h, int64_t n1, const char *path);
 int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs);
 
@@ -224,13 +261,15 @@ int nufi_backward(nufi_handle *h, int64_t n1, double *grad4);
  * velocity slice), one rho reduction and one field solve for all; the
  * whole run (and the whole adjoint sweep) is one CUDA-graph launch.
  * nufi_batch_create runs the autotuner (launch shapes timed on the device;
- * NUFI_BATCH_TUNE=0 keeps defaults) and reports its choice through
+ * nufi_options.batch_no_autotune keeps defaults) and reports its choice through
  * nufi_batch_describe.  nufi_batch_forward: J_i = 2 dt sum_n W_n of every
  * instance (count doubles, may be NULL).  nufi_batch_backward: dJ_i/d(alpha,
  * k, u_b, sigma_b) (count x 4 doubles; the FP64 adjoint of nufi_backward).
  * Errors: nufi_batch_last_error(batch) (or NULL after a failed create). */
 typedef struct nufi_batch nufi_batch;
 int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_batch **out);
+int nufi_batch_create_ex(const nufi_config *cfgs, int32_t count, const nufi_options *opt, int device,
+                         nufi_batch **out);
 int nufi_batch_destroy(nufi_batch *b);
 const char *nufi_batch_last_error(const nufi_batch *b);
 int nufi_batch_forward(nufi_batch *b, double *J);
@@ -284,6 +323,7 @@ int nufi_describe(const nufi_handle *h, char *buf, size_t len);
  * capacity planning; configuration errors as nufi_create's, via
  * nufi_last_error(NULL). */
 int nufi_plan(const nufi_config *cfg, int sms, char *buf, size_t len);
+int nufi_plan_ex(const nufi_config *cfg, const nufi_options *opt, int sms, char *buf, size_t len);
 /* No counterpart in the reference: the field solve's circulant kernels for
  * cfg, computed on the host with no CUDA call (what nufi_create uploads).
  * Row r of nconv rows of Ns values (x fastest) is G_r; with

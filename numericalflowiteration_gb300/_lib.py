@@ -32,6 +32,9 @@ _I64 = ctypes.c_int64
 SIGNATURES = {
     "nufi_last_error": (ctypes.c_char_p, [_P]),
     "nufi_create": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P)]),
+    "nufi_create_ex": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.POINTER(_P)]),
+    "nufi_plan_ex": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]),
+    "nufi_batch_create_ex": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int, _P]),
     "nufi_destroy": (ctypes.c_int, [_P]),
     "nufi_compute_rho": (ctypes.c_int, [_P, _I64, _I64, _I64]),
     "nufi_download_rho": (ctypes.c_int, [_P, _P]),
@@ -76,6 +79,32 @@ class NufiError(RuntimeError):
     pass
 
 
+class NufiOptionsC(ctypes.Structure):
+    """Byte-for-byte layout of ``struct nufi_options`` (launch options; every
+    field's 0 is the default)."""
+
+    _fields_ = [
+        ("split_global_loads", ctypes.c_int32),
+        ("split_plain_kick", ctypes.c_int32),
+        ("no_persistent", ctypes.c_int32),
+        ("split_ctas_per_sm", ctypes.c_int32),
+        ("split_threads_per_node", ctypes.c_int32),
+        ("batch_no_autotune", ctypes.c_int32),
+        ("batch_adjoint_ppt", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 9),
+    ]
+
+
+def options(opts: dict | None):
+    """A nufi_options struct from {field: value} (None: all defaults)."""
+    o = NufiOptionsC()
+    for k, v in (opts or {}).items():
+        if k == "reserved" or k not in dict(NufiOptionsC._fields_):
+            raise ValueError(f"unknown option {k!r}")
+        setattr(o, k, int(v))
+    return o
+
+
 def load(path: Path | None = None):
     """Load the CUDA library (raises if it is absent: there is no CPU path)."""
     global _lib
@@ -117,14 +146,16 @@ def _raise(code: int, msg: str):
     raise NufiError(f"[{code}] {msg}")
 
 
-def plan(cfg, sms: int = 152) -> dict:
-    """The launch plan a Simulation of cfg would choose on a device with
-    `sms` multiprocessors (nufi_plan), without touching CUDA."""
+def plan(cfg, sms: int = 152, opts: dict | None = None) -> dict:
+    """The launch plan a Simulation of cfg (with launch options `opts`)
+    would choose on a device with `sms` multiprocessors (nufi_plan_ex),
+    without touching CUDA."""
     import json
     lib = load()
     c = cfg.to_c()
+    o = options(opts)
     buf = ctypes.create_string_buffer(4096)
-    st = lib.nufi_plan(ctypes.byref(c), int(sms), buf, len(buf))
+    st = lib.nufi_plan_ex(ctypes.byref(c), ctypes.byref(o), int(sms), buf, len(buf))
     if st:
         _raise(st, lib.nufi_last_error(None).decode())
     return json.loads(buf.value.decode())
@@ -146,14 +177,17 @@ def solve_kernels(cfg) -> np.ndarray:
 
 
 class Simulation:
-    """One configuration on one GPU (one CUDA stream)."""
+    """One configuration on one GPU (one CUDA stream).  `opts`: launch
+    options (nufi_options fields, e.g. {"no_persistent": 1}); None keeps
+    the defaults."""
 
-    def __init__(self, cfg: Config, device: int = 0):
+    def __init__(self, cfg: Config, device: int = 0, opts: dict | None = None):
         self.cfg = cfg
         self._lib = load()
         self._c = cfg.to_c()
+        self._o = options(opts)
         h = ctypes.c_void_p()
-        st = self._lib.nufi_create(ctypes.byref(self._c), device, ctypes.byref(h))
+        st = self._lib.nufi_create_ex(ctypes.byref(self._c), ctypes.byref(self._o), device, ctypes.byref(h))
         if st:
             _raise(st, self._lib.nufi_last_error(None).decode())
         self._h = h
@@ -340,13 +374,14 @@ class Batch:
     """Many 1D instances advanced together (nufi_batch_*): one graph launch
     for the whole forward, one for the whole adjoint."""
 
-    def __init__(self, cfgs, device: int = 0):
+    def __init__(self, cfgs, device: int = 0, opts: dict | None = None):
         self.cfgs = list(cfgs)
         self._lib = load()
         arr = (NufiConfigC * len(self.cfgs))(*[c.to_c() for c in self.cfgs])
         self._arr = arr
+        self._o = options(opts)
         h = ctypes.c_void_p()
-        st = self._lib.nufi_batch_create(arr, len(self.cfgs), device, ctypes.byref(h))
+        st = self._lib.nufi_batch_create_ex(arr, len(self.cfgs), ctypes.byref(self._o), device, ctypes.byref(h))
         if st:
             _raise(st, self._lib.nufi_batch_last_error(None).decode())
         self._h = h

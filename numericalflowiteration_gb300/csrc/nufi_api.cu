@@ -40,6 +40,7 @@ thread_local std::string g_last_error = "";
 
 struct nufi_handle {
     nufi_config cfg{};
+    nufi_options opt{};
     Problem p{};
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -65,6 +66,12 @@ struct nufi_handle {
     std::vector<char> slab_set;   // slab n written (step, run, upload_phi)
     double *stage = nullptr;      // pinned staging buffer of upload_phi (one slab)
     cudaEvent_t stage_done = nullptr;
+    // Pinned block of the blocking calls: [0] the device error word (copied
+    // on the stream before the one synchronisation of a call), then rho
+    // (Ns), the field solve's slab (stride_t) and W, and its rho input (Ns).
+    double *pin = nullptr;
+    unsigned *pin_err = nullptr;
+    double *pin_rho = nullptr, *pin_slab = nullptr, *pin_rho_in = nullptr;
     std::vector<char> energy_set; // W_n recorded (step, run)
     SolvePlan plan;
     bool solve_ok = false;
@@ -286,9 +293,39 @@ Problem make_problem(const nufi_config &c)
     for (int i = 0; i < 8; ++i) p.f0p[i] = c.f0_params[i];
     p.wv = 1;
     for (int a = 0; a < c.dim; ++a) p.wv *= p.dv[a];
-    const char *plain = std::getenv("NUFI_SPLIT_PLAIN_KICK");
-    p.split_plain_kick = (plain && plain[0] == '1') ? 1 : 0;
+    p.split_plain_kick = 0;  // nufi_options.split_plain_kick, set by the caller
     return p;
+}
+
+// The launch options (nufi_options): NULL = all defaults; any other value
+// than the documented ones is refused.
+int validate_options(const nufi_options *o, nufi_options &out, std::string &why)
+{
+    out = nufi_options{};
+    if (!o) return NUFI_OK;
+    auto flag = [](int32_t v) { return v == 0 || v == 1; };
+    if (!flag(o->split_global_loads) || !flag(o->split_plain_kick) || !flag(o->no_persistent) ||
+        !flag(o->batch_no_autotune)) {
+        why = "options: flags must be 0 or 1";
+        return NUFI_ERR_INVALID;
+    }
+    if (o->split_ctas_per_sm < 0 || o->split_ctas_per_sm > 2 || o->split_threads_per_node < 0 ||
+        o->split_threads_per_node > 2) {
+        why = "options: split_ctas_per_sm and split_threads_per_node take 0, 1 or 2";
+        return NUFI_ERR_INVALID;
+    }
+    if (o->batch_adjoint_ppt != 0 && o->batch_adjoint_ppt != 1 && o->batch_adjoint_ppt != 2 &&
+        o->batch_adjoint_ppt != 4) {
+        why = "options: batch_adjoint_ppt takes 0, 1, 2 or 4";
+        return NUFI_ERR_INVALID;
+    }
+    for (int32_t r : o->reserved)
+        if (r != 0) {
+            why = "options: reserved fields must be 0";
+            return NUFI_ERR_INVALID;
+        }
+    out = *o;
+    return NUFI_OK;
 }
 
 // Trace tiling: the largest points-per-thread that still gives about four
@@ -317,14 +354,13 @@ LaunchShape choose_shape(const Problem &p, int sms)
 }
 
 // Trace launch shapes for p on a device with `sms` multiprocessors, with no
-// CUDA call (nufi_create and nufi_plan).  NUFI_SPLIT_STAGED=0 reads the
+// CUDA call (nufi_create and nufi_plan).  opt.split_global_loads reads the
 // split tables from global memory instead of the shared-memory ring.
-void plan_traces(const Problem &p, int sms, LaunchShape &shape, StagedShape &staged)
+void plan_traces(const Problem &p, int sms, const nufi_options &opt, LaunchShape &shape, StagedShape &staged)
 {
     shape = choose_shape(p, sms);
     staged = StagedShape{};
-    const char *env = std::getenv("NUFI_SPLIT_STAGED");
-    const bool no_ring = env && env[0] == '0';
+    const bool no_ring = opt.split_global_loads != 0;
     if (p.precision == NUFI_PREC_FP32_SPLIT && p.dim > 1) {
         staged = staged_shape_nd(p, sms);
         if (no_ring) {
@@ -332,7 +368,7 @@ void plan_traces(const Problem &p, int sms, LaunchShape &shape, StagedShape &sta
             staged.smem = 0;
         }
     } else if (p.precision == NUFI_PREC_FP32_SPLIT && !p.split_plain_kick && !no_ring) {
-        staged = staged_shape_1d(p, sms);
+        staged = staged_shape_1d(p, sms, opt.split_ctas_per_sm == 2 ? 2 : 1, opt.split_threads_per_node == 2 ? 2 : 1);
     }
 }
 
@@ -356,13 +392,12 @@ bool solve_geometry(const Problem &p, int sms, SolvePlan &pl, std::string &why)
 }
 
 // The whole-run kernel's shape where it applies (1D split with the staged
-// trace and the device solve); NUFI_PERSISTENT=0 turns it off.
+// trace and the device solve); opt.no_persistent turns it off.
 PersistentRun plan_persistent(const Problem &p, const StagedShape &staged, const SolvePlan &plan, bool solve_ok,
-                              int sms)
+                              int sms, const nufi_options &opt)
 {
     if (!(solve_ok && staged.ok)) return PersistentRun{};
-    const char *env = std::getenv("NUFI_PERSISTENT");
-    if (env && env[0] == '0') return PersistentRun{};
+    if (opt.no_persistent) return PersistentRun{};
     return persistent_shape_1d(p, staged, plan, sms);
 }
 
@@ -539,13 +574,12 @@ int build_split_tables(nufi_handle *h)
     return NUFI_OK;
 }
 
-// Read and clear the device error word (the stream must be idle).
-int check_device_flags(nufi_handle *h)
+// Turn the device error word `flags` (already read) into a status; a set
+// word is cleared on the device.
+int device_flags_status(nufi_handle *h, unsigned flags)
 {
-    unsigned flags = 0;
-    NUFI_CUDA(h, cudaMemcpy(&flags, h->err, sizeof(unsigned), cudaMemcpyDeviceToHost));
     if (flags) {
-        NUFI_CUDA(h, cudaMemset(h->err, 0, sizeof(unsigned)));
+        NUFI_CUDA(h, cudaMemsetAsync(h->err, 0, sizeof(unsigned), h->stream));
         std::string m = "device check failed:";
         if (flags & kErrCellIndex) m += " cell index out of range (non-finite position?)";
         if (flags & kErrKickRange) m += " split-mode kick displacement out of range";
@@ -566,10 +600,14 @@ void mark_steps(nufi_handle *h, int64_t n0, int64_t n1, bool energy)
     }
 }
 
+// Wait for the handle's stream and read its device error word: the word is
+// copied on the stream into pinned memory behind the work already queued,
+// so one synchronisation covers both.
 int sync_and_check(nufi_handle *h)
 {
+    NUFI_CUDA(h, cudaMemcpyAsync(h->pin_err, h->err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
     NUFI_CUDA(h, cudaStreamSynchronize(h->stream));
-    return check_device_flags(h);
+    return device_flags_status(h, *h->pin_err);
 }
 
 // Enqueue the trace of step n over [qb, qe) and the reduction into h->rho.
@@ -636,6 +674,8 @@ void release(nufi_handle *h)
     if (h->stage_done) cudaEventDestroy(h->stage_done);
     h->stage = nullptr;
     h->stage_done = nullptr;
+    if (h->pin) cudaFreeHost(h->pin);
+    h->pin = nullptr;
     if (h->stream) cudaStreamDestroy(h->stream);
     h->stream = nullptr;
 }
@@ -648,23 +688,32 @@ const char *nufi_last_error(const nufi_handle *h) { return h ? h->last_error.c_s
 
 int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
 {
+    return nufi_create_ex(cfg, nullptr, device, out);
+}
+
+int nufi_create_ex(const nufi_config *cfg, const nufi_options *opt, int device, nufi_handle **out)
+{
     if (!out) return fail(nullptr, NUFI_ERR_INVALID, "nufi_create: out is null");
     *out = nullptr;
     std::string why;
     int st = validate(cfg, why);
     if (st) return fail(nullptr, st, "nufi_create: " + why);
+    nufi_options o{};
+    if ((st = validate_options(opt, o, why))) return fail(nullptr, st, "nufi_create: " + why);
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
     if (device < 0 || device >= ndev) return fail(nullptr, NUFI_ERR_INVALID, "nufi_create: no such device");
     std::unique_ptr<nufi_handle> h(new nufi_handle);
     h->cfg = *cfg;
+    h->opt = o;
     h->device = device;
     h->p = make_problem(*cfg);
+    h->p.split_plain_kick = o.split_plain_kick;
     DeviceGuard g(device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    plan_traces(h->p, sms > 0 ? sms : 1, h->shape, h->staged);
+    plan_traces(h->p, sms > 0 ? sms : 1, h->opt, h->shape, h->staged);
     const Problem &p = h->p;
     const size_t partial_rows = size_t(std::max(h->shape.vblocks, h->staged.ok ? h->staged.ctas : 0));
     auto bail = [&](int code) {
@@ -680,12 +729,24 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
         (e = dalloc(h.get(), &h->rho, size_t(p.Ns))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->energy, nslab)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->rho_in, size_t(p.Ns))) != cudaSuccess ||
-        (e = dalloc(h.get(), &h->slab_out, size_t(p.hist_stride))) != cudaSuccess ||
-        (e = dalloc(h.get(), &h->energy_tmp, 1)) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->slab_out, size_t(p.hist_stride) + 1)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->mpartial, size_t(4 * ((p.Ns + 31) / 32) * h->shape.vblocks))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->metrics, 4)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->err, 1)) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMalloc"));
+    h->energy_tmp = h->slab_out + p.hist_stride;  // slab and W leave in one copy
+    {
+        const size_t pin_n = 2 + size_t(p.Ns) + size_t(p.hist_stride) + 1 + size_t(p.Ns);
+        void *pin = nullptr;
+        if ((e = cudaMallocHost(&pin, pin_n * sizeof(double))) != cudaSuccess)
+            return bail(cuda_fail(h.get(), e, "cudaMallocHost"));
+        h->pin = static_cast<double *>(pin);
+        h->pin_err = reinterpret_cast<unsigned *>(h->pin);
+        *h->pin_err = 0;
+        h->pin_rho = h->pin + 2;
+        h->pin_slab = h->pin_rho + p.Ns;
+        h->pin_rho_in = h->pin_slab + p.hist_stride + 1;
+    }
     if (p.precision == NUFI_PREC_FP32_SPLIT) {
         if ((e = dalloc(h.get(), &h->tables, nslab * p.table_stride)) != cudaSuccess)
             return bail(cuda_fail(h.get(), e, "cudaMalloc"));
@@ -703,7 +764,7 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
     h->slab_set.assign(nslab, 0);
     h->energy_set.assign(nslab, 0);
     h->aplan = adjoint_plan_1d(p);
-    h->persist = plan_persistent(p, h->staged, h->plan, h->solve_ok, sms > 0 ? sms : 1);
+    h->persist = plan_persistent(p, h->staged, h->plan, h->solve_ok, sms > 0 ? sms : 1, h->opt);
     if (h->persist.ok && ((e = dalloc(h.get(), &h->persist.sync, 2)) != cudaSuccess ||
                           (e = dalloc(h.get(), &h->persist.epart, nslab * size_t(p.N[0]))) != cudaSuccess))
         return bail(cuda_fail(h.get(), e, "cudaMalloc"));
@@ -735,11 +796,11 @@ int nufi_compute_rho(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end)
     return enqueue_trace(h, n, q_begin, q_end, 0);
 }
 
-static int download_rho_impl(nufi_handle *h, std::vector<double> &tmp)
+// rho into the pinned block, then one synchronisation (with the error word)
+static int download_rho_impl(nufi_handle *h)
 {
     DeviceGuard g(h->device);
-    tmp.resize(size_t(h->p.Ns));
-    NUFI_CUDA(h, cudaMemcpyAsync(tmp.data(), h->rho, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+    NUFI_CUDA(h, cudaMemcpyAsync(h->pin_rho, h->rho, size_t(h->p.Ns) * sizeof(double), cudaMemcpyDeviceToHost,
                                  h->stream));
     return sync_and_check(h);
 }
@@ -747,10 +808,10 @@ static int download_rho_impl(nufi_handle *h, std::vector<double> &tmp)
 int nufi_download_rho(nufi_handle *h, double *rho)
 {
     if (!h || !rho) return fail(h, NUFI_ERR_INVALID, "null argument");
-    std::vector<double> tmp;
-    int st = download_rho_impl(h, tmp);
+    int st = download_rho_impl(h);
     if (st) return st;
-    for (size_t i = 0; i < tmp.size(); ++i) rho[i] += tmp[i];
+    const double *src = h->pin_rho;
+    for (long long i = 0; i < h->p.Ns; ++i) rho[i] += src[i];
     return NUFI_OK;
 }
 
@@ -791,10 +852,10 @@ int nufi_download_metrics(nufi_handle *h, double *metrics4)
 int nufi_download_rho_f32(nufi_handle *h, float *rho)
 {
     if (!h || !rho) return fail(h, NUFI_ERR_INVALID, "null argument");
-    std::vector<double> tmp;
-    int st = download_rho_impl(h, tmp);
+    int st = download_rho_impl(h);
     if (st) return st;
-    for (size_t i = 0; i < tmp.size(); ++i) rho[i] += float(tmp[i]);
+    const double *src = h->pin_rho;
+    for (long long i = 0; i < h->p.Ns; ++i) rho[i] += float(src[i]);
     return NUFI_OK;
 }
 
@@ -947,17 +1008,30 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
     if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
     const Problem &p = h->p;
     DeviceGuard g(h->device);
-    NUFI_CUDA(h, cudaMemcpyAsync(h->rho_in, rho, size_t(p.Ns) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    cudaError_t e = launch_field_solve(p, h->plan, h->rho_in, h->slab_out, nullptr, h->energy_tmp, h->stream);
-    if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
-    h->launches += 1;
-    NUFI_CUDA(h, cudaMemcpyAsync(slab_out, h->slab_out, size_t(p.stride_t) * sizeof(double), cudaMemcpyDeviceToHost,
-                                 h->stream));
-    double en = 0;
-    NUFI_CUDA(h, cudaMemcpyAsync(&en, h->energy_tmp, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    // Every call leaves with its copies complete (synchronised, also on
+    // failure), so the pinned input is free to overwrite here.
+    std::memcpy(h->pin_rho_in, rho, size_t(p.Ns) * sizeof(double));
+    cudaError_t e = cudaMemcpyAsync(h->rho_in, h->pin_rho_in, size_t(p.Ns) * sizeof(double), cudaMemcpyHostToDevice,
+                                    h->stream);
+    const char *what = "rho copy";
+    if (e == cudaSuccess) {
+        e = launch_field_solve(p, h->plan, h->rho_in, h->slab_out, nullptr, h->energy_tmp, h->stream);
+        what = "field solve launch";
+        if (e == cudaSuccess) h->launches += 1;
+    }
+    if (e == cudaSuccess) {  // slab and W (adjacent on the device) in one copy
+        e = cudaMemcpyAsync(h->pin_slab, h->slab_out, (size_t(p.hist_stride) + 1) * sizeof(double),
+                            cudaMemcpyDeviceToHost, h->stream);
+        what = "slab copy";
+    }
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(h->stream);
+        return cuda_fail(h, e, what);
+    }
     int st = sync_and_check(h);
     if (st) return st;
-    if (energy) *energy = en;
+    std::memcpy(slab_out, h->pin_slab, size_t(p.stride_t) * sizeof(double));
+    if (energy) *energy = h->pin_slab[p.hist_stride];
     return NUFI_OK;
 }
 
@@ -1097,8 +1171,12 @@ int nufi_eval_points(nufi_handle *h, int64_t n, int mode, int64_t npts, const do
 // Coefficient history as text in the reference's layout
 // (bin/test_nufi_cpu_3d_isolated.cpp:64-72, 190-211): seven header lines
 // "Nt = ", "dt = ", "Nx = ", "Ny = ", "Nz = ", "order = " and a blank one,
-// then every coefficient of slabs 0..n1, one per line, slab after slab.
-// 17 significant digits, so FP64 values read back exactly.
+// then every coefficient of slabs 0..Nt, one per line, slab after slab.
+// As the reference, the header's Nt is the configuration's Nt and dt is
+// printed as std::to_string prints it (six decimals); the reference's
+// reader takes Nt + 1 slabs whatever the header says, so slabs after n1
+// (not computed yet) are written as zeros.  Values carry 17 significant
+// digits, so FP64 values read back exactly.
 int nufi_save_history(nufi_handle *h, int64_t n1, const char *path)
 {
     if (!h || !path) return fail(h, NUFI_ERR_INVALID, "null argument");
@@ -1109,16 +1187,20 @@ int nufi_save_history(nufi_handle *h, int64_t n1, const char *path)
     if (st) return st;
     FILE *f = std::fopen(path, "w");
     if (!f) return fail(h, NUFI_ERR_INVALID, std::string("save_history: cannot open ") + path);
-    std::fprintf(f, "Nt = %lld\ndt = %.17g\nNx = %d\nNy = %d\nNz = %d\norder = %d\n\n", (long long)n1, p.dt,
+    std::fprintf(f, "Nt = %lld\ndt = %f\nNx = %d\nNy = %d\nNz = %d\norder = %d\n\n", (long long)h->cfg.Nt, p.dt,
                  p.N[0], p.dim > 1 ? p.N[1] : 1, p.dim > 2 ? p.N[2] : 1, p.order);
     for (double v : all) std::fprintf(f, "%.17g\n", v);
+    for (long long i = (long long)(n1 + 1) * p.stride_t; i < (long long)(h->cfg.Nt + 1) * p.stride_t; ++i)
+        std::fputs("0\n", f);
     const bool ok = std::fclose(f) == 0;
     return ok ? NUFI_OK : fail(h, NUFI_ERR_INVALID, "save_history: write failed");
 }
 
 // Reads such a file (or one without the header, as bin/test_nufi_gpu_1d.cpp
-// writes) and uploads its slabs 0..n-1; *n_slabs = n.  A header that
-// disagrees with the handle's grid or order is NUFI_ERR_INVALID.
+// writes) and uploads its slabs 0..n-1; *n_slabs = n, where trailing
+// all-zero slabs (the steps a partial save had not computed) are not
+// counted, so a resumed run starts at step n.  A header that disagrees
+// with the handle's grid or order is NUFI_ERR_INVALID.
 int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs)
 {
     if (!h || !path) return fail(h, NUFI_ERR_INVALID, "null argument");
@@ -1164,9 +1246,14 @@ int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs)
     for (int i = 0; i < 4; ++i)
         if (hdr[i] >= 0 && hdr[i] != want[i])
             return fail(h, NUFI_ERR_INVALID, "load_history: header does not match the handle's grid or order");
-    const long long ns = (long long)(vals.size() / size_t(p.stride_t));
+    long long ns = (long long)(vals.size() / size_t(p.stride_t));
     if (ns < 1 || ns > h->cfg.Nt + 1)
         return fail(h, NUFI_ERR_RANGE, "load_history: no whole slab, or more than Nt + 1 slabs");
+    while (ns > 1) {  // drop trailing all-zero slabs
+        const double *sl = vals.data() + (ns - 1) * p.stride_t;
+        if (!std::all_of(sl, sl + p.stride_t, [](double v) { return v == 0.0; })) break;
+        --ns;
+    }
     for (long long n = 0; n < ns; ++n) {
         const int st = upload_slab(h, n, vals.data() + n * p.stride_t);
         if (st) return st;
@@ -1240,17 +1327,24 @@ int nufi_describe(const nufi_handle *h, char *buf, size_t len)
 
 int nufi_plan(const nufi_config *cfg, int sms, char *buf, size_t len)
 {
+    return nufi_plan_ex(cfg, nullptr, sms, buf, len);
+}
+
+int nufi_plan_ex(const nufi_config *cfg, const nufi_options *opt, int sms, char *buf, size_t len)
+{
     if (!buf || len == 0) return fail(nullptr, NUFI_ERR_INVALID, "nufi_plan: null argument");
     if (sms < 1 || sms > 4096) return fail(nullptr, NUFI_ERR_INVALID, "nufi_plan: sms outside [1, 4096]");
     std::string why;
-    const int st = validate(cfg, why);
+    int st = validate(cfg, why);
     if (st) return fail(nullptr, st, "nufi_plan: " + why);
     nufi_handle h;  // planning only: no stream, no device memory
+    if ((st = validate_options(opt, h.opt, why))) return fail(nullptr, st, "nufi_plan: " + why);
     h.cfg = *cfg;
     h.p = make_problem(*cfg);
-    plan_traces(h.p, sms, h.shape, h.staged);
+    h.p.split_plain_kick = h.opt.split_plain_kick;
+    plan_traces(h.p, sms, h.opt, h.shape, h.staged);
     h.solve_ok = solve_geometry(h.p, sms, h.plan, h.solve_why);
-    h.persist = plan_persistent(h.p, h.staged, h.plan, h.solve_ok, sms);
+    h.persist = plan_persistent(h.p, h.staged, h.plan, h.solve_ok, sms, h.opt);
     h.aplan = adjoint_plan_1d(h.p);
     return copy_out(plan_json(&h, true), buf, len, "nufi_plan");
 }
@@ -1281,6 +1375,7 @@ int nufi_solve_kernels(const nufi_config *cfg, double *kernels, int64_t len, int
 // ---------------------------------------------------------------------------
 struct nufi_batch {
     int device = 0;
+    nufi_options opt{};
     cudaStream_t stream = nullptr;
     int precision = 0;
     std::vector<nufi_handle *> inst;
@@ -1395,12 +1490,11 @@ float batch_time(nufi_batch *b, F fn, int reps)
 
 // The autotuner: times the candidate launch shapes of the batched trace
 // (chains per thread, slabs per ring chunk) at a mid-run step and of the
-// adjoint trace (chains per thread), keeps the fastest.  NUFI_BATCH_TUNE=0
-// keeps the defaults.
+// adjoint trace (chains per thread), keeps the fastest.  The option
+// batch_no_autotune keeps the defaults.
 int batch_autotune(nufi_batch *b)
 {
-    const char *env = std::getenv("NUFI_BATCH_TUNE");
-    const bool tune = !(env && env[0] == '0');
+    const bool tune = !b->opt.batch_no_autotune;
     const int n_t = std::max(1, b->maxNt / 2);
     size_t ts_max = 0;
     for (nufi_handle *h : b->inst) ts_max = std::max<size_t>(ts_max, size_t(h->p.table_stride));
@@ -1440,9 +1534,8 @@ int batch_autotune(nufi_batch *b)
     const bool split = b->precision == NUFI_PREC_FP32_SPLIT;
     std::vector<int> acands = tune ? (split ? std::vector<int>{2, 4} : std::vector<int>{1, 2, 4})
                                    : std::vector<int>{split ? 4 : 2};
-    // NUFI_BATCH_ADJ_PPT=k fixes the adjoint's chains per thread
-    if (const char *ap = std::getenv("NUFI_BATCH_ADJ_PPT")) {
-        const int k = std::atoi(ap);
+    // the option batch_adjoint_ppt = k fixes the adjoint's chains per thread
+    if (const int k = b->opt.batch_adjoint_ppt) {
         if (split ? (k == 2 || k == 4) : (k == 1 || k == 2 || k == 4)) acands = {k};
     }
     // FP32-split adjoint: a persistent grid (CTAs per SM from the occupancy
@@ -1538,8 +1631,20 @@ extern "C" {
 
 int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_batch **out)
 {
+    return nufi_batch_create_ex(cfgs, count, nullptr, device, out);
+}
+
+int nufi_batch_create_ex(const nufi_config *cfgs, int32_t count, const nufi_options *opt, int device,
+                         nufi_batch **out)
+{
     if (!out || !cfgs || count <= 0) return bfail(nullptr, NUFI_ERR_INVALID, "nufi_batch_create: bad arguments");
     *out = nullptr;
+    nufi_options o{};
+    {
+        std::string why;
+        const int st = validate_options(opt, o, why);
+        if (st) return bfail(nullptr, st, "nufi_batch_create: " + why);
+    }
     for (int32_t i = 0; i < count; ++i) {
         const nufi_config &c = cfgs[i];
         if (c.dim != 1 || c.order != 4 || c.precision != cfgs[0].precision)
@@ -1549,6 +1654,7 @@ int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_b
     }
     std::unique_ptr<nufi_batch> b(new nufi_batch);
     b->device = device;
+    b->opt = o;
     b->precision = cfgs[0].precision;
     auto bail = [&](int code) {
         const std::string msg = b->last_error;
@@ -1558,7 +1664,7 @@ int nufi_batch_create(const nufi_config *cfgs, int32_t count, int device, nufi_b
     };
     for (int32_t i = 0; i < count; ++i) {
         nufi_handle *h = nullptr;
-        int st = nufi_create(&cfgs[i], device, &h);
+        int st = nufi_create_ex(&cfgs[i], &o, device, &h);
         if (st) {
             b->last_error = "instance " + std::to_string(i) + ": " + g_last_error;
             return bail(st);

@@ -49,7 +49,7 @@ struct Problem {
     double f0p[8];
     double wv;           // prod_d dv_d, the quadrature weight of rho
     int split_plain_kick;  // split mode: 1 = uncompensated FP32 kick sum
-                           // (NUFI_SPLIT_PLAIN_KICK=1 at create; for measuring
+                           // (nufi_options.split_plain_kick; for measuring
                            // what the compensation buys)
 };
 

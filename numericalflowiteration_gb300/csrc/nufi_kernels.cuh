@@ -121,7 +121,7 @@ struct StagedShape {
     int ring = 3;  // shared-memory ring slots (0: 2D/3D tables read from global memory)
     size_t smem = 0;
 };
-StagedShape staged_shape_1d(const Problem &p, int sms);
+StagedShape staged_shape_1d(const Problem &p, int sms, int ctas_per_sm = 1, int threads_per_node = 1);
 // FP32-split 2D/3D trace (trace_split_nd.cu).
 StagedShape staged_shape_nd(const Problem &p, int sms);
 cudaError_t launch_trace_split_nd(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,

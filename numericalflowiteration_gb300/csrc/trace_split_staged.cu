@@ -147,15 +147,14 @@ cudaError_t launch_staged_ppt(const Problem &p, const StagedShape &sh, const flo
 
 }  // namespace
 
-StagedShape staged_shape_1d(const Problem &p, int sms)
+StagedShape staged_shape_1d(const Problem &p, int sms, int cps, int tpn_opt)
 {
     StagedShape sh;
     if (p.dim != 1 || p.N[0] > 256) return sh;  // not applicable (one thread per spatial node)
     const long long Nm = p.Nm;
-    // CTAs per SM: 1 by default; NUFI_SPLIT_CTAS_PER_SM=2 runs two smaller
-    // CTAs per SM (more warps, fewer chains each)
-    const char *cps_env = std::getenv("NUFI_SPLIT_CTAS_PER_SM");
-    const int cps = (cps_env && cps_env[0] == '2') ? 2 : 1;
+    // CTAs per SM (cps): 1 by default; 2 runs two smaller CTAs per SM (more
+    // warps, fewer chains each)
+    cps = cps == 2 ? 2 : 1;
     int G = int(std::min<long long>(Nm, (long long)sms * cps));
     int ppt = int((Nm + G - 1) / G);
     if (ppt > kStagedMaxPPT) {
@@ -170,13 +169,12 @@ StagedShape staged_shape_1d(const Problem &p, int sms)
     const size_t kOneCtaPerSm = cps == 2 ? 72 * 1024 : 120 * 1024;
     int S = int(std::max<size_t>(1, std::min<size_t>(32, kOneCtaPerSm / (size_t(kRing) * slab_bytes))));
     if (size_t(kRing) * S * slab_bytes > 200 * 1024) return sh;
-    // Threads per spatial node: 1 (measured faster on the two-stream
-    // workload: the loop is bound by shared-memory bandwidth, which more
-    // warps do not add); NUFI_SPLIT_TPN=2 splits the chains over two
+    // Threads per spatial node: 1 by default (measured faster on the
+    // two-stream workload: the loop is bound by shared-memory bandwidth,
+    // which more warps do not add); tpn_opt = 2 splits the chains over two
     // threads per node.
     const int Nr = (p.N[0] + 31) / 32 * 32;
-    const char *tpn_env = std::getenv("NUFI_SPLIT_TPN");
-    const int tpn = (tpn_env && tpn_env[0] == '2' && ppt >= 2 && 2 * Nr <= 512) ? 2 : 1;
+    const int tpn = (tpn_opt == 2 && ppt >= 2 && 2 * Nr <= 512) ? 2 : 1;
     sh.ctas = G;
     sh.tpn = tpn;
     sh.ppt = (ppt + tpn - 1) / tpn;

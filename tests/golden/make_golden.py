@@ -1,8 +1,10 @@
 """Generate the golden vectors in tests/golden/ from the REFERENCE's own
 code, built from its sources by oracle/ref/Makefile into oracle/_ref/.
 
-Run here (where the reference sources are mounted):
-    python tests/golden/make_golden.py [--ref /root/reference]
+Run where the reference sources are present (REF = their directory):
+    python tests/golden/make_golden.py --ref REF [--only NAME] [--full]
+(or set NUFI_REFERENCE_DIR instead of --ref).  --full adds the cases at
+the benchmark configurations' own sizes, which take many minutes each.
 
 Each case runs `ref_driver run` (the reference's eval_ftilda / eval /
 splines / poisson::solve / interpolate with LSMR, on the configured f0) and
@@ -67,6 +69,17 @@ RUN_CASES = {
     "params_bump_hi_1d_128x512_n40": (bump_on_tail_1d(Nx=128, Nv=512, Nt=40, alpha=0.01, k=0.5, u_b=5.0,
                                                       sigma_b=0.6), 40, [0, 1, 20, 40], [0, 20, 40]),
     "params_landau_k03_1d_64x256_n60": (landau_1d(Nt=60, alpha=0.05, k=0.3), 60, [0, 1, 30, 60], [0, 30, 60]),
+}
+
+# The benchmark configurations at their own sizes (generated with --full):
+# the two-stream 256 x 1024 run over all 800 steps, the 2D Landau
+# 32^2 x 64^2 run over all 160 steps, and the first 10 steps of the 3D
+# Landau 16^3 x 32^3 run (its whole run is hours of CPU time; its later
+# steps are pinned by FULL_POINT_CASES below)
+FULL_RUN_CASES = {
+    "two_stream_1d_256x1024_T50": (two_stream_1d(), 800, [0, 1, 200, 400, 600, 800], [0, 400, 799, 800]),
+    "landau_2d_32x64_T20": (landau_2d(), 160, [0, 1, 40, 80, 160], [0, 80, 159, 160]),
+    "landau_3d_16x32_n10": (landau_3d(), 10, [0, 1, 5, 10], [0, 10]),
 }
 
 # name -> (config, metrics steps): the reference's eval_f metrics of its own
@@ -155,9 +168,13 @@ def solve_case(name, cfg, tmp: Path, seed: int):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("NUFI_REFERENCE_DIR"),
+                    help="directory of the reference sources (default: $NUFI_REFERENCE_DIR)")
     ap.add_argument("--only", default=None)
+    ap.add_argument("--full", action="store_true", help="also the cases at the benchmark sizes (slow)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("the reference sources are needed: --ref REF or NUFI_REFERENCE_DIR")
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle" / "ref"), f"REF={args.ref}"], check=True)
     manifest = {"generator": "tests/golden/make_golden.py", "driver": "oracle/ref/ref_driver.cpp",
                 "cases": {}}
@@ -166,7 +183,8 @@ def main():
         manifest = json.loads(mpath.read_text())
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)
-        for name, (cfg, n_last, rk, sk) in RUN_CASES.items():
+        cases = dict(RUN_CASES, **(FULL_RUN_CASES if args.full else {}))
+        for name, (cfg, n_last, rk, sk) in cases.items():
             if args.only and args.only not in name:
                 continue
             manifest["cases"][name] = run_case(name, cfg, n_last, rk, sk, tmp)

@@ -334,3 +334,19 @@ def test_batch_python_errors(lib):
         nufi.Batch([])
     with pytest.raises(NotImplementedError):
         nufi.Batch([landau_2d(Nx=8, Nv=8, Nt=4)])
+
+
+def test_options_layout_matches_c(tmp_path):
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "opt.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "nufi_gb300.h"\n'
+        "int main(void){printf(\"%zu %zu %zu\\n\", sizeof(nufi_options), offsetof(nufi_options, batch_adjoint_ppt),"
+        " offsetof(nufi_options, reserved));return 0;}\n")
+    exe = tmp_path / "opt"
+    subprocess.run([gcc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = list(map(int, subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()))
+    O = _lib.NufiOptionsC
+    assert got == [ctypes.sizeof(O), O.batch_adjoint_ppt.offset, O.reserved.offset]

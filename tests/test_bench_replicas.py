@@ -112,7 +112,7 @@ def test_reference_arm_line():
     """bench.py --impl reference (the oracle port on the host cores, a
     bounded sample per step) prints one line with the contract's keys and a
     zero-copy e2e; under a multi-rank launch only rank 0 prints."""
-    (line,) = _bench(["--impl", "reference", "--steps", "1", "--warmup", "3", "--ref-steps", "2"])
+    (line,) = _bench(["--impl", "reference", "--steps", "1", "--warmup", "3", "--cpu-windows", "0:3,10:2,-1:1"])
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
                 "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert key in line, key
@@ -122,5 +122,15 @@ def test_reference_arm_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
-    assert _bench(["--impl", "reference", "--steps", "1", "--warmup", "3", "--ref-steps", "2"],
+    # the same workload as the GPU arm: the whole run's rate, extrapolated
+    # from the timed windows by the fitted per-step cost c0 + c1 n
+    cb = line["cpu_baseline"]
+    assert line["config"]["same_config"] is True and cb["same_config"] is True
+    assert cb["fit_c0_s"] >= 0 and cb["fit_c1_s"] > 0 and "0..2,10..11,800..800" in cb["sample"]
+    nt = line["config"]["Nt"]
+    assert abs(cb["full_run_s_extrapolated"] - ((nt + 1) * cb["fit_c0_s"] + cb["fit_c1_s"] * nt * (nt + 1) / 2)) \
+        <= 1e-9 * cb["full_run_s_extrapolated"]
+    assert abs(line["value"] * cb["full_run_s_extrapolated"] - line["config"]["point_steps_per_step"]) \
+        <= 1e-9 * line["config"]["point_steps_per_step"]
+    assert _bench(["--impl", "reference", "--steps", "1", "--warmup", "3", "--cpu-windows", "0:3,10:2,-1:1"],
                   {"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []

@@ -200,7 +200,7 @@ def test_split_dropin_matches_fp64(nufi):
 
 
 @pytest.mark.parametrize("cfgname", ["two_stream_1d_64x256_T50", "landau_1d_64x256_T30"])
-def test_split_staged_matches_unstaged(nufi, cfgname, monkeypatch):
+def test_split_staged_matches_unstaged(nufi, cfgname):
     """The shared-memory staged split trace (default: two-level kick sum)
     against the global-load form (Kahan-compensated kick per substep): two
     FP32-split arithmetics, each within the split gate of the FP64 history
@@ -209,8 +209,7 @@ def test_split_staged_matches_unstaged(nufi, cfgname, monkeypatch):
     cfg = cfg.replace(precision="fp32split", Nt=min(cfg.Nt, 300))
     with nufi.Simulation(cfg) as a:
         ea = a.run()
-    monkeypatch.setenv("NUFI_SPLIT_STAGED", "0")
-    with nufi.Simulation(cfg) as b:
+    with nufi.Simulation(cfg, opts={"split_global_loads": 1}) as b:
         eb = b.run()
     assert rel_max(ea, eb) <= 1e-6
     assert rel_max(ea, g["energy"][:cfg.Nt + 1]) <= 1e-6
@@ -218,7 +217,7 @@ def test_split_staged_matches_unstaged(nufi, cfgname, monkeypatch):
 
 
 @pytest.mark.parametrize("cfgname", ["two_stream_1d_64x256_T50", "landau_1d_64x256_T30", "bump_on_tail_1d_64x256_T20"])
-def test_persistent_run_matches_per_step_launches(nufi, cfgname, monkeypatch):
+def test_persistent_run_matches_per_step_launches(nufi, cfgname):
     """nufi_run as one cooperative launch (all steps, grid barriers between
     the phases) against the graph of per-step launches: same arithmetic,
     only the order of a few FP64 sums differs."""
@@ -228,8 +227,7 @@ def test_persistent_run_matches_per_step_launches(nufi, cfgname, monkeypatch):
         ea = a.run()
         ha = a.history()
         ra = a.download_rho(np.zeros(cfg.n_spatial))
-    monkeypatch.setenv("NUFI_PERSISTENT", "0")
-    with nufi.Simulation(cfg) as b:
+    with nufi.Simulation(cfg, opts={"no_persistent": 1}) as b:
         eb = b.run()
         hb = b.history()
         rb = b.download_rho(np.zeros(cfg.n_spatial))
@@ -255,7 +253,7 @@ def test_persistent_run_subrange_and_repeat(nufi):
 
 
 @pytest.mark.parametrize("cfgname", ["landau_2d_16x16_T20", "landau_3d_8x8_T2", "small_landau_2d_8x8"])
-def test_split_nd_staged_matches_global_loads(nufi, cfgname, monkeypatch):
+def test_split_nd_staged_matches_global_loads(nufi, cfgname):
     """2D/3D split trace with the slab tables streamed through shared memory
     against the same kernel reading them from global memory: same chunking
     of the kick sum, so the same bits."""
@@ -264,8 +262,7 @@ def test_split_nd_staged_matches_global_loads(nufi, cfgname, monkeypatch):
     with nufi.Simulation(cfg) as a:
         ea = a.run()
         ra = a.download_rho(np.zeros(cfg.n_spatial))
-    monkeypatch.setenv("NUFI_SPLIT_STAGED", "0")
-    with nufi.Simulation(cfg) as b:
+    with nufi.Simulation(cfg, opts={"split_global_loads": 1}) as b:
         eb = b.run()
         rb = b.download_rho(np.zeros(cfg.n_spatial))
     assert np.array_equal(ea, eb)

@@ -73,8 +73,12 @@ def test_history_round_trip_and_resume(nufi, tmp_path):
         a.save_history(tmp_path / "h.txt", 30)
         hist = a.history()
     text = (tmp_path / "h.txt").read_text().splitlines()
-    assert text[0].startswith("Nt = 30") and text[2] == "Nx = 32" and text[5] == "order = 4" and text[6] == ""
-    assert len(text) == 7 + 31 * cfg.stride_t
+    # the reference's header: the configuration's Nt, dt as std::to_string
+    assert text[0] == "Nt = 60" and text[1] == "dt = 0.062500" and text[2] == "Nx = 32"
+    assert text[5] == "order = 4" and text[6] == ""
+    # all Nt + 1 slabs, as the reference's reader takes; zeros after step 30
+    assert len(text) == 7 + 61 * cfg.stride_t
+    assert all(v == "0" for v in text[7 + 31 * cfg.stride_t:])
     with nufi.Simulation(cfg) as b:
         assert b.load_history(tmp_path / "h.txt") == 31
         e_rest = b.run(31, cfg.Nt)

@@ -185,3 +185,25 @@ def test_plan_errors():
         plan(landau_1d(order=12))
     with pytest.raises(IndexError):
         plan(landau_1d(Nt=2 ** 31))
+
+
+def test_launch_options_select_the_kernels():
+    """nufi_options (no environment variables): each option picks the
+    kernel or shape it documents, and an invalid value is refused before
+    any CUDA call."""
+    cfg = two_stream_1d(precision="fp32split")
+    assert plan(cfg, 152)["run"] == "run_split_1d_kernel"
+    assert plan(cfg, 152, {"no_persistent": 1})["run"] == "graph of per-step launches"
+    pl = plan(cfg, 152, {"split_global_loads": 1})
+    assert pl["trace"] == "trace_split_1d_kernel" and pl["staged"]["ok"] == 0
+    assert plan(cfg, 152, {"split_plain_kick": 1})["trace"] == "trace_split_1d_kernel"
+    assert plan(cfg, 152, {"split_ctas_per_sm": 2})["staged"]["ctas"] == 304
+    assert plan(cfg, 152, {"split_threads_per_node": 2})["staged_tpn"] == 2
+    pl = plan(landau_2d(precision="fp32split"), 152, {"split_global_loads": 1})
+    assert pl["staged"]["ring"] == 0 and pl["staged"]["smem"] == 0
+    for bad in ({"no_persistent": 2}, {"split_ctas_per_sm": 3}, {"batch_adjoint_ppt": 3},
+                {"split_threads_per_node": -1}):
+        with pytest.raises(ValueError):
+            plan(cfg, 152, bad)
+    with pytest.raises(ValueError):
+        plan(cfg, 152, {"not_an_option": 1})

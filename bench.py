@@ -300,6 +300,52 @@ def run_reference(args, cfg):
     return 0
 
 
+def e2e_c_loop(cfg, device: int, repeats: int, ws: int, ps: int):
+    """End to end through the C ABI with host buffers: the reference
+    drivers' loop (compute_rho, download_rho, field solve of the host rho,
+    upload_phi) as a compiled C++ caller runs it (numericalflowiteration_gb300/
+    e2e_loop.cpp), the median of `repeats` whole runs after one untimed run."""
+    import tempfile
+    exe = ROOT / "numericalflowiteration_gb300" / "e2e_loop"
+    with tempfile.TemporaryDirectory() as td:
+        cf = Path(td) / "cfg.bin"
+        cf.write_bytes(cfg.to_bytes())
+        r = subprocess.run([str(exe), str(cf), str(repeats), str(device)], capture_output=True, text=True,
+                           timeout=1800)
+    if r.returncode != 0:
+        raise RuntimeError(f"e2e_loop failed ({r.returncode}): {r.stderr[-2000:]}")
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    return {"value": ws * ps / d["seconds"], "unit": UNIT, "ms_per_step": d["seconds"] * 1e3,
+            "h2d_bytes_per_step": d["h2d_bytes"], "d2h_bytes_per_step": d["d2h_bytes"], "repeats": repeats,
+            "path": "C ABI with host buffers, the reference drivers' loop compiled as a C++ caller "
+                    "(compute_rho, download_rho, field_solve, upload_phi per time step)"}
+
+
+def e2e_python_loop(nufi, cfg, device: int, repeats: int, ws: int, ps: int):
+    """The same loop through the Python binding (ctypes), for comparison."""
+    import torch
+    sim2 = nufi.Simulation(cfg, device=device)
+    rho = np.zeros(cfg.n_spatial)
+    coeffs = np.zeros((cfg.Nt + 1) * cfg.stride_t)
+    times = []
+    for rep in range(1 + repeats):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for n in range(cfg.Nt + 1):
+            rho[:] = 0
+            sim2.compute_rho(n)
+            sim2.download_rho(rho)
+            slab, _ = sim2.field_solve(rho)
+            coeffs[n * cfg.stride_t:(n + 1) * cfg.stride_t] = slab
+            sim2.upload_phi(n, coeffs)
+        torch.cuda.synchronize()
+        if rep > 0:
+            times.append(time.perf_counter() - t0)
+    sim2.close()
+    s = statistics.median(times)
+    return {"value": ws * ps / s, "ms_per_step": s * 1e3}
+
+
 def run_ours(args, cfg):
     import torch
     import numericalflowiteration_gb300 as nufi
@@ -431,30 +477,8 @@ def run_ours(args, cfg):
     # -> field solve (host rho in, host slab out) -> upload_phi, per step.
     e2e = None
     if not args.no_e2e:
-        sim2 = nufi.Simulation(cfg_split, device=local)
-        rho = np.zeros(cfg.n_spatial)
-        coeffs = np.zeros((cfg.Nt + 1) * cfg.stride_t)
-        e2e_times = []
-        for rep in range(1 + max(1, args.steps // 2)):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            for n in range(cfg.Nt + 1):
-                rho[:] = 0
-                sim2.compute_rho(n)
-                sim2.download_rho(rho)
-                slab, _ = sim2.field_solve(rho)
-                coeffs[n * cfg.stride_t:(n + 1) * cfg.stride_t] = slab
-                sim2.upload_phi(n, coeffs)
-            torch.cuda.synchronize()
-            if rep > 0:
-                e2e_times.append(time.perf_counter() - t0)
-        sim2.close()
-        e2e_s = statistics.median(e2e_times)
-        steps = cfg.Nt + 1
-        e2e = {"value": ws * ps / e2e_s, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
-               "h2d_bytes_per_step": steps * 8 * (cfg.n_spatial + cfg.stride_t),
-               "d2h_bytes_per_step": steps * 8 * (cfg.n_spatial + cfg.stride_t + 1),
-               "path": "drop-in C ABI loop with host buffers (compute_rho, download_rho, field_solve, upload_phi)"}
+        e2e = e2e_c_loop(cfg_split, local, max(2, args.steps), ws, ps)
+        e2e["python_loop"] = e2e_python_loop(nufi, cfg_split, local, max(1, args.steps // 2), ws, ps)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:

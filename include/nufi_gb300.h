@@ -281,9 +281,11 @@ int nufi_batch_describe(const nufi_batch *b, char *buf, size_t len);
 /* ---- allocation-free rho ------------------------------------------------
  * No counterpart in the reference.  rho of step n over [q_begin, q_end)
  * for callers that must not allocate device memory (no cudaMalloc, no
- * allocating library call): for example code running inside someone
- * else's CUDA-graph capture or memory pool, or a real-time loop whose
- * device memory is reserved up front.  FP64 plain form only.  The caller
+ * allocating library call): a plugin hosted by a framework that owns all
+ * device memory through its own pool and forbids direct allocation, or a
+ * real-time loop that reserves its device memory up front because
+ * cudaMalloc can synchronise the device and take unbounded time.  FP64
+ * plain form only.  The caller
  * passes device buffers: hist (slab k at hist + k*hist_stride doubles,
  * reference layout inside a slab, stride_t <= hist_stride, and
  * (Nt + 1) * hist_stride * 8 <= 2^50 bytes) and rho (Ns
@@ -293,8 +295,10 @@ int nufi_batch_describe(const nufi_batch *b, char *buf, size_t len);
  * Scratch: a fixed 8 MiB array inside the library (held by every GPU that
  * loads it until the process exits) for the per-block partial sums; about
  * Nm * Ns / 16 * 8 bytes must fit, larger problems get NUFI_ERR_RANGE.
- * The first call on a device looks up the array's device address; make
- * that first call before any stream capture.  All calls share the array,
+ * The first call on a device looks up the array's device address (kept
+ * for the life of the process, so a cudaDeviceReset between calls is not
+ * supported); make that first call before any stream capture.  All calls
+ * share the array,
  * so calls that overlap on the GPU (other streams, other threads) race;
  * serialise them.  Device-side range flags are not reported here.
  * Handle-less: errors via nufi_last_error(NULL). */

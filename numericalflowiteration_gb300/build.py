@@ -21,6 +21,8 @@ BUILD = HERE / "_build"
 LIB = HERE / "libnufi_gb300.so"
 PROBES = HERE / "probes"
 PROBE_LIB = HERE / "libnufi_probes.so"
+E2E_SRC = HERE / "e2e_loop.cpp"
+E2E_EXE = HERE / "e2e_loop"
 INCLUDE = HERE.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -87,7 +89,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> Path:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed for {cmd[-3]}:\n{r.stdout}\n{r.stderr}")
+            raise RuntimeError(f"{Path(cmd[0]).name} failed for {cmd[-3]}:\n{r.stdout}\n{r.stderr}")
         if verbose and (r.stdout or r.stderr):
             print(r.stdout, r.stderr, flush=True)
 
@@ -98,6 +100,13 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> Path:
         tmp = LIB.with_suffix(".so.tmp")
         run([cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"])
         os.replace(tmp, LIB)
+    # the reference drivers' loop through the C ABI (timed by bench.py)
+    if E2E_SRC.exists() and (force or _stale(E2E_EXE, [E2E_SRC, LIB, *hdrs])):
+        cxx = shutil.which("g++") or "g++"
+        tmp = E2E_EXE.with_suffix(".tmp")
+        run([cxx, "-std=c++17", "-O2", f"-I{INCLUDE}", str(E2E_SRC), f"-L{HERE}", "-lnufi_gb300",
+             f"-Wl,-rpath,{HERE}", "-o", str(tmp)])
+        os.replace(tmp, E2E_EXE)
     probe_src = sorted(PROBES.glob("*.cu"))
     if probe_src and (force or _stale(PROBE_LIB, probe_src)):
         tmp = PROBE_LIB.with_suffix(".so.tmp")

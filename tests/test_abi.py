@@ -155,21 +155,38 @@ def test_split_needs_a_periodic_f0_phase(lib):
         nufi.Simulation(landau_1d(k=0.3, precision="fp32split"))
 
 
+_NOALLOC_REFUSALS = r"""
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+from numericalflowiteration_gb300 import _lib
+from numericalflowiteration_gb300.config import landau_1d
+lib = _lib.load()
+cfg = landau_1d(Nx=16, Nv=32, Nt=8)
+c = cfg.to_c()
+dummy = ctypes.c_void_p(0x1000)
+call = lambda stride, n: lib.nufi_compute_rho_noalloc(ctypes.byref(c), n, dummy, stride, 0, cfg.n_points,
+                                                      dummy, None)
+assert call(cfg.stride_t - 1, 1) == _lib.ERR_INVALID
+assert call(2 ** 62, 1) == _lib.ERR_RANGE
+assert "2^50" in lib.nufi_last_error(None).decode()
+assert call(cfg.stride_t, 9) == _lib.ERR_RANGE
+assert lib.nufi_compute_rho_noalloc(ctypes.byref(c), 1, None, cfg.stride_t, 0, 1, dummy, None) == _lib.ERR_INVALID
+print("refusals ok")
+"""
+
+
 def test_noalloc_rejects_bad_strides_before_cuda(lib):
     """nufi_compute_rho_noalloc checks the caller's history stride (at least
     one slab; history within 2^50 bytes) and the step before any CUDA call.
-    The device pointers are never touched on these paths."""
-    cfg = landau_1d(Nx=16, Nv=32, Nt=8)
-    c = cfg.to_c()
-    dummy = ctypes.c_void_p(0x1000)
-    call = lambda stride, n: lib.nufi_compute_rho_noalloc(ctypes.byref(c), n, dummy, stride, 0, cfg.n_points,
-                                                          dummy, None)
-    assert call(cfg.stride_t - 1, 1) == _lib.ERR_INVALID
-    assert call(2 ** 62, 1) == _lib.ERR_RANGE
-    assert "2^50" in lib.nufi_last_error(None).decode()
-    assert call(cfg.stride_t, 9) == _lib.ERR_RANGE
-    null = lib.nufi_compute_rho_noalloc(ctypes.byref(c), 1, None, cfg.stride_t, 0, 1, dummy, None)
-    assert null == _lib.ERR_INVALID
+    The calls pass a made-up device address; they run in a child process
+    that sees no GPU (CUDA_VISIBLE_DEVICES empty), so a regressed check
+    could never launch on that address."""
+    import os
+    import sys
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    r = subprocess.run([sys.executable, "-c", _NOALLOC_REFUSALS, str(ROOT)], env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0 and "refusals ok" in r.stdout, r.stderr[-2000:]
 
 
 def test_create_without_a_device_reports_the_cuda_error(lib):

@@ -1,9 +1,10 @@
 """The allocation-free rho entry point, nufi_compute_rho_noalloc, against
 the regular drop-in path (nufi_compute_rho + nufi_download_rho).
 
-It serves callers that must not allocate device memory: code running
-inside another library's CUDA-graph capture or memory pool, or a loop that
-reserves all of its device memory up front.  Such a caller hands in its own
+It serves callers that must not allocate device memory: a plugin whose
+host framework owns all device memory through its own pool, or a real-time
+loop that reserves its device memory up front (cudaMalloc can synchronise
+the device and take unbounded time).  Such a caller hands in its own
 device buffers (the test makes them with torch); the entry point keeps its
 scratch in a fixed 8 MiB array inside the library.  The file name sorts
 last so that a stop-at-first-failure run has already run every other test.
@@ -40,12 +41,16 @@ def test_noalloc_rho_matches_compute_rho_on_consecutive_calls():
         rho = torch.full((cfg.n_spatial,), float("nan"), dtype=torch.float64, device="cuda")
         c = cfg.to_c()
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-        for n in steps:  # two calls in a row share the library's scratch
+        for i, n in enumerate(steps):  # two calls in a row share the library's scratch
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
             st = lib.nufi_compute_rho_noalloc(ctypes.byref(c), n, ctypes.c_void_p(dev_hist.data_ptr()),
                                               cfg.stride_t, 0, cfg.n_points, ctypes.c_void_p(rho.data_ptr()),
                                               stream)
             assert st == 0, lib.nufi_last_error(None).decode()
             torch.cuda.synchronize()
+            if i > 0:  # after the first call (which may load the library's module): no device allocation
+                assert torch.cuda.mem_get_info()[0] == free0
             assert rel_max(rho.cpu().numpy(), want[n]) <= 1e-13
 
 
@@ -58,7 +63,11 @@ def test_noalloc_rejects_problems_beyond_its_scratch():
     torch.cuda.init()
     cfg = landau_3d()  # 16^3 x 32^3: partial sums need ~64 MiB
     c = cfg.to_c()
-    buf = torch.zeros(16, dtype=torch.float64, device="cuda")
-    st = lib.nufi_compute_rho_noalloc(ctypes.byref(c), 1, ctypes.c_void_p(buf.data_ptr()), cfg.stride_t, 0,
-                                      cfg.n_points, ctypes.c_void_p(buf.data_ptr()), None)
+    # buffers of their real sizes, so that a regressed size check would give
+    # a wrong status, not accesses past the caller's buffers
+    hist = torch.zeros((cfg.Nt + 1) * cfg.stride_t, dtype=torch.float64, device="cuda")
+    rho = torch.zeros(cfg.n_spatial, dtype=torch.float64, device="cuda")
+    st = lib.nufi_compute_rho_noalloc(ctypes.byref(c), 1, ctypes.c_void_p(hist.data_ptr()), cfg.stride_t, 0,
+                                      cfg.n_points, ctypes.c_void_p(rho.data_ptr()), None)
+    torch.cuda.synchronize()
     assert st == 2 and b"bytes of scratch" in lib.nufi_last_error(None)

@@ -46,6 +46,8 @@ struct nufi_handle {
     cudaStream_t stream = nullptr;
     double *hist = nullptr;
     float *tables = nullptr;
+    double *tables64 = nullptr;   // FP64 1D order 4: per-slab derivative tables (trace_fp64_table.cu)
+    bool fp64_table = false;      // the FP64 trace runs on tables64
     double *partial = nullptr;
     double *rho = nullptr;
     double *energy = nullptr;
@@ -86,6 +88,9 @@ struct nufi_handle {
 };
 
 namespace {
+
+int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, nufi_handle **out,
+                  bool batch_instance);
 
 int fail(nufi_handle *h, int code, const std::string &msg)
 {
@@ -616,7 +621,9 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
     const Problem &p = h->p;
     cudaError_t e;
     int rows = 0;
-    if (p.precision == NUFI_PREC_FP64)
+    if (p.precision == NUFI_PREC_FP64 && h->fp64_table && mode == 0)
+        e = launch_trace_fp64_table(p, h->shape, h->tables64, int(n), qb, qe, h->partial, &rows, h->err, h->stream);
+    else if (p.precision == NUFI_PREC_FP64)
         e = launch_trace_fp64(p, h->shape, h->hist, int(n), qb, qe, mode, h->partial, &rows, h->err, h->stream);
     else if (p.dim > 1)
         e = launch_trace_split_nd(p, h->staged, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows,
@@ -645,6 +652,11 @@ int enqueue_step(nufi_handle *h, long long n)
                                        h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
     h->launches += 1;
+    if (h->fp64_table) {
+        e = launch_derive_table64(p, h->hist + n * p.hist_stride, h->tables64 + n * fp64_table_stride(p), h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
+        h->launches += 1;
+    }
     return NUFI_OK;
 }
 
@@ -693,6 +705,17 @@ int nufi_create(const nufi_config *cfg, int device, nufi_handle **out)
 
 int nufi_create_ex(const nufi_config *cfg, const nufi_options *opt, int device, nufi_handle **out)
 {
+    return create_handle(cfg, opt, device, out, false);
+}
+
+}  // extern "C"
+
+namespace {
+
+// nufi_create_ex; a batch instance (batch_instance) runs on the batch's own
+// kernels and gets no FP64 derivative tables.
+int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, nufi_handle **out, bool batch_instance)
+{
     if (!out) return fail(nullptr, NUFI_ERR_INVALID, "nufi_create: out is null");
     *out = nullptr;
     std::string why;
@@ -710,6 +733,7 @@ int nufi_create_ex(const nufi_config *cfg, const nufi_options *opt, int device, 
     h->device = device;
     h->p = make_problem(*cfg);
     h->p.split_plain_kick = o.split_plain_kick;
+    h->fp64_table = !batch_instance && h->p.precision == NUFI_PREC_FP64 && fp64_table_supported(h->p, cfg->Nt);
     DeviceGuard g(device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -747,6 +771,13 @@ int nufi_create_ex(const nufi_config *cfg, const nufi_options *opt, int device, 
         h->pin_slab = h->pin_rho + p.Ns;
         h->pin_rho_in = h->pin_slab + p.hist_stride + 1;
     }
+    if (h->fp64_table) {
+        const size_t n64 = nslab * size_t(fp64_table_stride(p));
+        if ((e = dalloc(h.get(), &h->tables64, n64)) != cudaSuccess)
+            return bail(cuda_fail(h.get(), e, "cudaMalloc"));
+        if ((e = cudaMemset(h->tables64, 0, n64 * sizeof(double))) != cudaSuccess)
+            return bail(cuda_fail(h.get(), e, "cudaMemset"));
+    }
     if (p.precision == NUFI_PREC_FP32_SPLIT) {
         if ((e = dalloc(h.get(), &h->tables, nslab * p.table_stride)) != cudaSuccess)
             return bail(cuda_fail(h.get(), e, "cudaMalloc"));
@@ -772,6 +803,10 @@ int nufi_create_ex(const nufi_config *cfg, const nufi_options *opt, int device, 
     *out = h.release();
     return NUFI_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int nufi_destroy(nufi_handle *h)
 {
@@ -880,6 +915,12 @@ static int upload_slab(nufi_handle *h, int64_t n, const double *slab)
     NUFI_CUDA(h, cudaEventRecord(h->stage_done, h->stream));
     if (h->tables) {
         cudaError_t e = launch_derive_table(p, h->hist + n * p.hist_stride, h->tables + n * p.table_stride, h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
+        h->launches += 1;
+    }
+    if (h->tables64) {
+        cudaError_t e =
+            launch_derive_table64(p, h->hist + n * p.hist_stride, h->tables64 + n * fp64_table_stride(p), h->stream);
         if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
         h->launches += 1;
     }
@@ -1272,7 +1313,10 @@ std::string plan_json(const nufi_handle *h, bool layout)
 {
     const Problem &p = h->p;
     char tmp[1024];
-    const char *trace = p.precision == NUFI_PREC_FP64 ? "trace_fp64_kernel"
+    const char *fp64_trace = !h->fp64_table ? "trace_fp64_kernel"
+                             : p.dim == 1   ? "trace_fp64_1d_table_kernel"
+                                            : "trace_fp64_2d_table_kernel";
+    const char *trace = p.precision == NUFI_PREC_FP64 ? fp64_trace
                         : p.dim > 1                   ? "trace_split_nd_kernel"
                         : h->staged.ok                ? "trace_split_1d_staged_kernel"
                                                       : "trace_split_1d_kernel";
@@ -1342,6 +1386,7 @@ int nufi_plan_ex(const nufi_config *cfg, const nufi_options *opt, int sms, char 
     h.cfg = *cfg;
     h.p = make_problem(*cfg);
     h.p.split_plain_kick = h.opt.split_plain_kick;
+    h.fp64_table = h.p.precision == NUFI_PREC_FP64 && fp64_table_supported(h.p, cfg->Nt);
     plan_traces(h.p, sms, h.opt, h.shape, h.staged);
     h.solve_ok = solve_geometry(h.p, sms, h.plan, h.solve_why);
     h.persist = plan_persistent(h.p, h.staged, h.plan, h.solve_ok, sms, h.opt);
@@ -1664,7 +1709,7 @@ int nufi_batch_create_ex(const nufi_config *cfgs, int32_t count, const nufi_opti
     };
     for (int32_t i = 0; i < count; ++i) {
         nufi_handle *h = nullptr;
-        int st = nufi_create_ex(&cfgs[i], &o, device, &h);
+        int st = create_handle(&cfgs[i], &o, device, &h, true);
         if (st) {
             b->last_error = "instance " + std::to_string(i) + ": " + g_last_error;
             return bail(st);

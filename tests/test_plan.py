@@ -125,7 +125,9 @@ def test_plans_1d(sms):
             check_staged_1d(cfg, pl, sms)
             assert pl["trace"] in ("trace_split_1d_staged_kernel", "trace_split_1d_kernel")
         else:
-            assert pl["trace"] == "trace_fp64_kernel" and pl["staged"]["ok"] == 0
+            # order 4: the cell-unit trace over FP64 derivative tables
+            want = "trace_fp64_1d_table_kernel" if cfg.order == 4 else "trace_fp64_kernel"
+            assert pl["trace"] == want and pl["staged"]["ok"] == 0
 
 
 CASES_ND = [landau_2d(Nx=nx, Nv=nv, Nt=8, precision=prec)
@@ -144,7 +146,10 @@ def test_plans_nd(sms):
         check_common(cfg, pl, sms)
         check_adjoint(cfg, pl)
         check_staged_nd(cfg, pl, sms)
-        want = "trace_split_nd_kernel" if cfg.precision == "fp32split" else "trace_fp64_kernel"
+        if cfg.precision == "fp32split":
+            want = "trace_split_nd_kernel"
+        else:  # 2D order 4: the cell-unit trace over FP64 derivative tables
+            want = "trace_fp64_2d_table_kernel" if (cfg.dim == 2 and cfg.order == 4) else "trace_fp64_kernel"
         assert pl["trace"] == want
 
 

@@ -1,0 +1,78 @@
+"""GPU parity at the benchmark configurations' own sizes, over their whole
+runs, against the reference's own results (tests/golden/make_golden.py
+--full: the reference's eval_ftilda / poisson / interpolate loop, built from
+its sources).
+
+Measures: max |d| / max |ref| (rel_max) for energy histories, rho and
+slabs.  FP64 plain: 1e-12 against the reference run with compensated rho
+sums, and within the case's FP64 summation floor (conftest.energy_tol)
+against its in-order sums.  FP32-split: the metric's gate, max_n |dW_n| /
+max_n |W_n| <= 1e-6 against the reference's energy history; its pointwise
+max_n |dW_n| / |W_n| is checked to a looser bound (the energy passes near
+zero between its oscillations, where a relative error means little).
+"""
+import numpy as np
+import pytest
+
+from conftest import energy_tol, golden, rel_max
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nufi():
+    import numericalflowiteration_gb300 as m
+    from numericalflowiteration_gb300 import build
+    build.build()
+    m.load()
+    return m
+
+
+def _check_run(cfg, g, e, hist, rho_last, tol_comp=1e-12):
+    n_last = int(g["n_last"])
+    assert rel_max(e, g["energy_comp"][:n_last + 1]) <= tol_comp
+    assert rel_max(e, g["energy"][:n_last + 1]) <= max(tol_comp, energy_tol(g))
+    st = cfg.stride_t
+    for i, n in enumerate(g["slab_steps"]):
+        assert rel_max(hist[n * st:(n + 1) * st], g["slabs_comp"][i]) <= 1e-11, f"slab {n}"
+    assert rel_max(rho_last, g["rho_comp"][list(g["rho_steps"]).index(n_last)]) <= 1e-12
+
+
+def test_fp64_two_stream_256x1024_whole_run(nufi):
+    """The bench workload (two-stream 256 x 1024, T = 50, all 801 steps) in
+    FP64 against the reference's run of the same configuration."""
+    cfg, g = golden("two_stream_1d_256x1024_T50")
+    with nufi.Simulation(cfg) as sim:
+        e = sim.run()
+        hist = sim.history()
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+    _check_run(cfg, g, e, hist, rho)
+
+
+def test_split_two_stream_256x1024_whole_run_within_gate(nufi):
+    """The bench's headline form (the FP32-split whole-run kernel) over all
+    801 steps against the reference's energy history: the metric's gate."""
+    cfg, g = golden("two_stream_1d_256x1024_T50")
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        e = sim.run()
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+    assert rel_max(e, g["energy_comp"]) <= 1e-6
+    assert float(np.max(np.abs(e - g["energy_comp"]) / np.abs(g["energy_comp"]))) <= 1e-3
+    assert rel_max(rho, g["rho_comp"][-1]) <= 1e-6
+
+
+def test_split_dropin_two_stream_256x1024_later_steps(nufi):
+    """The per-step split trace (the drop-in compute_rho) at late steps on
+    the FP64 history (itself pinned to the reference's by the test above):
+    rho within the split form's accuracy of the reference's rho."""
+    cfg, g = golden("two_stream_1d_256x1024_T50")
+    with nufi.Simulation(cfg) as ref:
+        ref.run()
+        coeffs = ref.history()
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        for n in range(cfg.Nt + 1):
+            sim.upload_phi(n, coeffs)
+        for n in (400, 600, 800):
+            sim.compute_rho(n)
+            got = sim.download_rho(np.zeros(cfg.n_spatial))
+            assert rel_max(got, g["rho_comp"][list(g["rho_steps"]).index(n)]) <= 1e-6, n

@@ -105,10 +105,7 @@ const char *nufi_last_error(const nufi_handle *h);
  * rho and the metrics accumulators on `device`.  Checked before any CUDA
  * call: NUFI_ERR_RANGE for Nt > 2^30, more than 2^31 - 1 spatial or
  * velocity nodes, more than 2^20 nodes or 4096 velocity nodes on an axis,
- * or a history above 2^50 bytes; NUFI_ERR_UNSUPPORTED for FP64 handles with
- * more than 1048560 velocity nodes (the FP64 trace's launch grid; FP32-split
- * handles trace any size but nufi_compute_metrics, which runs the FP64
- * trace, refuses the same sizes); NUFI_ERR_INVALID / NUFI_ERR_UNSUPPORTED
+ * or a history above 2^50 bytes; NUFI_ERR_INVALID / NUFI_ERR_UNSUPPORTED
  * for the other configuration errors (among them non-finite domain bounds or
  * f0 parameters, and sigma_b <= 0 for bump-on-tail: NUFI_ERR_INVALID).
  * NUFI_ERR_CUDA (with the CUDA error's

@@ -206,10 +206,6 @@ int validate(const nufi_config *c, std::string &why)
         why = "FP64 trace not built for this (dim, order)";
         return NUFI_ERR_UNSUPPORTED;
     }
-    if (c->precision == NUFI_PREC_FP64 && nm > (long double)kMaxFp64VelocityNodes) {
-        why = "FP64 trace takes at most 65535 x 16 = 1048560 velocity nodes (blocks of 16 on the grid's y axis)";
-        return NUFI_ERR_UNSUPPORTED;
-    }
     if (c->precision == NUFI_PREC_FP32_SPLIT && !split_supported(c->dim, c->order, c->f0_kind)) {
         why = "FP32-split trace not built for this (dim, order, f0)";
         return NUFI_ERR_UNSUPPORTED;
@@ -364,6 +360,12 @@ LaunchShape choose_shape(const Problem &p, int sms)
 void plan_traces(const Problem &p, int sms, const nufi_options &opt, LaunchShape &shape, StagedShape &staged)
 {
     shape = choose_shape(p, sms);
+    // the FP64 3D cubic trace (trace_fp64_3d_cells_kernel) holds two blocks
+    // per SM in 128 registers at up to 2 points per thread; at 4 it spills
+    if (p.precision == NUFI_PREC_FP64 && p.dim == 3 && p.order == 4 && shape.ppt > 2) {
+        shape.vblocks = int((p.Nm + 2LL * shape.warps - 1) / (2LL * shape.warps));
+        shape.ppt = 2;
+    }
     staged = StagedShape{};
     const bool no_ring = opt.split_global_loads != 0;
     if (p.precision == NUFI_PREC_FP32_SPLIT && p.dim > 1) {
@@ -622,7 +624,8 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
     cudaError_t e;
     int rows = 0;
     if (p.precision == NUFI_PREC_FP64 && h->fp64_table && mode == 0)
-        e = launch_trace_fp64_table(p, h->shape, h->tables64, int(n), qb, qe, h->partial, &rows, h->err, h->stream);
+        e = launch_trace_fp64_table(p, h->shape, h->tables64, h->hist, int(n), qb, qe, h->partial, &rows, h->err,
+                                    h->stream);
     else if (p.precision == NUFI_PREC_FP64)
         e = launch_trace_fp64(p, h->shape, h->hist, int(n), qb, qe, mode, h->partial, &rows, h->err, h->stream);
     else if (p.dim > 1)
@@ -652,7 +655,7 @@ int enqueue_step(nufi_handle *h, long long n)
                                        h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
     h->launches += 1;
-    if (h->fp64_table) {
+    if (h->tables64) {
         e = launch_derive_table64(p, h->hist + n * p.hist_stride, h->tables64 + n * fp64_table_stride(p), h->stream);
         if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
         h->launches += 1;
@@ -739,7 +742,10 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     plan_traces(h->p, sms > 0 ? sms : 1, h->opt, h->shape, h->staged);
     const Problem &p = h->p;
-    const size_t partial_rows = size_t(std::max(h->shape.vblocks, h->staged.ok ? h->staged.ctas : 0));
+    // partial-sum rows: the FP64 traces' y blocks (fp64_rows), the global-
+    // load split trace's velocity blocks, or the staged traces' CTAs
+    const int trace_rows = p.precision == NUFI_PREC_FP64 ? fp64_rows(h->shape) : h->shape.vblocks;
+    const size_t partial_rows = size_t(std::max(trace_rows, h->staged.ok ? h->staged.ctas : 0));
     auto bail = [&](int code) {
         g_last_error = h->last_error;
         release(h.get());
@@ -754,7 +760,7 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
         (e = dalloc(h.get(), &h->energy, nslab)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->rho_in, size_t(p.Ns))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->slab_out, size_t(p.hist_stride) + 1)) != cudaSuccess ||
-        (e = dalloc(h.get(), &h->mpartial, size_t(4 * ((p.Ns + 31) / 32) * h->shape.vblocks))) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->mpartial, size_t(4 * ((p.Ns + 31) / 32) * fp64_rows(h->shape)))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->metrics, 4)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->err, 1)) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMalloc"));
@@ -771,7 +777,7 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
         h->pin_slab = h->pin_rho + p.Ns;
         h->pin_rho_in = h->pin_slab + p.hist_stride + 1;
     }
-    if (h->fp64_table) {
+    if (h->fp64_table && fp64_table_stride(p) > 0) {
         const size_t n64 = nslab * size_t(fp64_table_stride(p));
         if ((e = dalloc(h.get(), &h->tables64, n64)) != cudaSuccess)
             return bail(cuda_fail(h.get(), e, "cudaMalloc"));
@@ -857,8 +863,6 @@ int nufi_compute_metrics(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_e
     if (q_begin < 0 || q_end < q_begin || q_end > h->p.Nq)
         return fail(h, NUFI_ERR_RANGE, "quadrature range outside [0, Nq]");
     if (q_begin == q_end) return NUFI_OK;  // as the reference: no launch, sums untouched
-    if (h->p.Nm > kMaxFp64VelocityNodes)  // metrics run the FP64 trace in every precision
-        return fail(h, NUFI_ERR_UNSUPPORTED, "compute_metrics: the FP64 trace takes at most 1048560 velocity nodes");
     DeviceGuard g(h->device);
     const Problem &p = h->p;
     int rows = 0;
@@ -1315,7 +1319,8 @@ std::string plan_json(const nufi_handle *h, bool layout)
     char tmp[1024];
     const char *fp64_trace = !h->fp64_table ? "trace_fp64_kernel"
                              : p.dim == 1   ? "trace_fp64_1d_table_kernel"
-                                            : "trace_fp64_2d_table_kernel";
+                             : p.dim == 2   ? "trace_fp64_2d_table_kernel"
+                                            : "trace_fp64_3d_cells_kernel";
     const char *trace = p.precision == NUFI_PREC_FP64 ? fp64_trace
                         : p.dim > 1                   ? "trace_split_nd_kernel"
                         : h->staged.ok                ? "trace_split_1d_staged_kernel"

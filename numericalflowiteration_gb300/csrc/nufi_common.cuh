@@ -13,9 +13,6 @@ constexpr int kMaxOrder = 8;
 constexpr int kMaxVelocityTable = 4096;  // per-axis velocity nodes kept in tables
 constexpr long long kMaxSteps = 1LL << 30;  // time steps per run (kernels take 32-bit step indices)
 constexpr long long kMaxEvalPoints = 1LL << 36;  // points per nufi_eval_points call
-// FP64 trace launch: velocity blocks of 4 warps x 4 points on the grid's y
-// axis, which holds at most 65535 blocks
-constexpr long long kMaxFp64VelocityNodes = 65535LL * 16;
 
 // Bits of the device error word (checked by the host after each blocking
 // call).  Kernels set a bit and skip the offending access; they never trap.
@@ -126,6 +123,26 @@ __host__ __device__ __forceinline__ double deboor4_d1(double x, double c0, doubl
     const double e3 = a4 * d3 + b2 * d2;
     const double e2 = a3 * d2 + b1 * d1;
     return 0.5 * (a4 * e3 + b1 * e2);
+}
+
+// Cubic (order-4) B-spline values b[0..3] and derivatives d[0..3] (d/dt)
+// at the local coordinate t in [0, 1]: closed forms of splines1d::N<4,0>
+// and N<4,1> (nufi/splines.hpp:39-79),
+//   b0 = (1-t)^3/6, b3 = t^3/6, b1 = 2/3 - t^2 + t^3/2, b2 = 1 - b0 - b1 - b3,
+//   d0 = -(1-t)^2/2, d3 = t^2/2, d1 = t (3t/2 - 2), d2 = -(d0 + d1 + d3),
+// about 20 FP64 operations for both (the FP64 trace is bound by the FP64
+// pipe; the results agree with the recurrence to rounding).
+__device__ __forceinline__ void cubic_bd_fp64(double t, double (&b)[4], double (&d)[4])
+{
+    const double s = 1.0 - t, t2 = t * t, s2 = s * s;
+    b[0] = (s2 * s) * (1.0 / 6.0);
+    b[3] = (t2 * t) * (1.0 / 6.0);
+    b[1] = fma(0.5 * t, t2, 2.0 / 3.0 - t2);
+    b[2] = ((1.0 - b[0]) - b[1]) - b[3];
+    d[0] = -0.5 * s2;
+    d[3] = 0.5 * t2;
+    d[1] = t * fma(1.5, t, -2.0);
+    d[2] = -((d[0] + d[1]) + d[3]);
 }
 
 // Initial conditions in FP64, same expressions as the oracle's and the

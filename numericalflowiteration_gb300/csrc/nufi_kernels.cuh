@@ -14,6 +14,10 @@ struct LaunchShape {
     int ppt = 1;
     int vblocks = 1;
 };
+// The FP64 traces put min(vblocks, 65535) blocks on the grid's y axis and
+// stride over the velocity blocks; one partial-sum row per y block.
+constexpr int kMaxGridY = 65535;
+inline int fp64_rows(const LaunchShape &ls) { return ls.vblocks < kMaxGridY ? ls.vblocks : kMaxGridY; }
 
 // Per-velocity-node constants of the split form.  Axis a, node j is entry
 // a * kMaxVelocityTable + j ... stored compactly: offsets vel_off[a].
@@ -100,15 +104,16 @@ __device__ __forceinline__ void write_metrics_block(const double (&m4)[4], doubl
 cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
                               long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st);
 bool fp64_order_supported(int dim, int order);
-// FP64 1D order-4 trace in cell units over per-slab FP64 derivative tables
-// (trace_fp64_table.cu): tables of fp64_table_stride doubles per slab,
-// written by launch_derive_table64 from each FP64 slab.
+// FP64 order-4 trace in cell units (trace_fp64_table.cu): 1D and 2D over
+// per-slab FP64 derivative tables of fp64_table_stride doubles per slab
+// (written by launch_derive_table64 from each FP64 slab), 3D on the slabs
+// (stride 0: no table).
 bool fp64_table_supported(const Problem &p, long long Nt);
 long long fp64_table_stride(const Problem &p);
 cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, double *table_slab, cudaStream_t st);
-cudaError_t launch_trace_fp64_table(const Problem &p, const LaunchShape &ls, const double *tables, int n,
-                                    long long qb, long long qe, double *partial, int *rows, unsigned *err,
-                                    cudaStream_t st);
+cudaError_t launch_trace_fp64_table(const Problem &p, const LaunchShape &ls, const double *tables,
+                                    const double *hist, int n, long long qb, long long qe, double *partial,
+                                    int *rows, unsigned *err, cudaStream_t st);
 // eval_ftilda / eval_f / 1D eval_phase_flow at arbitrary points (FP64).
 cudaError_t launch_eval_points(const Problem &p, const double *hist, int n, int mode, long long npts,
                                const double *pts, double *f_out, double *feet, unsigned *err, cudaStream_t st);

@@ -62,26 +62,6 @@ __device__ __forceinline__ void field_1d(const Problem &p, const double *__restr
     }
 }
 
-// Cubic (order-4) B-spline values b[0..3] and derivatives d[0..3] (d/dt)
-// at the local coordinate t in [0, 1]: closed forms of splines1d::N<4,0>
-// and N<4,1> (nufi/splines.hpp:39-79),
-//   b0 = (1-t)^3/6, b3 = t^3/6, b1 = 2/3 - t^2 + t^3/2, b2 = 1 - b0 - b1 - b3,
-//   d0 = -(1-t)^2/2, d3 = t^2/2, d1 = t (3t/2 - 2), d2 = -(d0 + d1 + d3),
-// about 20 FP64 operations for both (the FP64 trace is bound by the FP64
-// pipe; the results agree with the recurrence to rounding).
-__device__ __forceinline__ void cubic_bd_fp64(double t, double (&b)[4], double (&d)[4])
-{
-    const double s = 1.0 - t, t2 = t * t, s2 = s * s;
-    b[0] = (s2 * s) * (1.0 / 6.0);
-    b[3] = (t2 * t) * (1.0 / 6.0);
-    b[1] = fma(0.5 * t, t2, 2.0 / 3.0 - t2);
-    b[2] = ((1.0 - b[0]) - b[1]) - b[3];
-    d[0] = -0.5 * s2;
-    d[3] = 0.5 * t2;
-    d[1] = t * fma(1.5, t, -2.0);
-    d[2] = -((d[0] + d[1]) + d[3]);
-}
-
 template <int ORDER>
 __device__ __forceinline__ void field_2d(const Problem &p, const double *__restrict__ c, const double *x, double *E,
                                          unsigned *err)
@@ -243,110 +223,117 @@ __device__ __forceinline__ double f0_fp64(const Problem &p, const double *x, con
 // slab n) of PPT points per thread; see the file comment.
 template <int D, int ORDER, int PPT>
 __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const double *__restrict__ hist, int n,
-                                                         long long q_begin, long long q_end, int mode,
+                                                         long long q_begin, long long q_end, int mode, int vblocks,
                                                          double *__restrict__ partial, unsigned *err)
 {
     const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
     const long long s = (long long)blockIdx.x * 32 + lane;
-    const long long mb = ((long long)blockIdx.y * W + warp) * PPT;
     const double dt = p.dt;
+    // metrics of cuda_eval_metrics (nufi/cuda_kernel.cu:53-79, 239-271,
+    // 428-466): weight * f, weight * f^2, weight * |u0|^2 f / 2 and
+    // -weight f log f, u0 the point's initial velocity; weight du (dx) in
+    // 1D, dx dy du dv in 2D, du dv dw in 3D (the reference's 3D kernel
+    // leaves out dx dy dz).
+    double w = p.wv;
+    if (D < 3)
+        for (int a = 0; a < D; ++a) w *= p.dx[a];
+    double acc = 0;
+    double m4[4] = {0, 0, 0, 0};
 
-    double x[PPT][D], u[PPT][D];
-    bool live[PPT];
-    {
-        long long rs = s < p.Ns ? s : 0;
-        int is[3] = {0, 0, 0};
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-            is[a] = int(rs % p.N[a]);
-            rs /= p.N[a];
-        }
-#pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            const long long m = mb + q;
-            const long long qq = s * p.Nm + m;
-            live[q] = (s < p.Ns) && (m < p.Nm) && (qq >= q_begin) && (qq < q_end);
-            long long rm = m < p.Nm ? m : 0;
+    // velocity blocks vb = blockIdx.y, blockIdx.y + gridDim.y, ...: one per
+    // block unless the velocity grid has more blocks than the grid's y axis
+    // holds; each block sums its points in this fixed order
+    for (int vb = blockIdx.y; vb < vblocks; vb += gridDim.y) {
+        const long long mb = ((long long)vb * W + warp) * PPT;
+        double x[PPT][D], u[PPT][D];
+        bool live[PPT];
+        {
+            long long rs = s < p.Ns ? s : 0;
+            int is[3] = {0, 0, 0};
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                const int im = int(rm % p.M[a]);
-                rm /= p.M[a];
-                x[q][a] = p.xmin[a] + is[a] * p.dx[a];
-                u[q][a] = p.vmin[a] + im * p.dv[a] + p.dv[a] / 2;
+                is[a] = int(rs % p.N[a]);
+                rs /= p.N[a];
+            }
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                const long long m = mb + q;
+                const long long qq = s * p.Nm + m;
+                live[q] = (s < p.Ns) && (m < p.Nm) && (qq >= q_begin) && (qq < q_end);
+                long long rm = m < p.Nm ? m : 0;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    const int im = int(rm % p.M[a]);
+                    rm /= p.M[a];
+                    x[q][a] = p.xmin[a] + is[a] * p.dx[a];
+                    u[q][a] = p.vmin[a] + im * p.dv[a] + p.dv[a] / 2;
+                }
             }
         }
-    }
 
-    double acc = 0;
-    if (n > 0) {
-        double E[D];
-        if (mode >= 1) {  // eval_f: initial half kick with slab n
-            const double *c = hist + (long long)n * p.hist_stride;
+        if (n > 0) {
+            double E[D];
+            if (mode >= 1) {  // eval_f: initial half kick with slab n
+                const double *c = hist + (long long)n * p.hist_stride;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    if (!live[q]) continue;
+                    field_fp64<D, ORDER>(p, c, x[q], E, err);
+#pragma unroll
+                    for (int a = 0; a < D; ++a) u[q][a] += 0.5 * dt * E[a];
+                }
+            }
+            for (int k = n - 1; k >= 1; --k) {
+                const double *c = hist + (long long)k * p.hist_stride;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    if (!live[q]) continue;
+#pragma unroll
+                    for (int a = 0; a < D; ++a) x[q][a] = x[q][a] - dt * u[q][a];
+                    field_fp64<D, ORDER>(p, c, x[q], E, err);
+#pragma unroll
+                    for (int a = 0; a < D; ++a) u[q][a] = u[q][a] + dt * E[a];
+                }
+            }
 #pragma unroll
             for (int q = 0; q < PPT; ++q) {
                 if (!live[q]) continue;
-                field_fp64<D, ORDER>(p, c, x[q], E, err);
+#pragma unroll
+                for (int a = 0; a < D; ++a) x[q][a] -= dt * u[q][a];
+                field_fp64<D, ORDER>(p, hist, x[q], E, err);
 #pragma unroll
                 for (int a = 0; a < D; ++a) u[q][a] += 0.5 * dt * E[a];
             }
         }
-        for (int k = n - 1; k >= 1; --k) {
-            const double *c = hist + (long long)k * p.hist_stride;
+        if (mode == 2) {
 #pragma unroll
             for (int q = 0; q < PPT; ++q) {
                 if (!live[q]) continue;
+                const double f = f0_fp64<D>(p, x[q], u[q]);
+                long long rm = mb + q;
+                double uu = 0;
 #pragma unroll
-                for (int a = 0; a < D; ++a) x[q][a] = x[q][a] - dt * u[q][a];
-                field_fp64<D, ORDER>(p, c, x[q], E, err);
-#pragma unroll
-                for (int a = 0; a < D; ++a) u[q][a] = u[q][a] + dt * E[a];
+                for (int a = 0; a < D; ++a) {
+                    const double u0 = p.vmin[a] + int(rm % p.M[a]) * p.dv[a] + p.dv[a] / 2;
+                    rm /= p.M[a];
+                    uu += u0 * u0;
+                }
+                const double wf = w * f;
+                m4[0] += wf;
+                m4[1] += wf * f;
+                m4[2] += w * (uu * f / 2);
+                m4[3] += (f > 0) ? -wf * log(f) : 0.0;
             }
-        }
+        } else {
 #pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            if (!live[q]) continue;
-#pragma unroll
-            for (int a = 0; a < D; ++a) x[q][a] -= dt * u[q][a];
-            field_fp64<D, ORDER>(p, hist, x[q], E, err);
-#pragma unroll
-            for (int a = 0; a < D; ++a) u[q][a] += 0.5 * dt * E[a];
+            for (int q = 0; q < PPT; ++q)
+                if (live[q]) acc += f0_fp64<D>(p, x[q], u[q]);
         }
     }
     if (mode == 2) {
-        // metrics of cuda_eval_metrics (nufi/cuda_kernel.cu:53-79, 239-271,
-        // 428-466): weight * f, weight * f^2, weight * |u0|^2 f / 2 and
-        // -weight f log f, u0 the point's initial velocity; weight du (dx)
-        // in 1D, dx dy du dv in 2D, du dv dw in 3D (the reference's 3D
-        // kernel leaves out dx dy dz).
-        double w = p.wv;
-        if (D < 3)
-            for (int a = 0; a < D; ++a) w *= p.dx[a];
-        double m4[4] = {0, 0, 0, 0};
-#pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            if (!live[q]) continue;
-            const double f = f0_fp64<D>(p, x[q], u[q]);
-            long long rm = mb + q;
-            double uu = 0;
-#pragma unroll
-            for (int a = 0; a < D; ++a) {
-                const double u0 = p.vmin[a] + int(rm % p.M[a]) * p.dv[a] + p.dv[a] / 2;
-                rm /= p.M[a];
-                uu += u0 * u0;
-            }
-            const double wf = w * f;
-            m4[0] += wf;
-            m4[1] += wf * f;
-            m4[2] += w * (uu * f / 2);
-            m4[3] += (f > 0) ? -wf * log(f) : 0.0;
-        }
         write_metrics_block(m4, partial);
         return;
     }
-#pragma unroll
-    for (int q = 0; q < PPT; ++q)
-        if (live[q]) acc += f0_fp64<D>(p, x[q], u[q]);
-
     write_partial_tiled(acc, s, p.Ns, partial);
 }
 
@@ -357,11 +344,12 @@ static cudaError_t launch_fp64_order(const Problem &p, const LaunchShape &ls, co
                                      cudaStream_t st)
 {
     const dim3 block(32, ls.warps);
-    const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(ls.vblocks));
+    const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(fp64_rows(ls)));
+    const int vb = ls.vblocks;
     switch (ls.ppt) {
-    case 1: trace_fp64_kernel<D, ORDER, 1><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
-    case 2: trace_fp64_kernel<D, ORDER, 2><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
-    case 4: trace_fp64_kernel<D, ORDER, 4><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, partial, err); break;
+    case 1: trace_fp64_kernel<D, ORDER, 1><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, vb, partial, err); break;
+    case 2: trace_fp64_kernel<D, ORDER, 2><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, vb, partial, err); break;
+    case 4: trace_fp64_kernel<D, ORDER, 4><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, vb, partial, err); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -370,7 +358,7 @@ static cudaError_t launch_fp64_order(const Problem &p, const LaunchShape &ls, co
 cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
                               long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st)
 {
-    *rows = ls.vblocks;
+    *rows = fp64_rows(ls);
 #define NUFI_CASE(D, O) \
     if (p.dim == D && p.order == O) return launch_fp64_order<D, O>(p, ls, hist, n, qb, qe, mode, partial, err, st);
     NUFI_CASE(1, 3) NUFI_CASE(1, 4) NUFI_CASE(1, 5) NUFI_CASE(1, 6) NUFI_CASE(1, 7) NUFI_CASE(1, 8)

@@ -36,6 +36,13 @@
 // (coefficient-major: each of the 24 loads of a warp is contiguous when its
 // lanes sit in neighbouring cells).
 //
+// 3D (order 4): a per-cell table would hold 144 doubles per cell, 477 MB
+// for the 16^3 x 32^3, 101-step run, beyond L2; the kernel keeps the 4^3
+// window contraction of trace_fp64.cu on the FP64 slab (55 KB, L2-resident)
+// and takes only the cell-unit drift and locate (4 DADD per axis against
+// about 9 for drift, wrap and locate) and the kick V += -(dt/dx)^2 dS/dxi
+// (one DFMA per axis).
+//
 // Thread mapping and the deterministic rho rows are trace_fp64.cu's: a warp
 // is 32 consecutive spatial nodes at one velocity node, PPT velocity nodes
 // per thread, write_partial_tiled then reduce_rho.
@@ -81,15 +88,17 @@ __device__ __forceinline__ int cell_of(int U, int N)
 template <int PPT, bool POW2>
 __global__ void __launch_bounds__(256) trace_fp64_1d_table_kernel(const Problem p, const double *__restrict__ tab,
                                                                   long long tstride, int n, long long q_begin,
-                                                                  long long q_end, double *__restrict__ partial,
-                                                                  unsigned *err)
+                                                                  long long q_end, int vblocks,
+                                                                  double *__restrict__ partial, unsigned *err)
 {
     const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
     const long long s = (long long)blockIdx.x * 32 + lane;
-    const long long mb = ((long long)blockIdx.y * W + warp) * PPT;
     const int N = p.N[0];
     const double vscale = p.dt * p.dxinv[0];  // V = u dt / dx
-
+    double acc = 0;
+    // velocity blocks strided over the grid's y axis (one each below 65536)
+    for (int vb = blockIdx.y; vb < vblocks; vb += gridDim.y) {
+    const long long mb = ((long long)vb * W + warp) * PPT;
     int U[PPT];
     double xi[PPT], V[PPT];
     bool live[PPT];
@@ -117,7 +126,6 @@ __global__ void __launch_bounds__(256) trace_fp64_1d_table_kernel(const Problem 
         for (int k = n - 1; k >= 1; --k) substep(tab + (long long)k * tstride, false);
         substep(tab, true);
     }
-    double acc = 0;
     const double udx = p.dx[0] / p.dt;
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
@@ -126,22 +134,24 @@ __global__ void __launch_bounds__(256) trace_fp64_1d_table_kernel(const Problem 
         if (!isfinite(xi[q])) atomicOr(err, kErrCellIndex);
         acc += f0_1d(p, fma(p.dx[0], double(U[q]) + xi[q], p.xmin[0]), V[q] * udx);
     }
+    }
     write_partial_tiled(acc, s, p.Ns, partial);
 }
 
 template <int PPT, bool POW2>
 __global__ void __launch_bounds__(256) trace_fp64_2d_table_kernel(const Problem p, const double *__restrict__ tab,
                                                                   long long tstride, int n, long long q_begin,
-                                                                  long long q_end, double *__restrict__ partial,
-                                                                  unsigned *err)
+                                                                  long long q_end, int vblocks,
+                                                                  double *__restrict__ partial, unsigned *err)
 {
     const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
     const long long s = (long long)blockIdx.x * 32 + lane;
-    const long long mb = ((long long)blockIdx.y * W + warp) * PPT;
     const int N0 = p.N[0], N1 = p.N[1];
     const long long Ns = p.Ns;
     const double vs0 = p.dt * p.dxinv[0], vs1 = p.dt * p.dxinv[1];
-
+    double acc = 0;
+    for (int vb = blockIdx.y; vb < vblocks; vb += gridDim.y) {
+    const long long mb = ((long long)vb * W + warp) * PPT;
     int U0[PPT], U1[PPT];
     double x0[PPT], x1[PPT], V0[PPT], V1[PPT];
     bool live[PPT];
@@ -186,7 +196,6 @@ __global__ void __launch_bounds__(256) trace_fp64_2d_table_kernel(const Problem 
         for (int k = n - 1; k >= 1; --k) substep(tab + (long long)k * tstride, false);
         substep(tab, true);
     }
-    double acc = 0;
     const double u0 = p.dx[0] / p.dt, u1 = p.dx[1] / p.dt;
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
@@ -194,6 +203,105 @@ __global__ void __launch_bounds__(256) trace_fp64_2d_table_kernel(const Problem 
         if (!isfinite(x0[q]) || !isfinite(x1[q])) atomicOr(err, kErrCellIndex);
         acc += f0_2d(p, fma(p.dx[0], double(U0[q]) + x0[q], p.xmin[0]), fma(p.dx[1], double(U1[q]) + x1[q], p.xmin[1]),
                      V0[q] * u0, V1[q] * u1);
+    }
+    }
+    write_partial_tiled(acc, s, Ns, partial);
+}
+
+template <int PPT, bool POW2>
+__global__ void __launch_bounds__(256, 2) trace_fp64_3d_cells_kernel(const Problem p, const double *__restrict__ hist,
+                                                                  int n, long long q_begin, long long q_end,
+                                                                  int vblocks, double *__restrict__ partial,
+                                                                  unsigned *err)
+{
+    const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
+    const long long s = (long long)blockIdx.x * 32 + lane;
+    const long long Ns = p.Ns;
+    const int sy = p.P[0], sz = p.P[0] * p.P[1];
+    double K[3], vs[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        vs[a] = p.dt * p.dxinv[a];
+        K[a] = -vs[a] * vs[a];
+    }
+    double acc = 0;
+    for (int vb = blockIdx.y; vb < vblocks; vb += gridDim.y) {
+    const long long mb = ((long long)vb * W + warp) * PPT;
+    int U[PPT][3];
+    double X[PPT][3], V[PPT][3];
+    bool live[PPT];
+    const long long sc = s < Ns ? s : 0;
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        const long long m = mb + q;
+        const long long qq = s * p.Nm + m;
+        live[q] = (s < Ns) && (m < p.Nm) && (qq >= q_begin) && (qq < q_end);
+        long long rs = sc, rm = m < p.Nm ? m : 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            U[q][a] = int(rs % p.N[a]);
+            rs /= p.N[a];
+            X[q][a] = 0.0;
+            V[q][a] = (p.vmin[a] + double(rm % p.M[a]) * p.dv[a] + p.dv[a] / 2) * vs[a];
+            rm /= p.M[a];
+        }
+    }
+    auto substep = [&](const double *__restrict__ c, double h) {
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) drift_cells(U[q][a], X[q][a], V[q][a]);
+            const double *__restrict__ w = c + (long long)cell_of<POW2>(U[q][2], p.N[2]) * sz +
+                                           (long long)cell_of<POW2>(U[q][1], p.N[1]) * sy +
+                                           cell_of<POW2>(U[q][0], p.N[0]);
+            double bx[4], dx[4], by[4], dy[4], bz[4], dz[4];
+            cubic_bd_fp64(X[q][0], bx, dx);
+            cubic_bd_fp64(X[q][1], by, dy);
+            cubic_bd_fp64(X[q][2], bz, dz);
+            double ex = 0, ey = 0, ez = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                double sx = 0, s_y = 0, s_z = 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    double r0 = 0, r1 = 0;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const double v = __ldg(w + k * sz + j * sy + i);
+                        r0 = fma(v, bx[i], r0);
+                        r1 = fma(v, dx[i], r1);
+                    }
+                    sx = fma(r1, by[j], sx);
+                    s_y = fma(r0, dy[j], s_y);
+                    s_z = fma(r0, by[j], s_z);
+                }
+                ex = fma(sx, bz[k], ex);
+                ey = fma(s_y, bz[k], ey);
+                ez = fma(s_z, dz[k], ez);
+            }
+            V[q][0] = fma(h * K[0], ex, V[q][0]);
+            V[q][1] = fma(h * K[1], ey, V[q][1]);
+            V[q][2] = fma(h * K[2], ez, V[q][2]);
+        }
+    };
+    if (n > 0) {
+        for (int k = n - 1; k >= 1; --k) substep(hist + (long long)k * p.hist_stride, 1.0);
+        substep(hist, 0.5);
+    }
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        if (!live[q]) continue;
+        double x[3], u[3];
+        bool finite = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            finite = finite && isfinite(X[q][a]);
+            x[a] = fma(p.dx[a], double(U[q][a]) + X[q][a], p.xmin[a]);
+            u[a] = V[q][a] * (p.dx[a] / p.dt);
+        }
+        if (!finite) atomicOr(err, kErrCellIndex);
+        acc += f0_3d(p, x[0], x[1], x[2], u[0], u[1], u[2]);
+    }
     }
     write_partial_tiled(acc, s, Ns, partial);
 }
@@ -267,10 +375,11 @@ __global__ void derive_table64_kernel(const Problem p, const double *__restrict_
 // The table trace where it applies: 1D, order 4, and an unwrapped cell
 // count that stays far inside int (|U| grows by at most |V| + 1 per
 // substep; the margin of 4 covers the kicks' change of V).
-// 2D: also a table of at most 4 GiB (24 doubles per cell and slab).
+// 2D: also a table of at most 4 GiB (24 doubles per cell and slab).  3D:
+// the cell-unit trace on the slab itself (no table).
 bool fp64_table_supported(const Problem &p, long long Nt)
 {
-    if ((p.dim != 1 && p.dim != 2) || p.order != 4) return false;
+    if (p.order != 4) return false;
     for (int a = 0; a < p.dim; ++a) {
         const double vmax = fmax(fabs(p.vmin[a]), fabs(p.vmin[a] + p.M[a] * p.dv[a]));
         if (!((double(Nt) + 1) * (vmax * p.dt * p.dxinv[a] + 1) * 4 + p.N[a] < 2147483647.0)) return false;
@@ -281,11 +390,12 @@ bool fp64_table_supported(const Problem &p, long long Nt)
 
 long long fp64_table_stride(const Problem &p)
 {
-    return p.dim == 1 ? (3LL * p.N[0] + 1) / 2 * 2 : (24LL * p.Ns + 1) / 2 * 2;
+    return p.dim == 1 ? (3LL * p.N[0] + 1) / 2 * 2 : p.dim == 2 ? (24LL * p.Ns + 1) / 2 * 2 : 0;
 }
 
 cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, double *table_slab, cudaStream_t st)
 {
+    if (p.dim == 3) return cudaSuccess;  // no table
     if (p.dim == 1)
         derive_table64_kernel<<<unsigned((p.N[0] + 127) / 128), 128, 0, st>>>(p, hist_slab, table_slab);
     else
@@ -293,26 +403,41 @@ cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, dou
     return cudaGetLastError();
 }
 
-cudaError_t launch_trace_fp64_table(const Problem &p, const LaunchShape &ls, const double *tables, int n,
-                                    long long qb, long long qe, double *partial, int *rows, unsigned *err,
-                                    cudaStream_t st)
+cudaError_t launch_trace_fp64_table(const Problem &p, const LaunchShape &ls, const double *tables,
+                                    const double *hist, int n, long long qb, long long qe, double *partial,
+                                    int *rows, unsigned *err, cudaStream_t st)
 {
-    *rows = ls.vblocks;
+    *rows = fp64_rows(ls);
     const dim3 block(32, ls.warps);
-    const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(ls.vblocks));
+    const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(fp64_rows(ls)));
+    const int vb = ls.vblocks;
     const long long ts = fp64_table_stride(p);
     bool pow2 = true;
     for (int a = 0; a < p.dim; ++a) pow2 = pow2 && (p.N[a] & (p.N[a] - 1)) == 0;
+    if (p.dim == 3) {  // the planner caps 3D at 2 points per thread
+#define NUFI_LAUNCH3(K)                                                                                        \
+    if (pow2)                                                                                                  \
+        trace_fp64_3d_cells_kernel<K, true><<<grid, block, 0, st>>>(p, hist, n, qb, qe, vb, partial, err);     \
+    else                                                                                                       \
+        trace_fp64_3d_cells_kernel<K, false><<<grid, block, 0, st>>>(p, hist, n, qb, qe, vb, partial, err);
+        switch (ls.ppt) {
+        case 1: NUFI_LAUNCH3(1) break;
+        case 2: NUFI_LAUNCH3(2) break;
+        default: return cudaErrorInvalidValue;
+        }
+#undef NUFI_LAUNCH3
+        return cudaGetLastError();
+    }
 #define NUFI_LAUNCH(K)                                                                                         \
     if (p.dim == 2) {                                                                                          \
         if (pow2)                                                                                              \
-            trace_fp64_2d_table_kernel<K, true><<<grid, block, 0, st>>>(p, tables, ts, n, qb, qe, partial, err); \
+            trace_fp64_2d_table_kernel<K, true><<<grid, block, 0, st>>>(p, tables, ts, n, qb, qe, vb, partial, err); \
         else                                                                                                   \
-            trace_fp64_2d_table_kernel<K, false><<<grid, block, 0, st>>>(p, tables, ts, n, qb, qe, partial, err); \
+            trace_fp64_2d_table_kernel<K, false><<<grid, block, 0, st>>>(p, tables, ts, n, qb, qe, vb, partial, err); \
     } else if (pow2)                                                                                           \
-        trace_fp64_1d_table_kernel<K, true><<<grid, block, 0, st>>>(p, tables, ts, n, qb, qe, partial, err);   \
+        trace_fp64_1d_table_kernel<K, true><<<grid, block, 0, st>>>(p, tables, ts, n, qb, qe, vb, partial, err);   \
     else                                                                                                       \
-        trace_fp64_1d_table_kernel<K, false><<<grid, block, 0, st>>>(p, tables, ts, n, qb, qe, partial, err);
+        trace_fp64_1d_table_kernel<K, false><<<grid, block, 0, st>>>(p, tables, ts, n, qb, qe, vb, partial, err);
     switch (ls.ppt) {
     case 1: NUFI_LAUNCH(1) break;
     case 2: NUFI_LAUNCH(2) break;

@@ -331,3 +331,30 @@ def test_metrics_match_reference(nufi, name, precision):
         assert np.allclose(parts, g["metrics"][-1], rtol=1e-12, atol=1e-15)
         with pytest.raises(IndexError):
             sim.compute_metrics(cfg.Nt + 1)
+
+
+def test_fp64_velocity_grid_beyond_one_launch_row(nufi, oracle_mod):
+    """A velocity grid with more blocks than the launch grid's y axis holds
+    (2D, 1024^2 velocity nodes: 65536 blocks of 16 against 65535): the FP64
+    traces stride over the extra blocks.  rho (the cell-unit order-4 trace)
+    and the metrics (the general FP64 trace) against the oracle on the same
+    history."""
+    from numericalflowiteration_gb300.config import landau_2d
+    cfg = landau_2d(Nx=4, Nv=1024, Nt=3)
+    with nufi.Simulation(cfg) as sim:
+        assert sim.describe()["fp64_shape"]["vblocks"] > 65535
+        sim.run(0, cfg.Nt)
+        hist = sim.history()
+        sim.compute_rho(cfg.Nt)
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+        sim.compute_metrics(cfg.Nt)
+        m = sim.download_metrics()
+    oracle_mod.set_summation(1)
+    try:
+        want = oracle_mod.rho(cfg, cfg.Nt, hist)
+        want_m = oracle_mod.metrics(cfg, cfg.Nt, hist)
+    finally:
+        oracle_mod.set_summation(0)
+    assert rel_max(rho, want) <= 1e-12
+    for k in range(4):
+        assert abs(m[k] - want_m[k]) <= 1e-12 * abs(want_m[k]), k

@@ -149,7 +149,8 @@ def test_plans_nd(sms):
         if cfg.precision == "fp32split":
             want = "trace_split_nd_kernel"
         else:  # 2D order 4: the cell-unit trace over FP64 derivative tables
-            want = "trace_fp64_2d_table_kernel" if (cfg.dim == 2 and cfg.order == 4) else "trace_fp64_kernel"
+            want = {2: "trace_fp64_2d_table_kernel", 3: "trace_fp64_3d_cells_kernel"}[cfg.dim] \
+                if cfg.order == 4 else "trace_fp64_kernel"
         assert pl["trace"] == want
 
 

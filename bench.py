@@ -480,6 +480,10 @@ def run_ours(args, cfg):
         e2e = e2e_c_loop(cfg_split, local, max(2, args.steps), ws, ps)
         e2e["python_loop"] = e2e_python_loop(nufi, cfg_split, local, max(1, args.steps // 2), ws, ps)
 
+    batch = None
+    if rank == 0 and ws == 1 and not args.no_batch:
+        batch = batch_leg(nufi, local, max(2, min(3, args.steps)))
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_windows(cfg.replace(precision="fp64"), parse_windows(args.cpu_windows, cfg.Nt),
@@ -494,7 +498,7 @@ def run_ours(args, cfg):
                            "point_steps_per_step": ps, "precision": "fp32-split (FP64 rho/solve)",
                            "l2": "flushed between timed steps (256 MB write)",
                            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
-                "fp64_plain": fp64, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "fp64_plain": fp64, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "batch": batch,
                 "gpu_launches": launches, "clocks": clocks}
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -570,6 +574,74 @@ def run_batch(args):
     return 0
 
 
+def batch_leg(nufi, device: int, reps: int, instances: int = 256, fd_instances: int = 4, fd_h: float = 1e-6):
+    """The batched workload (seeded bump-on-tail instances of uneven sizes,
+    Nx in {64,128,256}, Nv in {256,512,1024}, T = 20) in the FP32-split
+    form: forward and adjoint (gradient of J = int |E|^2 dt with respect to
+    alpha, k, u_b, sigma_b of every instance) timed with CUDA events on the
+    batch stream, clocks sampled over the timed calls, and the gradient of
+    `fd_instances` evenly spaced instances checked against central
+    differences of the FP64 forward (single-instance runs, h = fd_h
+    relative to each parameter's scale of 1)."""
+    import torch
+    from numericalflowiteration_gb300.config import batched_bump_on_tail
+    cfgs = batched_bump_on_tail(count=instances)
+    ps = sum(c.point_steps() for c in cfgs)
+
+    def timed(b, fn):
+        ext = torch.cuda.ExternalStream(b.stream, device=torch.device("cuda", device))
+        out = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(ext):
+                e0.record()
+            fn()
+            with torch.cuda.stream(ext):
+                e1.record()
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return statistics.median(out)
+
+    with nufi.Batch([c.replace(precision="fp32split") for c in cfgs], device=device) as b:
+        b.forward()
+        b.backward()  # warm-up of both graphs
+        torch.cuda.synchronize()
+        sampler = ClockSampler(device)
+        sampler.start()
+        t0 = time.monotonic()
+        ms_f = timed(b, b.forward)
+        ms_b = timed(b, b.backward)
+        t1 = time.monotonic()
+        clocks = sampler.stop(t0, t1)
+        G = b.backward()
+        chosen = b.describe()["autotune"]["chosen"]
+    # central differences of the FP64 forward on sampled instances
+    pick = [int(round(i * (instances - 1) / max(1, fd_instances - 1))) for i in range(fd_instances)]
+    fd_err = []
+    for i in pick:
+        c = cfgs[i]
+        fd = np.zeros(4)
+        for k in range(4):
+            pp = list(c.f0_params)
+            pp[k] += fd_h
+            with nufi.Simulation(c.replace(f0_params=list(pp)), device=device) as s:
+                jp = s.forward()
+            pp[k] -= 2 * fd_h
+            with nufi.Simulation(c.replace(f0_params=list(pp)), device=device) as s:
+                jm = s.forward()
+            fd[k] = (jp - jm) / (2 * fd_h)
+        fd_err.append(float(np.max(np.abs(G[i] - fd)) / np.max(np.abs(fd))))
+    return {"workload": f"batched_bump_on_tail_{instances}", "instances": instances, "point_steps": ps,
+            "precision": "fp32-split (FP64 rho/solve; FP64 sums of the table adjoints)",
+            "forward_ms": ms_f, "forward_point_steps_per_s": ps / (ms_f * 1e-3), "backward_ms": ms_b,
+            "backward_cost_vs_forward": ms_b / ms_f, "target_cost_vs_forward": 3.0,
+            "grad_vs_central_differences": {"instances": pick, "h": fd_h,
+                                            "max_err_rel_to_instance_max": max(fd_err), "per_instance": fd_err,
+                                            "tolerance": 1e-5},
+            "autotune_chosen": chosen, "timed_reps": reps, "clocks": clocks}
+
+
 def profile_case(args, cfg):
     """One run of steps 0..nt in one precision; prints the chosen kernels."""
     import numericalflowiteration_gb300 as nufi
@@ -596,6 +668,7 @@ def main(argv=None):
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="leave out the batched forward/adjoint leg")
     ap.add_argument("--cpu-windows", default="0:12,200:6,400:6,600:4,-4:4",
                     help="CPU baseline and reference arm: timed step windows first:count (negative first: "
                          "from the end); the whole run is extrapolated from them")

@@ -76,3 +76,25 @@ def test_split_dropin_two_stream_256x1024_later_steps(nufi):
             sim.compute_rho(n)
             got = sim.download_rho(np.zeros(cfg.n_spatial))
             assert rel_max(got, g["rho_comp"][list(g["rho_steps"]).index(n)]) <= 1e-6, n
+
+
+def test_fp64_landau_3d_16x32_first_steps(nufi):
+    """The 3D workload at its own size (16^3 x 32^3: 134M points per step)
+    over its first 10 steps, FP64, against the reference's run."""
+    cfg, g = golden("landau_3d_16x32_n10")
+    n_last = int(g["n_last"])
+    with nufi.Simulation(cfg) as sim:
+        e = sim.run(0, n_last)
+        hist = sim.history()
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+    _check_run(cfg, g, e, hist, rho)
+
+
+def test_split_landau_3d_16x32_first_steps_within_gate(nufi):
+    cfg, g = golden("landau_3d_16x32_n10")
+    n_last = int(g["n_last"])
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        e = sim.run(0, n_last)
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+    assert rel_max(e, g["energy_comp"][:n_last + 1]) <= 1e-6
+    assert rel_max(rho, g["rho_comp"][list(g["rho_steps"]).index(n_last)]) <= 1e-6

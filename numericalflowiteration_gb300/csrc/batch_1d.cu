@@ -179,18 +179,17 @@ __global__ void __launch_bounds__(256, 1) batch_trace_fp64_kernel(const BatchIns
 
 // rho of every instance: one warp per (instance, node), lanes over the
 // instance's unit rows in fixed stride with Neumaier compensation.
-__global__ void batch_reduce_kernel(const BatchInst *__restrict__ bi, const int *__restrict__ node_inst,
-                                    long long total_nodes, int n)
+__device__ __forceinline__ void batch_reduce_node(const BatchInst *__restrict__ bi, const int *__restrict__ node_inst,
+                                                  long long g, int lane, int n)
 {
-    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (g >= total_nodes) return;
     const BatchInst &I = bi[node_inst[g]];
     if (n > I.Nt) return;
     const int N = I.p.N[0];
     const int s = int(g - I.node_begin);
     double sum = 0, comp = 0;
-    for (int r = lane; r < I.units; r += 32) neumaier_add(sum, comp, I.partial[(long long)r * N + s]);
+    // __ldcg: in the whole-forward kernel the rows were written by other
+    // SMs during this launch (L1 is not coherent across SMs)
+    for (int r = lane; r < I.units; r += 32) neumaier_add(sum, comp, __ldcg(I.partial + (long long)r * N + s));
     for (int off = 16; off > 0; off >>= 1) {
         const double os = __shfl_down_sync(0xffffffffu, sum, off);
         const double oc = __shfl_down_sync(0xffffffffu, comp, off);
@@ -198,6 +197,14 @@ __global__ void batch_reduce_kernel(const BatchInst *__restrict__ bi, const int 
         comp += oc;
     }
     if (lane == 0) I.rho[s] = -I.p.wv * (sum + comp);
+}
+
+__global__ void batch_reduce_kernel(const BatchInst *__restrict__ bi, const int *__restrict__ node_inst,
+                                    long long total_nodes, int n)
+{
+    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g >= total_nodes) return;
+    batch_reduce_node(bi, node_inst, g, threadIdx.x & 31, n);
 }
 
 // Fixed-order block sum (any multiple of 32 threads).
@@ -213,20 +220,17 @@ __device__ __forceinline__ double bsum(double v, double *red)
 }
 
 // Field solve of every instance: block = 8 nodes of one instance, one warp
-// per node (circulant products of field_solve.cu; green from global).
+// per node (circulant products of field_solve.cu; green from global).  The
+// body, for solve block b of the batch, called by all 256 threads of a
+// block (rs, red, ered, last in shared memory).
 template <int NCONV>
-__global__ void __launch_bounds__(256, 1) batch_solve_kernel(const BatchInst *__restrict__ bi,
-                                                          const int *__restrict__ solve_inst, int n)
+__device__ __forceinline__ void batch_solve_block(const BatchInst &I, int b, int n, double *rs, double *red,
+                                                  double *ered, bool *last_flag)
 {
-    __shared__ double rs[kBatchMaxN];
-    __shared__ double red[8];
-    __shared__ double ered[8];
-    __shared__ bool last;
-    const BatchInst &I = bi[solve_inst[blockIdx.x]];
-    if (n > I.Nt) return;
+    bool &last = *last_flag;
     const Problem &p = I.p;
     const int N = p.N[0];
-    const int lb = blockIdx.x - I.solve_begin;
+    const int lb = b - I.solve_begin;
     double part = 0;
     for (int j = threadIdx.x; j < N; j += blockDim.x) {
         const double r = __ldcg(I.rho + j);
@@ -274,12 +278,154 @@ __global__ void __launch_bounds__(256, 1) batch_solve_kernel(const BatchInst *__
         last = atomicAdd(I.ecount, 1u) == unsigned(I.solve_blocks - 1);
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return;
-    __threadfence();
-    double tot = 0;
-    for (int b = 0; b < I.solve_blocks; ++b) tot += __ldcg(I.epart + b);
-    I.energy[n] = tot * (p.L[0] / (2.0 * double(N)));
-    *I.ecount = 0u;
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double tot = 0;
+        for (int q = 0; q < I.solve_blocks; ++q) tot += __ldcg(I.epart + q);
+        I.energy[n] = tot * (p.L[0] / (2.0 * double(N)));
+        *I.ecount = 0u;
+    }
+}
+
+template <int NCONV>
+__global__ void __launch_bounds__(256, 1) batch_solve_kernel(const BatchInst *__restrict__ bi,
+                                                          const int *__restrict__ solve_inst, int n)
+{
+    __shared__ double rs[kBatchMaxN];
+    __shared__ double red[8];
+    __shared__ double ered[8];
+    __shared__ bool last;
+    const BatchInst &I = bi[solve_inst[blockIdx.x]];
+    if (n > I.Nt) return;
+    batch_solve_block<NCONV>(I, blockIdx.x, n, rs, red, ered, &last);
+}
+
+// The whole batched FP32-split forward (steps n0..n1 of every instance) in
+// one cooperative launch, the treatment run_split_1d.cu gives one 1D run:
+// the grid stays resident (co-resident CTAs of 256 threads) and the phases
+// of each step are separated by the bounded grid barrier of
+// split_device.cuh:
+//   trace   units u = blockIdx.x, blockIdx.x + G, ...: the unit's chains
+//           through slabs n-1..0 of its instance's tables, streamed through
+//           this CTA's shared-memory ring (the chunk counter g runs on over
+//           the units, so every slot's phase stays consistent); its
+//           partial row, as batch_trace_split_kernel
+//   barrier
+//   reduce  warps over the (instance, node) pairs: rho (batch_reduce_node)
+//   barrier
+//   solve   solve blocks b = blockIdx.x, blockIdx.x + G, ...: 8 nodes of one
+//           instance each, slab n, table n and W_n (batch_solve_block)
+//   barrier
+// The next step's bulk copies read the tables the solve wrote (generic
+// stores made visible by the barrier); fence.proxy.async.global orders
+// them.  An instance whose Nt is below n sits the step out.  Same
+// arithmetic as the graph of per-step launches, and so the same results.
+template <int PPT, bool POW2>
+__global__ void __launch_bounds__(256, 1) batch_run_split_kernel(const BatchInst *__restrict__ bi,
+                                                              const int *__restrict__ unit_inst, int units,
+                                                              const int *__restrict__ node_inst,
+                                                              long long total_nodes,
+                                                              const int *__restrict__ solve_inst, int solve_blocks,
+                                                              int n0, int n1, int S, unsigned *sync, unsigned *err)
+{
+    extern __shared__ __align__(128) float ring[];
+    __shared__ __align__(8) unsigned long long full_bar[kRing];
+    __shared__ double comb[256];
+    __shared__ double rs[kBatchMaxN];
+    __shared__ double red[8];
+    __shared__ double ered[8];
+    __shared__ bool last;
+    unsigned *count = sync, *abort = sync + 1;
+    unsigned target = 0;
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < kRing; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned g = 0;  // chunks this CTA has consumed: slot g % kRing, parity (g / kRing) & 1
+    bool ok = true;
+    const int warps = int(blockDim.x >> 5), lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int n = n0; n <= n1; ++n) {
+        // ---------------- trace of step n over this CTA's units ----------------
+        if (threadIdx.x == 0) fence_proxy_async_global();
+        for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+            const BatchInst &I = bi[unit_inst[unit]];
+            if (n > I.Nt) continue;
+            const Problem &p = I.p;
+            const UnitMap um = unit_map(I, unit - I.unit_begin, PPT);
+            const int N = um.N;
+            const long long Nm = p.Nm;
+            int Ic[PPT], S0m[PPT];
+            float xi[PPT], dwT[PPT], dwTc[PPT], shi[PPT], slo[PPT];
+            bool live[PPT];
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                const long long m = um.m0 + q;
+                live[q] = m < Nm;
+                const SplitNode nd = I.nodes[live[q] ? m : 0];
+                S0m[q] = nd.S0 + kMagicBits;
+                shi[q] = nd.sig_hi;
+                slo[q] = nd.sig_lo;
+                Ic[q] = um.s;
+                xi[q] = 0.0f;
+                dwT[q] = slo[q];
+                dwTc[q] = 0.0f;
+            }
+            if (n > 0) {
+                const int TS = int(p.table_stride);
+                const int nchunks = (n + S - 1) / S;
+                const unsigned slab_bytes = unsigned(TS) * 4u;
+                auto issue = [&](int j) {  // chunk j of this unit into slot (g + j) % kRing
+                    const int k_hi = n - 1 - j * S;
+                    const int k_lo = max(0, k_hi - S + 1);
+                    const unsigned bytes = unsigned(k_hi - k_lo + 1) * slab_bytes;
+                    const unsigned slot = (g + unsigned(j)) % kRing;
+                    const unsigned bar = smem_addr(&full_bar[slot]);
+                    fence_proxy_async_shared();  // the slot's earlier reads (generic) before the copy
+                    mbar_expect_tx(bar, bytes);
+                    bulk_g2s(smem_addr(ring + slot * S * TS), I.tables + (long long)k_lo * TS, bytes, bar);
+                };
+                if (threadIdx.x == 0)
+                    for (int j = 0; j < kRing && j < nchunks; ++j) issue(j);
+                for (int j = 0; j < nchunks; ++j) {
+                    const unsigned gj = g + unsigned(j), slot = gj % kRing;
+                    ok &= mbar_wait(smem_addr(&full_bar[slot]), (gj / kRing) & 1u);
+                    const int k_hi = n - 1 - j * S;
+                    const int k_lo = max(0, k_hi - S + 1);
+                    trace_chunk<PPT, POW2>(ring + slot * S * TS, TS, k_hi, k_lo, N, Ic, xi, dwT, dwTc, shi, S0m,
+                                           err);
+                    __syncthreads();  // everyone is done with this slot
+                    if (threadIdx.x == 0 && j + kRing < nchunks) issue(j + kRing);
+                }
+                g += unsigned(nchunks);
+            }
+            const F0 f = make_f0(p);
+            double acc = 0;
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                if (!live[q]) continue;
+                const SplitNode nd = I.nodes[um.m0 + q];
+                acc += double(delta_f0(f, nd, __ldg(I.phase + Ic[q]), xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
+            }
+            acc = combine_groups(acc, um, comb);
+            if (um.grp == 0) I.partial[(long long)(unit - I.unit_begin) * N + um.s] = acc;
+            __syncthreads();  // comb is reused by the next unit
+        }
+        if (!grid_barrier(count, target, abort, err)) break;
+        // ---------------- rho of every instance ----------------
+        for (long long gw = (long long)blockIdx.x * warps + warp; gw < total_nodes; gw += (long long)gridDim.x * warps)
+            batch_reduce_node(bi, node_inst, gw, lane, n);
+        if (!grid_barrier(count, target, abort, err)) break;
+        // ---------------- field solve of every instance ----------------
+        for (int b = blockIdx.x; b < solve_blocks; b += gridDim.x) {
+            const BatchInst &I = bi[solve_inst[b]];
+            if (n > I.Nt) continue;
+            batch_solve_block<5>(I, b, n, rs, red, ered, &last);
+            __syncthreads();  // rs / red / ered / last are reused by the next block
+        }
+        if (!grid_barrier(count, target, abort, err)) break;
+    }
+    if (!ok) atomicOr(err, kErrStageTimeout);
 }
 
 // lambda_m of every instance (adjoint_1d.cu): one block per instance.
@@ -965,6 +1111,64 @@ int adjoint_split_ctas_per_sm(const BatchLaunch &L, int ppt)
     if (cudaFuncSetAttribute(fs, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fs, kAdjThreads, smem) != cudaSuccess) return 0;
     return nb;
+}
+
+namespace {
+
+using BatchRunFn = void (*)(const BatchInst *, const int *, int, const int *, long long, const int *, int, int, int,
+                            int, unsigned *, unsigned *);
+
+template <int PPT>
+BatchRunFn batch_run_fn(bool pow2)
+{
+    return pow2 ? batch_run_split_kernel<PPT, true> : batch_run_split_kernel<PPT, false>;
+}
+
+BatchRunFn batch_run_pick(const BatchLaunch &L)
+{
+    switch (L.ppt) {
+    case 1: return batch_run_fn<1>(L.pow2);
+    case 2: return batch_run_fn<2>(L.pow2);
+    case 4: return batch_run_fn<4>(L.pow2);
+    case 8: return batch_run_fn<8>(L.pow2);
+    default: return nullptr;
+    }
+}
+
+}  // namespace
+
+// Co-resident CTAs of the whole-forward kernel for L's shape on a device
+// with `sms` multiprocessors (0 if it cannot run).
+int batch_run_ctas(const BatchLaunch &L, int sms)
+{
+    const BatchRunFn fn = batch_run_pick(L);
+    if (!fn || L.precision != NUFI_PREC_FP32_SPLIT) return 0;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.smem)) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 256, L.smem) != cudaSuccess) return 0;
+    return std::min(L.units, nb * sms);
+}
+
+cudaError_t launch_batch_run(const BatchLaunch &L, int ctas, int n0, int n1, unsigned *sync, cudaStream_t st)
+{
+    const BatchRunFn fn = batch_run_pick(L);
+    if (!fn || ctas < 1) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.smem));
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(ctas));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = L.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, fn, L.inst, L.unit_inst, L.units, L.node_inst, L.total_nodes, L.solve_inst,
+                              L.solve_blocks, n0, n1, L.slabs_per_chunk, sync, L.err);
 }
 
 cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st)

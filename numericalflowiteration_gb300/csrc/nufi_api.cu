@@ -1439,6 +1439,10 @@ struct nufi_batch {
     long long point_steps = 0;
     cudaGraphExec_t fwd = nullptr, bwd = nullptr;
     bool forward_done = false;
+    // FP32-split forward as one cooperative launch (batch_run_split_kernel)
+    // when the autotuner found it faster: its CTAs (0: per-step launches)
+    int run_ctas = 0;
+    unsigned *run_sync = nullptr;
     std::string last_error, tune;
     std::vector<void *> allocations;
 };
@@ -1580,7 +1584,43 @@ int batch_autotune(nufi_batch *b)
     if (st) return st;
     b->L.slabs_per_chunk = std::max(1, bc.S);
     b->L.smem = size_t(kRingSlots) * b->L.slabs_per_chunk * ts_max * sizeof(float);
-    log += "], \"adjoint\": [";
+    // The whole forward as one cooperative launch against the per-step
+    // launches, both timed over three mid-run steps (trace, rho, solve).
+    int sms0 = 1;
+    cudaDeviceGetAttribute(&sms0, cudaDevAttrMultiProcessorCount, b->device);
+    const int run_ctas =
+        (b->precision == NUFI_PREC_FP32_SPLIT && !b->opt.no_persistent) ? batch_run_ctas(b->L, sms0) : 0;
+    {
+        const int n_a = n_t, n_b = std::min(b->maxNt, n_t + 2);
+        float ms_steps = 0, ms_run = -1;
+        if (tune && run_ctas > 0) {
+            ms_steps = batch_time(b, [&] {
+                cudaError_t e = cudaSuccess;
+                for (int n = n_a; n <= n_b && e == cudaSuccess; ++n) e = launch_batch_step(b->L, n, b->stream);
+                return e;
+            }, 1);
+            if (ms_steps < 0) return bcuda(b, cudaGetLastError(), "autotune forward steps");
+        }
+        if (run_ctas > 0) {
+            cudaError_t ea = balloc(b, &b->run_sync, 2);
+            if (ea != cudaSuccess) return bcuda(b, ea, "cudaMalloc");
+            ms_run = batch_time(b, [&] { return launch_batch_run(b->L, run_ctas, n_a, n_b, b->run_sync, b->stream); },
+                                1);
+            if (ms_run < 0) {  // the cooperative launch did not run here: keep the per-step launches
+                cudaGetLastError();
+                ms_run = -1;
+            }
+        }
+        b->run_ctas = (run_ctas > 0 && ms_run >= 0 && (!tune || ms_run <= ms_steps)) ? run_ctas : 0;
+        char item[256];
+        std::snprintf(item, sizeof(item),
+                      "], \"forward\": {\"per_step_launches_ms\": %.4f, \"one_launch_ms\": %.4f, "
+                      "\"one_launch_ctas\": %d, \"steps\": [%d, %d], \"chosen\": \"%s\"}",
+                      ms_steps, ms_run, run_ctas, n_a, n_b,
+                      b->run_ctas ? "one cooperative launch" : "graph of per-step launches");
+        log += item;
+    }
+    log += ", \"adjoint\": [";
     const bool split = b->precision == NUFI_PREC_FP32_SPLIT;
     std::vector<int> acands = tune ? (split ? std::vector<int>{2, 4} : std::vector<int>{1, 2, 4})
                                    : std::vector<int>{split ? 4 : 2};
@@ -1835,6 +1875,8 @@ int nufi_batch_forward(nufi_batch *b, double *J)
     DeviceGuard g(b->device);
     if (!b->fwd) {
         int st = capture(b, &b->fwd, [&] {
+            if (b->run_ctas > 0)  // the whole forward: one cooperative launch
+                return launch_batch_run(b->L, b->run_ctas, 0, b->maxNt, b->run_sync, b->stream);
             cudaError_t e = cudaSuccess;
             for (int n = 0; n <= b->maxNt && e == cudaSuccess; ++n) e = launch_batch_step(b->L, n, b->stream);
             return e;
@@ -1913,7 +1955,10 @@ int nufi_batch_stream(const nufi_batch *b, void **stream)
 int nufi_batch_describe(const nufi_batch *b, char *buf, size_t len)
 {
     if (!b || !buf || len == 0) return bfail(nullptr, NUFI_ERR_INVALID, "null argument");
-    const std::string s = "{\"instances\": " + std::to_string(b->L.count) + ", \"units\": " +
+    const std::string s = "{\"instances\": " + std::to_string(b->L.count) + ", \"forward_launch\": \"" +
+                          (b->run_ctas ? "batch_run_split_kernel (one cooperative launch)"
+                                       : "graph of per-step launches") +
+                          "\", \"forward_ctas\": " + std::to_string(b->run_ctas) + ", \"units\": " +
                           std::to_string(b->L.units) + ", \"adjoint_units\": " + std::to_string(b->L.adj_units) +
                           ", \"solve_blocks\": " + std::to_string(b->L.solve_blocks) + ", \"max_Nt\": " +
                           std::to_string(b->maxNt) + ", \"point_steps\": " + std::to_string(b->point_steps) +
@@ -1927,11 +1972,11 @@ int nufi_batch_describe(const nufi_batch *b, char *buf, size_t len)
 // ---------------------------------------------------------------------------
 // Allocation-free rho (nufi_compute_rho_noalloc).
 //
-// For callers that must not allocate device memory: code that runs while
-// allocations are forbidden or would stall (a host thread inside another
-// library's CUDA-graph capture or memory pool, a real-time loop that
-// pre-reserves everything, an embedding that owns the device memory
-// budget).  The caller passes the coefficient history and rho as device
+// For callers that must not allocate device memory: a plugin whose host
+// framework owns all device memory through its own pool and forbids direct
+// allocation, or a real-time loop that reserves its device memory up front
+// because cudaMalloc can synchronise the device and take unbounded time.
+// The caller passes the coefficient history and rho as device
 // buffers; the trace's scratch (per-block partial sums and an error word)
 // lives in the file-scope array below, which every GPU that loads
 // this library holds until the process exits.

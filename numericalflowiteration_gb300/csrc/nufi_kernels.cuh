@@ -247,6 +247,12 @@ struct BatchLaunch {
 };
 cudaError_t launch_batch_trace(const BatchLaunch &L, int n, cudaStream_t st);
 cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st);
+// The whole FP32-split batched forward, steps n0..n1, as one cooperative
+// launch of `ctas` CTAs (batch_run_split_kernel); sync = {barrier count,
+// abort flag}.  batch_run_ctas: the co-resident CTAs for L's shape (0: the
+// kernel cannot run, use the per-step launches).
+int batch_run_ctas(const BatchLaunch &L, int sms);
+cudaError_t launch_batch_run(const BatchLaunch &L, int ctas, int n0, int n1, unsigned *sync, cudaStream_t st);
 cudaError_t launch_batch_adjoint_step(const BatchLaunch &L, int m, cudaStream_t st);
 cudaError_t launch_batch_theta_reduce(const BatchLaunch &L, double *grad, cudaStream_t st);
 constexpr int kAdjChunk = 8;  // slabs per checkpointed chunk of the FP32-split adjoint

@@ -137,3 +137,28 @@ def test_batch_split_adjoint_matches_fp64_and_differences(nufi):
             fd = (bp.forward() - bm.forward()) / (2 * h)
         for j in range(2):
             assert abs(Gs[j, i] - fd[j]) <= 1e-5 * np.max(np.abs(G64[j])), (i, j, Gs[j, i], fd[j])
+
+
+def test_batch_split_one_launch_matches_per_step_launches(nufi):
+    """The whole FP32-split batched forward as one cooperative launch
+    (batch_run_split_kernel: all steps of all instances, grid barriers
+    between the phases) against the CUDA graph of per-step launches: the
+    same arithmetic in the same order, so the same bits; the adjoint runs
+    on either forward's history."""
+    cfgs = [c.replace(precision="fp32split") for c in small_batch()]
+    with nufi.Batch(cfgs, opts={"batch_no_autotune": 1}) as a:
+        d = a.describe()
+        assert d["forward_launch"].startswith("batch_run_split_kernel") and d["forward_ctas"] > 0
+        Ja = a.forward()
+        Ea = [a.energy(i) for i in range(len(cfgs))]
+        assert np.array_equal(a.forward(), Ja)
+        Ga = a.backward()
+    with nufi.Batch(cfgs, opts={"batch_no_autotune": 1, "no_persistent": 1}) as b:
+        assert b.describe()["forward_launch"] == "graph of per-step launches"
+        Jb = b.forward()
+        Eb = [b.energy(i) for i in range(len(cfgs))]
+        Gb = b.backward()
+    assert np.array_equal(Ja, Jb)
+    for i in range(len(cfgs)):
+        assert np.array_equal(Ea[i], Eb[i]), i
+    assert rel(Ga, Gb) <= 1e-6

@@ -22,7 +22,8 @@
  * k = 0.5; 2D: Landau with alpha = 0.5, k = 0.5; 3D: bump-on-tail with
  * alpha = 0.03, k = 0.3, u_b = 4.5, sigma_b = 0.5; nufi/config.hpp), each
  * reproduced to the last bit by the matching f0 kind.  real = double runs
- * the FP64 plain form, real = float the FP32-split form.
+ * the FP64 plain form, real = float the FP32-split form (built for order 4;
+ * float kernels of other orders run the FP64 plain form).
  */
 #ifndef NUFI_CUDA_KERNEL_HPP
 #define NUFI_CUDA_KERNEL_HPP
@@ -80,15 +81,22 @@ struct handle_deleter {
     void operator()(nufi_handle *h) const noexcept { nufi_destroy(h); }
 };
 
+// real = float runs the FP32-split form, which is built for cubic splines
+// (order 4); cuda_kernel<float, order> of any other order runs the FP64
+// plain form instead (results at FP64 accuracy, at the FP64 rate), so that
+// every <real, order> the reference instantiates has a kernel here.
 template <typename real>
-int precision_of() { return std::is_same<real, float>::value ? NUFI_PREC_FP32_SPLIT : NUFI_PREC_FP64; }
+int precision_of(int order)
+{
+    return (std::is_same<real, float>::value && order == 4) ? NUFI_PREC_FP32_SPLIT : NUFI_PREC_FP64;
+}
 
 // config_t -> nufi_config, per dimension (members of nufi/config.hpp).
 template <typename real>
 nufi_config to_c(const nufi::dim1::config_t<real> &c, int order)
 {
     nufi_config k{};
-    k.dim = 1; k.order = order; k.precision = precision_of<real>();
+    k.dim = 1; k.order = order; k.precision = precision_of<real>(order);
     k.Nx[0] = (int64_t)c.Nx; k.Nv[0] = (int64_t)c.Nu; k.Nx[1] = k.Nx[2] = k.Nv[1] = k.Nv[2] = 1;
     k.Nt = (int64_t)c.Nt; k.dt = c.dt;
     k.x_min[0] = c.x_min; k.x_max[0] = c.x_max; k.v_min[0] = c.u_min; k.v_max[0] = c.u_max;
@@ -103,7 +111,7 @@ template <typename real>
 nufi_config to_c(const nufi::dim2::config_t<real> &c, int order)
 {
     nufi_config k{};
-    k.dim = 2; k.order = order; k.precision = precision_of<real>();
+    k.dim = 2; k.order = order; k.precision = precision_of<real>(order);
     k.Nx[0] = (int64_t)c.Nx; k.Nx[1] = (int64_t)c.Ny; k.Nx[2] = 1;
     k.Nv[0] = (int64_t)c.Nu; k.Nv[1] = (int64_t)c.Nv; k.Nv[2] = 1;
     k.Nt = (int64_t)c.Nt; k.dt = c.dt;
@@ -120,7 +128,7 @@ template <typename real>
 nufi_config to_c(const nufi::dim3::config_t<real> &c, int order)
 {
     nufi_config k{};
-    k.dim = 3; k.order = order; k.precision = precision_of<real>();
+    k.dim = 3; k.order = order; k.precision = precision_of<real>(order);
     k.Nx[0] = (int64_t)c.Nx; k.Nx[1] = (int64_t)c.Ny; k.Nx[2] = (int64_t)c.Nz;
     k.Nv[0] = (int64_t)c.Nu; k.Nv[1] = (int64_t)c.Nv; k.Nv[2] = (int64_t)c.Nw;
     k.Nt = (int64_t)c.Nt; k.dt = c.dt;

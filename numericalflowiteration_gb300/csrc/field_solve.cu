@@ -218,8 +218,182 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Spectral form of the same solve for grids above kCirculantMaxNodes: the
+// dense circulant product costs Ns^2 FMAs per kernel, the transforms
+// Ns sum_a N_a.  rho' = rho - mean(rho); rho^ = DFT(rho') (sign -), one
+// axis at a time; c^ = D_c rho^, phi^ = D_phi rho^ with the diagonals the
+// circulant kernels are made from (host, long double); c, phi = the
+// unnormalised inverse DFTs (sign +; the 1/Ns is in D).  Each axis pass is a
+// dense DFT of one line per block in shared memory (N_a <= 4096), FP64.
+namespace {
+
+__global__ void spectral_mean_kernel(const Problem p, const double *__restrict__ rho, double *__restrict__ mean)
+{
+    __shared__ double red[kSolveThreads];
+    double part = 0;
+    for (long long j = threadIdx.x; j < p.Ns; j += blockDim.x) part += rho[j];
+    const double tot = block_sum_fixed(part, red);
+    if (threadIdx.x == 0) mean[0] = tot / double(p.Ns);
+}
+
+// One axis of the DFT over NA arrays in place: block = one line of axis a
+// (length N, stride S in the node index), x_k <- sum_j x_j w^{s jk}, with
+// w = e^{2 pi i / N} (tw) and s = -1 (forward) or +1.  REAL_IN: the line is
+// read from the real rho (minus the mean) instead of work[0].
+template <int NA, bool REAL_IN>
+__global__ void __launch_bounds__(kSolveThreads) spectral_axis_kernel(const Problem p, int N, long long S,
+                                                                    const double2 *__restrict__ tw, double sign,
+                                                                    double2 *work, const double *__restrict__ rho,
+                                                                    const double *__restrict__ mean)
+{
+    extern __shared__ double2 line[];  // [NA][N]
+    const long long l = blockIdx.x;    // line: (lo, hi) with node = hi * N * S + j * S + lo
+    const long long lo = l % S, hi = l / S;
+    const long long base = hi * (long long)N * S + lo;
+    const double m = REAL_IN ? mean[0] : 0.0;
+    for (int a = 0; a < NA; ++a)
+        for (int j = threadIdx.x; j < N; j += blockDim.x) {
+            const long long idx = base + (long long)j * S;
+            line[a * N + j] = REAL_IN ? make_double2(rho[idx] - m, 0.0) : work[(long long)a * p.Ns + idx];
+        }
+    __syncthreads();
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+        double re[NA], im[NA];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) re[a] = im[a] = 0.0;
+        int e = 0;  // (j k) mod N
+        for (int j = 0; j < N; ++j) {
+            const double2 w = tw[e];
+            const double wi = sign * w.y;
+#pragma unroll
+            for (int a = 0; a < NA; ++a) {
+                const double2 x = line[a * N + j];
+                re[a] = fma(x.x, w.x, fma(-x.y, wi, re[a]));
+                im[a] = fma(x.x, wi, fma(x.y, w.x, im[a]));
+            }
+            e += k;
+            if (e >= N) e -= N;
+        }
+#pragma unroll
+        for (int a = 0; a < NA; ++a) work[(long long)a * p.Ns + base + (long long)k * S] = make_double2(re[a], im[a]);
+    }
+}
+
+// c^ = D_c rho^ (work[1]), phi^ = D_phi rho^ (work[2])
+__global__ void spectral_scale_kernel(const Problem p, const double2 *__restrict__ diag, double2 *work)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.Ns) return;
+    const double2 x = work[i];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        const double2 d = diag[c * p.Ns + i];
+        work[(c + 1) * p.Ns + i] = make_double2(d.x * x.x - d.y * x.y, d.x * x.y + d.y * x.x);
+    }
+}
+
+// Slab (every padded position of node i) from Re c, and W_n = prod L /
+// (2 Ns) sum_i rho'_i phi_i (block parts in fixed order, the last block
+// sums them, as circulant_solve_kernel).
+__global__ void __launch_bounds__(kSolveThreads) spectral_finish_kernel(
+    const Problem p, const double *__restrict__ rho, const double *__restrict__ mean,
+    const double2 *__restrict__ work, double *__restrict__ slab, double *__restrict__ energy_partial,
+    unsigned *__restrict__ energy_counter, double *__restrict__ energy_out)
+{
+    __shared__ double red[kSolveThreads];
+    __shared__ bool last;
+    const long long Ns = p.Ns;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double e_local = 0;
+    if (i < Ns) {
+        const int N0 = p.N[0], N1 = p.N[1], N2 = p.N[2];
+        const int i0 = int(i % N0), i1 = int((i / N0) % N1), i2 = int(i / ((long long)N0 * N1));
+        const double cval = work[Ns + i].x;
+        for (int dz = 0; dz < 2; ++dz) {
+            const int k = i2 + dz * N2;
+            if (k >= p.P[2]) continue;
+            for (int dy = 0; dy < 2; ++dy) {
+                const int jj = i1 + dy * N1;
+                if (jj >= p.P[1]) continue;
+                for (int dx = 0; dx < 2; ++dx) {
+                    const int ii = i0 + dx * N0;
+                    if (ii >= p.P[0]) continue;
+                    slab[((long long)k * p.P[1] + jj) * p.P[0] + ii] = cval;
+                }
+            }
+        }
+        e_local = (rho[i] - mean[0]) * work[2 * Ns + i].x;
+    }
+    const double eb = block_sum_fixed(e_local, red);
+    if (threadIdx.x == 0) energy_partial[blockIdx.x] = eb;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(energy_counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double v = 0;
+    for (int b = threadIdx.x; b < int(gridDim.x); b += blockDim.x) v += __ldcg(energy_partial + b);
+    const double tot = block_sum_fixed(v, red);
+    if (threadIdx.x == 0) {
+        double Lp = 1;
+        for (int ax = 0; ax < p.dim; ++ax) Lp *= p.L[ax];
+        if (energy_out) energy_out[0] = tot * (Lp / (2.0 * double(Ns)));
+        energy_counter[0] = 0u;
+    }
+}
+
+cudaError_t launch_spectral_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
+                                  float *table_slab, double *energy_out, cudaStream_t st)
+{
+    spectral_mean_kernel<<<1, kSolveThreads, 0, st>>>(p, rho, plan.mean);
+    long long S = 1, toff = 0;
+    for (int a = 0; a < p.dim; ++a) {  // forward
+        const int N = p.N[a];
+        const unsigned lines = unsigned(p.Ns / N);
+        if (a == 0)
+            spectral_axis_kernel<1, true><<<lines, kSolveThreads, size_t(N) * 16, st>>>(
+                p, N, S, plan.twiddle + toff, -1.0, plan.work, rho, plan.mean);
+        else
+            spectral_axis_kernel<1, false><<<lines, kSolveThreads, size_t(N) * 16, st>>>(
+                p, N, S, plan.twiddle + toff, -1.0, plan.work, rho, plan.mean);
+        S *= N;
+        toff += N;
+    }
+    spectral_scale_kernel<<<unsigned((p.Ns + 255) / 256), 256, 0, st>>>(p, plan.diag, plan.work);
+    S = 1;
+    toff = 0;
+    for (int a = 0; a < p.dim; ++a) {  // inverse, c^ and phi^ together
+        const int N = p.N[a];
+        spectral_axis_kernel<2, false><<<unsigned(p.Ns / N), kSolveThreads, size_t(2 * N) * 16, st>>>(
+            p, N, S, plan.twiddle + toff, 1.0, plan.work + p.Ns, rho, plan.mean);
+        S *= N;
+        toff += N;
+    }
+    const unsigned fb = unsigned((p.Ns + kSolveThreads - 1) / kSolveThreads);
+    spectral_finish_kernel<<<fb, kSolveThreads, 0, st>>>(p, rho, plan.mean, plan.work, hist_slab,
+                                                         plan.energy_partial, plan.energy_counter, energy_out);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && table_slab) e = launch_derive_table(p, hist_slab, table_slab, st);
+    return e;
+}
+
+}  // namespace
+
 cudaError_t field_solve_prepare(const SolvePlan &plan)
 {
+    if (plan.spectral) {
+        cudaError_t e = cudaFuncSetAttribute(spectral_axis_kernel<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kSpectralMaxAxis * 16);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(spectral_axis_kernel<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kSpectralMaxAxis * 16);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(spectral_axis_kernel<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     2 * kSpectralMaxAxis * 16);
+        return e;
+    }
     cudaError_t e = cudaFuncSetAttribute(circulant_solve_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(plan.smem));
     if (e != cudaSuccess) return e;
@@ -230,6 +404,7 @@ cudaError_t field_solve_prepare(const SolvePlan &plan)
 cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
                                float *table_slab, double *energy_out, cudaStream_t st)
 {
+    if (plan.spectral) return launch_spectral_solve(p, plan, rho, hist_slab, table_slab, energy_out, st);
     if (plan.nconv == 5)
         circulant_solve_kernel<5><<<plan.blocks, kSolveThreads, plan.smem, st>>>(
             p, rho, plan.green, plan.green_in_smem, plan.nodes_per_block, hist_slab, table_slab, plan.energy_partial,

@@ -382,9 +382,20 @@ void plan_traces(const Problem &p, int sms, const nufi_options &opt, LaunchShape
 // Shape of the field solve (its node limit and grid), with no CUDA call.
 bool solve_geometry(const Problem &p, int sms, SolvePlan &pl, std::string &why)
 {
-    if (p.Ns > 16384) {
-        why = "device field solve holds at most 16384 grid nodes";
-        return false;
+    if (p.Ns > kCirculantMaxNodes) {
+        // the spectral form: per-axis DFTs, one line per block in shared memory
+        for (int a = 0; a < p.dim; ++a)
+            if (p.N[a] > kSpectralMaxAxis) {
+                why = "device field solve: above 16384 grid nodes every axis must hold at most 4096 nodes";
+                return false;
+            }
+        pl.spectral = true;
+        pl.nconv = 2;
+        pl.blocks = int((p.Ns + 255) / 256);  // the finishing kernel's blocks (energy parts)
+        pl.nodes_per_block = 0;
+        pl.smem = 0;
+        pl.green_in_smem = false;
+        return true;
     }
     pl.nconv = (p.precision == NUFI_PREC_FP32_SPLIT && p.dim == 1) ? 5 : 2;
     // nodes per block: enough blocks to cover the SMs, up to 8 warps per node
@@ -417,7 +428,9 @@ PersistentRun plan_persistent(const Problem &p, const StagedShape &staged, const
 // i.e. drops that mode: the same pseudo-inverse here.  In 1D split mode
 // three more kernels give K (A, B, C) of the per-cell quadratic directly
 // (shifts of c are phase factors of its diagonal).
-std::vector<double> solve_green(const Problem &p, int nconv)
+// The diagonals of the field solve in Fourier space (before the inverse
+// DFT of solve_green): [nconv][Ns] complex, long double.
+std::vector<std::complex<long double>> solve_diagonals(const Problem &p, int nconv)
 {
     const long long Ns = p.Ns;
     using cld = std::complex<long double>;
@@ -483,6 +496,15 @@ std::vector<double> solve_green(const Problem &p, int nconv)
             D[4 * Ns + s] = (K / 2) * (cld(-1, 0) + 3.0L * w(1) - 3.0L * w(2) + w(3)) * dc;
         }
     }
+    return D;
+}
+
+std::vector<double> solve_green(const Problem &p, int nconv)
+{
+    using cld = std::complex<long double>;
+    const long long Ns = p.Ns;
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    std::vector<cld> D = solve_diagonals(p, nconv);
     // inverse DFT (sign +, unnormalised), axis by axis, all kernels
     long long stride = 1;
     for (int a = 0; a < p.dim; ++a) {
@@ -518,8 +540,32 @@ int build_solve_plan(nufi_handle *h, int sms)
     const Problem &p = h->p;
     h->solve_ok = false;
     if (!solve_geometry(p, sms, h->plan, h->solve_why)) return NUFI_OK;
-    const std::vector<double> green = solve_green(p, h->plan.nconv);
     SolvePlan &pl = h->plan;
+    if (pl.spectral) {
+        const std::vector<std::complex<long double>> D = solve_diagonals(p, 2);
+        std::vector<double2> dg(D.size());
+        for (size_t i = 0; i < D.size(); ++i) dg[i] = make_double2(double(D[i].real()), double(D[i].imag()));
+        std::vector<double2> tw;
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        for (int a = 0; a < p.dim; ++a)
+            for (int k = 0; k < p.N[a]; ++k) {
+                const long double ang = two_pi * (long double)k / (long double)p.N[a];
+                tw.push_back(make_double2(double(cosl(ang)), double(sinl(ang))));
+            }
+        NUFI_CUDA(h, dalloc(h, &pl.diag, dg.size()));
+        NUFI_CUDA(h, dalloc(h, &pl.work, size_t(3) * size_t(p.Ns)));
+        NUFI_CUDA(h, dalloc(h, &pl.twiddle, tw.size()));
+        NUFI_CUDA(h, dalloc(h, &pl.mean, 1));
+        NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(pl.blocks)));
+        NUFI_CUDA(h, dalloc(h, &pl.energy_counter, 1));
+        NUFI_CUDA(h, cudaMemcpy(pl.diag, dg.data(), dg.size() * sizeof(double2), cudaMemcpyHostToDevice));
+        NUFI_CUDA(h, cudaMemcpy(pl.twiddle, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
+        NUFI_CUDA(h, cudaMemset(pl.energy_counter, 0, sizeof(unsigned)));
+        NUFI_CUDA(h, field_solve_prepare(pl));
+        h->solve_ok = true;
+        return NUFI_OK;
+    }
+    const std::vector<double> green = solve_green(p, h->plan.nconv);
     NUFI_CUDA(h, dalloc(h, &pl.green, green.size()));
     // also holds one part per CTA of the persistent run kernel
     NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(std::max(pl.blocks, kMaxCtasPerSm * sms))));
@@ -1142,6 +1188,8 @@ int nufi_backward(nufi_handle *h, int64_t n1, double *grad)
     if (!h->aplan.ok)
         return fail(h, NUFI_ERR_UNSUPPORTED, "backward: built for 1D, orders 4 and 6 (odd-degree splines)");
     if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
+    if (h->plan.spectral)
+        return fail(h, NUFI_ERR_UNSUPPORTED, "backward: grids of at most 16384 nodes (the circulant field solve)");
     for (int64_t n = 0; n <= n1; ++n)
         if (!h->slab_set[size_t(n)])
             return fail(h, NUFI_ERR_RANGE, "backward: slabs 0..n1 not present (run the forward first)");
@@ -1331,11 +1379,12 @@ std::string plan_json(const nufi_handle *h, bool layout)
         "\"staged\": {\"ok\": %d, \"ctas\": %d, \"threads\": %d, \"ppt\": %d, \"slabs_per_chunk\": %d, "
         "\"ring\": %d, \"smem\": %zu}, \"run\": \"%s\", \"persistent\": {\"ok\": %d, \"ctas\": %d, "
         "\"threads\": %d, \"ppt\": %d, \"smem\": %zu}, \"solve\": {\"ok\": %d, \"kernel\": "
-        "\"circulant_solve_kernel<%d>\", \"blocks\": %d, \"nodes_per_block\": %d}}",
+        "\"%s<%d>\", \"blocks\": %d, \"nodes_per_block\": %d}}",
         trace, h->shape.warps, h->shape.ppt, h->shape.vblocks, int(h->staged.ok), h->staged.ctas,
         h->staged.threads, h->staged.ppt, h->staged.slabs_per_chunk, h->staged.ring, h->staged.smem,
         h->persist.ok ? "run_split_1d_kernel" : "graph of per-step launches", int(h->persist.ok), h->persist.ctas,
-        h->persist.threads, h->persist.ppt, h->persist.smem, int(h->solve_ok), h->plan.nconv, h->plan.blocks,
+        h->persist.threads, h->persist.ppt, h->persist.smem, int(h->solve_ok),
+        h->plan.spectral ? "spectral_solve" : "circulant_solve_kernel", h->plan.nconv, h->plan.blocks,
         h->plan.nodes_per_block);
     if (k < 0 || size_t(k) >= sizeof(tmp)) return std::string();
     std::string s(tmp);

@@ -179,7 +179,16 @@ struct SolvePlan {
     bool green_in_smem = false;
     double *energy_partial = nullptr;  // [max(blocks, SMs)]
     unsigned *energy_counter = nullptr;
+    // Grids above kCirculantMaxNodes: the same diagonals applied between
+    // per-axis DFTs (spectral_*), O(Ns sum_a N_a) instead of O(Ns^2).
+    bool spectral = false;
+    double2 *diag = nullptr;     // [2][Ns] D_c, D_phi (complex)
+    double2 *work = nullptr;     // [3][Ns] rho^, c^, phi^
+    double2 *twiddle = nullptr;  // e^{+2 pi i k / N_a}, axes one after another
+    double *mean = nullptr;      // [1]
 };
+constexpr long long kCirculantMaxNodes = 16384;
+constexpr int kSpectralMaxAxis = 4096;  // a line (complex FP64) in shared memory
 
 // Poisson + collocation solve of one step: padded slab n (FP64), the FP32
 // table n (when table_slab != null) and the electric energy W_n.

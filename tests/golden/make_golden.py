@@ -103,6 +103,9 @@ SOLVE_CASES = {
     "solve_3d_16": landau_3d(),
     "solve_1d_64_order3": landau_1d(order=3),
     "solve_1d_64_order5": landau_1d(order=5),
+    # above 16384 nodes the device solve takes its spectral form
+    "solve_2d_256": landau_2d(Nx=256, Nv=4),
+    "solve_3d_32": landau_3d(Nx=32, Nv=4),
 }
 
 

@@ -303,10 +303,13 @@ def test_metrics_match_reference(nufi, name, precision):
     FP64, also behind a split handle); download accumulates."""
     cfg, g = golden(name)
     hist = np.ascontiguousarray(g["slabs"].reshape(-1))
-    try:
-        sim = nufi.Simulation(cfg.replace(precision=precision))
-    except NotImplementedError:
-        pytest.skip("split form not built for this order")
+    if precision == "fp32split" and cfg.order != 4:
+        # the FP32-split form is built for order 4; the C ABI refuses other
+        # orders (the C++ drop-in maps <float, order> to the FP64 form)
+        with pytest.raises(NotImplementedError):
+            nufi.Simulation(cfg.replace(precision=precision))
+        precision = "fp64"
+    sim = nufi.Simulation(cfg.replace(precision=precision))
     with sim:
         for n in range(int(g["n_last"]) + 1):
             sim.upload_phi(n, hist)
@@ -358,3 +361,27 @@ def test_fp64_velocity_grid_beyond_one_launch_row(nufi, oracle_mod):
     assert rel_max(rho, want) <= 1e-12
     for k in range(4):
         assert abs(m[k] - want_m[k]) <= 1e-12 * abs(want_m[k]), k
+
+
+@pytest.mark.parametrize("which", ["2d", "3d"])
+def test_spectral_solve_run_matches_oracle(nufi, oracle_mod, which):
+    """Grids above 16384 nodes take the spectral field solve (per-axis DFTs
+    around the same diagonals as the circulant kernels): a 256^2 (2D) and a
+    32^3 (3D) run, FP64 against the oracle with compensated sums (1e-12),
+    and the FP32-split form within its gate."""
+    from numericalflowiteration_gb300.config import landau_2d, landau_3d
+    cfg = landau_2d(Nx=256, Nv=4, Nt=3) if which == "2d" else landau_3d(Nx=32, Nv=2, Nt=3)
+    with nufi.Simulation(cfg) as sim:
+        assert sim.describe()["solve"]["kernel"] == "spectral_solve<2>"
+        e = sim.run()
+        hist = sim.history()
+    oracle_mod.set_summation(1)
+    try:
+        e_ref, _, h_ref = oracle_mod.run(cfg, 0, cfg.Nt)
+    finally:
+        oracle_mod.set_summation(0)
+    assert rel_max(e, e_ref) <= 1e-12
+    assert rel_max(hist, h_ref) <= 1e-11
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        es = sim.run()
+    assert rel_max(es, e_ref) <= 1e-6

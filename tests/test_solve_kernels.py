@@ -69,6 +69,6 @@ def test_split_rows_are_the_cell_quadratic(name):
 
 
 def test_kernel_errors():
-    from numericalflowiteration_gb300.config import landau_2d
+    from numericalflowiteration_gb300.config import landau_1d
     with pytest.raises(NotImplementedError):
-        solve_kernels(landau_2d(Nx=256, Nv=8, Nt=2))  # 65536 nodes
+        solve_kernels(landau_1d(Nx=20000, Nv=8, Nt=2))  # above 16384 nodes with an axis above 4096

@@ -615,7 +615,9 @@ def batch_leg(nufi, device: int, reps: int, instances: int = 256, fd_instances: 
         t1 = time.monotonic()
         clocks = sampler.stop(t0, t1)
         G = b.backward()
-        chosen = b.describe()["autotune"]["chosen"]
+        desc = b.describe()
+        chosen = dict(desc["autotune"]["chosen"], forward_launch=desc["forward_launch"],
+                      forward_timing=desc["autotune"].get("forward"))
     # central differences of the FP64 forward on sampled instances
     pick = [int(round(i * (instances - 1) / max(1, fd_instances - 1))) for i in range(fd_instances)]
     fd_err = []

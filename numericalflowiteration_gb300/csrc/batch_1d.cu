@@ -680,11 +680,11 @@ __device__ __forceinline__ void adj_chunk_primal(const float *__restrict__ chunk
             U[2 * pp + 1] = U[2 * pp + 1] - S0um[2 * pp + 1] + __float_as_int(mg1);
             const int J0 = U[2 * pp] & mask, J1 = U[2 * pp + 1] & mask;
             X[pp] = f2_sub(t, f2_sub(mg, MAG2));
-            const float2 ab0 = reinterpret_cast<const float2 *>(tk)[J0];
-            const float2 ab1 = reinterpret_cast<const float2 *>(tk)[J1];
-            const unsigned long long C2 = f2_pack(tk[2 * N + J0], tk[2 * N + J1]);
+            const float2 bc0 = reinterpret_cast<const float2 *>(tk)[J0];
+            const float2 bc1 = reinterpret_cast<const float2 *>(tk)[J1];
+            const unsigned long long C2 = f2_pack(bc0.y, bc1.y);
             const unsigned long long kq =
-                f2_fma(X[pp], f2_fma(X[pp], C2, f2_pack(ab0.y, ab1.y)), f2_pack(ab0.x, ab1.x));
+                f2_fma(X[pp], f2_fma(X[pp], C2, f2_pack(bc0.x, bc1.x)), f2_pack(tk[2 * N + J0], tk[2 * N + J1]));
             DC[pp] = i == 0 ? f2_fma(H0, kq, DC[pp]) : f2_add(DC[pp], kq);
             if constexpr (SAVE) {
                 Jp[i][pp] = unsigned(J0) | (unsigned(J1) << 16);
@@ -721,8 +721,10 @@ __device__ __forceinline__ void adj_chunk_reverse(const float *__restrict__ chun
         for (int pp = 0; pp < NP; ++pp) {
             const int J0 = int(Jp[i][pp] & 0xffffu), J1 = int(Jp[i][pp] >> 16);
             const unsigned long long x = Xs[i][pp];
-            const unsigned long long gp = f2_fma(f2_add(x, x), f2_pack(tk[2 * N + J0], tk[2 * N + J1]),
-                                                 f2_pack(tk[2 * J0 + 1], tk[2 * J1 + 1]));
+            // g' = K B + 2 K C xi from one float2 per chain
+            const float2 bc0 = reinterpret_cast<const float2 *>(tk)[J0];
+            const float2 bc1 = reinterpret_cast<const float2 *>(tk)[J1];
+            const unsigned long long gp = f2_fma(f2_add(x, x), f2_pack(bc0.y, bc1.y), f2_pack(bc0.x, bc1.x));
             const unsigned long long vh = i == 0 ? f2_mul(VB[pp], H0) : VB[pp];
             const unsigned long long vx = f2_mul(vh, x);
             const unsigned long long vxx = f2_mul(vx, x);

@@ -57,23 +57,25 @@ __device__ __forceinline__ void write_partial_tiled(double acc, long long s, lon
 
 // 1D split kick table of one slab: for cell i the derivative of the cubic
 // spline sum on [i, i+1) as a quadratic in xi, times K = -dt^2/dx^2:
-// K A, K B as a float2 at [2i, 2i+1] and K C at [2N + i] (3N floats, padded
+// K B, K C as a float2 at [2i, 2i+1] and K A at [2N + i] (3N floats, padded
 // to a multiple of 4).  Two loads per lookup, 12 bytes: three shared-memory
-// wavefronts per warp instead of four for a float4 with a dead lane.
+// wavefronts per warp instead of four for a float4 with a dead lane; the
+// adjoint's reverse sweep, which needs only the derivative K B + 2 K C xi,
+// reads the one float2.
 __device__ __forceinline__ void store_kick_entry(float *slab, int N, int i, float A, float B, float C)
 {
-    reinterpret_cast<float2 *>(slab)[i] = make_float2(A, B);
-    slab[2 * N + i] = C;
+    reinterpret_cast<float2 *>(slab)[i] = make_float2(B, C);
+    slab[2 * N + i] = A;
 }
 __device__ __forceinline__ float kick_lookup(const float *slab, int N, int i, float xi)
 {
-    const float2 ab = reinterpret_cast<const float2 *>(slab)[i];
-    return fmaf(xi, fmaf(xi, slab[2 * N + i], ab.y), ab.x);
+    const float2 bc = reinterpret_cast<const float2 *>(slab)[i];
+    return fmaf(xi, fmaf(xi, bc.y, bc.x), slab[2 * N + i]);
 }
 __device__ __forceinline__ float kick_lookup_ldg(const float *slab, int N, int i, float xi)
 {
-    const float2 ab = __ldg(reinterpret_cast<const float2 *>(slab) + i);
-    return fmaf(xi, fmaf(xi, __ldg(slab + 2 * N + i), ab.y), ab.x);
+    const float2 bc = __ldg(reinterpret_cast<const float2 *>(slab) + i);
+    return fmaf(xi, fmaf(xi, bc.y, bc.x), __ldg(slab + 2 * N + i));
 }
 
 // Block sums of the four metrics into partial[k * blocks + block] (fixed

@@ -321,7 +321,7 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
     float dwC_last = 0.0f;
     auto substep = [&](const float *__restrict__ tk, float h) {
         const unsigned long long H2 = f2_pack(h, h);
-        // table of this slab in the shared window: (K A, K B) at tb + 8 J, K C at tc + 4 J
+        // table of this slab in the shared window: (K B, K C) at tb + 8 J, K A at tc + 4 J
         const unsigned tb = smem_addr(tk), tc = tb + unsigned(N) * 8u;
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
@@ -334,13 +334,13 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
             I[2 * p] = J0;
             I[2 * p + 1] = J1;
             X[p] = f2_sub(t, f2_sub(mg, MAG2));
-            const float2 ab0 = lds_f32x2(tb + unsigned(J0) * 8u);
-            const float2 ab1 = lds_f32x2(tb + unsigned(J1) * 8u);
-            const float c0 = lds_f32(tc + unsigned(J0) * 4u);
-            const float c1 = lds_f32(tc + unsigned(J1) * 4u);
-            const unsigned long long C2 = f2_pack(c0, c1);
-            const unsigned long long q = f2_fma(X[p], C2, f2_pack(ab0.y, ab1.y));
-            const unsigned long long kq = f2_fma(X[p], q, f2_pack(ab0.x, ab1.x));
+            const float2 bc0 = lds_f32x2(tb + unsigned(J0) * 8u);
+            const float2 bc1 = lds_f32x2(tb + unsigned(J1) * 8u);
+            const float a0 = lds_f32(tc + unsigned(J0) * 4u);
+            const float a1 = lds_f32(tc + unsigned(J1) * 4u);
+            const unsigned long long C2 = f2_pack(bc0.y, bc1.y);
+            const unsigned long long q = f2_fma(X[p], C2, f2_pack(bc0.x, bc1.x));
+            const unsigned long long kq = f2_fma(X[p], q, f2_pack(a0, a1));
             DC[p] = (h == 1.0f) ? f2_add(DC[p], kq) : f2_fma(H2, kq, DC[p]);
         }
         if constexpr (PPT % 2 == 1) {

@@ -326,9 +326,10 @@ __global__ void __launch_bounds__(256, 1) batch_run_split_kernel(const BatchInst
                                                               const int *__restrict__ node_inst,
                                                               long long total_nodes,
                                                               const int *__restrict__ solve_inst, int solve_blocks,
-                                                              int n0, int n1, int S, unsigned *sync, unsigned *err)
+                                                              int n0, int n1, int S, int ts_max, unsigned *sync,
+                                                              unsigned *err)
 {
-    extern __shared__ __align__(128) float ring[];
+    extern __shared__ __align__(128) float ring[];  // [kRing][S][ts_max]
     __shared__ __align__(8) unsigned long long full_bar[kRing];
     __shared__ double comb[256];
     __shared__ double rs[kBatchMaxN];
@@ -347,10 +348,35 @@ __global__ void __launch_bounds__(256, 1) batch_run_split_kernel(const BatchInst
     const int warps = int(blockDim.x >> 5), lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int n = n0; n <= n1; ++n) {
         // ---------------- trace of step n over this CTA's units ----------------
+        // Slots have a fixed stride (S slabs of the batch's widest table), so
+        // thread 0 can fill a slot the current unit has released with the
+        // next unit's first chunks (prefetch; never past the step: the next
+        // step's newest tables come from this step's solve).
         if (threadIdx.x == 0) fence_proxy_async_global();
-        for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+        const int SW = S * ts_max;  // floats per slot
+        auto live_from = [&](int u) {  // the first unit from u on that takes part in step n
+            for (; u < units; u += gridDim.x)
+                if (n <= bi[unit_inst[u]].Nt) return u;
+            return units;
+        };
+        const int nchunks = n > 0 ? (n + S - 1) / S : 0;  // the same for every unit of the step
+        // chunk j of unit u into slot (gbase + j) % kRing
+        auto issue = [&](int u, int j, unsigned gbase) {
+            const BatchInst &J = bi[unit_inst[u]];
+            const int TS = int(J.p.table_stride);
+            const int k_hi = n - 1 - j * S;
+            const int k_lo = max(0, k_hi - S + 1);
+            const unsigned bytes = unsigned(k_hi - k_lo + 1) * unsigned(TS) * 4u;
+            const unsigned slot = (gbase + unsigned(j)) % kRing;
+            const unsigned bar = smem_addr(&full_bar[slot]);
+            fence_proxy_async_shared();  // the slot's earlier reads (generic) before the copy
+            mbar_expect_tx(bar, bytes);
+            bulk_g2s(smem_addr(ring + slot * SW), J.tables + (long long)k_lo * TS, bytes, bar);
+        };
+        int pre = 0;  // chunks of the current unit already issued by the previous one
+        for (int unit = live_from(blockIdx.x); unit < units;) {
+            const int nxt = live_from(unit + gridDim.x);
             const BatchInst &I = bi[unit_inst[unit]];
-            if (n > I.Nt) continue;
             const Problem &p = I.p;
             const UnitMap um = unit_map(I, unit - I.unit_begin, PPT);
             const int N = um.N;
@@ -371,33 +397,31 @@ __global__ void __launch_bounds__(256, 1) batch_run_split_kernel(const BatchInst
                 dwT[q] = slo[q];
                 dwTc[q] = 0.0f;
             }
-            if (n > 0) {
+            if (nchunks > 0) {
                 const int TS = int(p.table_stride);
-                const int nchunks = (n + S - 1) / S;
-                const unsigned slab_bytes = unsigned(TS) * 4u;
-                auto issue = [&](int j) {  // chunk j of this unit into slot (g + j) % kRing
-                    const int k_hi = n - 1 - j * S;
-                    const int k_lo = max(0, k_hi - S + 1);
-                    const unsigned bytes = unsigned(k_hi - k_lo + 1) * slab_bytes;
-                    const unsigned slot = (g + unsigned(j)) % kRing;
-                    const unsigned bar = smem_addr(&full_bar[slot]);
-                    fence_proxy_async_shared();  // the slot's earlier reads (generic) before the copy
-                    mbar_expect_tx(bar, bytes);
-                    bulk_g2s(smem_addr(ring + slot * S * TS), I.tables + (long long)k_lo * TS, bytes, bar);
-                };
-                if (threadIdx.x == 0)
-                    for (int j = 0; j < kRing && j < nchunks; ++j) issue(j);
+                if (threadIdx.x == 0) {
+                    for (int j = pre; j < kRing && j < nchunks; ++j) issue(unit, j, g);
+                    // slots this unit leaves unused take the next unit's first chunks
+                    if (nxt < units)
+                        for (int jn = 0; jn < kRing - nchunks && jn < nchunks; ++jn) issue(nxt, jn, g + nchunks);
+                }
                 for (int j = 0; j < nchunks; ++j) {
                     const unsigned gj = g + unsigned(j), slot = gj % kRing;
                     ok &= mbar_wait(smem_addr(&full_bar[slot]), (gj / kRing) & 1u);
                     const int k_hi = n - 1 - j * S;
                     const int k_lo = max(0, k_hi - S + 1);
-                    trace_chunk<PPT, POW2>(ring + slot * S * TS, TS, k_hi, k_lo, N, Ic, xi, dwT, dwTc, shi, S0m,
-                                           err);
+                    trace_chunk<PPT, POW2>(ring + slot * SW, TS, k_hi, k_lo, N, Ic, xi, dwT, dwTc, shi, S0m, err);
                     __syncthreads();  // everyone is done with this slot
-                    if (threadIdx.x == 0 && j + kRing < nchunks) issue(j + kRing);
+                    if (threadIdx.x == 0) {
+                        const int jj = j + kRing;
+                        if (jj < nchunks)
+                            issue(unit, jj, g);
+                        else if (nxt < units && jj - nchunks < nchunks)
+                            issue(nxt, jj - nchunks, g + nchunks);
+                    }
                 }
                 g += unsigned(nchunks);
+                pre = nxt < units ? (nchunks < kRing ? nchunks : kRing) : 0;
             }
             const F0 f = make_f0(p);
             double acc = 0;
@@ -410,6 +434,7 @@ __global__ void __launch_bounds__(256, 1) batch_run_split_kernel(const BatchInst
             acc = combine_groups(acc, um, comb);
             if (um.grp == 0) I.partial[(long long)(unit - I.unit_begin) * N + um.s] = acc;
             __syncthreads();  // comb is reused by the next unit
+            unit = nxt;
         }
         if (!grid_barrier(count, target, abort, err)) break;
         // ---------------- rho of every instance ----------------
@@ -1118,7 +1143,7 @@ int adjoint_split_ctas_per_sm(const BatchLaunch &L, int ppt)
 namespace {
 
 using BatchRunFn = void (*)(const BatchInst *, const int *, int, const int *, long long, const int *, int, int, int,
-                            int, unsigned *, unsigned *);
+                            int, int, unsigned *, unsigned *);
 
 template <int PPT>
 BatchRunFn batch_run_fn(bool pow2)
@@ -1170,7 +1195,7 @@ cudaError_t launch_batch_run(const BatchLaunch &L, int ctas, int n0, int n1, uns
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, fn, L.inst, L.unit_inst, L.units, L.node_inst, L.total_nodes, L.solve_inst,
-                              L.solve_blocks, n0, n1, L.slabs_per_chunk, sync, L.err);
+                              L.solve_blocks, n0, n1, L.slabs_per_chunk, L.ts_max, sync, L.err);
 }
 
 cudaError_t launch_batch_step(const BatchLaunch &L, int n, cudaStream_t st)

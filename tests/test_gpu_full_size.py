@@ -98,3 +98,54 @@ def test_split_landau_3d_16x32_first_steps_within_gate(nufi):
         rho = sim.download_rho(np.zeros(cfg.n_spatial))
     assert rel_max(e, g["energy_comp"][:n_last + 1]) <= 1e-6
     assert rel_max(rho, g["rho_comp"][list(g["rho_steps"]).index(n_last)]) <= 1e-6
+
+
+def _points_golden():
+    """The 3D Landau workload's later steps, pinned on a given history
+    (tests/golden/make_points_golden.py): the reference's rho at steps 10,
+    50, 100 over all 134M points, and its eval_ftilda at 2^20 seeded points
+    (the first 2^16 values exactly, all of them through the sums of 1024
+    blocks of 1024 points)."""
+    import importlib.util
+    from conftest import GOLDEN
+    from numericalflowiteration_gb300.config import Config
+    spec = importlib.util.spec_from_file_location("make_points_golden", GOLDEN / "make_points_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    z = np.load(GOLDEN / "landau_3d_16x32_points.npz")
+    return mod, Config.from_bytes(z["config"].tobytes()), z
+
+
+def test_fp64_landau_3d_16x32_later_steps_and_points(nufi):
+    """FP64 rho at steps 10, 50, 100 of the 16^3 x 32^3 workload (all 134M
+    points) and f~ at 2^20 points of phase space, on the history the
+    reference's code was evaluated on: 1e-12 (rel_max)."""
+    mod, cfg, z = _points_golden()
+    hist = np.ascontiguousarray(z["hist32"].astype(np.float64))
+    pts = mod.points_3d(int(z["npts"]), int(z["seed"]))
+    nb = int(z["block"])
+    with nufi.Simulation(cfg) as sim:
+        for n in range(cfg.Nt + 1):
+            sim.upload_phi(n, hist)
+        for i, n in enumerate(z["steps"]):
+            sim.compute_rho(int(n))
+            rho = sim.download_rho(np.zeros(cfg.n_spatial))
+            assert rel_max(rho, z["rho_comp"][i]) <= 1e-12, int(n)
+            f = sim.eval_points(int(n), pts, mode=sim.EVAL_FTILDA)
+            ne = z["f_exact"].shape[1]
+            assert rel_max(f[:ne], z["f_exact"][i]) <= 1e-12, int(n)
+            assert rel_max(f.reshape(-1, nb).sum(axis=1), z["f_block_sums"][i]) <= 1e-12, int(n)
+
+
+def test_split_landau_3d_16x32_later_steps_within_gate(nufi):
+    """The FP32-split rho at steps 10, 50, 100 on the same history (its
+    tables derived from the uploaded FP64 slabs) against the reference's."""
+    mod, cfg, z = _points_golden()
+    hist = np.ascontiguousarray(z["hist32"].astype(np.float64))
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        for n in range(cfg.Nt + 1):
+            sim.upload_phi(n, hist)
+        for i, n in enumerate(z["steps"]):
+            sim.compute_rho(int(n))
+            rho = sim.download_rho(np.zeros(cfg.n_spatial))
+            assert rel_max(rho, z["rho_comp"][i]) <= 1e-6, int(n)

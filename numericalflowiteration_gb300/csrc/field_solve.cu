@@ -22,6 +22,8 @@
 // to zero, and removing the O(1) background first keeps the rounding
 // relative to the perturbation.  W = prod L / (2 N) * sum_i rho'_i phi_i
 // (Parseval), equal to the reference's spectral sum.  Everything is FP64.
+#include <algorithm>
+
 #include "nufi_kernels.cuh"
 
 namespace nufi_gb300 {
@@ -66,6 +68,28 @@ __global__ void reduce_metrics_kernel(long long blocks, const double *__restrict
         comp += oc;
     }
     if (lane == 0) out[k] = sum + comp;
+}
+
+// Small transfers between device memory and the handle's pinned host
+// block, done by a kernel: the block is mapped into the device's address
+// space (unified addressing), so the copy is one queued launch behind the
+// work before it instead of a copy-engine transfer with its own start-up.
+// The device error word, when given, travels in the same launch.
+__global__ void copy_words_kernel(const double *__restrict__ src, double *__restrict__ dst, long long n,
+                                  const unsigned *__restrict__ err_src, unsigned *__restrict__ err_dst)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i];
+    if (err_src && blockIdx.x == 0 && threadIdx.x == 0) *err_dst = *err_src;
+}
+
+cudaError_t launch_copy_words(const double *src, double *dst, long long n, const unsigned *err_src, unsigned *err_dst,
+                              cudaStream_t st)
+{
+    const int threads = 256;
+    const int blocks = int(std::min<long long>(std::max<long long>((n + threads - 1) / threads, 1), 32));
+    copy_words_kernel<<<blocks, threads, 0, st>>>(src, dst, n, err_src, err_dst);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_reduce_metrics(long long blocks, const double *partial, double *metrics, cudaStream_t st)

@@ -67,13 +67,17 @@ struct nufi_handle {
     double *grad = nullptr;       // [4]
     std::vector<char> slab_set;   // slab n written (step, run, upload_phi)
     double *stage = nullptr;      // pinned staging buffer of upload_phi (one slab)
+    double *stage_dev = nullptr;  // the same, as the device addresses it
     cudaEvent_t stage_done = nullptr;
     // Pinned block of the blocking calls: [0] the device error word (copied
     // on the stream before the one synchronisation of a call), then rho
     // (Ns), the field solve's slab (stride_t) and W, and its rho input (Ns).
+    // The *_dev pointers are the block's device addresses: copy_words_kernel
+    // moves the small per-step transfers through them.
     double *pin = nullptr;
-    unsigned *pin_err = nullptr;
+    unsigned *pin_err = nullptr, *pin_err_dev = nullptr;
     double *pin_rho = nullptr, *pin_slab = nullptr, *pin_rho_in = nullptr;
+    double *pin_rho_dev = nullptr, *pin_slab_dev = nullptr, *pin_rho_in_dev = nullptr;
     std::vector<char> energy_set; // W_n recorded (step, run)
     SolvePlan plan;
     bool solve_ok = false;
@@ -640,6 +644,7 @@ int device_flags_status(nufi_handle *h, unsigned flags)
         if (flags & kErrStageTimeout) m += " shared-memory staging wait timed out";
         if (flags & kErrBarrierTimeout) m += " grid barrier wait timed out";
         if (flags & kErrAdjointRange) m += " adjoint fixed-point sum out of range";
+        if (flags & kErrRhoRange) m += " fixed-point rho part out of range";
         return fail(h, NUFI_ERR_DEVICE, m);
     }
     return NUFI_OK;
@@ -659,6 +664,14 @@ void mark_steps(nufi_handle *h, int64_t n0, int64_t n1, bool energy)
 int sync_and_check(nufi_handle *h)
 {
     NUFI_CUDA(h, cudaMemcpyAsync(h->pin_err, h->err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    NUFI_CUDA(h, cudaStreamSynchronize(h->stream));
+    return device_flags_status(h, *h->pin_err);
+}
+
+// As sync_and_check, when the last launch on the stream (launch_copy_words
+// with the error word) has already put the word into the pinned block.
+int sync_published(nufi_handle *h)
+{
     NUFI_CUDA(h, cudaStreamSynchronize(h->stream));
     return device_flags_status(h, *h->pin_err);
 }
@@ -822,6 +835,14 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
         h->pin_rho = h->pin + 2;
         h->pin_slab = h->pin_rho + p.Ns;
         h->pin_rho_in = h->pin_slab + p.hist_stride + 1;
+        void *dev = nullptr;
+        if ((e = cudaHostGetDevicePointer(&dev, pin, 0)) != cudaSuccess)
+            return bail(cuda_fail(h.get(), e, "cudaHostGetDevicePointer"));
+        double *pd = static_cast<double *>(dev);
+        h->pin_err_dev = reinterpret_cast<unsigned *>(pd);
+        h->pin_rho_dev = pd + 2;
+        h->pin_slab_dev = h->pin_rho_dev + p.Ns;
+        h->pin_rho_in_dev = h->pin_slab_dev + p.hist_stride + 1;
     }
     if (h->fp64_table && fp64_table_stride(p) > 0) {
         const size_t n64 = nslab * size_t(fp64_table_stride(p));
@@ -849,7 +870,8 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
     h->aplan = adjoint_plan_1d(p);
     h->persist = plan_persistent(p, h->staged, h->plan, h->solve_ok, sms > 0 ? sms : 1, h->opt);
     if (h->persist.ok && ((e = dalloc(h.get(), &h->persist.sync, 2)) != cudaSuccess ||
-                          (e = dalloc(h.get(), &h->persist.epart, nslab * size_t(p.N[0]))) != cudaSuccess))
+                          (e = dalloc(h.get(), &h->persist.epart, nslab * size_t(p.N[0]))) != cudaSuccess ||
+                          (e = dalloc(h.get(), &h->persist.rho_fix, 2 * size_t(p.N[0]))) != cudaSuccess))
         return bail(cuda_fail(h.get(), e, "cudaMalloc"));
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(cuda_fail(h.get(), e, "nufi_create"));
     *out = h.release();
@@ -883,13 +905,14 @@ int nufi_compute_rho(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end)
     return enqueue_trace(h, n, q_begin, q_end, 0);
 }
 
-// rho into the pinned block, then one synchronisation (with the error word)
+// rho and the error word into the pinned block (one launch), then one
+// synchronisation
 static int download_rho_impl(nufi_handle *h)
 {
     DeviceGuard g(h->device);
-    NUFI_CUDA(h, cudaMemcpyAsync(h->pin_rho, h->rho, size_t(h->p.Ns) * sizeof(double), cudaMemcpyDeviceToHost,
-                                 h->stream));
-    return sync_and_check(h);
+    NUFI_CUDA(h, launch_copy_words(h->rho, h->pin_rho_dev, h->p.Ns, h->err, h->pin_err_dev, h->stream));
+    h->launches += 1;
+    return sync_published(h);
 }
 
 int nufi_download_rho(nufi_handle *h, double *rho)
@@ -956,12 +979,16 @@ static int upload_slab(nufi_handle *h, int64_t n, const double *slab)
     const size_t bytes = size_t(p.stride_t) * sizeof(double);
     if (!h->stage) {
         NUFI_CUDA(h, cudaMallocHost(&h->stage, bytes));
+        void *dev = nullptr;
+        NUFI_CUDA(h, cudaHostGetDevicePointer(&dev, h->stage, 0));
+        h->stage_dev = static_cast<double *>(dev);
         NUFI_CUDA(h, cudaEventCreateWithFlags(&h->stage_done, cudaEventDisableTiming));
     } else {
         NUFI_CUDA(h, cudaEventSynchronize(h->stage_done));
     }
     std::memcpy(h->stage, slab, bytes);
-    NUFI_CUDA(h, cudaMemcpyAsync(h->hist + n * p.hist_stride, h->stage, bytes, cudaMemcpyHostToDevice, h->stream));
+    NUFI_CUDA(h, launch_copy_words(h->stage_dev, h->hist + n * p.hist_stride, p.stride_t, nullptr, nullptr, h->stream));
+    h->launches += 1;
     NUFI_CUDA(h, cudaEventRecord(h->stage_done, h->stream));
     if (h->tables) {
         cudaError_t e = launch_derive_table(p, h->hist + n * p.hist_stride, h->tables + n * p.table_stride, h->stream);
@@ -1102,24 +1129,24 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
     // Every call leaves with its copies complete (synchronised, also on
     // failure), so the pinned input is free to overwrite here.
     std::memcpy(h->pin_rho_in, rho, size_t(p.Ns) * sizeof(double));
-    cudaError_t e = cudaMemcpyAsync(h->rho_in, h->pin_rho_in, size_t(p.Ns) * sizeof(double), cudaMemcpyHostToDevice,
-                                    h->stream);
+    cudaError_t e = launch_copy_words(h->pin_rho_in_dev, h->rho_in, p.Ns, nullptr, nullptr, h->stream);
     const char *what = "rho copy";
     if (e == cudaSuccess) {
+        h->launches += 1;
         e = launch_field_solve(p, h->plan, h->rho_in, h->slab_out, nullptr, h->energy_tmp, h->stream);
         what = "field solve launch";
         if (e == cudaSuccess) h->launches += 1;
     }
-    if (e == cudaSuccess) {  // slab and W (adjacent on the device) in one copy
-        e = cudaMemcpyAsync(h->pin_slab, h->slab_out, (size_t(p.hist_stride) + 1) * sizeof(double),
-                            cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) {  // slab and W (adjacent on the device) and the error word in one launch
+        e = launch_copy_words(h->slab_out, h->pin_slab_dev, p.hist_stride + 1, h->err, h->pin_err_dev, h->stream);
         what = "slab copy";
+        if (e == cudaSuccess) h->launches += 1;
     }
     if (e != cudaSuccess) {
         cudaStreamSynchronize(h->stream);
         return cuda_fail(h, e, what);
     }
-    int st = sync_and_check(h);
+    int st = sync_published(h);
     if (st) return st;
     std::memcpy(slab_out, h->pin_slab, size_t(p.stride_t) * sizeof(double));
     if (energy) *energy = h->pin_slab[p.hist_stride];

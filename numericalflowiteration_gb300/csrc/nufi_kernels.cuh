@@ -156,13 +156,19 @@ struct PersistentRun {
     int ctas = 0, threads = 0, ppt = 0, slabs_per_chunk = 0, tpn = 1;
     size_t smem = 0;
     unsigned *sync = nullptr;
-    double *epart = nullptr;  // [(Nt+1)][N] rho'_i phi_i per step and node
+    double *epart = nullptr;                // [(Nt+1)][N] rho_i phi_i per step and node
+    unsigned long long *rho_fix = nullptr;  // [2][N] rho's fixed-point sums, steps n % 2
+    double fix_scale = 0, fix_limit = 0;    // 2^F, and the bound on one CTA's scaled part
 };
 
 // rho[s] = -wv * sum over the rows of partial[row][s]: one warp per node,
 // lanes take rows in a fixed stride with Neumaier compensation, then a
 // fixed xor-shuffle tree; deterministic.
 cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st);
+// dst[0..n) = src[0..n) by a kernel (either side may be mapped pinned host
+// memory); *err_dst = *err_src too when err_src is given
+cudaError_t launch_copy_words(const double *src, double *dst, long long n, const unsigned *err_src, unsigned *err_dst,
+                              cudaStream_t st);
 // metrics[k] = sum over the blocks of partial[k][block] (one warp per
 // metric, Neumaier lanes and a fixed shuffle tree).
 cudaError_t launch_reduce_metrics(long long blocks, const double *partial, double *metrics, cudaStream_t st);

@@ -7,20 +7,20 @@
 // and a cold start (about 20 us per step in total, against ~100 us of trace
 // at mid-run).  Here the grid stays resident (one CTA per SM, co-resident
 // by the cooperative launch) and the phases are separated by a bounded grid
-// barrier:
+// barrier, two per step:
 //   trace    each CTA: its velocity chains through slabs n-1..0, streamed
 //            through the shared-memory ring (as trace_split_staged.cu);
-//            writes partial[s][cta] (node-major: the reduce reads a node's
-//            parts contiguously)
+//            the CTA's sum of f~ for each node is added into
+//            rho_fix[n % 2][s] as a 64-bit fixed-point integer (scale 2^F,
+//            chosen on the host so that no sum leaves the range): integer
+//            sums are exact and independent of their order, so rho is
+//            deterministic without a reduction phase of its own
 //   barrier
-//   reduce   node s is reduced by CTA s mod G, one warp per node, lanes in
-//            fixed stride with Neumaier compensation, fixed shuffle tree
-//   barrier
-//   solve    every CTA loads rho, removes the mean (fixed order) and
-//            computes its nodes' circulant products c, phi, K(A,B,C) from
-//            the Green's kernels held in shared memory for the whole run;
-//            writes slab n (FP64), table n (store_kick_entry) and, per
-//            node, rho'_i phi_i into row n of epart
+//   solve    every CTA reads rho from the integers and computes its nodes'
+//            circulant products c, phi, K(A,B,C) from the Green's kernels
+//            held in shared memory for the whole run; writes slab n (FP64),
+//            table n (store_kick_entry) and, per node, rho_i phi_i into row
+//            n of epart; CTA 0 writes rho and clears rho_fix[(n+1) % 2]
 //   barrier
 // After the last step, W_n = L/(2N) sum_i epart[n][i] for all n at once
 // (no per-step energy reduction on the critical path).
@@ -34,12 +34,18 @@ namespace nufi_gb300 {
 
 using namespace split;
 
+// 64-bit integer add into global memory, no value returned
+__device__ __forceinline__ void red_global_add_u64(unsigned long long *addr, unsigned long long v)
+{
+    asm volatile("red.global.add.u64 [%0], %1;" ::"l"(addr), "l"(v) : "memory");
+}
+
 template <int PPT, bool POW2>
 __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     const Problem p, float *__restrict__ tables, double *__restrict__ hist, const SplitNode *__restrict__ nodes,
-    const float2 *__restrict__ phase, const double *__restrict__ green, double *__restrict__ partial,
-    double *__restrict__ rho, double *__restrict__ energy, double *__restrict__ epart, int n0, int n1, int S, int Nr,
-    unsigned *sync, unsigned *err)
+    const float2 *__restrict__ phase, const double *__restrict__ green, unsigned long long *__restrict__ rho_fix,
+    double fix_scale, double fix_limit, double *__restrict__ rho, double *__restrict__ energy,
+    double *__restrict__ epart, int n0, int n1, int S, int Nr, unsigned *sync, unsigned *err)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long full_bar[kRing];
@@ -89,7 +95,7 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     const F0 f = make_f0(p);
     const unsigned slab_bytes = unsigned(p.table_stride) * 4u;
     unsigned target = 0;
-    // nodes of this CTA in the reduce and solve phases: blockIdx.x + k*G
+    // nodes of this CTA in the solve phase: blockIdx.x + k*G
     const int K = blockIdx.x < N ? (N - 1 - int(blockIdx.x)) / G + 1 : 0;
     int Kp = 1;
     while (Kp < K) Kp <<= 1;
@@ -227,30 +233,28 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
             __syncthreads();
             if (grp == 0) acc += combine[s];
         }
-        if (grp == 0 && s < N) partial[(long long)s * G + blockIdx.x] = acc;
-        if (!barrier(n)) return;
-
-        // ---------------- rho: node blockIdx.x + warp*G ----------------
-        if (warp < K) {
-            const int node = int(blockIdx.x) + warp * G;
-            double sum = 0, comp = 0;
-            for (int r = lane; r < G; r += 32) neumaier_add(sum, comp, __ldcg(partial + (long long)node * G + r));
-            for (int off = 16; off > 0; off >>= 1) {
-                const double os = __shfl_down_sync(0xffffffffu, sum, off);
-                const double oc = __shfl_down_sync(0xffffffffu, comp, off);
-                neumaier_add(sum, comp, os);
-                comp += oc;
-            }
-            if (lane == 0) rho[node] = -p.wv * (sum + comp);
+        unsigned long long *fix_n = rho_fix + (long long)(n & 1) * N;
+        if (grp == 0 && s < N) {
+            const double v = acc * fix_scale;
+            if (!(fabs(v) < fix_limit)) atomicOr(err, kErrRhoRange);  // outside the host's bound: not expected
+            red_global_add_u64(fix_n + s, (unsigned long long)__double2ll_rn(fmin(fmax(v, -fix_limit), fix_limit)));
         }
         if (!barrier(n)) return;
 
         // ---------------- field solve ----------------
-        // rho itself, not rho - mean: every circulant kernel sums to zero
-        // (the k = 0 mode is dropped), so the mean only costs a block-wide
-        // sum per step; the rounding it would remove is ~1e-13 of the
-        // field, far below the FP32-split arithmetic
-        for (int j = threadIdx.x; j < N; j += blockDim.x) rs[j] = __ldcg(rho + j);
+        // rho from the exact integer sums.  rho itself, not rho - mean:
+        // every circulant kernel sums to zero (the k = 0 mode is dropped),
+        // so the mean only costs a block-wide sum per step; the rounding it
+        // would remove is ~1e-13 of the field, far below the FP32-split
+        // arithmetic
+        const double to_rho = -p.wv / fix_scale;
+        for (int j = threadIdx.x; j < N; j += blockDim.x) {
+            rs[j] = double((long long)__ldcg(fix_n + j)) * to_rho;
+            if (blockIdx.x == 0) {
+                rho[j] = rs[j];
+                rho_fix[(long long)((n + 1) & 1) * N + j] = 0ull;  // the next step's sums start from zero
+            }
+        }
         __syncthreads();
         const int slotn = warp / wpn, pw = warp % wpn;
         double a[5] = {0, 0, 0, 0, 0};
@@ -307,13 +311,13 @@ namespace {
 
 template <int PPT>
 cudaError_t launch_run_ppt(const Problem &p, const PersistentRun &pr, const SolvePlan &plan, float *tables,
-                           double *hist, const SplitNode *nodes, const float2 *phase, double *partial, double *rho,
-                           double *energy, int n0, int n1, unsigned *err, cudaStream_t st)
+                           double *hist, const SplitNode *nodes, const float2 *phase, double *rho, double *energy,
+                           int n0, int n1, unsigned *err, cudaStream_t st)
 {
     const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
-    void (*fn)(const Problem, float *, double *, const SplitNode *, const float2 *, const double *, double *,
-               double *, double *, double *, int, int, int, int, unsigned *, unsigned *) =
-        pow2 ? run_split_1d_kernel<PPT, true> : run_split_1d_kernel<PPT, false>;
+    void (*fn)(const Problem, float *, double *, const SplitNode *, const float2 *, const double *,
+               unsigned long long *, double, double, double *, double *, double *, int, int, int, int, unsigned *,
+               unsigned *) = pow2 ? run_split_1d_kernel<PPT, true> : run_split_1d_kernel<PPT, false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(pr.smem));
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
@@ -327,10 +331,11 @@ cudaError_t launch_run_ppt(const Problem &p, const PersistentRun &pr, const Solv
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     e = cudaMemsetAsync(pr.sync, 0, 2 * sizeof(unsigned), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(pr.rho_fix, 0, 2 * size_t(p.N[0]) * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, fn, p, tables, hist, nodes, phase, (const double *)plan.green, partial, rho,
-                              energy, pr.epart, n0, n1, pr.slabs_per_chunk, pr.threads / pr.tpn, pr.sync,
-                              err);
+    return cudaLaunchKernelEx(&cfg, fn, p, tables, hist, nodes, phase, (const double *)plan.green, pr.rho_fix,
+                              pr.fix_scale, pr.fix_limit, rho, energy, pr.epart, n0, n1, pr.slabs_per_chunk,
+                              pr.threads / pr.tpn, pr.sync, err);
 }
 
 }  // namespace
@@ -341,7 +346,7 @@ PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const
     if (!sh.ok || p.dim != 1 || plan.nconv != 5 || sh.threads > 512 || sh.threads < 32) return pr;
     if (sh.ppt > 4 && sh.threads > 256) return pr;  // launch bounds of the PPT > 4 instances
     const int W = sh.threads / 32;
-    const int K = (p.N[0] + sh.ctas - 1) / sh.ctas;  // nodes per CTA in reduce/solve
+    const int K = (p.N[0] + sh.ctas - 1) / sh.ctas;  // nodes per CTA in the solve
     // at most two CTAs per SM (cooperative launch: all co-resident), and
     // energy_partial holds one part per CTA up to kMaxCtasPerSm * sms
     if (K > W || sh.ctas > kMaxCtasPerSm * sms) return pr;
@@ -353,6 +358,23 @@ PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const
     const size_t ring = size_t(kRing) * sh.slabs_per_chunk * size_t(p.table_stride) * sizeof(float);
     pr.smem = std::max(ring + size_t(6) * p.N[0] * sizeof(double), sh.smem);
     if (pr.smem > 220 * 1024) return pr;
+    // rho's fixed-point scale 2^F.  A CTA adds, per node, the f~ of its
+    // ppt * tpn chains of that node; f~ is f0 at a foot, so each is at most
+    // max f0 over (x, u).  fmax bounds that with a margin of 2; with G such
+    // parts below 2^62 / G each, no node's sum leaves int64.
+    const double alpha = std::fabs(p.f0p[0]), inv_sqrt_2pi = 0.39894228040143267794;
+    double fmax;
+    switch (p.f0_kind) {
+    case NUFI_F0_LANDAU: fmax = (1 + alpha) * inv_sqrt_2pi; break;                        // max exp(-u^2/2) = 1
+    case NUFI_F0_TWO_STREAM: fmax = (1 + alpha) * 2.0 * std::exp(-1.0) * inv_sqrt_2pi; break;  // u^2 e^{-u^2/2} <= 2/e
+    case NUFI_F0_BUMP_ON_TAIL: fmax = (1 + alpha) * (0.9 + 0.1 / p.f0p[3]) * inv_sqrt_2pi; break;
+    default: return pr;
+    }
+    const double part_max = 2.0 * double(sh.ppt) * double(sh.tpn) * fmax;
+    const int F = std::min(60, int(std::floor(62.0 - std::log2(double(sh.ctas) * part_max))));
+    if (!(F >= 24)) return pr;  // a bound this loose is not met by any real grid: per-step launches instead
+    pr.fix_scale = std::ldexp(1.0, F);
+    pr.fix_limit = std::ldexp(1.0, 62) / double(sh.ctas);
     pr.ok = true;
     return pr;
 }
@@ -361,9 +383,10 @@ cudaError_t launch_run_split_1d(const Problem &p, const PersistentRun &pr, const
                                 double *hist, const SplitNode *nodes, const float2 *phase, double *partial,
                                 double *rho, double *energy, int n0, int n1, unsigned *err, cudaStream_t st)
 {
+    (void)partial;  // rho is summed in the kernel's fixed-point integers
     switch (pr.ppt) {
 #define NUFI_CASE(K) \
-    case K: return launch_run_ppt<K>(p, pr, plan, tables, hist, nodes, phase, partial, rho, energy, n0, n1, err, st);
+    case K: return launch_run_ppt<K>(p, pr, plan, tables, hist, nodes, phase, rho, energy, n0, n1, err, st);
         NUFI_CASE(1) NUFI_CASE(2) NUFI_CASE(3) NUFI_CASE(4) NUFI_CASE(5) NUFI_CASE(6) NUFI_CASE(7) NUFI_CASE(8)
 #undef NUFI_CASE
     default: return cudaErrorInvalidValue;

@@ -100,7 +100,7 @@ def test_fp64_two_stream_through_saturation(nufi):
 
 
 @pytest.mark.parametrize("name", ["solve_1d_64", "solve_1d_256", "solve_2d_32", "solve_3d_16",
-                                  "solve_1d_64_order3", "solve_1d_64_order5"])
+                                  "solve_1d_64_order3", "solve_1d_64_order5", "solve_2d_256", "solve_3d_32"])
 def test_device_field_solve_matches_reference(nufi, name):
     cfg, g = golden(name)
     with nufi.Simulation(cfg) as sim:

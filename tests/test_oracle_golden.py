@@ -88,7 +88,7 @@ def test_compensated_oracle_matches_compensated_reference(name, oracle_mod):
 
 
 @pytest.mark.parametrize("name", ["solve_1d_64", "solve_1d_256", "solve_2d_32", "solve_3d_16",
-                                  "solve_1d_64_order3", "solve_1d_64_order5"])
+                                  "solve_1d_64_order3", "solve_1d_64_order5", "solve_2d_256", "solve_3d_32"])
 def test_oracle_field_solve_matches_reference(name, oracle_mod):
     cfg, g = golden(name)
     slab, e = oracle_mod.field_solve(cfg, g["rho"])

@@ -28,7 +28,7 @@ def circ(G, r, shape):
 
 
 @pytest.mark.parametrize("name", ["solve_1d_64", "solve_1d_256", "solve_2d_32", "solve_3d_16",
-                                  "solve_1d_64_order3", "solve_1d_64_order5"])
+                                  "solve_1d_64_order3", "solve_1d_64_order5", "solve_2d_256", "solve_3d_32"])
 def test_kernels_reproduce_the_reference_solve(name):
     cfg, g = golden(name)
     G = solve_kernels(cfg)

@@ -318,7 +318,8 @@ def e2e_c_loop(cfg, device: int, repeats: int, ws: int, ps: int):
     return {"value": ws * ps / d["seconds"], "unit": UNIT, "ms_per_step": d["seconds"] * 1e3,
             "h2d_bytes_per_step": d["h2d_bytes"], "d2h_bytes_per_step": d["d2h_bytes"], "repeats": repeats,
             "path": "C ABI with host buffers, the reference drivers' loop compiled as a C++ caller "
-                    "(compute_rho, download_rho, field_solve, upload_phi per time step)"}
+                    "(compute_rho, download_rho, field_solve, upload_phi per time step)",
+            "call_us_per_time_step": d.get("call_us_per_step")}
 
 
 def e2e_python_loop(nufi, cfg, device: int, repeats: int, ws: int, ps: int):

@@ -29,8 +29,13 @@
 namespace nufi_gb300 {
 
 __global__ void reduce_rho_kernel(const Problem p, int rows, const double *__restrict__ partial,
-                                  double *__restrict__ rho)
+                                  double *__restrict__ rho, double *__restrict__ pub, const unsigned *__restrict__ err,
+                                  unsigned *__restrict__ err_pub)
 {
+    // rho (and the error word the traces before this launch left) also into
+    // the mapped pinned block, when given: a following download needs no
+    // launch of its own
+    if (err_pub && blockIdx.x == 0 && threadIdx.x == 0) *err_pub = *err;
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     const int Ns = int(p.Ns);
@@ -43,16 +48,21 @@ __global__ void reduce_rho_kernel(const Problem p, int rows, const double *__res
             neumaier_add(sum, comp, os);
             comp += oc;
         }
-        if (lane == 0) rho[s] = -p.wv * (sum + comp);
+        if (lane == 0) {
+            const double v = -p.wv * (sum + comp);
+            rho[s] = v;
+            if (pub) pub[s] = v;
+        }
     }
 }
 
-cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st)
+cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st,
+                              double *pub, const unsigned *err, unsigned *err_pub)
 {
     // one warp per block: the FP64 work of the few nodes spreads over all SMs
     const int warps_per_block = 1;
     const int blocks = int((p.Ns + warps_per_block - 1) / warps_per_block);
-    reduce_rho_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(p, rows, partial, rho);
+    reduce_rho_kernel<<<blocks, 32 * warps_per_block, 0, st>>>(p, rows, partial, rho, pub, err, err_pub);
     return cudaGetLastError();
 }
 
@@ -455,9 +465,11 @@ __device__ __forceinline__ void cubic_kick_poly(double c0, double c1, double c2,
 
 }  // namespace
 
-__global__ void derive_table_kernel(const Problem p, const double *__restrict__ slab, float *__restrict__ table)
+__global__ void derive_table_kernel(const Problem p, const double *__restrict__ slab, float *__restrict__ table,
+                                    double *__restrict__ hist_out)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (hist_out && idx < p.stride_t) hist_out[idx] = slab[idx];  // the slab itself, when it comes from elsewhere
     if (p.dim == 1) {
         if (idx >= p.N[0]) return;
         const double K = -p.dt * p.dt * p.dxinv[0] * p.dxinv[0];
@@ -469,10 +481,11 @@ __global__ void derive_table_kernel(const Problem p, const double *__restrict__ 
     }
 }
 
-cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st)
+cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st,
+                                double *hist_out)
 {
-    const long long n = p.dim == 1 ? p.N[0] : p.stride_t;
-    derive_table_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(p, hist_slab, table_slab);
+    const long long n = hist_out || p.dim > 1 ? p.stride_t : p.N[0];  // stride_t >= N
+    derive_table_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(p, hist_slab, table_slab, hist_out);
     return cudaGetLastError();
 }
 

@@ -51,7 +51,6 @@ struct nufi_handle {
     double *partial = nullptr;
     double *rho = nullptr;
     double *energy = nullptr;
-    double *rho_in = nullptr;     // nufi_field_solve scratch
     double *slab_out = nullptr;   // nufi_field_solve scratch
     double *energy_tmp = nullptr; // nufi_field_solve scratch
     unsigned *err = nullptr;
@@ -78,6 +77,10 @@ struct nufi_handle {
     unsigned *pin_err = nullptr, *pin_err_dev = nullptr;
     double *pin_rho = nullptr, *pin_slab = nullptr, *pin_rho_in = nullptr;
     double *pin_rho_dev = nullptr, *pin_slab_dev = nullptr, *pin_rho_in_dev = nullptr;
+    // value of `launches` right after a compute_rho whose reduction also
+    // wrote rho and the error word into the pinned block: while no launch
+    // has followed, download_rho only synchronises
+    long long rho_pub_at = -1;
     std::vector<char> energy_set; // W_n recorded (step, run)
     SolvePlan plan;
     bool solve_ok = false;
@@ -645,6 +648,8 @@ int device_flags_status(nufi_handle *h, unsigned flags)
         if (flags & kErrBarrierTimeout) m += " grid barrier wait timed out";
         if (flags & kErrAdjointRange) m += " adjoint fixed-point sum out of range";
         if (flags & kErrRhoRange) m += " fixed-point rho part out of range";
+        *h->pin_err = 0;  // the stream is idle here: nothing writes the block
+        h->rho_pub_at = -1;
         return fail(h, NUFI_ERR_DEVICE, m);
     }
     return NUFI_OK;
@@ -676,8 +681,9 @@ int sync_published(nufi_handle *h)
     return device_flags_status(h, *h->pin_err);
 }
 
-// Enqueue the trace of step n over [qb, qe) and the reduction into h->rho.
-int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int mode)
+// Enqueue the trace of step n over [qb, qe) and the reduction into h->rho
+// (with `publish`, also into the pinned block with the error word).
+int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int mode, bool publish = false)
 {
     const Problem &p = h->p;
     cudaError_t e;
@@ -698,9 +704,11 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
                                h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "trace launch");
     h->launches += 1;
-    e = launch_reduce_rho(p, rows, h->partial, h->rho, h->stream);
+    e = publish ? launch_reduce_rho(p, rows, h->partial, h->rho, h->stream, h->pin_rho_dev, h->err, h->pin_err_dev)
+                : launch_reduce_rho(p, rows, h->partial, h->rho, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "reduce launch");
     h->launches += 1;
+    if (publish) h->rho_pub_at = h->launches;
     return NUFI_OK;
 }
 
@@ -817,7 +825,6 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
         (e = dalloc(h.get(), &h->partial, partial_rows * p.Ns)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->rho, size_t(p.Ns))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->energy, nslab)) != cudaSuccess ||
-        (e = dalloc(h.get(), &h->rho_in, size_t(p.Ns))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->slab_out, size_t(p.hist_stride) + 1)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->mpartial, size_t(4 * ((p.Ns + 31) / 32) * fp64_rows(h->shape)))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->metrics, 4)) != cudaSuccess ||
@@ -825,24 +832,27 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
         return bail(cuda_fail(h.get(), e, "cudaMalloc"));
     h->energy_tmp = h->slab_out + p.hist_stride;  // slab and W leave in one copy
     {
-        const size_t pin_n = 2 + size_t(p.Ns) + size_t(p.hist_stride) + 1 + size_t(p.Ns);
+        // regions on 256-byte boundaries: [err][rho Ns][slab hist_stride, W][rho input Ns]
+        auto up = [](size_t n) { return (n + 31) & ~size_t(31); };
+        const size_t o_rho = 32, o_slab = o_rho + up(size_t(p.Ns)), o_in = o_slab + up(size_t(p.hist_stride) + 1);
+        const size_t pin_n = o_in + up(size_t(p.Ns));
         void *pin = nullptr;
         if ((e = cudaMallocHost(&pin, pin_n * sizeof(double))) != cudaSuccess)
             return bail(cuda_fail(h.get(), e, "cudaMallocHost"));
         h->pin = static_cast<double *>(pin);
         h->pin_err = reinterpret_cast<unsigned *>(h->pin);
         *h->pin_err = 0;
-        h->pin_rho = h->pin + 2;
-        h->pin_slab = h->pin_rho + p.Ns;
-        h->pin_rho_in = h->pin_slab + p.hist_stride + 1;
+        h->pin_rho = h->pin + o_rho;
+        h->pin_slab = h->pin + o_slab;
+        h->pin_rho_in = h->pin + o_in;
         void *dev = nullptr;
         if ((e = cudaHostGetDevicePointer(&dev, pin, 0)) != cudaSuccess)
             return bail(cuda_fail(h.get(), e, "cudaHostGetDevicePointer"));
         double *pd = static_cast<double *>(dev);
         h->pin_err_dev = reinterpret_cast<unsigned *>(pd);
-        h->pin_rho_dev = pd + 2;
-        h->pin_slab_dev = h->pin_rho_dev + p.Ns;
-        h->pin_rho_in_dev = h->pin_slab_dev + p.hist_stride + 1;
+        h->pin_rho_dev = pd + o_rho;
+        h->pin_slab_dev = pd + o_slab;
+        h->pin_rho_in_dev = pd + o_in;
     }
     if (h->fp64_table && fp64_table_stride(p) > 0) {
         const size_t n64 = nslab * size_t(fp64_table_stride(p));
@@ -902,7 +912,7 @@ int nufi_compute_rho(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end)
         return fail(h, NUFI_ERR_RANGE, "quadrature range outside [0, Nq]");
     if (q_begin == q_end) return NUFI_OK;  // as the reference: no launch, rho untouched
     DeviceGuard g(h->device);
-    return enqueue_trace(h, n, q_begin, q_end, 0);
+    return enqueue_trace(h, n, q_begin, q_end, 0, true);
 }
 
 // rho and the error word into the pinned block (one launch), then one
@@ -910,8 +920,10 @@ int nufi_compute_rho(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end)
 static int download_rho_impl(nufi_handle *h)
 {
     DeviceGuard g(h->device);
-    NUFI_CUDA(h, launch_copy_words(h->rho, h->pin_rho_dev, h->p.Ns, h->err, h->pin_err_dev, h->stream));
-    h->launches += 1;
+    if (h->rho_pub_at != h->launches) {  // something ran after the last compute_rho's reduction
+        NUFI_CUDA(h, launch_copy_words(h->rho, h->pin_rho_dev, h->p.Ns, h->err, h->pin_err_dev, h->stream));
+        h->launches += 1;
+    }
     return sync_published(h);
 }
 
@@ -987,20 +999,25 @@ static int upload_slab(nufi_handle *h, int64_t n, const double *slab)
         NUFI_CUDA(h, cudaEventSynchronize(h->stage_done));
     }
     std::memcpy(h->stage, slab, bytes);
-    NUFI_CUDA(h, launch_copy_words(h->stage_dev, h->hist + n * p.hist_stride, p.stride_t, nullptr, nullptr, h->stream));
+    // One launch reads the staged slab from the mapped pinned buffer, writes
+    // it into the history and derives the slab's table from it; without a
+    // table of that form, a copy and then the derivation from the history.
+    double *dst = h->hist + n * p.hist_stride;
+    cudaError_t e;
+    if (h->tables) {
+        e = launch_derive_table(p, h->stage_dev, h->tables + n * p.table_stride, h->stream, dst);
+    } else if (h->tables64 && p.dim == 1) {
+        e = launch_derive_table64(p, h->stage_dev, h->tables64 + n * fp64_table_stride(p), h->stream, dst);
+    } else {
+        e = launch_copy_words(h->stage_dev, dst, p.stride_t, nullptr, nullptr, h->stream);
+        if (e == cudaSuccess && h->tables64) {
+            h->launches += 1;
+            e = launch_derive_table64(p, dst, h->tables64 + n * fp64_table_stride(p), h->stream);
+        }
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "slab upload launch");
     h->launches += 1;
     NUFI_CUDA(h, cudaEventRecord(h->stage_done, h->stream));
-    if (h->tables) {
-        cudaError_t e = launch_derive_table(p, h->hist + n * p.hist_stride, h->tables + n * p.table_stride, h->stream);
-        if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
-        h->launches += 1;
-    }
-    if (h->tables64) {
-        cudaError_t e =
-            launch_derive_table64(p, h->hist + n * p.hist_stride, h->tables64 + n * fp64_table_stride(p), h->stream);
-        if (e != cudaSuccess) return cuda_fail(h, e, "derive table launch");
-        h->launches += 1;
-    }
     h->slab_set[size_t(n)] = 1;
     return NUFI_OK;
 }
@@ -1128,15 +1145,11 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
     DeviceGuard g(h->device);
     // Every call leaves with its copies complete (synchronised, also on
     // failure), so the pinned input is free to overwrite here.
+    // the solve reads rho straight from the mapped pinned block
     std::memcpy(h->pin_rho_in, rho, size_t(p.Ns) * sizeof(double));
-    cudaError_t e = launch_copy_words(h->pin_rho_in_dev, h->rho_in, p.Ns, nullptr, nullptr, h->stream);
-    const char *what = "rho copy";
-    if (e == cudaSuccess) {
-        h->launches += 1;
-        e = launch_field_solve(p, h->plan, h->rho_in, h->slab_out, nullptr, h->energy_tmp, h->stream);
-        what = "field solve launch";
-        if (e == cudaSuccess) h->launches += 1;
-    }
+    cudaError_t e = launch_field_solve(p, h->plan, h->pin_rho_in_dev, h->slab_out, nullptr, h->energy_tmp, h->stream);
+    const char *what = "field solve launch";
+    if (e == cudaSuccess) h->launches += 1;
     if (e == cudaSuccess) {  // slab and W (adjacent on the device) and the error word in one launch
         e = launch_copy_words(h->slab_out, h->pin_slab_dev, p.hist_stride + 1, h->err, h->pin_err_dev, h->stream);
         what = "slab copy";

@@ -112,7 +112,10 @@ bool fp64_order_supported(int dim, int order);
 // (stride 0: no table).
 bool fp64_table_supported(const Problem &p, long long Nt);
 long long fp64_table_stride(const Problem &p);
-cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, double *table_slab, cudaStream_t st);
+// the FP64 derivative table of one slab (1D, 2D); with hist_out (1D), the
+// slab is also copied there
+cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, double *table_slab, cudaStream_t st,
+                                  double *hist_out = nullptr);
 cudaError_t launch_trace_fp64_table(const Problem &p, const LaunchShape &ls, const double *tables,
                                     const double *hist, int n, long long qb, long long qe, double *partial,
                                     int *rows, unsigned *err, cudaStream_t st);
@@ -164,7 +167,10 @@ struct PersistentRun {
 // rho[s] = -wv * sum over the rows of partial[row][s]: one warp per node,
 // lanes take rows in a fixed stride with Neumaier compensation, then a
 // fixed xor-shuffle tree; deterministic.
-cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st);
+// rho[s] = -wv * (sum over the rows of partial); also into pub (and *err
+// into *err_pub) when given
+cudaError_t launch_reduce_rho(const Problem &p, int rows, const double *partial, double *rho, cudaStream_t st,
+                              double *pub = nullptr, const unsigned *err = nullptr, unsigned *err_pub = nullptr);
 // dst[0..n) = src[0..n) by a kernel (either side may be mapped pinned host
 // memory); *err_dst = *err_src too when err_src is given
 cudaError_t launch_copy_words(const double *src, double *dst, long long n, const unsigned *err_src, unsigned *err_dst,
@@ -279,6 +285,9 @@ size_t adjoint_split_smem(const BatchLaunch &L);
 int adjoint_split_ctas_per_sm(const BatchLaunch &L, int ppt);
 
 // FP32 table of one FP64 slab (after upload_phi).
-cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st);
+// the split kick table of one slab; with hist_out, the slab is also
+// copied there (an upload from the mapped pinned block in one launch)
+cudaError_t launch_derive_table(const Problem &p, const double *hist_slab, float *table_slab, cudaStream_t st,
+                                double *hist_out = nullptr);
 
 }  // namespace nufi_gb300

@@ -361,10 +361,12 @@ __global__ void derive_table64_2d_kernel(const Problem p, const double *__restri
 
 // (a, b, c) of every cell of one slab (see the file comment): one thread
 // per cell, from the padded FP64 slab.
-__global__ void derive_table64_kernel(const Problem p, const double *__restrict__ slab, double *__restrict__ tab)
+__global__ void derive_table64_kernel(const Problem p, const double *__restrict__ slab, double *__restrict__ tab,
+                                      double *__restrict__ hist_out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = p.N[0];
+    if (hist_out && i < p.stride_t) hist_out[i] = slab[i];  // the slab itself, when it comes from elsewhere
     if (i >= N) return;
     const double K = -(p.dt * p.dxinv[0]) * (p.dt * p.dxinv[0]);
     const double c0 = slab[i], c1 = slab[i + 1], c2 = slab[i + 2], c3 = slab[i + 3];
@@ -393,12 +395,15 @@ long long fp64_table_stride(const Problem &p)
     return p.dim == 1 ? (3LL * p.N[0] + 1) / 2 * 2 : p.dim == 2 ? (24LL * p.Ns + 1) / 2 * 2 : 0;
 }
 
-cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, double *table_slab, cudaStream_t st)
+cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, double *table_slab, cudaStream_t st,
+                                  double *hist_out)
 {
-    if (p.dim == 3) return cudaSuccess;  // no table
-    if (p.dim == 1)
-        derive_table64_kernel<<<unsigned((p.N[0] + 127) / 128), 128, 0, st>>>(p, hist_slab, table_slab);
-    else
+    if (hist_out && p.dim != 1) return cudaErrorInvalidValue;  // the copy form is 1D only
+    if (p.dim == 3) return cudaSuccess;                          // no table
+    if (p.dim == 1) {
+        const long long n = hist_out ? p.stride_t : p.N[0];
+        derive_table64_kernel<<<unsigned((n + 127) / 128), 128, 0, st>>>(p, hist_slab, table_slab, hist_out);
+    } else
         derive_table64_2d_kernel<<<unsigned((p.Ns + 127) / 128), 128, 0, st>>>(p, hist_slab, table_slab);
     return cudaGetLastError();
 }

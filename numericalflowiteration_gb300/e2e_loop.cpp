@@ -11,7 +11,9 @@
 //   e2e_loop <config file (struct nufi_config, raw bytes)> <repeats> [device]
 //
 // Prints one JSON object: the median seconds of a whole run over `repeats`
-// timed runs (after one untimed run), and the bytes copied per run.
+// timed runs (after one untimed run), the bytes copied per run, and the
+// host time inside each call per time step (microseconds, mean over the
+// timed runs; a blocking call's time includes its wait for the device).
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -54,19 +56,31 @@ int main(int argc, char **argv)
     const int64_t Nt = cfg.Nt;
     std::vector<double> rho(static_cast<size_t>(ns)), coeffs(static_cast<size_t>((Nt + 1) * stride_t)),
         energy(static_cast<size_t>(Nt + 1));
+    using clk = std::chrono::steady_clock;
+    double call_s[4] = {0, 0, 0, 0};  // compute_rho, download_rho, field_solve, upload_phi
     auto run = [&]() -> int {
         for (int64_t n = 0; n <= Nt; ++n) {
             std::fill(rho.begin(), rho.end(), 0.0);
-            if (check(h, nufi_compute_rho(h, n, 0, nq), "compute_rho") ||
-                check(h, nufi_download_rho(h, rho.data()), "download_rho") ||
-                check(h, nufi_field_solve(h, rho.data(), coeffs.data() + n * stride_t, &energy[size_t(n)]),
-                      "field_solve") ||
-                check(h, nufi_upload_phi(h, n, coeffs.data()), "upload_phi"))
+            const auto t0 = clk::now();
+            if (check(h, nufi_compute_rho(h, n, 0, nq), "compute_rho")) return 1;
+            const auto t1 = clk::now();
+            if (check(h, nufi_download_rho(h, rho.data()), "download_rho")) return 1;
+            const auto t2 = clk::now();
+            if (check(h, nufi_field_solve(h, rho.data(), coeffs.data() + n * stride_t, &energy[size_t(n)]),
+                      "field_solve"))
                 return 1;
+            const auto t3 = clk::now();
+            if (check(h, nufi_upload_phi(h, n, coeffs.data()), "upload_phi")) return 1;
+            const auto t4 = clk::now();
+            call_s[0] += std::chrono::duration<double>(t1 - t0).count();
+            call_s[1] += std::chrono::duration<double>(t2 - t1).count();
+            call_s[2] += std::chrono::duration<double>(t3 - t2).count();
+            call_s[3] += std::chrono::duration<double>(t4 - t3).count();
         }
         return check(h, nufi_synchronize(h), "synchronize");
     };
     if (run()) return 4;
+    for (double &c : call_s) c = 0;
     std::vector<double> secs;
     for (int r = 0; r < repeats; ++r) {
         const auto t0 = std::chrono::steady_clock::now();
@@ -79,9 +93,12 @@ int main(int argc, char **argv)
     // per step: slab H2D (upload_phi) and rho H2D (field solve); rho D2H,
     // slab + W D2H (field solve)
     const long long h2d = steps * 8LL * (stride_t + ns), d2h = steps * 8LL * (ns + stride_t + 1);
+    const double per = 1e6 / (double(repeats) * double(steps));
     std::printf("{\"seconds\": %.9f, \"repeats\": %d, \"h2d_bytes\": %lld, \"d2h_bytes\": %lld, "
-                "\"energy_last\": %.17g}\n",
-                med, repeats, h2d, d2h, energy[size_t(Nt)]);
+                "\"energy_last\": %.17g, \"call_us_per_step\": {\"compute_rho\": %.3f, \"download_rho\": %.3f, "
+                "\"field_solve\": %.3f, \"upload_phi\": %.3f}}\n",
+                med, repeats, h2d, d2h, energy[size_t(Nt)], call_s[0] * per, call_s[1] * per, call_s[2] * per,
+                call_s[3] * per);
     nufi_destroy(h);
     return 0;
 }

@@ -78,6 +78,28 @@ def test_split_dropin_two_stream_256x1024_later_steps(nufi):
             assert rel_max(got, g["rho_comp"][list(g["rho_steps"]).index(n)]) <= 1e-6, n
 
 
+def test_fp64_landau_2d_32x64_whole_run(nufi):
+    """The 2D workload (Landau 32^2 x 64^2, T = 20, all 161 steps) in FP64
+    against the reference's run of the same configuration."""
+    cfg, g = golden("landau_2d_32x64_T20")
+    with nufi.Simulation(cfg) as sim:
+        e = sim.run()
+        hist = sim.history()
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+    _check_run(cfg, g, e, hist, rho)
+
+
+def test_split_landau_2d_32x64_whole_run_within_gate(nufi):
+    """The 2D FP32-split run over all 161 steps against the reference's
+    energy history and its last rho: the metric's gate."""
+    cfg, g = golden("landau_2d_32x64_T20")
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        e = sim.run()
+        rho = sim.download_rho(np.zeros(cfg.n_spatial))
+    assert rel_max(e, g["energy_comp"]) <= 1e-6
+    assert rel_max(rho, g["rho_comp"][-1]) <= 1e-6
+
+
 def test_fp64_landau_3d_16x32_first_steps(nufi):
     """The 3D workload at its own size (16^3 x 32^3: 134M points per step)
     over its first 10 steps, FP64, against the reference's run."""

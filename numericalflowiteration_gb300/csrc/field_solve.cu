@@ -129,31 +129,48 @@ __device__ __forceinline__ double block_sum_fixed(double v, double *red)
 
 }  // namespace
 
-// Each block owns `nodes_per_block` nodes; each node's sum over j is split
-// across wpn = 8 / nodes_per_block warps (warp w of a node takes the j-range
-// quarter w), the warps' sums combined in fixed order:
+// Each block of 32 * nodes_per_block threads owns nodes_per_block nodes, one
+// warp per node: the lanes stride over j and one shuffle tree finishes each
+// sum,
 //   acc[c] = sum_j green[c][(i - j) mod N] * rho'[j]      (mod per axis)
 // then the slab (all padded positions of i), the table, and rho'_i phi_i.
+// GB300 issues FP64 at 1/64 of the FP32 rate, so the kernel's time is its
+// FP64 instruction count: NCONV (Ns/32 + 5) warp instructions per node this
+// way, against NCONV (Ns/32 + 6 w) with a node's sum split over w warps.
 template <int NCONV>
 __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     const Problem p, const double *__restrict__ rho, const double *__restrict__ green, int green_in_smem,
-    int nodes_per_block, double *__restrict__ slab, float *__restrict__ table, double *__restrict__ energy_partial,
+    double *__restrict__ slab, float *__restrict__ table, double *__restrict__ energy_partial,
     unsigned *__restrict__ energy_counter, double *__restrict__ energy_out)
 {
     extern __shared__ double sm[];
     __shared__ double red[kSolveThreads];
-    __shared__ double wacc[kSolveWarps][NCONV];
+    __shared__ double eacc[kSolveWarps];
     __shared__ bool last;
     const int Ns = int(p.Ns);
     const int N0 = p.N[0], N1 = p.N[1], N2 = p.N[2];
     double *rs = sm;                                    // rho' [Ns]
     const double *G = green_in_smem ? sm + Ns : green;  // [NCONV][Ns]
-    // 1. rho' = rho - mean(rho), the mean in fixed order (every block alike)
+    // 1. rho' = rho - mean(rho), the mean in fixed order (every block alike).
+    // Loads in batches of 8 issued before their use: the input may sit in
+    // mapped host memory, where each dependent round trip costs ~1 us.
+    constexpr int kLd = 8;
     double part = 0;
-    for (int j = threadIdx.x; j < Ns; j += blockDim.x) {
-        const double r = rho[j];
-        rs[j] = r;
-        part += r;
+    for (int jb = threadIdx.x; jb < Ns; jb += kLd * int(blockDim.x)) {
+        double r[kLd];
+#pragma unroll
+        for (int u = 0; u < kLd; ++u) {
+            const int j = jb + u * int(blockDim.x);
+            r[u] = j < Ns ? rho[j] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kLd; ++u) {
+            const int j = jb + u * int(blockDim.x);
+            if (j < Ns) {
+                rs[j] = r[u];
+                part += r[u];
+            }
+        }
     }
     if (green_in_smem)
         for (int j = threadIdx.x; j < NCONV * Ns; j += blockDim.x) sm[Ns + j] = green[j];
@@ -161,55 +178,58 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     for (int j = threadIdx.x; j < Ns; j += blockDim.x) rs[j] -= mean;
     __syncthreads();
 
-    // 2. circulant products
+    // 2. circulant products, node i = this warp's; the green loads of kLd
+    // consecutive j-steps are issued together (they come from L2 when the
+    // kernels are not staged in shared memory)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int wpn = kSolveWarps / nodes_per_block;  // warps per node
-    const int slot = warp / wpn, part_w = warp % wpn;
-    const int i = blockIdx.x * nodes_per_block + slot;
-    const int jlen = (Ns + wpn - 1) / wpn;
-    const int jbeg = part_w * jlen, jend = min(Ns, jbeg + jlen);
+    const int i = blockIdx.x * int(blockDim.x >> 5) + warp;
     double acc[NCONV];
 #pragma unroll
     for (int c = 0; c < NCONV; ++c) acc[c] = 0;
     if (i < Ns) {
         const int i0 = i % N0, i1 = (i / N0) % N1, i2 = i / (N0 * N1);
         const int step0 = 32 % N0, step1 = (32 / N0) % N1, step2 = 32 / (N0 * N1);
-        int j = jbeg + lane;
+        int j = lane;
         int j0 = j % N0, j1 = (j / N0) % N1, j2 = j / (N0 * N1);
-        for (; j < jend; j += 32) {
-            int m0 = i0 - j0, m1 = i1 - j1, m2 = i2 - j2;
-            m0 += m0 < 0 ? N0 : 0;
-            m1 += m1 < 0 ? N1 : 0;
-            m2 += m2 < 0 ? N2 : 0;
-            const int m = (m2 * N1 + m1) * N0 + m0;
-            const double r = rs[j];
+        while (j < Ns) {
+            int mm[kLd], jj[kLd];
 #pragma unroll
-            for (int c = 0; c < NCONV; ++c) acc[c] = fma(G[c * Ns + m], r, acc[c]);
-            // (j0, j1, j2) of j + 32
-            j0 += step0;
-            j1 += step1;
-            j2 += step2;
-            if (j0 >= N0) { j0 -= N0; ++j1; }
-            if (j1 >= N1) { j1 -= N1; ++j2; }
+            for (int u = 0; u < kLd; ++u) {
+                int m0 = i0 - j0, m1 = i1 - j1, m2 = i2 - j2;
+                m0 += m0 < 0 ? N0 : 0;
+                m1 += m1 < 0 ? N1 : 0;
+                m2 += m2 < 0 ? N2 : 0;
+                mm[u] = (m2 * N1 + m1) * N0 + m0;
+                jj[u] = j;
+                // (j0, j1, j2) of j + 32
+                j += 32;
+                j0 += step0;
+                j1 += step1;
+                j2 += step2;
+                if (j0 >= N0) { j0 -= N0; ++j1; }
+                if (j1 >= N1) { j1 -= N1; ++j2; }
+            }
+            double g[kLd][NCONV];
+#pragma unroll
+            for (int u = 0; u < kLd; ++u)
+#pragma unroll
+                for (int c = 0; c < NCONV; ++c) g[u][c] = jj[u] < Ns ? G[c * Ns + mm[u]] : 0.0;
+#pragma unroll
+            for (int u = 0; u < kLd; ++u) {
+                if (jj[u] >= Ns) break;
+                const double r = rs[jj[u]];
+#pragma unroll
+                for (int c = 0; c < NCONV; ++c) acc[c] = fma(g[u][c], r, acc[c]);
+            }
         }
     }
 #pragma unroll
     for (int c = 0; c < NCONV; ++c)
         for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
-    if (lane == 0)
-#pragma unroll
-        for (int c = 0; c < NCONV; ++c) wacc[warp][c] = acc[c];
-    __syncthreads();
     double e_local = 0;
-    if (part_w == 0 && lane == 0 && i < Ns) {
-        double a[NCONV];
-#pragma unroll
-        for (int c = 0; c < NCONV; ++c) {
-            a[c] = wacc[warp][c];
-            for (int w = 1; w < wpn; ++w) a[c] += wacc[warp + w][c];
-        }
+    if (lane == 0 && i < Ns) {
         const int i0 = i % N0, i1 = (i / N0) % N1, i2 = i / (N0 * N1);
-        const double cval = a[0];
+        const double cval = acc[0];
         // every padded position of node i: i_a and i_a + N_a while < P_a
         for (int dz = 0; dz < 2; ++dz) {
             const int k = i2 + dz * N2;
@@ -228,13 +248,18 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
         }
         if constexpr (NCONV == 5) {
             if (table)
-                store_kick_entry(table, N0, i, float(a[2]), float(a[3]), float(a[4]));
+                store_kick_entry(table, N0, i, float(acc[2]), float(acc[3]), float(acc[4]));
         }
-        e_local = rs[i] * a[1];
+        e_local = rs[i] * acc[1];
     }
-    // 3. energy: block partial (fixed order), the last block sums the blocks
-    const double eb = block_sum_fixed(e_local, red);
-    if (threadIdx.x == 0) energy_partial[blockIdx.x] = eb;
+    if (lane == 0) eacc[warp] = e_local;
+    __syncthreads();
+    // 3. energy: block partial (warps in order), the last block sums the blocks
+    if (threadIdx.x == 0) {
+        double eb = 0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) eb += eacc[w];
+        energy_partial[blockIdx.x] = eb;
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = (atomicAdd(energy_counter, 1u) == gridDim.x - 1);
@@ -439,14 +464,16 @@ cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const do
                                float *table_slab, double *energy_out, cudaStream_t st)
 {
     if (plan.spectral) return launch_spectral_solve(p, plan, rho, hist_slab, table_slab, energy_out, st);
-    if (plan.nconv == 5)
-        circulant_solve_kernel<5><<<plan.blocks, kSolveThreads, plan.smem, st>>>(
-            p, rho, plan.green, plan.green_in_smem, plan.nodes_per_block, hist_slab, table_slab, plan.energy_partial,
-            plan.energy_counter, energy_out);
+    // without a table, c and phi only: the green rows 0 and 1 of either form
+    const unsigned threads = 32u * unsigned(plan.nodes_per_block);
+    if (plan.nconv == 5 && table_slab)
+        circulant_solve_kernel<5><<<plan.blocks, threads, plan.smem, st>>>(
+            p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
+            energy_out);
     else
-        circulant_solve_kernel<2><<<plan.blocks, kSolveThreads, plan.smem, st>>>(
-            p, rho, plan.green, plan.green_in_smem, plan.nodes_per_block, hist_slab, table_slab, plan.energy_partial,
-            plan.energy_counter, energy_out);
+        circulant_solve_kernel<2><<<plan.blocks, threads, plan.smem, st>>>(
+            p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
+            energy_out);
     return cudaGetLastError();
 }
 

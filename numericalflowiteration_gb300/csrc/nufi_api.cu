@@ -88,6 +88,11 @@ struct nufi_handle {
     LaunchShape shape;
     StagedShape staged;
     PersistentRun persist;
+    // the staged 1D trace's fixed-point rho (RhoFix): sums [N] and ticket,
+    // zero between launches; step_fix_scale == 0: partial rows instead
+    unsigned long long *step_fix = nullptr;
+    unsigned *step_ticket = nullptr;
+    double step_fix_scale = 0, step_fix_limit = 0;
     std::string last_error;
     long long launches = 0;
     std::map<std::pair<long long, long long>, std::pair<cudaGraphExec_t, long long>> graphs;
@@ -405,13 +410,15 @@ bool solve_geometry(const Problem &p, int sms, SolvePlan &pl, std::string &why)
         return true;
     }
     pl.nconv = (p.precision == NUFI_PREC_FP32_SPLIT && p.dim == 1) ? 5 : 2;
-    // nodes per block: enough blocks to cover the SMs, up to 8 warps per node
+    // one warp per node; warps (nodes) per block: at most 8, fewer until the
+    // blocks fill every SM twice
     int npb = 8;
-    while (npb > 1 && (p.Ns + npb - 1) / npb < sms) npb /= 2;
+    while (npb > 1 && (p.Ns + npb - 1) / npb < 2LL * sms) npb /= 2;
     pl.nodes_per_block = npb;
     pl.blocks = int((p.Ns + npb - 1) / npb);
+    // the green kernels staged per block only where a block's warps share them
     const size_t with_green = size_t(p.Ns) * 8 * (1 + pl.nconv);
-    pl.green_in_smem = with_green <= 160 * 1024;
+    pl.green_in_smem = npb >= 4 && with_green <= 160 * 1024;
     pl.smem = pl.green_in_smem ? with_green : size_t(p.Ns) * 8;
     return true;
 }
@@ -696,18 +703,31 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
     else if (p.dim > 1)
         e = launch_trace_split_nd(p, h->staged, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows,
                                   h->err, h->stream);
-    else if (h->staged.ok)
+    else if (h->staged.ok) {
+        RhoFix fx;
+        if (h->step_fix_scale > 0) {
+            fx.sum = h->step_fix;
+            fx.ticket = h->step_ticket;
+            fx.scale = h->step_fix_scale;
+            fx.limit = h->step_fix_limit;
+            fx.rho = h->rho;
+            fx.pub = publish ? h->pin_rho_dev : nullptr;
+            fx.err_pub = publish ? h->pin_err_dev : nullptr;
+        }
         e = launch_trace_split_staged(p, h->staged, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows,
-                                      h->err, h->stream);
-    else
+                                      h->err, h->stream, fx);
+    } else
         e = launch_trace_split(p, h->shape, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows, h->err,
                                h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "trace launch");
     h->launches += 1;
-    e = publish ? launch_reduce_rho(p, rows, h->partial, h->rho, h->stream, h->pin_rho_dev, h->err, h->pin_err_dev)
-                : launch_reduce_rho(p, rows, h->partial, h->rho, h->stream);
-    if (e != cudaSuccess) return cuda_fail(h, e, "reduce launch");
-    h->launches += 1;
+    if (rows > 0) {  // rows == 0: the trace wrote rho itself (fixed-point sums)
+        e = publish ? launch_reduce_rho(p, rows, h->partial, h->rho, h->stream, h->pin_rho_dev, h->err,
+                                        h->pin_err_dev)
+                    : launch_reduce_rho(p, rows, h->partial, h->rho, h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "reduce launch");
+        h->launches += 1;
+    }
     if (publish) h->rho_pub_at = h->launches;
     return NUFI_OK;
 }
@@ -883,6 +903,16 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
                           (e = dalloc(h.get(), &h->persist.epart, nslab * size_t(p.N[0]))) != cudaSuccess ||
                           (e = dalloc(h.get(), &h->persist.rho_fix, 2 * size_t(p.N[0]))) != cudaSuccess))
         return bail(cuda_fail(h.get(), e, "cudaMalloc"));
+    if (p.dim == 1 && p.precision == NUFI_PREC_FP32_SPLIT && h->staged.ok &&
+        rho_fixed_point(p, h->staged.ctas, h->staged.ppt * h->staged.tpn, h->step_fix_scale, h->step_fix_limit)) {
+        if ((e = dalloc(h.get(), &h->step_fix, size_t(p.N[0]))) != cudaSuccess ||
+            (e = dalloc(h.get(), &h->step_ticket, 1)) != cudaSuccess ||
+            (e = cudaMemset(h->step_fix, 0, size_t(p.N[0]) * sizeof(unsigned long long))) != cudaSuccess ||
+            (e = cudaMemset(h->step_ticket, 0, sizeof(unsigned))) != cudaSuccess)
+            return bail(cuda_fail(h.get(), e, "cudaMalloc"));
+    } else {
+        h->step_fix_scale = 0;
+    }
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(cuda_fail(h.get(), e, "nufi_create"));
     *out = h.release();
     return NUFI_OK;

@@ -23,7 +23,7 @@ enum : unsigned {
     kErrStageTimeout = 1u << 3, // a bounded wait on a shared-memory staging barrier gave up
     kErrBarrierTimeout = 1u << 4, // a bounded wait on the persistent kernel's grid barrier gave up
     kErrAdjointRange = 1u << 5,   // FP32-split adjoint: a fixed-point table-adjoint sum left its range
-    kErrRhoRange = 1u << 6,       // 1D whole-run kernel: a fixed-point part of rho left its range
+    kErrRhoRange = 1u << 6,       // 1D split traces: a fixed-point part of rho left its range
 };
 
 // Everything a kernel needs to know about one configuration, by value.

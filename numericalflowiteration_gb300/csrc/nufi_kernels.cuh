@@ -146,9 +146,25 @@ StagedShape staged_shape_nd(const Problem &p, int sms);
 cudaError_t launch_trace_split_nd(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
                                   const float2 *phase, int n, long long qb, long long qe, double *partial, int *rows,
                                   unsigned *err, cudaStream_t st);
+// rho of the 1D split traces as 64-bit fixed-point sums (scale 2^F): the
+// parts of every CTA are added into sum[N] (zero between launches), the
+// last CTA (ticket) writes rho (and pub, *err_pub when given) and clears
+// the sums.  sum == nullptr: partial rows for reduce_rho instead.
+struct RhoFix {
+    unsigned long long *sum = nullptr;
+    unsigned *ticket = nullptr;
+    double scale = 0, limit = 0;
+    double *rho = nullptr, *pub = nullptr;
+    unsigned *err_pub = nullptr;
+};
+// 2^F and the bound on one CTA's scaled part for `ctas` CTAs each adding,
+// per node, the f~ of `chains` chains: no node's sum leaves int64.  False
+// when F would be below 24 (then the partial rows).
+bool rho_fixed_point(const Problem &p, int ctas, int chains, double &scale, double &limit);
 cudaError_t launch_trace_split_staged(const Problem &p, const StagedShape &sh, const float *tables,
                                       const SplitNode *nodes, const float2 *phase, int n, long long qb, long long qe,
-                                      double *partial, int *rows, unsigned *err, cudaStream_t st);
+                                      double *partial, int *rows, unsigned *err, cudaStream_t st,
+                                      const RhoFix &fx = RhoFix());
 
 // Whole FP32-split 1D simulation in one cooperative launch
 // (run_split_1d.cu): staged trace, rho, circulant solve and W_n per step,
@@ -188,7 +204,7 @@ struct SolvePlan {
     double *green = nullptr;
     int nconv = 0;
     int blocks = 0;              // grid of the solve kernel
-    int nodes_per_block = 8;     // 1, 2, 4 or 8 (8 / warps per node)
+    int nodes_per_block = 8;     // 1, 2, 4 or 8: warps per block, one node each
     size_t smem = 0;             // rho' (+ green when staged) in shared memory
     bool green_in_smem = false;
     double *energy_partial = nullptr;  // [max(blocks, SMs)]

@@ -34,12 +34,6 @@ namespace nufi_gb300 {
 
 using namespace split;
 
-// 64-bit integer add into global memory, no value returned
-__device__ __forceinline__ void red_global_add_u64(unsigned long long *addr, unsigned long long v)
-{
-    asm volatile("red.global.add.u64 [%0], %1;" ::"l"(addr), "l"(v) : "memory");
-}
-
 template <int PPT, bool POW2>
 __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     const Problem p, float *__restrict__ tables, double *__restrict__ hist, const SplitNode *__restrict__ nodes,
@@ -358,25 +352,32 @@ PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const
     const size_t ring = size_t(kRing) * sh.slabs_per_chunk * size_t(p.table_stride) * sizeof(float);
     pr.smem = std::max(ring + size_t(6) * p.N[0] * sizeof(double), sh.smem);
     if (pr.smem > 220 * 1024) return pr;
-    // rho's fixed-point scale 2^F.  A CTA adds, per node, the f~ of its
-    // ppt * tpn chains of that node; f~ is f0 at a foot, so each is at most
-    // max f0 over (x, u).  fmax bounds that with a margin of 2; with G such
-    // parts below 2^62 / G each, no node's sum leaves int64.
+    if (!rho_fixed_point(p, sh.ctas, sh.ppt * sh.tpn, pr.fix_scale, pr.fix_limit)) return pr;
+    pr.ok = true;
+    return pr;
+}
+
+bool rho_fixed_point(const Problem &p, int ctas, int chains, double &scale, double &limit)
+{
+    // A CTA adds, per node, the f~ of its `chains` chains of that node; f~
+    // is f0 at a foot, so each is at most max f0 over (x, u).  fmax bounds
+    // that with a margin of 2; with `ctas` parts below 2^62 / ctas each, no
+    // node's sum leaves int64.
+    if (p.dim != 1 || ctas < 1 || chains < 1) return false;
     const double alpha = std::fabs(p.f0p[0]), inv_sqrt_2pi = 0.39894228040143267794;
     double fmax;
     switch (p.f0_kind) {
     case NUFI_F0_LANDAU: fmax = (1 + alpha) * inv_sqrt_2pi; break;                        // max exp(-u^2/2) = 1
     case NUFI_F0_TWO_STREAM: fmax = (1 + alpha) * 2.0 * std::exp(-1.0) * inv_sqrt_2pi; break;  // u^2 e^{-u^2/2} <= 2/e
     case NUFI_F0_BUMP_ON_TAIL: fmax = (1 + alpha) * (0.9 + 0.1 / p.f0p[3]) * inv_sqrt_2pi; break;
-    default: return pr;
+    default: return false;
     }
-    const double part_max = 2.0 * double(sh.ppt) * double(sh.tpn) * fmax;
-    const int F = std::min(60, int(std::floor(62.0 - std::log2(double(sh.ctas) * part_max))));
-    if (!(F >= 24)) return pr;  // a bound this loose is not met by any real grid: per-step launches instead
-    pr.fix_scale = std::ldexp(1.0, F);
-    pr.fix_limit = std::ldexp(1.0, 62) / double(sh.ctas);
-    pr.ok = true;
-    return pr;
+    const double part_max = 2.0 * double(chains) * fmax;
+    const int F = std::min(60, int(std::floor(62.0 - std::log2(double(ctas) * part_max))));
+    if (!(F >= 24)) return false;  // a bound this loose is not met by any real grid
+    scale = std::ldexp(1.0, F);
+    limit = std::ldexp(1.0, 62) / double(ctas);
+    return true;
 }
 
 cudaError_t launch_run_split_1d(const Problem &p, const PersistentRun &pr, const SolvePlan &plan, float *tables,

@@ -95,6 +95,12 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p)
 // or when another block has already given up (*abort != 0) it raises
 // kErrBarrierTimeout, sets *abort and returns false, and the caller leaves
 // the kernel (no hang).
+// 64-bit integer add into global memory, no value returned
+__device__ __forceinline__ void red_global_add_u64(unsigned long long *addr, unsigned long long v)
+{
+    asm volatile("red.global.add.u64 [%0], %1;" ::"l"(addr), "l"(v) : "memory");
+}
+
 __device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned &target, unsigned *abort, unsigned *err)
 {
     __shared__ int ok;

@@ -14,8 +14,13 @@
 // one spatial node (x-lanes, so the 32 lanes of a warp read neighbouring
 // cells: few bank conflicts) and PPT velocity nodes, i.e. PPT
 // independent dependency chains.  CTA c owns the velocity nodes c, c + G,
-// c + 2G, ... (interleaved, so that each CTA holds a spread of velocities).  rho: per thread over its chains (FP64) into
-// partial[c][s]; reduce_rho sums the G rows.
+// c + 2G, ... (interleaved, so that each CTA holds a spread of velocities).
+// rho: per thread over its chains (FP64), then either into partial[c][s]
+// (reduce_rho sums the G rows) or, with a RhoFix, added as a 64-bit
+// fixed-point integer (scale 2^F) into fx.sum[s]; the last CTA to finish
+// (a ticket) turns the sums into rho and clears them.  The integer sums are
+// exact and order-free, so rho is deterministic, and bit for bit that of
+// the whole-run kernel (run_split_1d.cu), which sums the same parts alike.
 //
 // The per-point arithmetic is that of trace_split.cu (same substep order as
 // the reference's eval_ftilda, nufi/rho.hpp:31-61).
@@ -37,11 +42,12 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
                                                                      const float2 *__restrict__ phase, int n,
                                                                      long long q_begin, long long q_end, int S,
                                                                      int Nr, double *__restrict__ partial,
-                                                                     unsigned *err)
+                                                                     const RhoFix fx, unsigned *err)
 {
     extern __shared__ __align__(128) float ring[];
     __shared__ __align__(8) unsigned long long full_bar[kRing];
     __shared__ double combine[256];
+    __shared__ bool last;
 
     const int N = p.N[0];
     const int s = threadIdx.x % Nr;    // spatial node
@@ -117,7 +123,34 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
         __syncthreads();
         if (grp == 0) acc += combine[s];
     }
-    if (grp == 0 && s < N) partial[(long long)blockIdx.x * N + s] = acc;
+    if (!fx.sum) {
+        if (grp == 0 && s < N) partial[(long long)blockIdx.x * N + s] = acc;
+        return;
+    }
+    if (grp == 0 && s < N) {
+        const double v = acc * fx.scale;
+        if (!(fabs(v) < fx.limit)) atomicOr(err, kErrRhoRange);  // outside the host's bound: not expected
+        red_global_add_u64(fx.sum + s, (unsigned long long)__double2ll_rn(fmin(fmax(v, -fx.limit), fx.limit)));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(fx.ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const double to_rho = -p.wv / fx.scale;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const double r = double((long long)__ldcg(fx.sum + j)) * to_rho;
+        fx.rho[j] = r;
+        if (fx.pub) fx.pub[j] = r;
+        fx.sum[j] = 0ull;
+    }
+    if (threadIdx.x == 0) {
+        *fx.ticket = 0u;
+        if (fx.err_pub) *fx.err_pub = atomicOr(err, 0u);
+    }
 }
 
 namespace {
@@ -125,7 +158,7 @@ namespace {
 template <int PPT>
 cudaError_t launch_staged_ppt(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
                               const float2 *phase, int n, long long qb, long long qe, double *partial,
-                              unsigned *err, cudaStream_t st)
+                              const RhoFix &fx, unsigned *err, cudaStream_t st)
 {
     const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
     const dim3 grid(sh.ctas), block(sh.threads);
@@ -134,13 +167,13 @@ cudaError_t launch_staged_ppt(const Problem &p, const StagedShape &sh, const flo
                                                              cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (attr != cudaSuccess) return attr;
         trace_split_1d_staged_kernel<PPT, true><<<grid, block, sh.smem, st>>>(p, tables, nodes, phase, n, qb, qe,
-                                                                              sh.slabs_per_chunk, sh.threads / sh.tpn, partial, err);
+                                                                              sh.slabs_per_chunk, sh.threads / sh.tpn, partial, fx, err);
     } else {
         static const cudaError_t attr = cudaFuncSetAttribute(trace_split_1d_staged_kernel<PPT, false>,
                                                              cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (attr != cudaSuccess) return attr;
         trace_split_1d_staged_kernel<PPT, false><<<grid, block, sh.smem, st>>>(p, tables, nodes, phase, n, qb, qe,
-                                                                               sh.slabs_per_chunk, sh.threads / sh.tpn, partial, err);
+                                                                               sh.slabs_per_chunk, sh.threads / sh.tpn, partial, fx, err);
     }
     return cudaGetLastError();
 }
@@ -187,12 +220,12 @@ StagedShape staged_shape_1d(const Problem &p, int sms, int cps, int tpn_opt)
 
 cudaError_t launch_trace_split_staged(const Problem &p, const StagedShape &sh, const float *tables,
                                       const SplitNode *nodes, const float2 *phase, int n, long long qb, long long qe,
-                                      double *partial, int *rows, unsigned *err, cudaStream_t st)
+                                      double *partial, int *rows, unsigned *err, cudaStream_t st, const RhoFix &fx)
 {
-    *rows = sh.ctas;
+    *rows = fx.sum ? 0 : sh.ctas;  // no rows to reduce: the kernel writes rho itself
     switch (sh.ppt) {
 #define NUFI_CASE(K) \
-    case K: return launch_staged_ppt<K>(p, sh, tables, nodes, phase, n, qb, qe, partial, err, st);
+    case K: return launch_staged_ppt<K>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
         NUFI_CASE(1) NUFI_CASE(2) NUFI_CASE(3) NUFI_CASE(4) NUFI_CASE(5) NUFI_CASE(6) NUFI_CASE(7) NUFI_CASE(8)
 #undef NUFI_CASE
     default: return cudaErrorInvalidValue;

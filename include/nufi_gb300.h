@@ -59,10 +59,13 @@ extern "C" {
  * perturbation of its value at the grid velocity; FP64 only in the rho
  * accumulator, the Poisson solve and the spline interpolation solve.
  * f0's phase comes from the cell the foot lands in (the foot wrapped into
- * the domain), so k (x_max - x_min) must be a multiple of 2 pi on every
- * axis, to 2.5e-7 relative (a single-precision domain length passes);
- * NUFI_ERR_UNSUPPORTED otherwise.  FP64 evaluates f0 at the unwrapped foot,
- * as the reference, for any k.                                              */
+ * the domain); when k (x_max - x_min) is not a multiple of 2 pi (to 2.5e-7
+ * relative: a single-precision domain length passes) the phase is turned
+ * by k (x_max - x_min) per wrap of the foot, which 1D handles with Nx a
+ * power of two up to 256 do (not with the split_global_loads or
+ * split_plain_kick options, nor in batches); NUFI_ERR_UNSUPPORTED for other
+ * such handles.  FP64 evaluates f0 at the unwrapped foot, as the
+ * reference, for any k.                                                     */
 #define NUFI_PREC_FP32_SPLIT  1
 
 /* ---- initial conditions (f0) ------------------------------------------- */

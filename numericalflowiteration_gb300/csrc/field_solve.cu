@@ -141,7 +141,7 @@ template <int NCONV>
 __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     const Problem p, const double *__restrict__ rho, const double *__restrict__ green, int green_in_smem,
     double *__restrict__ slab, float *__restrict__ table, double *__restrict__ energy_partial,
-    unsigned *__restrict__ energy_counter, double *__restrict__ energy_out)
+    unsigned *__restrict__ energy_counter, double *__restrict__ energy_out, unsigned *err, unsigned *err_pub)
 {
     extern __shared__ double sm[];
     __shared__ double red[kSolveThreads];
@@ -274,6 +274,7 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
         for (int ax = 0; ax < p.dim; ++ax) Lp *= p.L[ax];
         if (energy_out) energy_out[0] = tot * (Lp / (2.0 * double(Ns)));
         energy_counter[0] = 0u;
+        if (err_pub) *err_pub = atomicOr(err, 0u);  // after every block: the word as this solve leaves it
     }
 }
 
@@ -461,19 +462,23 @@ cudaError_t field_solve_prepare(const SolvePlan &plan)
 }
 
 cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
-                               float *table_slab, double *energy_out, cudaStream_t st)
+                               float *table_slab, double *energy_out, cudaStream_t st, unsigned *err,
+                               unsigned *err_pub)
 {
-    if (plan.spectral) return launch_spectral_solve(p, plan, rho, hist_slab, table_slab, energy_out, st);
+    if (plan.spectral) {
+        if (err_pub) return cudaErrorInvalidValue;  // the spectral form publishes no error word
+        return launch_spectral_solve(p, plan, rho, hist_slab, table_slab, energy_out, st);
+    }
     // without a table, c and phi only: the green rows 0 and 1 of either form
     const unsigned threads = 32u * unsigned(plan.nodes_per_block);
     if (plan.nconv == 5 && table_slab)
         circulant_solve_kernel<5><<<plan.blocks, threads, plan.smem, st>>>(
             p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
-            energy_out);
+            energy_out, err, err_pub);
     else
         circulant_solve_kernel<2><<<plan.blocks, threads, plan.smem, st>>>(
             p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
-            energy_out);
+            energy_out, err, err_pub);
     return cudaGetLastError();
 }
 

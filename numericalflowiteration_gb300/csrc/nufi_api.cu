@@ -147,6 +147,13 @@ void stencil(int order, double *Nb)
     }
 }
 
+// k L a multiple of 2 pi, to 2.5e-7 relative (see validate)
+bool phase_is_periodic(double k, double L)
+{
+    const double r = k * L / 6.283185307179586476925286766559;
+    return std::fabs(r - std::nearbyint(r)) <= 2.5e-7 * std::max(1.0, std::fabs(r));
+}
+
 int validate(const nufi_config *c, std::string &why)
 {
     if (!c) { why = "null config"; return NUFI_ERR_INVALID; }
@@ -229,14 +236,16 @@ int validate(const nufi_config *c, std::string &why)
     // to 2.5e-7 relative: a domain length rounded to single precision (the
     // reference's <float> configurations: 4 pi in float is 2.8e-8 above 4 pi)
     // passes, and the phase at the foot then moves by at most 2 pi 2.5e-7
-    // per wrap of the domain, within the FP32-split form's accuracy.
+    // per wrap of the domain, within the FP32-split form's accuracy.  Other
+    // k: the 1D staged traces count each chain's wraps and turn the phase by
+    // k L per wrap (Problem::phase_wrap), for N a power of two up to 256.
     if (c->precision == NUFI_PREC_FP32_SPLIT) {
-        const double k = c->f0_params[1];
         for (int a = 0; a < c->dim; ++a) {
-            const double r = k * (c->x_max[a] - c->x_min[a]) / 6.283185307179586476925286766559;
-            if (!(std::fabs(r - std::nearbyint(r)) <= 2.5e-7 * std::max(1.0, std::fabs(r)))) {
-                why = "FP32-split needs k (x_max - x_min) a multiple of 2 pi on every axis (f0 from per-cell "
-                      "phases of the wrapped foot); the FP64 trace takes any k";
+            if (phase_is_periodic(c->f0_params[1], c->x_max[a] - c->x_min[a])) continue;
+            const long long N = c->Nx[0];
+            if (c->dim != 1 || N > 256 || (N & (N - 1)) != 0) {
+                why = "FP32-split with k (x_max - x_min) not a multiple of 2 pi: 1D with Nx a power of two up to "
+                      "256 (f0's phase at the unwrapped foot); the FP64 trace takes any k";
                 return NUFI_ERR_UNSUPPORTED;
             }
         }
@@ -307,6 +316,13 @@ Problem make_problem(const nufi_config &c)
     p.wv = 1;
     for (int a = 0; a < c.dim; ++a) p.wv *= p.dv[a];
     p.split_plain_kick = 0;  // nufi_options.split_plain_kick, set by the caller
+    // 1D split: the phase f0 gains per wrap of the domain (validate admits
+    // a non-periodic phase for the staged traces only)
+    p.phase_wrap = 0.0;
+    if (c.precision == NUFI_PREC_FP32_SPLIT && c.dim == 1 && !phase_is_periodic(c.f0_params[1], p.L[0])) {
+        const double two_pi = 6.283185307179586476925286766559, kL = c.f0_params[1] * p.L[0];
+        p.phase_wrap = kL - two_pi * std::floor(kL / two_pi);
+    }
     return p;
 }
 
@@ -828,6 +844,10 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     plan_traces(h->p, sms > 0 ? sms : 1, h->opt, h->shape, h->staged);
+    if (h->p.phase_wrap != 0.0 && !h->staged.ok)
+        return fail(nullptr, NUFI_ERR_UNSUPPORTED,
+                    "nufi_create: k (x_max - x_min) not a multiple of 2 pi needs the staged FP32-split trace (the "
+                    "options chose the global-load form, which takes f0 at the wrapped foot)");
     const Problem &p = h->p;
     // partial-sum rows: the FP64 traces' y blocks (fp64_rows), the global-
     // load split trace's velocity blocks, or the staged traces' CTAs
@@ -1175,15 +1195,25 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
     DeviceGuard g(h->device);
     // Every call leaves with its copies complete (synchronised, also on
     // failure), so the pinned input is free to overwrite here.
-    // the solve reads rho straight from the mapped pinned block
+    // The solve reads rho straight from the mapped pinned block; the
+    // circulant form also writes the slab, W and the error word there (one
+    // launch), the spectral form into device memory and a copy follows.
     std::memcpy(h->pin_rho_in, rho, size_t(p.Ns) * sizeof(double));
-    cudaError_t e = launch_field_solve(p, h->plan, h->pin_rho_in_dev, h->slab_out, nullptr, h->energy_tmp, h->stream);
+    cudaError_t e;
     const char *what = "field solve launch";
-    if (e == cudaSuccess) h->launches += 1;
-    if (e == cudaSuccess) {  // slab and W (adjacent on the device) and the error word in one launch
-        e = launch_copy_words(h->slab_out, h->pin_slab_dev, p.hist_stride + 1, h->err, h->pin_err_dev, h->stream);
-        what = "slab copy";
+    if (!h->plan.spectral) {
+        e = launch_field_solve(p, h->plan, h->pin_rho_in_dev, h->pin_slab_dev, nullptr, h->pin_slab_dev + p.hist_stride,
+                               h->stream, h->err, h->pin_err_dev);
         if (e == cudaSuccess) h->launches += 1;
+    } else {
+        e = launch_field_solve(p, h->plan, h->pin_rho_in_dev, h->slab_out, nullptr, h->energy_tmp, h->stream);
+        if (e == cudaSuccess) {  // slab and W (adjacent on the device) and the error word in one launch
+            h->launches += 1;
+            e = launch_copy_words(h->slab_out, h->pin_slab_dev, p.hist_stride + 1, h->err, h->pin_err_dev,
+                                  h->stream);
+            what = "slab copy";
+            if (e == cudaSuccess) h->launches += 1;
+        }
     }
     if (e != cudaSuccess) {
         cudaStreamSynchronize(h->stream);
@@ -1512,6 +1542,9 @@ int nufi_plan_ex(const nufi_config *cfg, const nufi_options *opt, int sms, char 
     h.p.split_plain_kick = h.opt.split_plain_kick;
     h.fp64_table = h.p.precision == NUFI_PREC_FP64 && fp64_table_supported(h.p, cfg->Nt);
     plan_traces(h.p, sms, h.opt, h.shape, h.staged);
+    if (h.p.phase_wrap != 0.0 && !h.staged.ok)
+        return fail(nullptr, NUFI_ERR_UNSUPPORTED,
+                    "nufi_plan: k (x_max - x_min) not a multiple of 2 pi needs the staged FP32-split trace");
     h.solve_ok = solve_geometry(h.p, sms, h.plan, h.solve_why);
     h.persist = plan_persistent(h.p, h.staged, h.plan, h.solve_ok, sms, h.opt);
     h.aplan = adjoint_plan_1d(h.p);
@@ -1858,6 +1891,9 @@ int nufi_batch_create_ex(const nufi_config *cfgs, int32_t count, const nufi_opti
         const nufi_config &c = cfgs[i];
         if (c.dim != 1 || c.order != 4 || c.precision != cfgs[0].precision)
             return bfail(nullptr, NUFI_ERR_UNSUPPORTED, "nufi_batch_create: 1D, order 4, one precision per batch");
+        if (c.precision == NUFI_PREC_FP32_SPLIT && !phase_is_periodic(c.f0_params[1], c.x_max[0] - c.x_min[0]))
+            return bfail(nullptr, NUFI_ERR_UNSUPPORTED,
+                         "nufi_batch_create: FP32-split instances need k (x_max - x_min) a multiple of 2 pi");
         if (c.Nx[0] < 1 || c.Nx[0] > kBatchMaxN || kBatchMaxN % c.Nx[0] != 0)
             return bfail(nullptr, NUFI_ERR_UNSUPPORTED, "nufi_batch_create: Nx must divide 256");
     }

@@ -49,6 +49,8 @@ struct Problem {
     int split_plain_kick;  // split mode: 1 = uncompensated FP32 kick sum
                            // (nufi_options.split_plain_kick; for measuring
                            // what the compensation buys)
+    double phase_wrap;     // 1D split: k L reduced to [0, 2 pi), the phase f0 gains per wrap of the
+                           // domain; 0 when k L is a multiple of 2 pi (the wrapped foot's phase is exact)
 };
 
 // n!, evaluated at compile time where the spline kernels use it (a runtime

@@ -221,9 +221,13 @@ constexpr long long kCirculantMaxNodes = 16384;
 constexpr int kSpectralMaxAxis = 4096;  // a line (complex FP64) in shared memory
 
 // Poisson + collocation solve of one step: padded slab n (FP64), the FP32
-// table n (when table_slab != null) and the electric energy W_n.
+// table n (when table_slab != null) and the electric energy W_n.  With
+// err_pub (circulant form only), *err as the solve leaves it is written
+// there too, so that a caller reading slab, W and the word from mapped host
+// memory needs no further launch.
 cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
-                               float *table_slab, double *energy_out, cudaStream_t st);
+                               float *table_slab, double *energy_out, cudaStream_t st, unsigned *err = nullptr,
+                               unsigned *err_pub = nullptr);
 cudaError_t field_solve_prepare(const SolvePlan &plan);
 
 PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const SolvePlan &plan, int sms);

@@ -34,7 +34,7 @@ namespace nufi_gb300 {
 
 using namespace split;
 
-template <int PPT, bool POW2>
+template <int PPT, bool POW2, bool UNWRAP>
 __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     const Problem p, float *__restrict__ tables, double *__restrict__ hist, const SplitNode *__restrict__ nodes,
     const float2 *__restrict__ phase, const double *__restrict__ green, unsigned long long *__restrict__ rho_fix,
@@ -54,6 +54,7 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     const int grp = threadIdx.x / Nr;  // its chain group
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int TS = int(p.table_stride);  // floats per slab table
+    const int log2n = __ffs(N) - 1;      // UNWRAP: N is a power of two
     float *ring = reinterpret_cast<float *>(smem_raw);
     double *rs = reinterpret_cast<double *>(smem_raw + size_t(kRing) * S * TS * sizeof(float));  // rho' [N]
     double *gs = rs + N;                                                                       // green [5][N]
@@ -181,11 +182,12 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
 
     for (int n = n0; n <= n1; ++n) {
         // ---------------- trace of step n ----------------
-        int I[PPT];
+        int I[PPT], Wr[PPT];
         float xi[PPT], dwT[PPT], dwTc[PPT];
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
             I[q] = s < N ? s : 0;
+            Wr[q] = 0;
             xi[q] = 0.0f;
             dwT[q] = slo[q];
             dwTc[q] = 0.0f;
@@ -203,7 +205,8 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
                 const float *__restrict__ chunk = ring + slot * S * TS;
                 int k_lo, k_hi;
                 chunk_range(n, j, k_lo, k_hi);
-                trace_chunk<PPT, POW2>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err);
+                trace_chunk<PPT, POW2, UNWRAP>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err, &Wr,
+                                               log2n);
                 __syncwarp();
                 if (lane == 0 && atom_add_acq_rel_cta(&released[slot], 1u) == unsigned(W - 1)) {
                     released[slot] = 0;
@@ -220,7 +223,9 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
         for (int q = 0; q < PPT; ++q) {
             if (!live[q]) continue;
             const SplitNode nd = nodes[mv[q]];
-            acc += double(delta_f0(f, nd, __ldg(phase + I[q]), xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
+            float2 cs = __ldg(phase + I[q]);
+            if constexpr (UNWRAP) cs = phase_unwrapped(cs, Wr[q] - n * ((nd.S0u - nd.S0) / N), p.phase_wrap);
+            acc += double(delta_f0(f, nd, cs, xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
         }
         if (blockDim.x > unsigned(Nr)) {
             if (grp == 1) combine[s] = acc;
@@ -311,7 +316,11 @@ cudaError_t launch_run_ppt(const Problem &p, const PersistentRun &pr, const Solv
     const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
     void (*fn)(const Problem, float *, double *, const SplitNode *, const float2 *, const double *,
                unsigned long long *, double, double, double *, double *, double *, int, int, int, int, unsigned *,
-               unsigned *) = pow2 ? run_split_1d_kernel<PPT, true> : run_split_1d_kernel<PPT, false>;
+               unsigned *) = pow2 ? run_split_1d_kernel<PPT, true, false> : run_split_1d_kernel<PPT, false, false>;
+    if (p.phase_wrap != 0.0) {  // f0's phase at the unwrapped foot (admitted for N a power of two only)
+        if (!pow2) return cudaErrorInvalidValue;
+        fn = run_split_1d_kernel<PPT, true, true>;
+    }
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(pr.smem));
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};

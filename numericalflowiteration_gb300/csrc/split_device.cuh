@@ -280,6 +280,18 @@ __device__ __forceinline__ float lds_f32(unsigned addr)
     return v;
 }
 
+// (cos, sin) of k x at a foot that wrapped the domain w times (unwrapped
+// cell I + N w): the wrapped cell's phase turned by w k L (phase_wrap = k L
+// mod 2 pi; the product reduced in FP64 before the FP32 sincos)
+__device__ __forceinline__ float2 phase_unwrapped(float2 cs, int w, double phase_wrap)
+{
+    if (w == 0) return cs;
+    const double a = fmod(double(w) * phase_wrap, 6.283185307179586476925286766559);
+    float sr, cr;
+    sincosf(float(a), &sr, &cr);
+    return make_float2(cs.x * cr - cs.y * sr, cs.y * cr + cs.x * sr);
+}
+
 template <bool POW2>
 __device__ __forceinline__ int wrap_cell(int J, int N, unsigned *err)
 {
@@ -306,14 +318,19 @@ __device__ __forceinline__ int wrap_cell(int J, int N, unsigned *err)
 //           floor(t) by a round-down add of 1.5*2^23, whose bit pattern
 //           minus S0m = S0 + bits(1.5*2^23) moves the cell
 //   kick:   dwC += K (A + B xi + C xi^2) of the cell (halved for k = 0)
+// With UNWRAP (N a power of two), Wr counts each chain's wraps of the
+// domain: the new cell before the mask, divided by N (arithmetic shift by
+// log2n), adds to Wr, so the unwrapped cell is I + N Wr - n (S0u - S0).
 // Chains go two at a time through the packed FP32 instructions (the FP32
 // part of a substep, 9 operations, in 9 instructions for two chains); the
 // integer cell update and the two shared loads stay per chain.
-template <int PPT, bool POW2>
+template <int PPT, bool POW2, bool UNWRAP = false>
 __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int TS, int k_hi, int k_lo, int N,
                                             int (&I)[PPT], float (&xi)[PPT], float (&dwT)[PPT], float (&dwTc)[PPT],
-                                            const float (&shi)[PPT], const int (&S0m)[PPT], unsigned *err)
+                                            const float (&shi)[PPT], const int (&S0m)[PPT], unsigned *err,
+                                            int (*Wr)[PPT] = nullptr, int log2n = 0)
 {
+    static_assert(POW2 || !UNWRAP, "wrap counts need N a power of two");
     constexpr int NP = PPT / 2;  // packed pairs; chain PPT-1 alone when PPT is odd
     const unsigned long long MAG2 = f2_pack(kMagic, kMagic);
     unsigned long long X[NP > 0 ? NP : 1], SH[NP > 0 ? NP : 1], DT[NP > 0 ? NP : 1], DC[NP > 0 ? NP : 1];
@@ -335,8 +352,14 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
             const unsigned long long mg = f2_add_rm(t, MAG2);
             float mg0, mg1;
             f2_unpack(mg, mg0, mg1);
-            const int J0 = wrap_cell<POW2>(I[2 * p] - S0m[2 * p] + __float_as_int(mg0), N, err);
-            const int J1 = wrap_cell<POW2>(I[2 * p + 1] - S0m[2 * p + 1] + __float_as_int(mg1), N, err);
+            const int r0 = I[2 * p] - S0m[2 * p] + __float_as_int(mg0);
+            const int r1 = I[2 * p + 1] - S0m[2 * p + 1] + __float_as_int(mg1);
+            const int J0 = wrap_cell<POW2>(r0, N, err);
+            const int J1 = wrap_cell<POW2>(r1, N, err);
+            if constexpr (UNWRAP) {
+                (*Wr)[2 * p] += r0 >> log2n;
+                (*Wr)[2 * p + 1] += r1 >> log2n;
+            }
             I[2 * p] = J0;
             I[2 * p + 1] = J1;
             X[p] = f2_sub(t, f2_sub(mg, MAG2));
@@ -353,7 +376,9 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
             constexpr int q = PPT - 1;
             const float t = ((xi[q] - shi[q]) - dwT[q]) - dwC_last;
             const float mg = __fadd_rd(t, kMagic);
-            const int J = wrap_cell<POW2>(I[q] - S0m[q] + __float_as_int(mg), N, err);
+            const int r = I[q] - S0m[q] + __float_as_int(mg);
+            const int J = wrap_cell<POW2>(r, N, err);
+            if constexpr (UNWRAP) (*Wr)[q] += r >> log2n;
             I[q] = J;
             xi[q] = t - (mg - kMagic);
             // the odd chain keeps the plain loads: with the ordering of

@@ -36,7 +36,7 @@ namespace nufi_gb300 {
 
 using namespace split;
 
-template <int PPT, bool POW2>
+template <int PPT, bool POW2, bool UNWRAP>
 __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Problem p, const float *__restrict__ tables,
                                                                      const SplitNode *__restrict__ nodes,
                                                                      const float2 *__restrict__ phase, int n,
@@ -55,11 +55,13 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
     const int G = gridDim.x;
     // velocity nodes interleaved over the CTAs: chain j of CTA c is c + j G
     long long mv[PPT];
-    int I[PPT], S0m[PPT];
+    int I[PPT], S0m[PPT], Wr[PPT];
     float xi[PPT], dwT[PPT], dwTc[PPT], shi[PPT], slo[PPT];
     bool live[PPT];
+    const int log2n = __ffs(N) - 1;
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
+        Wr[q] = 0;
         const long long m = blockIdx.x + (long long)(grp * PPT + q) * G;
         const long long qq = (long long)s * p.Nm + m;
         live[q] = (s < N) && (m < p.Nm) && (qq >= q_begin) && (qq < q_end);
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
             const float *__restrict__ chunk = ring + slot * S * TS;
             const int k_hi = n - 1 - j * S;
             const int k_lo = max(0, k_hi - S + 1);
-            trace_chunk<PPT, POW2>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err);
+            trace_chunk<PPT, POW2, UNWRAP>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err, &Wr, log2n);
             __syncthreads();  // everyone is done with this slot
             if (threadIdx.x == 0 && j + kRing < nchunks) issue(j + kRing);
         }
@@ -115,7 +117,9 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
     for (int q = 0; q < PPT; ++q) {
         if (!live[q]) continue;
         const SplitNode nd = nodes[mv[q]];
-        acc += double(delta_f0(f, nd, __ldg(phase + I[q]), xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
+        float2 cs = __ldg(phase + I[q]);
+        if constexpr (UNWRAP) cs = phase_unwrapped(cs, Wr[q] - n * ((nd.S0u - nd.S0) / N), p.phase_wrap);
+        acc += double(delta_f0(f, nd, cs, xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
     }
     // groups of the same node combined in group order
     if (blockDim.x > unsigned(Nr)) {
@@ -155,27 +159,31 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
 
 namespace {
 
+template <int PPT, bool POW2, bool UNWRAP>
+cudaError_t launch_staged_form(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
+                               const float2 *phase, int n, long long qb, long long qe, double *partial,
+                               const RhoFix &fx, unsigned *err, cudaStream_t st)
+{
+    static const cudaError_t attr = cudaFuncSetAttribute(trace_split_1d_staged_kernel<PPT, POW2, UNWRAP>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (attr != cudaSuccess) return attr;
+    trace_split_1d_staged_kernel<PPT, POW2, UNWRAP><<<dim3(sh.ctas), dim3(sh.threads), sh.smem, st>>>(
+        p, tables, nodes, phase, n, qb, qe, sh.slabs_per_chunk, sh.threads / sh.tpn, partial, fx, err);
+    return cudaGetLastError();
+}
+
 template <int PPT>
 cudaError_t launch_staged_ppt(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
                               const float2 *phase, int n, long long qb, long long qe, double *partial,
                               const RhoFix &fx, unsigned *err, cudaStream_t st)
 {
     const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
-    const dim3 grid(sh.ctas), block(sh.threads);
-    if (pow2) {
-        static const cudaError_t attr = cudaFuncSetAttribute(trace_split_1d_staged_kernel<PPT, true>,
-                                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        if (attr != cudaSuccess) return attr;
-        trace_split_1d_staged_kernel<PPT, true><<<grid, block, sh.smem, st>>>(p, tables, nodes, phase, n, qb, qe,
-                                                                              sh.slabs_per_chunk, sh.threads / sh.tpn, partial, fx, err);
-    } else {
-        static const cudaError_t attr = cudaFuncSetAttribute(trace_split_1d_staged_kernel<PPT, false>,
-                                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        if (attr != cudaSuccess) return attr;
-        trace_split_1d_staged_kernel<PPT, false><<<grid, block, sh.smem, st>>>(p, tables, nodes, phase, n, qb, qe,
-                                                                               sh.slabs_per_chunk, sh.threads / sh.tpn, partial, fx, err);
+    if (p.phase_wrap != 0.0) {  // f0's phase at the unwrapped foot (admitted for N a power of two only)
+        if (!pow2) return cudaErrorInvalidValue;
+        return launch_staged_form<PPT, true, true>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
     }
-    return cudaGetLastError();
+    if (pow2) return launch_staged_form<PPT, true, false>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
+    return launch_staged_form<PPT, false, false>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
 }
 
 }  // namespace

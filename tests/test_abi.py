@@ -12,7 +12,7 @@ import pytest
 from conftest import ROOT
 
 import numericalflowiteration_gb300 as nufi
-from numericalflowiteration_gb300 import _lib
+from numericalflowiteration_gb300 import _lib, plan
 from numericalflowiteration_gb300.config import NufiConfigC, landau_1d, two_stream_1d
 
 HEADER = ROOT / "include" / "nufi_gb300.h"
@@ -129,33 +129,42 @@ def test_bump_on_tail_in_3d_is_fp64_only(lib):
     assert st == _lib.ERR_UNSUPPORTED
 
 
-def test_split_needs_a_periodic_f0_phase(lib):
-    """The FP32-split traces evaluate cos(k x) at the foot wrapped into the
-    domain; the reference (nufi/rho.hpp:59-60) and the FP64 trace at the
-    unwrapped foot.  Split handles whose k (x_max - x_min) is not a multiple
-    of 2 pi on some axis are refused at create; FP64 takes them."""
+def test_split_f0_phase_at_the_unwrapped_foot(lib):
+    """The reference (nufi/rho.hpp:59-60) and the FP64 trace evaluate
+    cos(k x) at the unwrapped foot.  The FP32-split traces take the wrapped
+    cell's phase; when k (x_max - x_min) is not a multiple of 2 pi, the 1D
+    staged traces also count each chain's wraps and turn the phase by k L
+    per wrap, for Nx a power of two up to 256.  Other split handles with
+    such a k are refused at create (and by nufi_plan), as are the options
+    that select the global-load 1D trace; FP64 takes any k."""
     from numericalflowiteration_gb300.config import bump_on_tail_1d, landau_2d, landau_3d
-    for cfg in (landau_1d(k=0.3, precision="fp32split"), two_stream_1d(k=0.45, precision="fp32split"),
+    for cfg in (landau_1d(k=0.3, Nx=100, precision="fp32split"), landau_1d(k=0.3, Nx=512, precision="fp32split"),
                 landau_2d(k=0.25, precision="fp32split"), landau_3d(k=0.75, precision="fp32split")):
         st, msg = _create_status(lib, cfg.to_c())
         assert st == _lib.ERR_UNSUPPORTED and "2 pi" in msg, (cfg, msg)
-    # the reference's <float, 4> 1D configuration through the drop-in header:
-    # x_max = 4 pi computed in float (2.8e-8 above 4 pi) must pass
+    # admitted: 1D staged forms, and the reference's <float, 4> 1D
+    # configuration through the drop-in header (x_max = 4 pi computed in
+    # float, 2.8e-8 above 4 pi: periodic within the tolerance)
     float_4pi = float(np.float32(4 * np.pi))
-    for cfg in (landau_1d(k=0.3), landau_1d(k=1.0, precision="fp32split"), landau_2d(k=1.5, precision="fp32split"),
-                bump_on_tail_1d(k=0.37, precision="fp32split"), bump_on_tail_1d(k=0.3, precision="fp32split"),
-                landau_3d(precision="fp32split"),
+    for cfg in (landau_1d(k=0.3), landau_1d(k=0.3, Nx=64, precision="fp32split"),
+                two_stream_1d(k=0.45, precision="fp32split"), landau_1d(k=1.0, precision="fp32split"),
+                landau_2d(k=1.5, precision="fp32split"), bump_on_tail_1d(k=0.37, precision="fp32split"),
+                bump_on_tail_1d(k=0.3, precision="fp32split"), landau_3d(precision="fp32split"),
                 two_stream_1d(Nx=256, Nv=512, Nt=1600, precision="fp32split").replace(x_max=[float_4pi])):
         st, msg = _create_status(lib, cfg.to_c())
         assert not msg.startswith("nufi_create:"), (cfg, msg)
+    for opts in ({"split_global_loads": 1}, {"split_plain_kick": 1}):
+        with pytest.raises(NotImplementedError, match="staged"):
+            plan(landau_1d(k=0.3, Nx=64, precision="fp32split"), 152, opts)
+    assert plan(landau_1d(k=0.3, Nx=64, precision="fp32split"), 152)["trace"] == "trace_split_1d_staged_kernel"
     with pytest.raises(NotImplementedError):
-        nufi.Simulation(landau_1d(k=0.3, precision="fp32split"))
+        nufi.Simulation(landau_1d(k=0.3, Nx=100, precision="fp32split"))
 
 
 _NOALLOC_REFUSALS = r"""
 import ctypes, sys
 sys.path.insert(0, sys.argv[1])
-from numericalflowiteration_gb300 import _lib
+from numericalflowiteration_gb300 import _lib, plan
 from numericalflowiteration_gb300.config import landau_1d
 lib = _lib.load()
 cfg = landau_1d(Nx=16, Nv=32, Nt=8)

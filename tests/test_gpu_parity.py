@@ -237,6 +237,36 @@ def test_persistent_run_matches_per_step_launches(nufi, cfgname):
     assert rel_max(ea, g["energy"][:cfg.Nt + 1]) <= 1e-6
 
 
+def test_split_landau_k03_phase_at_the_unwrapped_foot(nufi):
+    """k = 0.3 on [0, 4 pi) (k L = 1.2 pi, feet wrap up to 3 times): f0's
+    phase at the unwrapped foot (wrap counts in the staged traces), in the
+    whole-run kernel, the per-step launches and the drop-in compute_rho on
+    the FP64 history, against the reference's energy history and rho: the
+    split gate.  The wrapped foot's phase would miss it by orders
+    of magnitude (a 1.2 pi phase error per wrap of an alpha = 0.05 mode)."""
+    cfg, g = golden("params_landau_k03_1d_64x256_n60")
+    n = int(g["n_last"])
+    c = cfg.replace(precision="fp32split")
+    for opts in (None, {"no_persistent": 1}):
+        with nufi.Simulation(c, opts=opts) as sim:
+            e = sim.run(0, n)
+            rho = sim.download_rho(np.zeros(cfg.n_spatial))
+        assert rel_max(e, g["energy_comp"][:n + 1]) <= 1e-6, opts
+        assert rel_max(rho, g["rho_comp"][list(g["rho_steps"]).index(n)]) <= 1e-6, opts
+    # the drop-in compute_rho on the FP64 history (itself the reference's to
+    # 1e-12, test_fp64_graph_run_matches_reference)
+    with nufi.Simulation(cfg) as ref:
+        ref.run(0, n)
+        coeffs = ref.history()
+    with nufi.Simulation(c) as sim:
+        for k in range(n + 1):
+            sim.upload_phi(k, coeffs)
+        for k in (1, 30, 60):
+            sim.compute_rho(k)
+            got = sim.download_rho(np.zeros(cfg.n_spatial))
+            assert rel_max(got, g["rho_comp"][list(g["rho_steps"]).index(k)]) <= 1e-6, k
+
+
 def test_persistent_run_subrange_and_repeat(nufi):
     """Steps in two calls (0..k, k+1..Nt) and a repeated run give the same
     history as one call."""

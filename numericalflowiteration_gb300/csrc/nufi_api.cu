@@ -426,16 +426,20 @@ bool solve_geometry(const Problem &p, int sms, SolvePlan &pl, std::string &why)
         return true;
     }
     pl.nconv = (p.precision == NUFI_PREC_FP32_SPLIT && p.dim == 1) ? 5 : 2;
-    // one warp per node; warps (nodes) per block: at most 8, fewer until the
-    // blocks fill every SM twice
+    // one warp per node; warps (nodes) per block: at most 8, fewer until
+    // there are 64 blocks.  Measured on the two-stream grid (256 nodes, the
+    // drop-in field solve): 4 nodes per block 18.8 us per call, 1 node
+    // 21.1 us, 8 nodes 20.4 us; each block reads rho once (mapped host memory
+    // in the drop-in call), so fewer blocks read it fewer times, while more
+    // nodes per block serialise more FP64 work on one SM.  The green kernels
+    // are read from L2 (batched loads), not staged per block.
+    (void)sms;
     int npb = 8;
-    while (npb > 1 && (p.Ns + npb - 1) / npb < 2LL * sms) npb /= 2;
+    while (npb > 1 && (p.Ns + npb - 1) / npb < 64) npb /= 2;
     pl.nodes_per_block = npb;
     pl.blocks = int((p.Ns + npb - 1) / npb);
-    // the green kernels staged per block only where a block's warps share them
-    const size_t with_green = size_t(p.Ns) * 8 * (1 + pl.nconv);
-    pl.green_in_smem = npb >= 4 && with_green <= 160 * 1024;
-    pl.smem = pl.green_in_smem ? with_green : size_t(p.Ns) * 8;
+    pl.green_in_smem = false;
+    pl.smem = size_t(p.Ns) * 8;
     return true;
 }
 

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(256, 1) batch_trace_split_kernel(const BatchIn
             ok &= mbar_wait(smem_addr(&full_bar[slot]), unsigned((j / kRing) & 1));
             const int k_hi = n - 1 - j * S;
             const int k_lo = max(0, k_hi - S + 1);
-            trace_chunk<PPT, POW2>(ring + slot * S * TS, TS, k_hi, k_lo, N, Ic, xi, dwT, dwTc, shi, S0m, err);
+            trace_chunk<PPT, POW2, false, 2>(ring + slot * S * TS, TS, k_hi, k_lo, N, Ic, xi, dwT, dwTc, shi, S0m, err);
             __syncthreads();  // everyone is done with this slot
             if (threadIdx.x == 0 && j + kRing < nchunks) issue(j + kRing);
         }
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(256, 1) batch_run_split_kernel(const BatchInst
                     ok &= mbar_wait(smem_addr(&full_bar[slot]), (gj / kRing) & 1u);
                     const int k_hi = n - 1 - j * S;
                     const int k_lo = max(0, k_hi - S + 1);
-                    trace_chunk<PPT, POW2>(ring + slot * SW, TS, k_hi, k_lo, N, Ic, xi, dwT, dwTc, shi, S0m, err);
+                    trace_chunk<PPT, POW2, false, 2>(ring + slot * SW, TS, k_hi, k_lo, N, Ic, xi, dwT, dwTc, shi, S0m, err);
                     __syncthreads();  // everyone is done with this slot
                     if (threadIdx.x == 0) {
                         const int jj = j + kRing;

@@ -205,8 +205,8 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
                 const float *__restrict__ chunk = ring + slot * S * TS;
                 int k_lo, k_hi;
                 chunk_range(n, j, k_lo, k_hi);
-                trace_chunk<PPT, POW2, UNWRAP>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err, &Wr,
-                                               log2n);
+                trace_chunk<PPT, POW2, UNWRAP, 2>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err, &Wr,
+                                                  log2n);
                 __syncwarp();
                 if (lane == 0 && atom_add_acq_rel_cta(&released[slot], 1u) == unsigned(W - 1)) {
                     released[slot] = 0;

@@ -324,7 +324,7 @@ __device__ __forceinline__ int wrap_cell(int J, int N, unsigned *err)
 // Chains go two at a time through the packed FP32 instructions (the FP32
 // part of a substep, 9 operations, in 9 instructions for two chains); the
 // integer cell update and the two shared loads stay per chain.
-template <int PPT, bool POW2, bool UNWRAP = false>
+template <int PPT, bool POW2, bool UNWRAP = false, int UNROLL = 1>
 __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int TS, int k_hi, int k_lo, int N,
                                             int (&I)[PPT], float (&xi)[PPT], float (&dwT)[PPT], float (&dwTc)[PPT],
                                             const float (&shi)[PPT], const int (&S0m)[PPT], unsigned *err,
@@ -394,10 +394,10 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
         }
     };
     const int k_stop = max(k_lo, 1);
-    // two substeps per loop trip: the loop's own work (counter, slab
-    // address) is shared, and the second substep's independent address
-    // arithmetic overlaps the first (62.9 -> 60.7 ms on the whole run)
-#pragma unroll 2
+    // UNROLL substeps per loop trip: the whole-run kernel takes 2 (the
+    // loop's own work is shared and the second substep's address arithmetic
+    // overlaps the first: 62.9 -> 60.7 ms on the whole two-stream run)
+#pragma unroll UNROLL
     for (int k = k_hi; k >= k_stop; --k) substep(chunk + (k - k_lo) * TS, 1.0f);
     if (k_lo == 0) substep(chunk, 0.5f);
     // fold this chunk's kicks into the compensated totals

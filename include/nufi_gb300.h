@@ -175,12 +175,24 @@ int nufi_upload_phi_f32(nufi_handle *h, int64_t n, const float *coeffs_base);
  *   m[2] = sum w |u0|^2 f / 2 (kinetic energy)
  *   m[3] = sum -w f log f over f > 0 (entropy)
  * w = du dx (1D), dx dy du dv (2D), du dv dw (3D: as the reference, without
- * dx dy dz).  The metrics grid is the rho grid (the reference drivers set
- * conf_metrics to the same Nx, Nu; bin/test_nufi_gpu_1d.cpp:216-221).  Always
- * evaluated in FP64 on the FP64 history, also for FP32-split handles.  An
- * empty range returns without touching the device sums (as the reference);
- * n > Nt is NUFI_ERR_RANGE (the reference does not check).  Asynchronous. */
+ * dx dy dz).  The points lie on the metrics grid: the rho grid, or the grid
+ * nufi_set_metrics_grid gave (then q ranges over its Ns * Nm points).
+ * Always evaluated in FP64 on the FP64 history, also for FP32-split
+ * handles.  An empty range returns without touching the device sums (as the
+ * reference); n > Nt is NUFI_ERR_RANGE (the reference does not check).
+ * Asynchronous. */
 int nufi_compute_metrics(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end);
+/* The metrics grid of the reference's two-config constructor
+ * cuda_kernel(conf, conf_metrics) (nufi/cuda_kernel.cu:96-108, 53-79): point
+ * (ix, iu) at x = x_min + ix dx, u = v_min + iu du + du / 2 with dx =
+ * (x_max - x_min) / Nx, du = (v_max - v_min) / Nv per axis, weight as in
+ * nufi_compute_metrics with these dx, du.  Only dim, Nx, Nv, x_min, x_max,
+ * v_min and v_max of `metrics` are read; dim must be the handle's.  f is
+ * still evaluated with the handle's own history and splines.  NULL returns
+ * to the rho grid.  At most 2^31 - 1 spatial and 2^31 - 1 velocity points
+ * (NUFI_ERR_RANGE beyond).  Blocks (one allocation the first time a grid
+ * needs more partial sums than the handle holds). */
+int nufi_set_metrics_grid(nufi_handle *h, const nufi_config *metrics);
 /* cuda_kernel::download_metrics (nufi/cuda_kernel.cu:177-189): m[k] += the
  * device sums.  Blocks. */
 int nufi_download_metrics(nufi_handle *h, double *metrics4);

@@ -142,22 +142,6 @@ nufi_config to_c(const nufi::dim3::config_t<real> &c, int order)
     return k;
 }
 
-// The reference's metrics kernel puts its points on conf_metrics's grid
-// (nufi/cuda_kernel.cu:53-79); here the metrics use the rho grid, which is
-// what the reference's drivers pass (bin/test_nufi_gpu_1d.cpp:216-221).  A
-// different metrics grid is refused instead of silently replaced.
-template <typename real, typename conf_t>
-const conf_t &same_metrics_grid(const conf_t &conf, const conf_t &conf_metrics)
-{
-    const nufi_config a = to_c<real>(conf, 4), b = to_c<real>(conf_metrics, 4);
-    for (int i = 0; i < 3; ++i)
-        if (a.Nx[i] != b.Nx[i] || a.Nv[i] != b.Nv[i] || a.x_min[i] != b.x_min[i] || a.x_max[i] != b.x_max[i] ||
-            a.v_min[i] != b.v_min[i] || a.v_max[i] != b.v_max[i])
-            throw std::invalid_argument("nufi_gb300: metrics on a grid other than rho's are not supported "
-                                        "(conf_metrics must have conf's node counts and domain)");
-    return conf;
-}
-
 // The body shared by dim1/dim2/dim3::cuda_kernel.
 template <typename conf_t, typename real, size_t order>
 class kernel_impl {
@@ -189,6 +173,14 @@ public:
             throw_status(handle.get(), nufi_upload_phi_f32(handle.get(), (int64_t)n, reinterpret_cast<const float *>(coeffs)));
         else
             throw_status(handle.get(), nufi_upload_phi(handle.get(), (int64_t)n, reinterpret_cast<const double *>(coeffs)));
+    }
+
+    // The reference's metrics points lie on conf_metrics's grid
+    // (nufi/cuda_kernel.cu:53-79, 96-108): nufi_set_metrics_grid.
+    void set_metrics_grid(const conf_t &conf_metrics)
+    {
+        const nufi_config k = to_c<real>(conf_metrics, int(order));
+        throw_status(handle.get(), nufi_set_metrics_grid(handle.get(), &k));
     }
 
     void compute_metrics(size_t n, size_t q_min, size_t q_max)
@@ -237,8 +229,9 @@ namespace nufi {
         cuda_kernel(const config_t<real> &conf, int dev = cuda::get_device()) : impl(conf, dev) {} \
         cuda_kernel(const config_t<real> &conf, const config_t<real> &conf_metrics,                \
                     int dev = cuda::get_device())                                                   \
-            : impl(nufi_gb300::same_metrics_grid<real>(conf, conf_metrics), dev)                    \
+            : impl(conf, dev)                                                                       \
         {                                                                                           \
+            impl.set_metrics_grid(conf_metrics);                                                    \
         }                                                                                           \
         cuda_kernel(const cuda_kernel &rhs) = delete;                                               \
         cuda_kernel(cuda_kernel &&rhs) = default;                                                   \

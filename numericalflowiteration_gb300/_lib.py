@@ -60,6 +60,7 @@ SIGNATURES = {
     "nufi_batch_stream": (ctypes.c_int, [_P, _P]),
     "nufi_batch_describe": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "nufi_download_metrics": (ctypes.c_int, [_P, _P]),
+    "nufi_set_metrics_grid": (ctypes.c_int, [_P, _P]),
     "nufi_step": (ctypes.c_int, [_P, _I64, _P]),
     "nufi_run": (ctypes.c_int, [_P, _I64, _I64, _P]),
     "nufi_download_history": (ctypes.c_int, [_P, _I64, _I64, _P]),
@@ -194,6 +195,7 @@ class Simulation:
         self.stride_t = cfg.stride_t
         self.n_spatial = cfg.n_spatial
         self.n_points = cfg.n_points
+        self._metrics_points = cfg.n_points
 
     # -- plumbing ---------------------------------------------------------
     def _check(self, st: int):
@@ -289,9 +291,21 @@ class Simulation:
         return json.loads(buf.value.decode())
 
     def compute_metrics(self, n: int, q_begin: int = 0, q_end: int | None = None):
-        """L1 norm, sum w f^2, kinetic energy and entropy of f(n) (eval_f)."""
-        q_end = self.n_points if q_end is None else q_end
+        """L1 norm, sum w f^2, kinetic energy and entropy of f(n) (eval_f),
+        over the metrics grid's points (by default all of them)."""
+        q_end = self._metrics_points if q_end is None else q_end
         self._check(self._lib.nufi_compute_metrics(self._h, n, q_begin, q_end))
+
+    def set_metrics_grid(self, metrics_cfg=None):
+        """The metrics points on another grid (the reference's conf_metrics):
+        its Nx, Nv and domain; None returns to the rho grid."""
+        if metrics_cfg is None:
+            self._check(self._lib.nufi_set_metrics_grid(self._h, None))
+            self._metrics_points = self.n_points
+            return
+        c = metrics_cfg.to_c()
+        self._check(self._lib.nufi_set_metrics_grid(self._h, ctypes.byref(c)))
+        self._metrics_points = metrics_cfg.n_points
 
     def download_metrics(self, metrics: np.ndarray | None = None) -> np.ndarray:
         """metrics += device sums (4 doubles); a new zeroed array if None."""

@@ -57,6 +57,11 @@ struct nufi_handle {
     SplitNode *nodes = nullptr;
     float2 *phase = nullptr;
     double *mpartial = nullptr;  // [4][trace blocks] metrics block sums
+    size_t mpartial_n = 0;       // its doubles
+    // nufi_set_metrics_grid: the metrics points' grid and its FP64 shape
+    bool mgrid_set = false;
+    PointGrid mgrid;
+    LaunchShape mshape;
     double *metrics = nullptr;   // [4]
     // adjoint (allocated on first nufi_backward)
     AdjointPlan aplan;
@@ -870,7 +875,8 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
         (e = dalloc(h.get(), &h->rho, size_t(p.Ns))) != cudaSuccess ||
         (e = dalloc(h.get(), &h->energy, nslab)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->slab_out, size_t(p.hist_stride) + 1)) != cudaSuccess ||
-        (e = dalloc(h.get(), &h->mpartial, size_t(4 * ((p.Ns + 31) / 32) * fp64_rows(h->shape)))) != cudaSuccess ||
+        (e = dalloc(h.get(), &h->mpartial, h->mpartial_n = size_t(4 * ((p.Ns + 31) / 32) * fp64_rows(h->shape)))) !=
+            cudaSuccess ||
         (e = dalloc(h.get(), &h->metrics, 4)) != cudaSuccess ||
         (e = dalloc(h.get(), &h->err, 1)) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMalloc"));
@@ -995,19 +1001,74 @@ int nufi_compute_metrics(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_e
 {
     if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
     if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
-    if (q_begin < 0 || q_end < q_begin || q_end > h->p.Nq)
-        return fail(h, NUFI_ERR_RANGE, "quadrature range outside [0, Nq]");
+    const PointGrid grid = h->mgrid_set ? h->mgrid : point_grid_of(h->p);
+    if (q_begin < 0 || q_end < q_begin || q_end > grid.Ns * grid.Nm)
+        return fail(h, NUFI_ERR_RANGE, "quadrature range outside the metrics grid's [0, Ns Nm]");
     if (q_begin == q_end) return NUFI_OK;  // as the reference: no launch, sums untouched
     DeviceGuard g(h->device);
     const Problem &p = h->p;
+    const LaunchShape &shape = h->mgrid_set ? h->mshape : h->shape;
     int rows = 0;
-    cudaError_t e = launch_trace_fp64(p, h->shape, h->hist, int(n), q_begin, q_end, 2, h->mpartial, &rows, h->err,
-                                      h->stream);
+    cudaError_t e = launch_trace_fp64(p, shape, h->hist, int(n), q_begin, q_end, 2, h->mpartial, &rows, h->err,
+                                      h->stream, &grid);
     if (e != cudaSuccess) return cuda_fail(h, e, "metrics launch");
     h->launches += 1;
-    e = launch_reduce_metrics((p.Ns + 31) / 32 * (long long)rows, h->mpartial, h->metrics, h->stream);
+    e = launch_reduce_metrics((grid.Ns + 31) / 32 * (long long)rows, h->mpartial, h->metrics, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "metrics reduce launch");
     h->launches += 1;
+    return NUFI_OK;
+}
+
+int nufi_set_metrics_grid(nufi_handle *h, const nufi_config *m)
+{
+    if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (!m) {
+        h->mgrid_set = false;
+        return NUFI_OK;
+    }
+    const Problem &p = h->p;
+    if (m->dim != p.dim) return fail(h, NUFI_ERR_INVALID, "nufi_set_metrics_grid: dim must be the handle's");
+    PointGrid g = point_grid_of(p);
+    g.Ns = 1;
+    g.Nm = 1;
+    g.w = 1;
+    for (int a = 0; a < p.dim; ++a) {
+        if (m->Nx[a] < 1 || m->Nv[a] < 1 || !(m->x_max[a] > m->x_min[a]) || !(m->v_max[a] > m->v_min[a]) ||
+            !std::isfinite(m->x_max[a] - m->x_min[a]) || !std::isfinite(m->v_max[a] - m->v_min[a]))
+            return fail(h, NUFI_ERR_INVALID, "nufi_set_metrics_grid: node counts >= 1 and x_max > x_min, v_max > v_min");
+        if (m->Nx[a] > INT32_MAX || m->Nv[a] > INT32_MAX)
+            return fail(h, NUFI_ERR_RANGE, "nufi_set_metrics_grid: too many nodes on an axis");
+        g.N[a] = int(m->Nx[a]);
+        g.M[a] = int(m->Nv[a]);
+        g.xmin[a] = m->x_min[a];
+        g.dx[a] = (m->x_max[a] - m->x_min[a]) / double(m->Nx[a]);
+        g.vmin[a] = m->v_min[a];
+        g.dv[a] = (m->v_max[a] - m->v_min[a]) / double(m->Nv[a]);
+        g.Ns *= m->Nx[a];
+        g.Nm *= m->Nv[a];
+        if (g.Ns > INT32_MAX || g.Nm > INT32_MAX)
+            return fail(h, NUFI_ERR_RANGE, "nufi_set_metrics_grid: at most 2^31 - 1 spatial and velocity points");
+    }
+    for (int a = 0; a < p.dim; ++a) g.w *= g.dv[a];  // as Problem::wv, then dx below 3D (point_grid_of)
+    if (p.dim < 3)
+        for (int a = 0; a < p.dim; ++a) g.w *= g.dx[a];
+    DeviceGuard dg(h->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    Problem q = p;
+    q.Ns = g.Ns;
+    q.Nm = g.Nm;
+    const LaunchShape shape = choose_shape(q, sms > 0 ? sms : 1);
+    const size_t need = size_t(4) * size_t((g.Ns + 31) / 32) * size_t(fp64_rows(shape));
+    if (need > h->mpartial_n) {
+        // the old buffer may still be read by queued work: it stays allocated
+        // until the handle is destroyed
+        NUFI_CUDA(h, dalloc(h, &h->mpartial, need));
+        h->mpartial_n = need;
+    }
+    h->mgrid = g;
+    h->mshape = shape;
+    h->mgrid_set = true;
     return NUFI_OK;
 }
 

@@ -53,6 +53,35 @@ struct Problem {
                            // domain; 0 when k L is a multiple of 2 pi (the wrapped foot's phase is exact)
 };
 
+// The points an FP64 trace starts from and their metric weight: the
+// handle's own grid (point_grid_of), or for nufi_compute_metrics the
+// reference's metrics grid (conf_metrics, nufi/cuda_kernel.cu:53-79: x =
+// x_min + ix dx, u = u_min + iu du + du / 2, weight du dx).
+struct PointGrid {
+    int N[3], M[3];
+    long long Ns, Nm;
+    double xmin[3], dx[3], vmin[3], dv[3];
+    double w;  // prod_a dv_a, times prod_a dx_a below 3D (the reference's 3D metrics leave dx dy dz out)
+};
+
+inline PointGrid point_grid_of(const Problem &p)
+{
+    PointGrid g;
+    g.Ns = p.Ns;
+    g.Nm = p.Nm;
+    g.w = p.wv;
+    for (int a = 0; a < 3; ++a) {
+        g.N[a] = p.N[a];
+        g.M[a] = p.M[a];
+        g.xmin[a] = p.xmin[a];
+        g.dx[a] = p.dx[a];
+        g.vmin[a] = p.vmin[a];
+        g.dv[a] = p.dv[a];
+        if (p.dim < 3 && a < p.dim) g.w *= p.dx[a];
+    }
+    return g;
+}
+
 // n!, evaluated at compile time where the spline kernels use it (a runtime
 // call would recurse and divide in every spline evaluation)
 __host__ __device__ constexpr double faculty(int n) { return (n > 1) ? double(n) * faculty(n - 1) : 1.0; }

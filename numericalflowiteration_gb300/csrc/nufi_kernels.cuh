@@ -103,8 +103,10 @@ __device__ __forceinline__ void write_metrics_block(const double (&m4)[4], doubl
 // The trace kernels write per-block partial sums of f~ ([rows][Ns]); the
 // launchers return the row count through *rows.  mode 0: f~ (eval_ftilda);
 // mode 2: the four metrics of f (eval_f) into [4][blocks] block sums.
+// grid: the points' grid (metrics on conf_metrics); nullptr: p's own
 cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
-                              long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st);
+                              long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st,
+                              const PointGrid *grid = nullptr);
 bool fp64_order_supported(int dim, int order);
 // FP64 order-4 trace in cell units (trace_fp64_table.cu): 1D and 2D over
 // per-slab FP64 derivative tables of fp64_table_stride doubles per slab

@@ -222,8 +222,9 @@ __device__ __forceinline__ double f0_fp64(const Problem &p, const double *x, con
 // eval_ftilda (mode 0) or eval_f (mode 1, with the first half kick from
 // slab n) of PPT points per thread; see the file comment.
 template <int D, int ORDER, int PPT>
-__global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const double *__restrict__ hist, int n,
-                                                         long long q_begin, long long q_end, int mode, int vblocks,
+__global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const PointGrid g,
+                                                         const double *__restrict__ hist, int n, long long q_begin,
+                                                         long long q_end, int mode, int vblocks,
                                                          double *__restrict__ partial, unsigned *err)
 {
     const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
@@ -233,10 +234,9 @@ __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const 
     // 428-466): weight * f, weight * f^2, weight * |u0|^2 f / 2 and
     // -weight f log f, u0 the point's initial velocity; weight du (dx) in
     // 1D, dx dy du dv in 2D, du dv dw in 3D (the reference's 3D kernel
-    // leaves out dx dy dz).
-    double w = p.wv;
-    if (D < 3)
-        for (int a = 0; a < D; ++a) w *= p.dx[a];
+    // leaves out dx dy dz).  The points and the weight come from g (the
+    // handle's grid, or the metrics grid); the history and splines from p.
+    const double w = g.w;
     double acc = 0;
     double m4[4] = {0, 0, 0, 0};
 
@@ -248,25 +248,25 @@ __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const 
         double x[PPT][D], u[PPT][D];
         bool live[PPT];
         {
-            long long rs = s < p.Ns ? s : 0;
+            long long rs = s < g.Ns ? s : 0;
             int is[3] = {0, 0, 0};
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-                is[a] = int(rs % p.N[a]);
-                rs /= p.N[a];
+                is[a] = int(rs % g.N[a]);
+                rs /= g.N[a];
             }
 #pragma unroll
             for (int q = 0; q < PPT; ++q) {
                 const long long m = mb + q;
-                const long long qq = s * p.Nm + m;
-                live[q] = (s < p.Ns) && (m < p.Nm) && (qq >= q_begin) && (qq < q_end);
-                long long rm = m < p.Nm ? m : 0;
+                const long long qq = s * g.Nm + m;
+                live[q] = (s < g.Ns) && (m < g.Nm) && (qq >= q_begin) && (qq < q_end);
+                long long rm = m < g.Nm ? m : 0;
 #pragma unroll
                 for (int a = 0; a < D; ++a) {
-                    const int im = int(rm % p.M[a]);
-                    rm /= p.M[a];
-                    x[q][a] = p.xmin[a] + is[a] * p.dx[a];
-                    u[q][a] = p.vmin[a] + im * p.dv[a] + p.dv[a] / 2;
+                    const int im = int(rm % g.M[a]);
+                    rm /= g.M[a];
+                    x[q][a] = g.xmin[a] + is[a] * g.dx[a];
+                    u[q][a] = g.vmin[a] + im * g.dv[a] + g.dv[a] / 2;
                 }
             }
         }
@@ -314,8 +314,8 @@ __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const 
                 double uu = 0;
 #pragma unroll
                 for (int a = 0; a < D; ++a) {
-                    const double u0 = p.vmin[a] + int(rm % p.M[a]) * p.dv[a] + p.dv[a] / 2;
-                    rm /= p.M[a];
+                    const double u0 = g.vmin[a] + int(rm % g.M[a]) * g.dv[a] + g.dv[a] / 2;
+                    rm /= g.M[a];
                     uu += u0 * u0;
                 }
                 const double wf = w * f;
@@ -334,33 +334,35 @@ __global__ void __launch_bounds__(256) trace_fp64_kernel(const Problem p, const 
         write_metrics_block(m4, partial);
         return;
     }
-    write_partial_tiled(acc, s, p.Ns, partial);
+    write_partial_tiled(acc, s, g.Ns, partial);
 }
 
 // Launch table: dims x orders x points-per-thread.
 template <int D, int ORDER>
-static cudaError_t launch_fp64_order(const Problem &p, const LaunchShape &ls, const double *hist, int n,
-                                     long long qb, long long qe, int mode, double *partial, unsigned *err,
+static cudaError_t launch_fp64_order(const Problem &p, const PointGrid &g, const LaunchShape &ls, const double *hist,
+                                     int n, long long qb, long long qe, int mode, double *partial, unsigned *err,
                                      cudaStream_t st)
 {
     const dim3 block(32, ls.warps);
-    const dim3 grid(unsigned((p.Ns + 31) / 32), unsigned(fp64_rows(ls)));
+    const dim3 grid(unsigned((g.Ns + 31) / 32), unsigned(fp64_rows(ls)));
     const int vb = ls.vblocks;
     switch (ls.ppt) {
-    case 1: trace_fp64_kernel<D, ORDER, 1><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, vb, partial, err); break;
-    case 2: trace_fp64_kernel<D, ORDER, 2><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, vb, partial, err); break;
-    case 4: trace_fp64_kernel<D, ORDER, 4><<<grid, block, 0, st>>>(p, hist, n, qb, qe, mode, vb, partial, err); break;
+    case 1: trace_fp64_kernel<D, ORDER, 1><<<grid, block, 0, st>>>(p, g, hist, n, qb, qe, mode, vb, partial, err); break;
+    case 2: trace_fp64_kernel<D, ORDER, 2><<<grid, block, 0, st>>>(p, g, hist, n, qb, qe, mode, vb, partial, err); break;
+    case 4: trace_fp64_kernel<D, ORDER, 4><<<grid, block, 0, st>>>(p, g, hist, n, qb, qe, mode, vb, partial, err); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const double *hist, int n, long long qb,
-                              long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st)
+                              long long qe, int mode, double *partial, int *rows, unsigned *err, cudaStream_t st,
+                              const PointGrid *grid)
 {
     *rows = fp64_rows(ls);
+    const PointGrid g = grid ? *grid : point_grid_of(p);
 #define NUFI_CASE(D, O) \
-    if (p.dim == D && p.order == O) return launch_fp64_order<D, O>(p, ls, hist, n, qb, qe, mode, partial, err, st);
+    if (p.dim == D && p.order == O) return launch_fp64_order<D, O>(p, g, ls, hist, n, qb, qe, mode, partial, err, st);
     NUFI_CASE(1, 3) NUFI_CASE(1, 4) NUFI_CASE(1, 5) NUFI_CASE(1, 6) NUFI_CASE(1, 7) NUFI_CASE(1, 8)
     NUFI_CASE(2, 3) NUFI_CASE(2, 4) NUFI_CASE(2, 5) NUFI_CASE(2, 6)
     NUFI_CASE(3, 3) NUFI_CASE(3, 4) NUFI_CASE(3, 5)

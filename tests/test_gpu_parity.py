@@ -366,6 +366,61 @@ def test_metrics_match_reference(nufi, name, precision):
             sim.compute_metrics(cfg.Nt + 1)
 
 
+@pytest.mark.parametrize("name", ["metrics_landau_1d_64x256_T30", "metrics_small_landau_2d_8x8"])
+def test_metrics_on_the_conf_metrics_grid(nufi, oracle_mod, name):
+    """The reference's two-config kernel (nufi/cuda_kernel.cu:53-79,
+    96-108): metrics points on another grid (finer, over a sub-domain),
+    f = eval_f on the handle's own history.  Against the oracle's eval_f at
+    the same points (itself bit for bit the reference's point function),
+    summed exactly (math.fsum): 1e-12 per component.  A q range split in
+    two sums to the whole; None returns to the rho grid."""
+    import math
+    cfg, g = golden(name)
+    hist = np.ascontiguousarray(g["slabs"].reshape(-1))
+    n = int(g["steps"][-1])
+    d = cfg.dim
+    Nx = [int(v) * 3 // 2 for v in cfg.Nx[:d]]
+    Nv = [int(v) * 2 for v in cfg.Nv[:d]]
+    xlo = [a + 0.1 * (b - a) for a, b in zip(cfg.x_min[:d], cfg.x_max[:d])]
+    xhi = [a + 0.9 * (b - a) for a, b in zip(cfg.x_min[:d], cfg.x_max[:d])]
+    vlo = [0.8 * a for a in cfg.v_min[:d]]
+    vhi = [0.8 * b for b in cfg.v_max[:d]]
+    mcfg = cfg.replace(Nx=Nx, Nv=Nv, x_min=xlo, x_max=xhi, v_min=vlo, v_max=vhi)
+    dx = [(b - a) / k for a, b, k in zip(xlo, xhi, Nx)]
+    dv = [(b - a) / k for a, b, k in zip(vlo, vhi, Nv)]
+    # point q = s * Nm + m, s and m x-fastest over the axes (as the rho grid)
+    xs = [xlo[a] + np.arange(Nx[a]) * dx[a] for a in range(d)]
+    vs = [vlo[a] + np.arange(Nv[a]) * dv[a] + dv[a] / 2 for a in range(d)]
+    X = np.stack(np.meshgrid(*xs[::-1], indexing="ij")[::-1], -1).reshape(-1, d)
+    V = np.stack(np.meshgrid(*vs[::-1], indexing="ij")[::-1], -1).reshape(-1, d)
+    pts = np.concatenate([np.repeat(X, len(V), 0), np.tile(V, (len(X), 1))], 1)
+    f = oracle_mod.eval_points(cfg, n, hist, np.ascontiguousarray(pts), mode=1)
+    w = float(np.prod(dv)) * (float(np.prod(dx)) if d < 3 else 1.0)
+    u2 = np.sum(pts[:, d:] ** 2, 1)
+    pos = f > 0
+    ref = np.array([math.fsum(w * f), math.fsum(w * f * f), math.fsum(w * (u2 * f / 2)),
+                    math.fsum(-w * f[pos] * np.log(f[pos]))])
+    with nufi.Simulation(cfg) as sim:
+        for k in range(int(g["n_last"]) + 1):
+            sim.upload_phi(k, hist)
+        sim.set_metrics_grid(mcfg)
+        sim.compute_metrics(n)
+        got = sim.download_metrics()
+        assert np.max(np.abs(got - ref) / np.abs(ref)) <= 1e-12, (got, ref)
+        cut = len(pts) // 3
+        sim.compute_metrics(n, 0, cut)
+        parts = sim.download_metrics()
+        sim.compute_metrics(n, cut, len(pts))
+        sim.download_metrics(parts)
+        assert np.max(np.abs(parts - ref) / np.abs(ref)) <= 1e-12
+        with pytest.raises(IndexError):
+            sim.compute_metrics(n, 0, len(pts) + 1)
+        sim.set_metrics_grid(None)
+        sim.compute_metrics(n)
+        back = sim.download_metrics()
+        assert np.max(np.abs(back - g["metrics"][-1]) / np.abs(g["metrics"][-1])) <= 1e-12
+
+
 def test_fp64_velocity_grid_beyond_one_launch_row(nufi, oracle_mod):
     """A velocity grid with more blocks than the launch grid's y axis holds
     (2D, 1024^2 velocity nodes: 65536 blocks of 16 against 65535): the FP64

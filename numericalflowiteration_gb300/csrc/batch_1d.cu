@@ -707,9 +707,12 @@ __device__ __forceinline__ void adj_chunk_primal(const float *__restrict__ chunk
             X[pp] = f2_sub(t, f2_sub(mg, MAG2));
             const float2 bc0 = reinterpret_cast<const float2 *>(tk)[J0];
             const float2 bc1 = reinterpret_cast<const float2 *>(tk)[J1];
-            const unsigned long long C2 = f2_pack(bc0.y, bc1.y);
-            const unsigned long long kq =
-                f2_fma(X[pp], f2_fma(X[pp], C2, f2_pack(bc0.x, bc1.x)), f2_pack(tk[2 * N + J0], tk[2 * N + J1]));
+            // the quadratic per chain in scalar FMAs (the packed form's
+            // roundings; its operands arrive in different register pairs)
+            float x0, x1;
+            f2_unpack(X[pp], x0, x1);
+            const unsigned long long kq = f2_pack(fmaf(x0, fmaf(x0, bc0.y, bc0.x), tk[2 * N + J0]),
+                                                  fmaf(x1, fmaf(x1, bc1.y, bc1.x), tk[2 * N + J1]));
             DC[pp] = i == 0 ? f2_fma(H0, kq, DC[pp]) : f2_add(DC[pp], kq);
             if constexpr (SAVE) {
                 Jp[i][pp] = unsigned(J0) | (unsigned(J1) << 16);
@@ -749,7 +752,9 @@ __device__ __forceinline__ void adj_chunk_reverse(const float *__restrict__ chun
             // g' = K B + 2 K C xi from one float2 per chain
             const float2 bc0 = reinterpret_cast<const float2 *>(tk)[J0];
             const float2 bc1 = reinterpret_cast<const float2 *>(tk)[J1];
-            const unsigned long long gp = f2_fma(f2_add(x, x), f2_pack(bc0.y, bc1.y), f2_pack(bc0.x, bc1.x));
+            float xa, xb;
+            f2_unpack(x, xa, xb);
+            const unsigned long long gp = f2_pack(fmaf(xa + xa, bc0.y, bc0.x), fmaf(xb + xb, bc1.y, bc1.x));
             const unsigned long long vh = i == 0 ? f2_mul(VB[pp], H0) : VB[pp];
             const unsigned long long vx = f2_mul(vh, x);
             const unsigned long long vxx = f2_mul(vx, x);

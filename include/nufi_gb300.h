@@ -61,9 +61,9 @@ extern "C" {
  * f0's phase comes from the cell the foot lands in (the foot wrapped into
  * the domain); when k (x_max - x_min) is not a multiple of 2 pi (to 2.5e-7
  * relative: a single-precision domain length passes) the phase is turned
- * by k (x_max - x_min) per wrap of the foot, which 1D handles with Nx a
- * power of two up to 256 do (not with the split_global_loads or
- * split_plain_kick options, nor in batches); NUFI_ERR_UNSUPPORTED for other
+ * by k (x_max - x_min) per wrap of the foot, which handles with every Nx a
+ * power of two do (in 1D up to 256, and not with the split_global_loads or
+ * split_plain_kick options; not in batches); NUFI_ERR_UNSUPPORTED for other
  * such handles.  FP64 evaluates f0 at the unwrapped foot, as the
  * reference, for any k.                                                     */
 #define NUFI_PREC_FP32_SPLIT  1

@@ -242,17 +242,19 @@ int validate(const nufi_config *c, std::string &why)
     // reference's <float> configurations: 4 pi in float is 2.8e-8 above 4 pi)
     // passes, and the phase at the foot then moves by at most 2 pi 2.5e-7
     // per wrap of the domain, within the FP32-split form's accuracy.  Other
-    // k: the 1D staged traces count each chain's wraps and turn the phase by
-    // k L per wrap (Problem::phase_wrap), for N a power of two up to 256.
+    // k: the split traces count each chain's wraps per axis and turn the
+    // phase by k L_a per wrap (Problem::phase_wrap), for every N_a a power of
+    // two (and in 1D up to 256: the staged trace).
     if (c->precision == NUFI_PREC_FP32_SPLIT) {
+        bool wraps = false, pow2 = true;
         for (int a = 0; a < c->dim; ++a) {
-            if (phase_is_periodic(c->f0_params[1], c->x_max[a] - c->x_min[a])) continue;
-            const long long N = c->Nx[0];
-            if (c->dim != 1 || N > 256 || (N & (N - 1)) != 0) {
-                why = "FP32-split with k (x_max - x_min) not a multiple of 2 pi: 1D with Nx a power of two up to "
-                      "256 (f0's phase at the unwrapped foot); the FP64 trace takes any k";
-                return NUFI_ERR_UNSUPPORTED;
-            }
+            wraps = wraps || !phase_is_periodic(c->f0_params[1], c->x_max[a] - c->x_min[a]);
+            pow2 = pow2 && (c->Nx[a] & (c->Nx[a] - 1)) == 0;
+        }
+        if (wraps && (!pow2 || (c->dim == 1 && c->Nx[0] > 256))) {
+            why = "FP32-split with k (x_max - x_min) not a multiple of 2 pi: every Nx a power of two (in 1D up to "
+                  "256) (f0's phase at the unwrapped foot); the FP64 trace takes any k";
+            return NUFI_ERR_UNSUPPORTED;
         }
     }
     return NUFI_OK;
@@ -323,10 +325,12 @@ Problem make_problem(const nufi_config &c)
     p.split_plain_kick = 0;  // nufi_options.split_plain_kick, set by the caller
     // 1D split: the phase f0 gains per wrap of the domain (validate admits
     // a non-periodic phase for the staged traces only)
-    p.phase_wrap = 0.0;
-    if (c.precision == NUFI_PREC_FP32_SPLIT && c.dim == 1 && !phase_is_periodic(c.f0_params[1], p.L[0])) {
-        const double two_pi = 6.283185307179586476925286766559, kL = c.f0_params[1] * p.L[0];
-        p.phase_wrap = kL - two_pi * std::floor(kL / two_pi);
+    for (int a = 0; a < 3; ++a) {
+        p.phase_wrap[a] = 0.0;
+        if (c.precision == NUFI_PREC_FP32_SPLIT && a < c.dim && !phase_is_periodic(c.f0_params[1], p.L[a])) {
+            const double two_pi = 6.283185307179586476925286766559, kL = c.f0_params[1] * p.L[a];
+            p.phase_wrap[a] = kL - two_pi * std::floor(kL / two_pi);
+        }
     }
     return p;
 }
@@ -853,7 +857,7 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     plan_traces(h->p, sms > 0 ? sms : 1, h->opt, h->shape, h->staged);
-    if (h->p.phase_wrap != 0.0 && !h->staged.ok)
+    if (h->p.dim == 1 && phase_wraps(h->p) && !h->staged.ok)
         return fail(nullptr, NUFI_ERR_UNSUPPORTED,
                     "nufi_create: k (x_max - x_min) not a multiple of 2 pi needs the staged FP32-split trace (the "
                     "options chose the global-load form, which takes f0 at the wrapped foot)");
@@ -1607,7 +1611,7 @@ int nufi_plan_ex(const nufi_config *cfg, const nufi_options *opt, int sms, char 
     h.p.split_plain_kick = h.opt.split_plain_kick;
     h.fp64_table = h.p.precision == NUFI_PREC_FP64 && fp64_table_supported(h.p, cfg->Nt);
     plan_traces(h.p, sms, h.opt, h.shape, h.staged);
-    if (h.p.phase_wrap != 0.0 && !h.staged.ok)
+    if (h.p.dim == 1 && phase_wraps(h.p) && !h.staged.ok)
         return fail(nullptr, NUFI_ERR_UNSUPPORTED,
                     "nufi_plan: k (x_max - x_min) not a multiple of 2 pi needs the staged FP32-split trace");
     h.solve_ok = solve_geometry(h.p, sms, h.plan, h.solve_why);

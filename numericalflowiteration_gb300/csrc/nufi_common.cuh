@@ -49,9 +49,16 @@ struct Problem {
     int split_plain_kick;  // split mode: 1 = uncompensated FP32 kick sum
                            // (nufi_options.split_plain_kick; for measuring
                            // what the compensation buys)
-    double phase_wrap;     // 1D split: k L reduced to [0, 2 pi), the phase f0 gains per wrap of the
-                           // domain; 0 when k L is a multiple of 2 pi (the wrapped foot's phase is exact)
+    double phase_wrap[3];  // split: k L_a reduced to [0, 2 pi), the phase f0 gains per wrap of the
+                           // domain along axis a; 0 when k L_a is a multiple of 2 pi (the wrapped
+                           // foot's phase is exact)
 };
+
+// Some axis of a split problem turns f0's phase per wrap (the traces count wraps)
+__host__ __device__ inline bool phase_wraps(const Problem &p)
+{
+    return p.phase_wrap[0] != 0.0 || p.phase_wrap[1] != 0.0 || p.phase_wrap[2] != 0.0;
+}
 
 // The points an FP64 trace starts from and their metric weight: the
 // handle's own grid (point_grid_of), or for nufi_compute_metrics the

@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
             if (!live[q]) continue;
             const SplitNode nd = nodes[mv[q]];
             float2 cs = __ldg(phase + I[q]);
-            if constexpr (UNWRAP) cs = phase_unwrapped(cs, Wr[q] - n * ((nd.S0u - nd.S0) / N), p.phase_wrap);
+            if constexpr (UNWRAP) cs = phase_unwrapped(cs, Wr[q] - n * ((nd.S0u - nd.S0) / N), p.phase_wrap[0]);
             acc += double(delta_f0(f, nd, cs, xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
         }
         if (blockDim.x > unsigned(Nr)) {
@@ -317,7 +317,7 @@ cudaError_t launch_run_ppt(const Problem &p, const PersistentRun &pr, const Solv
     void (*fn)(const Problem, float *, double *, const SplitNode *, const float2 *, const double *,
                unsigned long long *, double, double, double *, double *, double *, int, int, int, int, unsigned *,
                unsigned *) = pow2 ? run_split_1d_kernel<PPT, true, false> : run_split_1d_kernel<PPT, false, false>;
-    if (p.phase_wrap != 0.0) {  // f0's phase at the unwrapped foot (admitted for N a power of two only)
+    if (phase_wraps(p)) {  // f0's phase at the unwrapped foot (admitted for N a power of two only)
         if (!pow2) return cudaErrorInvalidValue;
         fn = run_split_1d_kernel<PPT, true, true>;
     }

@@ -66,18 +66,21 @@ __device__ __forceinline__ void cubic_basis(float x, float (&Nv)[4], float (&Dv)
 
 template <int D>
 struct Chain {
-    int I[D], S0m[D];
+    int I[D], S0m[D], Wr[D];  // Wr: wraps of the domain per axis (UNWRAP)
     float xi[D], dwT[D], dwTc[D], dwC[D], shi[D];
 };
 
-// Drift of one axis: as the 1D chunk loop (split_device.cuh).
-template <bool POW2>
+// Drift of one axis: as the 1D chunk loop (split_device.cuh); with UNWRAP
+// (N a power of two) the wraps of the domain add to Wr.
+template <bool POW2, bool UNWRAP>
 __device__ __forceinline__ void drift_axis(int &I, float &xi, float dwT, float dwC, float shi, int S0m, int N,
-                                           unsigned *err)
+                                           unsigned *err, int &Wr, int log2n)
 {
+    static_assert(POW2 || !UNWRAP, "wrap counts need N a power of two");
     const float t = ((xi - shi) - dwT) - dwC;
     const float mg = __fadd_rd(t, kMagic);
     int J = I - S0m + __float_as_int(mg);
+    if constexpr (UNWRAP) Wr += J >> log2n;
     if constexpr (POW2) {
         J &= N - 1;
     } else {
@@ -170,7 +173,7 @@ __device__ __forceinline__ void field_grad(const float *__restrict__ slab, int s
 
 }  // namespace
 
-template <int D, int PPT, bool POW2, bool STAGED>
+template <int D, int PPT, bool POW2, bool STAGED, bool UNWRAP>
 __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p, const float *__restrict__ tables,
                                                                 const SplitNode *__restrict__ nodes,
                                                                 const float2 *__restrict__ phase, int n,
@@ -261,6 +264,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
             for (int a = 0; a < D; ++a) {
                 const SplitNode nd = nodes[(a > 0 ? p.M[0] : 0) + (a > 1 ? p.M[1] : 0) + int(rm % p.M[a])];
                 ch[q].I[a] = int(rs % p.N[a]);
+                ch[q].Wr[a] = 0;
                 rs /= p.N[a];
                 rm /= p.M[a];
                 ch[q].S0m[a] = nd.S0 + kMagicBits;
@@ -276,8 +280,8 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
             for (int q = 0; q < PPT; ++q) {
 #pragma unroll
                 for (int a = 0; a < D; ++a)
-                    drift_axis<POW2>(ch[q].I[a], ch[q].xi[a], ch[q].dwT[a], ch[q].dwC[a], ch[q].shi[a], ch[q].S0m[a],
-                                     p.N[a], err);
+                    drift_axis<POW2, UNWRAP>(ch[q].I[a], ch[q].xi[a], ch[q].dwT[a], ch[q].dwC[a], ch[q].shi[a],
+                                             ch[q].S0m[a], p.N[a], err, ch[q].Wr[a], __ffs(p.N[a]) - 1);
                 float gr[D];
                 field_grad<D>(sl, sy, sz, ch[q], gr);
 #pragma unroll
@@ -343,7 +347,9 @@ __global__ void __launch_bounds__(512, 1) trace_split_nd_kernel(const Problem p,
                 rm /= p.M[a];
                 const float du = ((ch[q].dwT[a] - ch[q].dwTc[a]) - nd.sig_lo) * float(p.dx[a] / p.dt);
                 delta = fmaf(du, nd.u0f + 0.5f * du, delta);
-                const float2 cs = __ldg(phase + (a > 0 ? p.N[0] : 0) + (a > 1 ? p.N[1] : 0) + ch[q].I[a]);
+                float2 cs = __ldg(phase + (a > 0 ? p.N[0] : 0) + (a > 1 ? p.N[1] : 0) + ch[q].I[a]);
+                if constexpr (UNWRAP)
+                    cs = phase_unwrapped(cs, ch[q].Wr[a] - n * ((nd.S0u - nd.S0) / p.N[a]), p.phase_wrap[a]);
                 float sp, cp;
                 sincosf(float(p.f0p[1] * p.dx[a]) * ch[q].xi[a], &sp, &cp);
                 csum += cs.x * cp - cs.y * sp;
@@ -369,8 +375,12 @@ cudaError_t launch_nd(const Problem &p, const StagedShape &sh, const float *tabl
     bool pow2 = true;
     for (int a = 0; a < D; ++a) pow2 = pow2 && ((p.N[a] & (p.N[a] - 1)) == 0);
     void (*fn)(const Problem, const float *, const SplitNode *, const float2 *, int, long long, long long, int, int,
-               double *, unsigned *) =
-        pow2 ? trace_split_nd_kernel<D, PPT, true, STAGED> : trace_split_nd_kernel<D, PPT, false, STAGED>;
+               double *, unsigned *) = pow2 ? trace_split_nd_kernel<D, PPT, true, STAGED, false>
+                                            : trace_split_nd_kernel<D, PPT, false, STAGED, false>;
+    if (phase_wraps(p)) {  // f0's phase at the unwrapped foot (admitted for every N a power of two)
+        if (!pow2) return cudaErrorInvalidValue;
+        fn = trace_split_nd_kernel<D, PPT, true, STAGED, true>;
+    }
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sh.smem));
     if (e != cudaSuccess) return e;
     fn<<<sh.ctas, sh.threads, sh.smem, st>>>(p, tables, nodes, phase, n, qb, qe, sh.slabs_per_chunk,

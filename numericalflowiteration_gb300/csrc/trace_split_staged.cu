@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
         if (!live[q]) continue;
         const SplitNode nd = nodes[mv[q]];
         float2 cs = __ldg(phase + I[q]);
-        if constexpr (UNWRAP) cs = phase_unwrapped(cs, Wr[q] - n * ((nd.S0u - nd.S0) / N), p.phase_wrap);
+        if constexpr (UNWRAP) cs = phase_unwrapped(cs, Wr[q] - n * ((nd.S0u - nd.S0) / N), p.phase_wrap[0]);
         acc += double(delta_f0(f, nd, cs, xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
     }
     // groups of the same node combined in group order
@@ -178,7 +178,7 @@ cudaError_t launch_staged_ppt(const Problem &p, const StagedShape &sh, const flo
                               const RhoFix &fx, unsigned *err, cudaStream_t st)
 {
     const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
-    if (p.phase_wrap != 0.0) {  // f0's phase at the unwrapped foot (admitted for N a power of two only)
+    if (phase_wraps(p)) {  // f0's phase at the unwrapped foot (admitted for N a power of two only)
         if (!pow2) return cudaErrorInvalidValue;
         return launch_staged_form<PPT, true, true>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
     }

@@ -132,14 +132,15 @@ def test_bump_on_tail_in_3d_is_fp64_only(lib):
 def test_split_f0_phase_at_the_unwrapped_foot(lib):
     """The reference (nufi/rho.hpp:59-60) and the FP64 trace evaluate
     cos(k x) at the unwrapped foot.  The FP32-split traces take the wrapped
-    cell's phase; when k (x_max - x_min) is not a multiple of 2 pi, the 1D
-    staged traces also count each chain's wraps and turn the phase by k L
-    per wrap, for Nx a power of two up to 256.  Other split handles with
-    such a k are refused at create (and by nufi_plan), as are the options
-    that select the global-load 1D trace; FP64 takes any k."""
+    cell's phase; when k (x_max - x_min) is not a multiple of 2 pi they also
+    count each chain's wraps per axis and turn the phase by k L per wrap,
+    for every Nx a power of two (in 1D up to 256, the staged trace).  Other
+    split handles with such a k are refused at create (and by nufi_plan), as
+    are the options that select the global-load 1D trace; FP64 takes any
+    k."""
     from numericalflowiteration_gb300.config import bump_on_tail_1d, landau_2d, landau_3d
     for cfg in (landau_1d(k=0.3, Nx=100, precision="fp32split"), landau_1d(k=0.3, Nx=512, precision="fp32split"),
-                landau_2d(k=0.25, precision="fp32split"), landau_3d(k=0.75, precision="fp32split")):
+                landau_2d(k=0.25, Nx=12, precision="fp32split"), landau_3d(k=0.75, Nx=12, precision="fp32split")):
         st, msg = _create_status(lib, cfg.to_c())
         assert st == _lib.ERR_UNSUPPORTED and "2 pi" in msg, (cfg, msg)
     # admitted: 1D staged forms, and the reference's <float, 4> 1D
@@ -147,6 +148,7 @@ def test_split_f0_phase_at_the_unwrapped_foot(lib):
     # float, 2.8e-8 above 4 pi: periodic within the tolerance)
     float_4pi = float(np.float32(4 * np.pi))
     for cfg in (landau_1d(k=0.3), landau_1d(k=0.3, Nx=64, precision="fp32split"),
+                landau_2d(k=0.25, precision="fp32split"), landau_3d(k=0.75, precision="fp32split"),
                 two_stream_1d(k=0.45, precision="fp32split"), landau_1d(k=1.0, precision="fp32split"),
                 landau_2d(k=1.5, precision="fp32split"), bump_on_tail_1d(k=0.37, precision="fp32split"),
                 bump_on_tail_1d(k=0.3, precision="fp32split"), landau_3d(precision="fp32split"),

@@ -267,6 +267,21 @@ def test_split_landau_k03_phase_at_the_unwrapped_foot(nufi):
             assert rel_max(got, g["rho_comp"][list(g["rho_steps"]).index(k)]) <= 1e-6, k
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_split_nd_phase_at_the_unwrapped_foot(nufi, oracle_mod, dim):
+    """2D/3D Landau with k = 0.3 on [0, 4 pi) per axis (feet wrap the domain):
+    the split trace counts wraps per axis and turns each axis's phase by
+    k L per wrap; the energy history against the oracle's (the reference's
+    algorithm, f0 at the unwrapped foot): the split gate."""
+    from numericalflowiteration_gb300.config import landau_2d, landau_3d
+    cfg = (landau_2d(Nx=16, Nv=32, Nt=30, alpha=0.05, k=0.3) if dim == 2 else
+           landau_3d(Nx=8, Nv=8, Nt=12, alpha=0.05, k=0.3))
+    ref, _, _ = oracle_mod.run(cfg)
+    with nufi.Simulation(cfg.replace(precision="fp32split")) as sim:
+        e = sim.run()
+    assert rel_max(e, ref) <= 1e-6
+
+
 def test_persistent_run_subrange_and_repeat(nufi):
     """Steps in two calls (0..k, k+1..Nt) and a repeated run give the same
     history as one call."""

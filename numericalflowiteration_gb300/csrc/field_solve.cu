@@ -141,7 +141,8 @@ template <int NCONV>
 __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     const Problem p, const double *__restrict__ rho, const double *__restrict__ green, int green_in_smem,
     double *__restrict__ slab, float *__restrict__ table, double *__restrict__ energy_partial,
-    unsigned *__restrict__ energy_counter, double *__restrict__ energy_out, unsigned *err, unsigned *err_pub)
+    unsigned *__restrict__ energy_counter, double *__restrict__ energy_out, unsigned *err, unsigned *err_pub,
+    unsigned *seq_pub, unsigned seq)
 {
     extern __shared__ double sm[];
     __shared__ double red[kSolveThreads];
@@ -260,7 +261,10 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
         for (int w = 0; w < int(blockDim.x >> 5); ++w) eb += eacc[w];
         energy_partial[blockIdx.x] = eb;
     }
-    __threadfence();
+    if (seq_pub)
+        __threadfence_system();  // the slab writes (host memory) before the ticket, for the host
+    else
+        __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = (atomicAdd(energy_counter, 1u) == gridDim.x - 1);
     __syncthreads();
@@ -275,6 +279,10 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
         if (energy_out) energy_out[0] = tot * (Lp / (2.0 * double(Ns)));
         energy_counter[0] = 0u;
         if (err_pub) *err_pub = atomicOr(err, 0u);  // after every block: the word as this solve leaves it
+        if (seq_pub) {  // after the slab, W and the word: a host that sees seq sees them
+            __threadfence_system();
+            *reinterpret_cast<volatile unsigned *>(seq_pub) = seq;
+        }
     }
 }
 
@@ -463,10 +471,10 @@ cudaError_t field_solve_prepare(const SolvePlan &plan)
 
 cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
                                float *table_slab, double *energy_out, cudaStream_t st, unsigned *err,
-                               unsigned *err_pub)
+                               unsigned *err_pub, unsigned *seq_pub, unsigned seq)
 {
     if (plan.spectral) {
-        if (err_pub) return cudaErrorInvalidValue;  // the spectral form publishes no error word
+        if (err_pub || seq_pub) return cudaErrorInvalidValue;  // the spectral form publishes neither
         return launch_spectral_solve(p, plan, rho, hist_slab, table_slab, energy_out, st);
     }
     // without a table, c and phi only: the green rows 0 and 1 of either form
@@ -474,11 +482,11 @@ cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const do
     if (plan.nconv == 5 && table_slab)
         circulant_solve_kernel<5><<<plan.blocks, threads, plan.smem, st>>>(
             p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
-            energy_out, err, err_pub);
+            energy_out, err, err_pub, seq_pub, seq);
     else
         circulant_solve_kernel<2><<<plan.blocks, threads, plan.smem, st>>>(
             p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
-            energy_out, err, err_pub);
+            energy_out, err, err_pub, seq_pub, seq);
     return cudaGetLastError();
 }
 

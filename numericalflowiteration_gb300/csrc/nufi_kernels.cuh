@@ -158,6 +158,8 @@ struct RhoFix {
     double scale = 0, limit = 0;
     double *rho = nullptr, *pub = nullptr;
     unsigned *err_pub = nullptr;
+    unsigned *seq_pub = nullptr;  // when given: seq written there after rho and the error word
+    unsigned seq = 0;
 };
 // 2^F and the bound on one CTA's scaled part for `ctas` CTAs each adding,
 // per node, the f~ of `chains` chains: no node's sum leaves int64.  False
@@ -226,10 +228,12 @@ constexpr int kSpectralMaxAxis = 4096;  // a line (complex FP64) in shared memor
 // table n (when table_slab != null) and the electric energy W_n.  With
 // err_pub (circulant form only), *err as the solve leaves it is written
 // there too, so that a caller reading slab, W and the word from mapped host
-// memory needs no further launch.
+// memory needs no further launch; with seq_pub, the blocks' writes are
+// fenced at system scope and seq is written there last (the caller may
+// wait for it instead of for the stream).
 cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
                                float *table_slab, double *energy_out, cudaStream_t st, unsigned *err = nullptr,
-                               unsigned *err_pub = nullptr);
+                               unsigned *err_pub = nullptr, unsigned *seq_pub = nullptr, unsigned seq = 0);
 cudaError_t field_solve_prepare(const SolvePlan &plan);
 
 PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const SolvePlan &plan, int sms);

@@ -151,9 +151,17 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
         if (fx.pub) fx.pub[j] = r;
         fx.sum[j] = 0ull;
     }
+    if (fx.seq_pub) {
+        __threadfence_system();
+        __syncthreads();
+    }
     if (threadIdx.x == 0) {
         *fx.ticket = 0u;
         if (fx.err_pub) *fx.err_pub = atomicOr(err, 0u);
+        if (fx.seq_pub) {  // after rho and the word: a host that sees seq sees them
+            __threadfence_system();
+            *reinterpret_cast<volatile unsigned *>(fx.seq_pub) = fx.seq;
+        }
     }
 }
 

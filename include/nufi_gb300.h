@@ -162,7 +162,11 @@ int nufi_download_rho_f32(nufi_handle *h, float *rho);
 /* cuda_kernel::upload_phi (nufi/cuda_kernel.cu:147-156): copies slab n from
  * coeffs_base + n*stride_t of the caller's history to the device.  Returns
  * once the caller's values have been read (the buffer may be reused); the
- * transfer is ordered before the handle's later work. */
+ * transfer is ordered before the handle's later work.  1D FP32-split
+ * handles keep the newest uploaded slab staged in pinned host memory: the
+ * next compute_rho(n + 1) derives its table inside the trace, and any other
+ * call of this library that reads the device history (and nufi_stream, for
+ * the caller's own work on the stream) applies it first. */
 int nufi_upload_phi(nufi_handle *h, int64_t n, const double *coeffs_base);
 int nufi_upload_phi_f32(nufi_handle *h, int64_t n, const float *coeffs_base);
 /* cuda_kernel::compute_metrics (nufi/cuda_kernel.cu:158-175, 341-358,

@@ -490,21 +490,6 @@ cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const do
     return cudaGetLastError();
 }
 
-namespace {
-
-// K (A, B, C) of cell i from c[i..i+3]: the derivative of the cubic
-// B-spline sum on [i, i+1) as a quadratic in xi, times K = -dt^2/dx^2.
-__device__ __forceinline__ void cubic_kick_poly(double c0, double c1, double c2, double c3, double K, float *slab,
-                                                int N, int i)
-{
-    const double A = (c2 - c0) * 0.5;
-    const double B = (c0 - 2.0 * c1) + c2;
-    const double C = ((3.0 * (c1 - c2) - c0) + c3) * 0.5;
-    store_kick_entry(slab, N, i, float(K * A), float(K * B), float(K * C));
-}
-
-}  // namespace
-
 __global__ void derive_table_kernel(const Problem p, const double *__restrict__ slab, float *__restrict__ table,
                                     double *__restrict__ hist_out)
 {

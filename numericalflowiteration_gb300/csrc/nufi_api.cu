@@ -71,9 +71,17 @@ struct nufi_handle {
     double *theta_acc = nullptr;  // [4][adjoint blocks]
     double *grad = nullptr;       // [4]
     std::vector<char> slab_set;   // slab n written (step, run, upload_phi)
-    double *stage = nullptr;      // pinned staging buffer of upload_phi (one slab)
-    double *stage_dev = nullptr;  // the same, as the device addresses it
-    cudaEvent_t stage_done = nullptr;
+    // upload_phi's pinned staging slots (one slab each, mapped), the device
+    // addresses of the same, and the event after the launch that last read each
+    double *stage[2] = {nullptr, nullptr};
+    double *stage_dev[2] = {nullptr, nullptr};
+    cudaEvent_t stage_done[2] = {nullptr, nullptr};
+    int stage_next = 0;
+    // 1D split (staged trace): the slab upload_phi staged but has not derived
+    // yet (-1: none).  compute_rho(pending_k + 1) derives it inside its trace;
+    // every other call that reads the history applies it first (flush_upload).
+    long long pending_k = -1;
+    int pending_slot = 0;
     // Pinned block of the blocking calls: [0] the device error word (copied
     // on the stream before the one synchronisation of a call), then rho
     // (Ns), the field solve's slab (stride_t) and W, and its rho input (Ns).
@@ -747,6 +755,68 @@ int wait_published(nufi_handle *h, unsigned seq)
     return sync_published(h);
 }
 
+// The calling thread's current device set to the handle's for the scope
+// of a call (and restored after).
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// Derivation of slab n from a staging slot: one launch reads the slab from
+// the mapped pinned slot, writes it into the history and derives its table;
+// without a table of that form, a copy and then the derivation.
+int derive_staged(nufi_handle *h, int64_t n, int slot)
+{
+    const Problem &p = h->p;
+    double *dst = h->hist + n * p.hist_stride;
+    cudaError_t e;
+    if (h->tables) {
+        e = launch_derive_table(p, h->stage_dev[slot], h->tables + n * p.table_stride, h->stream, dst);
+    } else if (h->tables64 && p.dim == 1) {
+        e = launch_derive_table64(p, h->stage_dev[slot], h->tables64 + n * fp64_table_stride(p), h->stream, dst);
+    } else {
+        e = launch_copy_words(h->stage_dev[slot], dst, p.stride_t, nullptr, nullptr, h->stream);
+        if (e == cudaSuccess && h->tables64) {
+            h->launches += 1;
+            e = launch_derive_table64(p, dst, h->tables64 + n * fp64_table_stride(p), h->stream);
+        }
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "slab upload launch");
+    h->launches += 1;
+    NUFI_CUDA(h, cudaEventRecord(h->stage_done[slot], h->stream));
+    return NUFI_OK;
+}
+
+// Derive a slab upload_phi left pending (before any work that reads the
+// history or the tables).
+int flush_upload(nufi_handle *h)
+{
+    if (h->pending_k < 0) return NUFI_OK;
+    const long long k = h->pending_k;
+    h->pending_k = -1;
+    DeviceGuard g(h->device);
+    return derive_staged(h, k, h->pending_slot);
+}
+
+// The 1D split handles with the staged trace leave the newest upload
+// pending: the next compute_rho(n + 1) derives it inside its trace (one
+// launch fewer per step of the reference drivers' loop).
+bool upload_can_wait(const nufi_handle *h)
+{
+    return h->p.dim == 1 && h->p.precision == NUFI_PREC_FP32_SPLIT && h->staged.ok && h->step_fix_scale > 0 &&
+           h->tables;
+}
+
 // Enqueue the trace of step n over [qb, qe) and the reduction into h->rho
 // (with `publish`, also into the pinned block with the error word).
 int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int mode, bool publish = false)
@@ -754,6 +824,10 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
     const Problem &p = h->p;
     cudaError_t e;
     int rows = 0;
+    if (!h->staged.ok || p.dim != 1 || p.precision != NUFI_PREC_FP32_SPLIT) {
+        const int st = flush_upload(h);
+        if (st) return st;
+    }
     if (p.precision == NUFI_PREC_FP64 && h->fp64_table && mode == 0)
         e = launch_trace_fp64_table(p, h->shape, h->tables64, h->hist, int(n), qb, qe, h->partial, &rows, h->err,
                                     h->stream);
@@ -763,6 +837,17 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
         e = launch_trace_split_nd(p, h->staged, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows,
                                   h->err, h->stream);
     else if (h->staged.ok) {
+        PendingSlab pend;
+        const int pslot = h->pending_slot;
+        if (publish && h->pending_k >= 0 && h->pending_k == n - 1) {  // the trace derives the newest slab itself
+            pend.stage = h->stage_dev[pslot];
+            pend.k = h->pending_k;
+            pend.hist_out = h->hist + pend.k * p.hist_stride;
+            pend.table_out = h->tables + pend.k * p.table_stride;
+        } else if (h->pending_k >= 0) {
+            const int st = flush_upload(h);
+            if (st) return st;
+        }
         RhoFix fx;
         if (h->step_fix_scale > 0) {
             fx.sum = h->step_fix;
@@ -778,7 +863,11 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
             }
         }
         e = launch_trace_split_staged(p, h->staged, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows,
-                                      h->err, h->stream, fx);
+                                      h->err, h->stream, fx, pend);
+        if (e == cudaSuccess && pend.k >= 0) {
+            h->pending_k = -1;  // derived and stored by the trace; its staging slot is free after it
+            NUFI_CUDA(h, cudaEventRecord(h->stage_done[pslot], h->stream));
+        }
     } else
         e = launch_trace_split(p, h->shape, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows, h->err,
                                h->stream);
@@ -816,20 +905,6 @@ int enqueue_step(nufi_handle *h, long long n)
     return NUFI_OK;
 }
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev)
-    {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard()
-    {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
 
 void release(nufi_handle *h)
 {
@@ -840,11 +915,13 @@ void release(nufi_handle *h)
     h->graphs.clear();
     for (void *p : h->allocations) cudaFree(p);
     h->allocations.clear();
-    if (h->stage_done) cudaEventSynchronize(h->stage_done);
-    if (h->stage) cudaFreeHost(h->stage);
-    if (h->stage_done) cudaEventDestroy(h->stage_done);
-    h->stage = nullptr;
-    h->stage_done = nullptr;
+    for (int s = 0; s < 2; ++s) {
+        if (h->stage_done[s]) cudaEventSynchronize(h->stage_done[s]);
+        if (h->stage[s]) cudaFreeHost(h->stage[s]);
+        if (h->stage_done[s]) cudaEventDestroy(h->stage_done[s]);
+        h->stage[s] = nullptr;
+        h->stage_done[s] = nullptr;
+    }
     if (h->pin) cudaFreeHost(h->pin);
     h->pin = nullptr;
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -1048,6 +1125,7 @@ int nufi_download_rho(nufi_handle *h, double *rho)
 int nufi_compute_metrics(nufi_handle *h, int64_t n, int64_t q_begin, int64_t q_end)
 {
     if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
     const PointGrid grid = h->mgrid_set ? h->mgrid : point_grid_of(h->p);
     if (q_begin < 0 || q_end < q_begin || q_end > grid.Ns * grid.Nm)
@@ -1142,47 +1220,38 @@ int nufi_download_rho_f32(nufi_handle *h, float *rho)
     return NUFI_OK;
 }
 
-// The slab goes through a pinned staging buffer, so the call returns as
-// soon as the caller's buffer has been read (as the reference's blocking
-// copy), and the transfer and table derivation stay ordered on the stream
-// before the next trace.  The staging buffer is reused after the previous
-// upload's copy has completed (event).
+// The slab goes through a pinned staging slot (two, in turn), so the call
+// returns as soon as the caller's buffer has been read (as the reference's
+// blocking copy), and the transfer and table derivation stay ordered on the
+// stream before the next trace.  A slot is reused after the launch that last
+// read it has completed (its event).
+//
 static int upload_slab(nufi_handle *h, int64_t n, const double *slab)
 {
     const Problem &p = h->p;
     DeviceGuard g(h->device);
+    int st = flush_upload(h);  // an older pending slab is derived now (from the other slot)
+    if (st) return st;
     const size_t bytes = size_t(p.stride_t) * sizeof(double);
-    if (!h->stage) {
-        NUFI_CUDA(h, cudaMallocHost(&h->stage, bytes));
+    const int slot = h->stage_next;
+    h->stage_next ^= 1;
+    if (!h->stage[slot]) {
+        NUFI_CUDA(h, cudaMallocHost(&h->stage[slot], bytes));
         void *dev = nullptr;
-        NUFI_CUDA(h, cudaHostGetDevicePointer(&dev, h->stage, 0));
-        h->stage_dev = static_cast<double *>(dev);
-        NUFI_CUDA(h, cudaEventCreateWithFlags(&h->stage_done, cudaEventDisableTiming));
+        NUFI_CUDA(h, cudaHostGetDevicePointer(&dev, h->stage[slot], 0));
+        h->stage_dev[slot] = static_cast<double *>(dev);
+        NUFI_CUDA(h, cudaEventCreateWithFlags(&h->stage_done[slot], cudaEventDisableTiming));
     } else {
-        NUFI_CUDA(h, cudaEventSynchronize(h->stage_done));
+        NUFI_CUDA(h, cudaEventSynchronize(h->stage_done[slot]));
     }
-    std::memcpy(h->stage, slab, bytes);
-    // One launch reads the staged slab from the mapped pinned buffer, writes
-    // it into the history and derives the slab's table from it; without a
-    // table of that form, a copy and then the derivation from the history.
-    double *dst = h->hist + n * p.hist_stride;
-    cudaError_t e;
-    if (h->tables) {
-        e = launch_derive_table(p, h->stage_dev, h->tables + n * p.table_stride, h->stream, dst);
-    } else if (h->tables64 && p.dim == 1) {
-        e = launch_derive_table64(p, h->stage_dev, h->tables64 + n * fp64_table_stride(p), h->stream, dst);
-    } else {
-        e = launch_copy_words(h->stage_dev, dst, p.stride_t, nullptr, nullptr, h->stream);
-        if (e == cudaSuccess && h->tables64) {
-            h->launches += 1;
-            e = launch_derive_table64(p, dst, h->tables64 + n * fp64_table_stride(p), h->stream);
-        }
-    }
-    if (e != cudaSuccess) return cuda_fail(h, e, "slab upload launch");
-    h->launches += 1;
-    NUFI_CUDA(h, cudaEventRecord(h->stage_done, h->stream));
+    std::memcpy(h->stage[slot], slab, bytes);
     h->slab_set[size_t(n)] = 1;
-    return NUFI_OK;
+    if (upload_can_wait(h)) {
+        h->pending_k = n;
+        h->pending_slot = slot;
+        return NUFI_OK;
+    }
+    return derive_staged(h, n, slot);
 }
 
 int nufi_upload_phi(nufi_handle *h, int64_t n, const double *coeffs_base)
@@ -1205,6 +1274,7 @@ int nufi_upload_phi_f32(nufi_handle *h, int64_t n, const float *coeffs_base)
 int nufi_step(nufi_handle *h, int64_t n, double *energy)
 {
     if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
     if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
     DeviceGuard g(h->device);
@@ -1221,6 +1291,7 @@ int nufi_step(nufi_handle *h, int64_t n, double *energy)
 int nufi_run(nufi_handle *h, int64_t n0, int64_t n1, double *energy_hist)
 {
     if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     if (n0 < 0 || n1 < n0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step range outside [0, Nt]");
     if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
     DeviceGuard g(h->device);
@@ -1280,6 +1351,7 @@ int nufi_run(nufi_handle *h, int64_t n0, int64_t n1, double *energy_hist)
 int nufi_download_history(nufi_handle *h, int64_t n0, int64_t n1, double *coeffs_base)
 {
     if (!h || !coeffs_base) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     if (n0 < 0 || n1 < n0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step range outside [0, Nt]");
     const Problem &p = h->p;
     DeviceGuard g(h->device);
@@ -1344,6 +1416,7 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
 int nufi_synchronize(nufi_handle *h)
 {
     if (!h) return fail(nullptr, NUFI_ERR_INVALID, "null handle");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     DeviceGuard g(h->device);
     return sync_and_check(h);
 }
@@ -1360,6 +1433,9 @@ int nufi_sizes(const nufi_handle *h, int64_t *stride_t, int64_t *n_spatial, int6
 int nufi_stream(const nufi_handle *h, void **stream)
 {
     if (!h || !stream) return fail(nullptr, NUFI_ERR_INVALID, "null argument");
+    // the caller's own work on the stream may read the history: a pending
+    // upload_phi is launched first (the handle's state, not its identity)
+    if (int fst = flush_upload(const_cast<nufi_handle *>(h))) return fst;
     *stream = static_cast<void *>(h->stream);
     return NUFI_OK;
 }
@@ -1374,6 +1450,7 @@ int nufi_launch_count(const nufi_handle *h, int64_t *count)
 int nufi_objective(nufi_handle *h, int64_t n1, double *J)
 {
     if (!h || !J) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     if (n1 < 0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step outside [0, Nt]");
     for (int64_t n = 0; n <= n1; ++n)
         if (!h->energy_set[size_t(n)])
@@ -1399,6 +1476,7 @@ int nufi_forward(nufi_handle *h, int64_t n1, double *J)
 int nufi_backward(nufi_handle *h, int64_t n1, double *grad)
 {
     if (!h || !grad) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     if (n1 < 0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step outside [0, Nt]");
     if (!h->aplan.ok)
         return fail(h, NUFI_ERR_UNSUPPORTED, "backward: built for 1D, orders 4 and 6 (odd-degree splines)");
@@ -1436,6 +1514,7 @@ int nufi_eval_points(nufi_handle *h, int64_t n, int mode, int64_t npts, const do
                      double *feet)
 {
     if (!h || (npts > 0 && !pts)) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     if (n < 0 || n > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "Time-step out of range.");
     if (mode < NUFI_EVAL_FTILDA || mode > NUFI_EVAL_PHASE_FLOW || (mode == NUFI_EVAL_PHASE_FLOW && h->p.dim != 1))
         return fail(h, NUFI_ERR_INVALID, "eval_points: mode (phase flow is 1D, as the reference's)");
@@ -1488,6 +1567,7 @@ int nufi_eval_points(nufi_handle *h, int64_t n, int mode, int64_t npts, const do
 int nufi_save_history(nufi_handle *h, int64_t n1, const char *path)
 {
     if (!h || !path) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     if (n1 < 0 || n1 > h->cfg.Nt) return fail(h, NUFI_ERR_RANGE, "step outside [0, Nt]");
     const Problem &p = h->p;
     std::vector<double> all(size_t(n1 + 1) * p.stride_t);
@@ -1512,6 +1592,7 @@ int nufi_save_history(nufi_handle *h, int64_t n1, const char *path)
 int nufi_load_history(nufi_handle *h, const char *path, int64_t *n_slabs)
 {
     if (!h || !path) return fail(h, NUFI_ERR_INVALID, "null argument");
+    if (int fst = flush_upload(h)) return fst;  // a pending upload_phi first
     const Problem &p = h->p;
     FILE *f = std::fopen(path, "r");
     if (!f) return fail(h, NUFI_ERR_INVALID, std::string("load_history: cannot open ") + path);

@@ -67,6 +67,18 @@ __device__ __forceinline__ void store_kick_entry(float *slab, int N, int i, floa
     reinterpret_cast<float2 *>(slab)[i] = make_float2(B, C);
     slab[2 * N + i] = A;
 }
+// K (A, B, C) of cell i from c[i..i+3]: the derivative of the cubic
+// B-spline sum on [i, i+1) as a quadratic in xi, times K = -dt^2/dx^2 (the
+// derive_table kernel, and the staged trace when it derives the newest
+// table itself).
+__device__ __forceinline__ void cubic_kick_poly(double c0, double c1, double c2, double c3, double K, float *slab,
+                                                int N, int i)
+{
+    const double A = (c2 - c0) * 0.5;
+    const double B = (c0 - 2.0 * c1) + c2;
+    const double C = ((3.0 * (c1 - c2) - c0) + c3) * 0.5;
+    store_kick_entry(slab, N, i, float(K * A), float(K * B), float(K * C));
+}
 __device__ __forceinline__ float kick_lookup(const float *slab, int N, int i, float xi)
 {
     const float2 bc = reinterpret_cast<const float2 *>(slab)[i];
@@ -165,10 +177,20 @@ struct RhoFix {
 // per node, the f~ of `chains` chains: no node's sum leaves int64.  False
 // when F would be below 24 (then the partial rows).
 bool rho_fixed_point(const Problem &p, int ctas, int chains, double &scale, double &limit);
+// The newest slab of a staged 1D trace given as FP64 coefficients in mapped
+// host memory (an upload not yet derived): every CTA derives its kick table
+// into its own ring, and CTA 0 also writes the slab and the table into the
+// history.  k = the slab (n - 1 of the trace), -1: none.
+struct PendingSlab {
+    const double *stage = nullptr;
+    long long k = -1;
+    double *hist_out = nullptr;
+    float *table_out = nullptr;
+};
 cudaError_t launch_trace_split_staged(const Problem &p, const StagedShape &sh, const float *tables,
                                       const SplitNode *nodes, const float2 *phase, int n, long long qb, long long qe,
                                       double *partial, int *rows, unsigned *err, cudaStream_t st,
-                                      const RhoFix &fx = RhoFix());
+                                      const RhoFix &fx = RhoFix(), const PendingSlab &pend = PendingSlab());
 
 // Whole FP32-split 1D simulation in one cooperative launch
 // (run_split_1d.cu): staged trace, rho, circulant solve and W_n per step,

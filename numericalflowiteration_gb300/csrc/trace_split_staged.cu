@@ -42,7 +42,8 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
                                                                      const float2 *__restrict__ phase, int n,
                                                                      long long q_begin, long long q_end, int S,
                                                                      int Nr, double *__restrict__ partial,
-                                                                     const RhoFix fx, unsigned *err)
+                                                                     const RhoFix fx, const PendingSlab pend,
+                                                                     unsigned *err)
 {
     extern __shared__ __align__(128) float ring[];
     __shared__ __align__(8) unsigned long long full_bar[kRing];
@@ -85,18 +86,38 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
             mbar_fence_init();
         }
         __syncthreads();
-        // chunk j holds slabs k in [k_lo, k_hi], k_hi = n-1-j*S
+        // chunk j holds slabs k in [k_lo, k_hi], k_hi = n-1-j*S; with a
+        // pending newest slab (n - 1), chunk 0 copies only [k_lo, n-2] and
+        // the CTA derives slab n - 1's table in place
+        const bool fuse = pend.k >= 0 && pend.k == n - 1;
         auto issue = [&](int j) {
             const int k_hi = n - 1 - j * S;
             const int k_lo = max(0, k_hi - S + 1);
-            const unsigned bytes = unsigned(k_hi - k_lo + 1) * slab_bytes;
+            const int k_top = (fuse && j == 0) ? k_hi - 1 : k_hi;
+            const unsigned bytes = unsigned(k_top - k_lo + 1) * slab_bytes;
             const unsigned bar = smem_addr(&full_bar[j % kRing]);
-            mbar_expect_tx(bar, bytes);
-            bulk_g2s(smem_addr(ring + (j % kRing) * S * TS), tables + (long long)k_lo * p.table_stride, bytes,
-                     bar);
+            mbar_expect_tx(bar, bytes);  // 0 bytes: the arrival alone completes the phase
+            if (bytes > 0)
+                bulk_g2s(smem_addr(ring + (j % kRing) * S * TS), tables + (long long)k_lo * p.table_stride, bytes,
+                         bar);
         };
         if (threadIdx.x == 0)
             for (int j = 0; j < kRing && j < nchunks; ++j) issue(j);
+        if (fuse) {
+            // the table of slab n - 1 from its FP64 coefficients (mapped host
+            // memory), as derive_table_kernel computes it
+            float *newest = ring + (n - 1 - max(0, n - S)) * TS;  // chunk 0, slot 0
+            const double K = -p.dt * p.dt * p.dxinv[0] * p.dxinv[0];
+            for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                const double c0 = pend.stage[i], c1 = pend.stage[i + 1], c2 = pend.stage[i + 2],
+                             c3 = pend.stage[i + 3];
+                cubic_kick_poly(c0, c1, c2, c3, K, newest, N, i);
+                if (blockIdx.x == 0) cubic_kick_poly(c0, c1, c2, c3, K, pend.table_out, N, i);
+            }
+            if (blockIdx.x == 0)
+                for (long long i = threadIdx.x; i < p.stride_t; i += blockDim.x) pend.hist_out[i] = pend.stage[i];
+            __syncthreads();
+        }
         bool ok = true;
         for (int j = 0; j < nchunks; ++j) {
             const int slot = j % kRing;
@@ -170,28 +191,31 @@ namespace {
 template <int PPT, bool POW2, bool UNWRAP>
 cudaError_t launch_staged_form(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
                                const float2 *phase, int n, long long qb, long long qe, double *partial,
-                               const RhoFix &fx, unsigned *err, cudaStream_t st)
+                               const RhoFix &fx, const PendingSlab &pend, unsigned *err, cudaStream_t st)
 {
     static const cudaError_t attr = cudaFuncSetAttribute(trace_split_1d_staged_kernel<PPT, POW2, UNWRAP>,
                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (attr != cudaSuccess) return attr;
     trace_split_1d_staged_kernel<PPT, POW2, UNWRAP><<<dim3(sh.ctas), dim3(sh.threads), sh.smem, st>>>(
-        p, tables, nodes, phase, n, qb, qe, sh.slabs_per_chunk, sh.threads / sh.tpn, partial, fx, err);
+        p, tables, nodes, phase, n, qb, qe, sh.slabs_per_chunk, sh.threads / sh.tpn, partial, fx, pend, err);
     return cudaGetLastError();
 }
 
 template <int PPT>
 cudaError_t launch_staged_ppt(const Problem &p, const StagedShape &sh, const float *tables, const SplitNode *nodes,
                               const float2 *phase, int n, long long qb, long long qe, double *partial,
-                              const RhoFix &fx, unsigned *err, cudaStream_t st)
+                              const RhoFix &fx, const PendingSlab &pend, unsigned *err, cudaStream_t st)
 {
     const bool pow2 = (p.N[0] & (p.N[0] - 1)) == 0;
     if (phase_wraps(p)) {  // f0's phase at the unwrapped foot (admitted for N a power of two only)
         if (!pow2) return cudaErrorInvalidValue;
-        return launch_staged_form<PPT, true, true>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
+        return launch_staged_form<PPT, true, true>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, pend, err,
+                                                   st);
     }
-    if (pow2) return launch_staged_form<PPT, true, false>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
-    return launch_staged_form<PPT, false, false>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
+    if (pow2)
+        return launch_staged_form<PPT, true, false>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, pend, err,
+                                                    st);
+    return launch_staged_form<PPT, false, false>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, pend, err, st);
 }
 
 }  // namespace
@@ -236,12 +260,15 @@ StagedShape staged_shape_1d(const Problem &p, int sms, int cps, int tpn_opt)
 
 cudaError_t launch_trace_split_staged(const Problem &p, const StagedShape &sh, const float *tables,
                                       const SplitNode *nodes, const float2 *phase, int n, long long qb, long long qe,
-                                      double *partial, int *rows, unsigned *err, cudaStream_t st, const RhoFix &fx)
+                                      double *partial, int *rows, unsigned *err, cudaStream_t st, const RhoFix &fx,
+                                      const PendingSlab &pend)
 {
     *rows = fx.sum ? 0 : sh.ctas;  // no rows to reduce: the kernel writes rho itself
+    if (pend.k >= 0 && (pend.k != n - 1 || size_t(p.table_stride) * 4 * size_t(sh.slabs_per_chunk) == 0))
+        return cudaErrorInvalidValue;  // a pending slab is only the trace's newest
     switch (sh.ppt) {
 #define NUFI_CASE(K) \
-    case K: return launch_staged_ppt<K>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, err, st);
+    case K: return launch_staged_ppt<K>(p, sh, tables, nodes, phase, n, qb, qe, partial, fx, pend, err, st);
         NUFI_CASE(1) NUFI_CASE(2) NUFI_CASE(3) NUFI_CASE(4) NUFI_CASE(5) NUFI_CASE(6) NUFI_CASE(7) NUFI_CASE(8)
 #undef NUFI_CASE
     default: return cudaErrorInvalidValue;

@@ -282,6 +282,48 @@ def test_split_nd_phase_at_the_unwrapped_foot(nufi, oracle_mod, dim):
     assert rel_max(e, ref) <= 1e-6
 
 
+def test_dropin_pending_upload_is_applied_everywhere(nufi):
+    """upload_phi on a 1D split handle leaves the newest slab pending:
+    compute_rho(n + 1) derives its table inside the trace, every other call
+    applies it first.  The reference drivers' loop (compute_rho, download,
+    upload per step) gives the same rho and history bits as the same loop
+    with a synchronize after each upload (the table derived by its own
+    launch), and metrics and eval_points between an upload and the next
+    trace see the uploaded slab."""
+    from numericalflowiteration_gb300.config import two_stream_1d
+    cfg = two_stream_1d(Nx=64, Nv=256, Nt=40, precision="fp32split")
+    with nufi.Simulation(cfg.replace(precision="fp64")) as ref:
+        ref.run()
+        coeffs = ref.history()
+
+    def loop(sync_after_upload):
+        rhos = []
+        with nufi.Simulation(cfg) as sim:
+            for n in range(cfg.Nt + 1):
+                sim.compute_rho(n)
+                rhos.append(sim.download_rho(np.zeros(cfg.n_spatial)))
+                sim.upload_phi(n, coeffs)
+                if sync_after_upload:
+                    sim.synchronize()
+            return np.array(rhos), sim.history()
+
+    ra, ha = loop(False)
+    rb, hb = loop(True)
+    assert np.array_equal(ra, rb) and np.array_equal(ha, hb)
+    assert np.array_equal(ha, coeffs)
+    # a pending slab read by the metrics (FP64 eval_f on the history) and by
+    # eval_points before any trace has derived it
+    with nufi.Simulation(cfg) as sim, nufi.Simulation(cfg.replace(precision="fp64")) as ref:
+        for n in range(6):
+            sim.upload_phi(n, coeffs)
+            ref.upload_phi(n, coeffs)
+        sim.compute_metrics(5)
+        ref.compute_metrics(5)
+        assert np.array_equal(sim.download_metrics(), ref.download_metrics())
+        pts = np.array([[1.0, 0.5], [7.0, -1.2], [3.3, 2.0]])
+        assert np.array_equal(sim.eval_points(5, pts), ref.eval_points(5, pts))
+
+
 def test_persistent_run_subrange_and_repeat(nufi):
     """Steps in two calls (0..k, k+1..Nt) and a repeated run give the same
     history as one call."""

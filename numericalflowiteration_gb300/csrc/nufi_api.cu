@@ -431,7 +431,7 @@ void plan_traces(const Problem &p, int sms, const nufi_options &opt, LaunchShape
 }
 
 // Shape of the field solve (its node limit and grid), with no CUDA call.
-bool solve_geometry(const Problem &p, int sms, SolvePlan &pl, std::string &why)
+bool solve_geometry(const Problem &p, SolvePlan &pl, std::string &why)
 {
     if (p.Ns > kCirculantMaxNodes) {
         // the spectral form: per-axis DFTs, one line per block in shared memory
@@ -456,7 +456,6 @@ bool solve_geometry(const Problem &p, int sms, SolvePlan &pl, std::string &why)
     // in the drop-in call), so fewer blocks read it fewer times, while more
     // nodes per block serialise more FP64 work on one SM.  The green kernels
     // are read from L2 (batched loads), not staged per block.
-    (void)sms;
     int npb = 8;
     while (npb > 1 && (p.Ns + npb - 1) / npb < 64) npb /= 2;
     pl.nodes_per_block = npb;
@@ -592,11 +591,11 @@ std::vector<double> solve_green(const Problem &p, int nconv)
     return green;
 }
 
-int build_solve_plan(nufi_handle *h, int sms)
+int build_solve_plan(nufi_handle *h)
 {
     const Problem &p = h->p;
     h->solve_ok = false;
-    if (!solve_geometry(p, sms, h->plan, h->solve_why)) return NUFI_OK;
+    if (!solve_geometry(p, h->plan, h->solve_why)) return NUFI_OK;
     SolvePlan &pl = h->plan;
     if (pl.spectral) {
         const std::vector<std::complex<long double>> D = solve_diagonals(p, 2);
@@ -624,8 +623,7 @@ int build_solve_plan(nufi_handle *h, int sms)
     }
     const std::vector<double> green = solve_green(p, h->plan.nconv);
     NUFI_CUDA(h, dalloc(h, &pl.green, green.size()));
-    // also holds one part per CTA of the persistent run kernel
-    NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(std::max(pl.blocks, kMaxCtasPerSm * sms))));
+    NUFI_CUDA(h, dalloc(h, &pl.energy_partial, size_t(pl.blocks)));
     NUFI_CUDA(h, dalloc(h, &pl.energy_counter, 1));
     NUFI_CUDA(h, cudaMemcpy(pl.green, green.data(), green.size() * sizeof(double), cudaMemcpyHostToDevice));
     NUFI_CUDA(h, cudaMemset(pl.energy_counter, 0, sizeof(unsigned)));
@@ -1048,7 +1046,7 @@ int create_handle(const nufi_config *cfg, const nufi_options *opt, int device, n
         (e = cudaMemset(h->metrics, 0, 4 * sizeof(double))) != cudaSuccess ||
         (e = cudaMemset(h->err, 0, sizeof(unsigned))) != cudaSuccess)
         return bail(cuda_fail(h.get(), e, "cudaMemset"));
-    if ((st = build_solve_plan(h.get(), sms > 0 ? sms : 1))) return bail(st);
+    if ((st = build_solve_plan(h.get()))) return bail(st);
     h->slab_set.assign(nslab, 0);
     h->energy_set.assign(nslab, 0);
     h->aplan = adjoint_plan_1d(p);
@@ -1298,8 +1296,8 @@ int nufi_run(nufi_handle *h, int64_t n0, int64_t n1, double *energy_hist)
     if (h->persist.ok) {
         // one cooperative launch for all steps (run_split_1d.cu)
         const Problem &p = h->p;
-        cudaError_t e = launch_run_split_1d(p, h->persist, h->plan, h->tables, h->hist, h->nodes, h->phase, h->partial,
-                                            h->rho, h->energy, int(n0), int(n1), h->err, h->stream);
+        cudaError_t e = launch_run_split_1d(p, h->persist, h->plan, h->tables, h->hist, h->nodes, h->phase, h->rho,
+                                            h->energy, int(n0), int(n1), h->err, h->stream);
         if (e == cudaSuccess) {
             h->launches += 1;
             mark_steps(h, n0, n1, true);
@@ -1741,7 +1739,7 @@ int nufi_plan_ex(const nufi_config *cfg, const nufi_options *opt, int sms, char 
     if (h.p.dim == 1 && phase_wraps(h.p) && !h.staged.ok)
         return fail(nullptr, NUFI_ERR_UNSUPPORTED,
                     "nufi_plan: k (x_max - x_min) not a multiple of 2 pi needs the staged FP32-split trace");
-    h.solve_ok = solve_geometry(h.p, sms, h.plan, h.solve_why);
+    h.solve_ok = solve_geometry(h.p, h.plan, h.solve_why);
     h.persist = plan_persistent(h.p, h.staged, h.plan, h.solve_ok, sms, h.opt);
     h.aplan = adjoint_plan_1d(h.p);
     return copy_out(plan_json(&h, true), buf, len, "nufi_plan");
@@ -1754,7 +1752,7 @@ int nufi_solve_kernels(const nufi_config *cfg, double *kernels, int64_t len, int
     if (st) return fail(nullptr, st, "nufi_solve_kernels: " + why);
     const Problem p = make_problem(*cfg);
     SolvePlan geom;
-    if (!solve_geometry(p, 1, geom, why)) return fail(nullptr, NUFI_ERR_UNSUPPORTED, "nufi_solve_kernels: " + why);
+    if (!solve_geometry(p, geom, why)) return fail(nullptr, NUFI_ERR_UNSUPPORTED, "nufi_solve_kernels: " + why);
     if (nconv) *nconv = geom.nconv;
     if (!kernels) return NUFI_OK;  // size query
     if (len < geom.nconv * p.Ns)

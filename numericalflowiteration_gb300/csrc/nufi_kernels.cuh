@@ -260,8 +260,7 @@ cudaError_t field_solve_prepare(const SolvePlan &plan);
 
 PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const SolvePlan &plan, int sms);
 cudaError_t launch_run_split_1d(const Problem &p, const PersistentRun &pr, const SolvePlan &plan, float *tables,
-                                double *hist, const SplitNode *nodes, const float2 *phase, double *partial,
-                                double *rho, double *energy, int n0, int n1, unsigned *err, cudaStream_t st);
+                                double *hist, const SplitNode *nodes, const float2 *phase, double *rho, double *energy, int n0, int n1, unsigned *err, cudaStream_t st);
 // Reverse-mode gradient of J = 2 dt sum_n W_n with respect to f0's
 // (alpha, k, u_b, sigma_b), 1D, FP64 (adjoint_1d.cu).  mu: (Nt+1) x P
 // slab adjoints (zeroed by the caller), theta_acc: [4][grid_x*grid_y]

@@ -350,8 +350,7 @@ PersistentRun persistent_shape_1d(const Problem &p, const StagedShape &sh, const
     if (sh.ppt > 4 && sh.threads > 256) return pr;  // launch bounds of the PPT > 4 instances
     const int W = sh.threads / 32;
     const int K = (p.N[0] + sh.ctas - 1) / sh.ctas;  // nodes per CTA in the solve
-    // at most two CTAs per SM (cooperative launch: all co-resident), and
-    // energy_partial holds one part per CTA up to kMaxCtasPerSm * sms
+    // at most two CTAs per SM (cooperative launch: all co-resident)
     if (K > W || sh.ctas > kMaxCtasPerSm * sms) return pr;
     pr.ctas = sh.ctas;
     pr.threads = sh.threads;
@@ -390,10 +389,9 @@ bool rho_fixed_point(const Problem &p, int ctas, int chains, double &scale, doub
 }
 
 cudaError_t launch_run_split_1d(const Problem &p, const PersistentRun &pr, const SolvePlan &plan, float *tables,
-                                double *hist, const SplitNode *nodes, const float2 *phase, double *partial,
-                                double *rho, double *energy, int n0, int n1, unsigned *err, cudaStream_t st)
+                                double *hist, const SplitNode *nodes, const float2 *phase, double *rho,
+                                double *energy, int n0, int n1, unsigned *err, cudaStream_t st)
 {
-    (void)partial;  // rho is summed in the kernel's fixed-point integers
     switch (pr.ppt) {
 #define NUFI_CASE(K) \
     case K: return launch_run_ppt<K>(p, pr, plan, tables, hist, nodes, phase, rho, energy, n0, n1, err, st);

@@ -394,9 +394,10 @@ __device__ __forceinline__ void trace_chunk(const float *__restrict__ chunk, int
         }
     };
     const int k_stop = max(k_lo, 1);
-    // UNROLL substeps per loop trip: the 1D traces take 2 (the loop's own
-    // work is shared and the second substep's address arithmetic overlaps
-    // the first: 62.9 -> 60.7 ms on the whole two-stream run)
+    // UNROLL substeps per loop trip: the whole-run and batch traces take 2
+    // (the loop's own work is shared and the second substep's address
+    // arithmetic overlaps the first: 62.9 -> 60.7 ms on the whole two-stream
+    // run); the per-step staged trace measured faster with 1
 #pragma unroll UNROLL
     for (int k = k_hi; k >= k_stop; --k) substep(chunk + (k - k_lo) * TS, 1.0f);
     if (k_lo == 0) substep(chunk, 0.5f);

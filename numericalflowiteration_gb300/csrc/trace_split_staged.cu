@@ -5,11 +5,10 @@
 // slabs), so with plain global loads nearly every warp's table load of a
 // substep pays an L2 round trip (compulsory L1 misses, the long-scoreboard
 // stall of the first form).  Here each CTA streams the history through a
-// ring of R shared-memory slots, S slabs per slot: cp.async.bulk (global
-// -> shared, completion counted on an mbarrier) R chunks ahead, the first R
-// issued by thread 0 and each later one by the last warp to release its
-// slot, so the loads on the critical path of a substep are shared-memory
-// reads of a table already on chip and no warp waits for another.
+// ring of R shared-memory slots, S slabs per slot: one elected thread
+// issues cp.async.bulk (global -> shared, completion counted on an
+// mbarrier) R chunks ahead, so the loads on the critical path of a substep
+// are 16-byte shared-memory reads of a table already on chip.
 //
 // Geometry: a persistent grid of about one CTA per SM.  Each thread owns
 // one spatial node (x-lanes, so the 32 lanes of a warp read neighbouring
@@ -50,7 +49,6 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
     __shared__ __align__(8) unsigned long long full_bar[kRing];
     __shared__ double combine[256];
     __shared__ bool last;
-    __shared__ unsigned released[kRing];  // warps done with the slot's chunk
 
     const int N = p.N[0];
     const int s = threadIdx.x % Nr;    // spatial node
@@ -84,10 +82,7 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
         const int nchunks = (n + S - 1) / S;
         const unsigned slab_bytes = unsigned(p.table_stride) * 4u;
         if (threadIdx.x == 0) {
-            for (int r = 0; r < kRing; ++r) {
-                mbar_init(smem_addr(&full_bar[r]), 1);
-                released[r] = 0;
-            }
+            for (int r = 0; r < kRing; ++r) mbar_init(smem_addr(&full_bar[r]), 1);
             mbar_fence_init();
         }
         __syncthreads();
@@ -123,10 +118,6 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
                 for (long long i = threadIdx.x; i < p.stride_t; i += blockDim.x) pend.hist_out[i] = pend.stage[i];
             __syncthreads();
         }
-        // A slot is refilled by the last warp to release it (a count per slot
-        // in shared memory, acquire-release), as in run_split_1d.cu: no warp
-        // waits for another, only for its data.
-        const unsigned W = blockDim.x >> 5;
         bool ok = true;
         for (int j = 0; j < nchunks; ++j) {
             const int slot = j % kRing;
@@ -134,13 +125,13 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
             const float *__restrict__ chunk = ring + slot * S * TS;
             const int k_hi = n - 1 - j * S;
             const int k_lo = max(0, k_hi - S + 1);
-            trace_chunk<PPT, POW2, UNWRAP, 2>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err, &Wr, log2n);
-            __syncwarp();
-            if ((threadIdx.x & 31) == 0 && atom_add_acq_rel_cta(&released[slot], 1u) == W - 1) {
-                released[slot] = 0;
-                fence_proxy_async_shared();  // the warps' reads (and a derived table) before the copy's writes
-                if (j + kRing < nchunks) issue(j + kRing);
-            }
+            trace_chunk<PPT, POW2, UNWRAP>(chunk, TS, k_hi, k_lo, N, I, xi, dwT, dwTc, shi, S0m, err, &Wr, log2n);
+            // everyone is done with this slot.  A CTA barrier here, not the
+            // whole-run kernel's per-slot release counts: one launch per step
+            // (the drop-in loop) measured 2.5 ms faster over the two-stream run
+            // this way, and one substep per loop trip faster than two
+            __syncthreads();
+            if (threadIdx.x == 0 && j + kRing < nchunks) issue(j + kRing);
         }
         if (!ok) atomicOr(err, kErrStageTimeout);
     }

@@ -131,7 +131,10 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
             // (the drop-in loop) measured 2.5 ms faster over the two-stream run
             // this way, and one substep per loop trip faster than two
             __syncthreads();
-            if (threadIdx.x == 0 && j + kRing < nchunks) issue(j + kRing);
+            if (threadIdx.x == 0 && j + kRing < nchunks) {
+                if (fuse && j == 0) fence_proxy_async_shared();  // the derived table's stores before the copy's
+                issue(j + kRing);
+            }
         }
         if (!ok) atomicOr(err, kErrStageTimeout);
     }

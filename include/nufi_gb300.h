@@ -218,7 +218,15 @@ int nufi_download_energy(nufi_handle *h, int64_t n0, int64_t n1, double *energy)
 /* Replaces poisson<double>::solve + dimN::interpolate<double,order>
  * (nufi/poisson.cpp:66-89, 190-219, 328-362; nufi/fields.hpp:63-142,
  * 186-300, 352-490) on host buffers: rho (N values, x fastest) in,
- * padded slab (stride_t values) out, returns W in *energy.  Blocks. */
+ * padded slab (stride_t values) out, returns W in *energy.  Blocks.
+ * When rho is, bit for bit, the rho the last nufi_compute_rho published
+ * (a zeroed buffer filled by nufi_download_rho) on a handle whose 1D split
+ * trace sums rho itself, the call enables a speculative solve: the
+ * following nufi_compute_rho calls also queue the device solve of their own
+ * rho behind the trace, and a nufi_field_solve given that same rho returns
+ * those results without a launch of its own (identical values: the same
+ * kernel on the same input).  Any other input, or a compute_rho whose solve
+ * went unused, switches the speculation off again. */
 int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double *energy);
 
 /* ---- phase-space sampling and the history on disk ----------------------- */

@@ -100,6 +100,15 @@ struct nufi_handle {
     // wrote rho and the error word into the pinned block: while no launch
     // has followed, download_rho only synchronises
     long long rho_pub_at = -1;
+    // Speculative field solve: while callers pass nufi_field_solve the rho
+    // that the last compute_rho published, compute_rho queues the circulant
+    // solve of the device rho behind its trace (results into the pinned
+    // block, sequence spec_seq) and field_solve returns them when its input
+    // matches that rho bit for bit.  spec_at: `launches` right after that
+    // solve (-1: none outstanding).
+    bool spec_solve = false;
+    unsigned spec_seq = 0;
+    long long spec_at = -1;
     std::vector<char> energy_set; // W_n recorded (step, run)
     SolvePlan plan;
     bool solve_ok = false;
@@ -737,17 +746,20 @@ unsigned next_seq(nufi_handle *h)
     return h->seq;
 }
 
-// Wait for the completion word to read `seq`: the results and the error
-// word the kernel wrote before it are then visible here.  About 2.4 us
-// sooner than the stream's synchronisation after a short kernel on this
-// hardware (the kernel's exit and the stream's completion signal are not
-// waited for).  Past 1 ms of polling, the stream's synchronisation instead
-// (a long kernel, or one that failed and will never write the word).
+// Wait for the completion word to reach `seq`: the results and the error
+// word the kernel wrote before it are then visible here.  Kernels write
+// the word in stream order with increasing numbers, so a later one may
+// already have overwritten it (a signed difference >= 0 counts).  About
+// 2.4 us sooner than the stream's synchronisation after a short kernel on
+// this hardware (the kernel's exit and the stream's completion signal are
+// not waited for).  Past 1 ms of polling, the stream's synchronisation
+// instead (a long kernel, or one that failed and will never write the word).
 int wait_published(nufi_handle *h, unsigned seq)
 {
     const auto t0 = std::chrono::steady_clock::now();
     for (unsigned it = 0;; ++it) {
-        if (__atomic_load_n(h->pin_seq, __ATOMIC_ACQUIRE) == seq) return device_flags_status(h, *h->pin_err);
+        if (int(__atomic_load_n(h->pin_seq, __ATOMIC_ACQUIRE) - seq) >= 0)
+            return device_flags_status(h, *h->pin_err);
         if ((it & 255u) == 255u && std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(1)) break;
     }
     return sync_published(h);
@@ -879,8 +891,20 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
         h->launches += 1;
     }
     if (publish) {
-        h->rho_pub_at = h->launches;
         h->rho_seq = rows == 0 ? h->seq : 0u;  // the trace itself wrote rho, the word and seq
+        if (h->spec_at >= 0) h->spec_solve = false;  // the last speculative solve went unused
+        h->spec_at = -1;
+        if (rows == 0 && h->spec_solve && h->solve_ok && !h->plan.spectral) {
+            // reads the device rho, writes only the pinned block: rho stays published
+            const unsigned s = next_seq(h);
+            e = launch_field_solve(p, h->plan, h->rho, h->pin_slab_dev, nullptr, h->pin_slab_dev + p.hist_stride,
+                                   h->stream, h->err, h->pin_err_dev, h->pin_seq_dev, s);
+            if (e != cudaSuccess) return cuda_fail(h, e, "field solve launch");
+            h->launches += 1;
+            h->spec_seq = s;
+            h->spec_at = h->launches;
+        }
+        h->rho_pub_at = h->launches;
     }
     return NUFI_OK;
 }
@@ -1376,6 +1400,21 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
     if (!h->solve_ok) return fail(h, NUFI_ERR_UNSUPPORTED, h->solve_why);
     const Problem &p = h->p;
     DeviceGuard g(h->device);
+    const size_t rho_bytes = size_t(p.Ns) * sizeof(double);
+    if (h->spec_at >= 0) {
+        const bool current = h->spec_at == h->launches;  // nothing launched since the speculative solve
+        h->spec_at = -1;
+        if (current) {
+            int st = wait_published(h, h->spec_seq);  // the trace's rho and the solve's results
+            if (st) return st;
+            if (std::memcmp(rho, h->pin_rho, rho_bytes) == 0) {  // the same input: the same results
+                std::memcpy(slab_out, h->pin_slab, size_t(p.stride_t) * sizeof(double));
+                if (energy) *energy = h->pin_slab[p.hist_stride];
+                return NUFI_OK;
+            }
+        }
+        h->spec_solve = false;
+    }
     // Every call leaves with its copies complete (synchronised, also on
     // failure), so the pinned input is free to overwrite here.
     // The solve reads rho straight from the mapped pinned block; the
@@ -1408,6 +1447,10 @@ int nufi_field_solve(nufi_handle *h, const double *rho, double *slab_out, double
     if (st) return st;
     std::memcpy(slab_out, h->pin_slab, size_t(p.stride_t) * sizeof(double));
     if (energy) *energy = h->pin_slab[p.hist_stride];
+    // the input was the rho the last compute_rho published (its trace is
+    // complete here): speculate from the next compute_rho on
+    if (seq && h->rho_seq && h->rho_pub_at >= 0 && std::memcmp(h->pin_rho_in, h->pin_rho, rho_bytes) == 0)
+        h->spec_solve = true;
     return NUFI_OK;
 }
 

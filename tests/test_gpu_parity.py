@@ -324,6 +324,50 @@ def test_dropin_pending_upload_is_applied_everywhere(nufi):
         assert np.array_equal(sim.eval_points(5, pts), ref.eval_points(5, pts))
 
 
+def test_dropin_speculative_field_solve(nufi):
+    """The reference drivers' loop with the device field solve (compute_rho,
+    download, field_solve, upload per step): after the first step the
+    handle queues the solve of its own rho behind each trace and returns it
+    when field_solve's input is that rho.  Every rho, slab and energy is
+    bit-identical to the same loop solved on a second handle (which never
+    speculates); a different input at one step (the speculative result is
+    discarded), a second compute_rho before the solve (the speculation goes
+    unused) and the switch back on all keep the results exact."""
+    from numericalflowiteration_gb300.config import two_stream_1d
+    cfg = two_stream_1d(Nx=64, Nv=256, Nt=40, precision="fp32split")
+
+    def loop(own_solver):
+        rhos, energies, extra = [], [], []
+        with nufi.Simulation(cfg) as sim, nufi.Simulation(cfg) as other:
+            solver = sim if own_solver else other
+            coeffs = np.zeros((cfg.Nt + 1) * sim.stride_t)
+            for n in range(cfg.Nt + 1):
+                if n == 25:  # a trace whose rho nobody solves
+                    sim.compute_rho(n)
+                    sim.download_rho(np.zeros(cfg.n_spatial))
+                sim.compute_rho(n)
+                rho = sim.download_rho(np.zeros(cfg.n_spatial))
+                if n == 12:  # another input first, then the step's own
+                    extra.append(solver.field_solve(rho * 1.01))
+                slab, e = solver.field_solve(rho)
+                coeffs[n * sim.stride_t:(n + 1) * sim.stride_t] = slab
+                sim.upload_phi(n, coeffs)
+                rhos.append(rho)
+                energies.append(e)
+            return np.array(rhos), np.array(energies), coeffs, extra
+
+    ra, ea, ca, xa = loop(True)
+    rb, eb, cb, xb = loop(False)
+    assert np.array_equal(ra, rb)
+    assert np.array_equal(ea, eb)
+    assert np.array_equal(ca, cb)
+    assert np.array_equal(xa[0][0], xb[0][0]) and xa[0][1] == xb[0][1]
+    # the loop is the simulation: its energies against the whole-run kernel's
+    with nufi.Simulation(cfg) as sim:
+        er = sim.run()
+    assert rel_max(ea, er) <= 1e-6
+
+
 def test_persistent_run_subrange_and_repeat(nufi):
     """Steps in two calls (0..k, k+1..Nt) and a repeated run give the same
     history as one call."""

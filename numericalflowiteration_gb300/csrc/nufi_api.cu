@@ -76,6 +76,9 @@ struct nufi_handle {
     double *stage[2] = {nullptr, nullptr};
     double *stage_dev[2] = {nullptr, nullptr};
     cudaEvent_t stage_done[2] = {nullptr, nullptr};
+    // the completion number of the publishing trace that last read each slot
+    // (0: another launch read it, wait for its event instead)
+    unsigned stage_seq[2] = {0u, 0u};
     int stage_next = 0;
     // 1D split (staged trace): the slab upload_phi staged but has not derived
     // yet (-1: none).  compute_rho(pending_k + 1) derives it inside its trace;
@@ -804,6 +807,7 @@ int derive_staged(nufi_handle *h, int64_t n, int slot)
     if (e != cudaSuccess) return cuda_fail(h, e, "slab upload launch");
     h->launches += 1;
     NUFI_CUDA(h, cudaEventRecord(h->stage_done[slot], h->stream));
+    h->stage_seq[slot] = 0u;
     return NUFI_OK;
 }
 
@@ -877,6 +881,7 @@ int enqueue_trace(nufi_handle *h, long long n, long long qb, long long qe, int m
         if (e == cudaSuccess && pend.k >= 0) {
             h->pending_k = -1;  // derived and stored by the trace; its staging slot is free after it
             NUFI_CUDA(h, cudaEventRecord(h->stage_done[pslot], h->stream));
+            h->stage_seq[pslot] = fx.seq;  // every CTA read the slot before the last one wrote seq
         }
     } else
         e = launch_trace_split(p, h->shape, h->tables, h->nodes, h->phase, int(n), qb, qe, h->partial, &rows, h->err,
@@ -1263,7 +1268,10 @@ static int upload_slab(nufi_handle *h, int64_t n, const double *slab)
         NUFI_CUDA(h, cudaHostGetDevicePointer(&dev, h->stage[slot], 0));
         h->stage_dev[slot] = static_cast<double *>(dev);
         NUFI_CUDA(h, cudaEventCreateWithFlags(&h->stage_done[slot], cudaEventDisableTiming));
-    } else {
+    } else if (!h->stage_seq[slot] || int(__atomic_load_n(h->pin_seq, __ATOMIC_ACQUIRE) - h->stage_seq[slot]) < 0) {
+        // the slot's reader has not been seen to finish through the
+        // completion word (a read of the pinned word; the event's
+        // synchronisation costs ~2 us even when it has completed)
         NUFI_CUDA(h, cudaEventSynchronize(h->stage_done[slot]));
     }
     std::memcpy(h->stage[slot], slab, bytes);

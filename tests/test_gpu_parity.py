@@ -332,12 +332,14 @@ def test_dropin_speculative_field_solve(nufi):
     bit-identical to the same loop solved on a second handle (which never
     speculates); a different input at one step (the speculative result is
     discarded), a second compute_rho before the solve (the speculation goes
-    unused) and the switch back on all keep the results exact."""
+    unused) and the switch back on all keep the results exact.  While it
+    speculates, each compute_rho is two launches (the trace, the solve);
+    the solving handle's compute_rho stays one."""
     from numericalflowiteration_gb300.config import two_stream_1d
     cfg = two_stream_1d(Nx=64, Nv=256, Nt=40, precision="fp32split")
 
     def loop(own_solver):
-        rhos, energies, extra = [], [], []
+        rhos, energies, extra, per_call = [], [], [], []
         with nufi.Simulation(cfg) as sim, nufi.Simulation(cfg) as other:
             solver = sim if own_solver else other
             coeffs = np.zeros((cfg.Nt + 1) * sim.stride_t)
@@ -345,7 +347,9 @@ def test_dropin_speculative_field_solve(nufi):
                 if n == 25:  # a trace whose rho nobody solves
                     sim.compute_rho(n)
                     sim.download_rho(np.zeros(cfg.n_spatial))
+                l0 = sim.launches
                 sim.compute_rho(n)
+                per_call.append(sim.launches - l0)
                 rho = sim.download_rho(np.zeros(cfg.n_spatial))
                 if n == 12:  # another input first, then the step's own
                     extra.append(solver.field_solve(rho * 1.01))
@@ -354,10 +358,11 @@ def test_dropin_speculative_field_solve(nufi):
                 sim.upload_phi(n, coeffs)
                 rhos.append(rho)
                 energies.append(e)
-            return np.array(rhos), np.array(energies), coeffs, extra
+            return np.array(rhos), np.array(energies), coeffs, extra, per_call
 
-    ra, ea, ca, xa = loop(True)
-    rb, eb, cb, xb = loop(False)
+    ra, ea, ca, xa, la = loop(True)
+    rb, eb, cb, xb, lb = loop(False)
+    assert la[30:40] == [2] * 10 and lb[30:40] == [1] * 10
     assert np.array_equal(ra, rb)
     assert np.array_equal(ea, eb)
     assert np.array_equal(ca, cb)

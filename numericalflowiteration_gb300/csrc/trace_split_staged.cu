@@ -172,6 +172,9 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
     __syncthreads();
     if (!last) return;
     __threadfence();
+    // the error word as the trace leaves it (every CTA's atomics are
+    // performed in L2 before its ticket), loaded beside the sums
+    const unsigned ew = (fx.err_pub && threadIdx.x == 0) ? __ldcg(err) : 0u;
     const double to_rho = -p.wv / fx.scale;
     for (int j = threadIdx.x; j < N; j += blockDim.x) {
         const double r = double((long long)__ldcg(fx.sum + j)) * to_rho;
@@ -179,17 +182,14 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
         if (fx.pub) fx.pub[j] = r;
         fx.sum[j] = 0ull;
     }
-    if (fx.seq_pub) {
-        __threadfence_system();
-        __syncthreads();
-    }
     if (threadIdx.x == 0) {
         *fx.ticket = 0u;
-        if (fx.err_pub) *fx.err_pub = atomicOr(err, 0u);
-        if (fx.seq_pub) {  // after rho and the word: a host that sees seq sees them
-            __threadfence_system();
-            *reinterpret_cast<volatile unsigned *>(fx.seq_pub) = fx.seq;
-        }
+        if (fx.err_pub) *fx.err_pub = ew;
+    }
+    if (fx.seq_pub) {  // every thread's rho and the word, a system fence each, then seq
+        __threadfence_system();
+        __syncthreads();
+        if (threadIdx.x == 0) *reinterpret_cast<volatile unsigned *>(fx.seq_pub) = fx.seq;
     }
 }
 

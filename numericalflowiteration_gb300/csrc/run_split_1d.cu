@@ -34,6 +34,14 @@ namespace nufi_gb300 {
 
 using namespace split;
 
+// Which of the five solve sums lane `lane` holds after the butterfly in
+// the solve phase (lanes 4q..4q+3 share one; -1: none).
+__device__ __forceinline__ int lane_sum_of(int lane)
+{
+    const int q = lane >> 2;
+    return q < 3 ? q : (q == 4 || q == 5) ? q - 1 : -1;
+}
+
 template <int PPT, bool POW2, bool UNWRAP>
 __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
     const Problem p, float *__restrict__ tables, double *__restrict__ hist, const SplitNode *__restrict__ nodes,
@@ -255,7 +263,9 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
             }
         }
         __syncthreads();
-        const int slotn = warp / wpn, pw = warp % wpn;
+        // node slot warp % Kp, part warp / Kp: the slots' part-0 warps (which
+        // finish the nodes) sit on different SM sub-partitions
+        const int slotn = warp % Kp, pw = warp / Kp;
         double a[5] = {0, 0, 0, 0, 0};
         if (slotn < K) {
             const int node = int(blockIdx.x) + slotn * G;
@@ -269,26 +279,47 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
                 for (int c = 0; c < 5; ++c) a[c] = fma(gs[c * N + m], r, a[c]);
             }
         }
-#pragma unroll
-        for (int c = 0; c < 5; ++c)
-            for (int off = 16; off > 0; off >>= 1) a[c] += __shfl_down_sync(0xffffffffu, a[c], off);
-        if (lane == 0)
-#pragma unroll
-            for (int c = 0; c < 5; ++c) wacc[warp][c] = a[c];
+        // the five lane sums by a reduce-scatter butterfly (8 FP64 adds per
+        // warp instead of five shuffle trees' 25; FP64 issues at 1/64 of
+        // the FP32 rate): after it, lanes 4c' hold sum c of lane_sum_of
+        const int c_of_lane = lane_sum_of(lane);
+        {
+            const bool hi16 = lane & 16, hi8 = lane & 8, hi4 = lane & 4;
+            // xor 16: the lower half keeps sums 0..2, the upper half 3, 4
+            const double k0 = hi16 ? a[3] : a[0], k1 = hi16 ? a[4] : a[1], k2 = hi16 ? 0.0 : a[2];
+            const double g0 = hi16 ? a[0] : a[3], g1 = hi16 ? a[1] : a[4], g2 = hi16 ? a[2] : 0.0;
+            const double b0 = k0 + __shfl_xor_sync(0xffffffffu, g0, 16);
+            const double b1 = k1 + __shfl_xor_sync(0xffffffffu, g1, 16);
+            const double b2 = k2 + __shfl_xor_sync(0xffffffffu, g2, 16);
+            // xor 8: slots 0, 1 or slot 2
+            const double d0 = (hi8 ? b2 : b0) + __shfl_xor_sync(0xffffffffu, hi8 ? b0 : b2, 8);
+            const double d1 = (hi8 ? 0.0 : b1) + __shfl_xor_sync(0xffffffffu, hi8 ? b1 : 0.0, 8);
+            // xor 4: one slot; then xor 2, xor 1 over the four lanes that share it
+            double e = (hi4 ? d1 : d0) + __shfl_xor_sync(0xffffffffu, hi4 ? d0 : d1, 4);
+            e += __shfl_xor_sync(0xffffffffu, e, 2);
+            e += __shfl_xor_sync(0xffffffffu, e, 1);
+            if ((lane & 3) == 0 && c_of_lane >= 0) wacc[slotn * wpn + pw][c_of_lane] = e;
+        }
         __syncthreads();
-        if (lane == 0 && pw == 0 && slotn < K) {
-            const int node = int(blockIdx.x) + slotn * G;
+        if (pw == 0 && slotn < K) {  // uniform over the warp
+            // lane c < 5: sum c over the node's parts in part order; lane 0 gathers the five
+            double vc = 0;
+            if (lane < 5) {
+                vc = wacc[slotn * wpn][lane];
+                for (int w = 1; w < wpn; ++w) vc += wacc[slotn * wpn + w][lane];
+            }
             double v[5];
 #pragma unroll
-            for (int c = 0; c < 5; ++c) {
-                v[c] = wacc[warp][c];
-                for (int w = 1; w < wpn; ++w) v[c] += wacc[warp + w][c];
+            for (int c = 0; c < 5; ++c) v[c] = __shfl_sync(0xffffffffu, vc, c);
+            if (lane == 0) {
+                const int node = int(blockIdx.x) + slotn * G;
+                double *slab = hist + (long long)n * p.hist_stride;
+                slab[node] = v[0];
+                if (node + N < p.P[0]) slab[node + N] = v[0];
+                store_kick_entry(tables + (long long)n * p.table_stride, N, node, float(v[2]), float(v[3]),
+                                 float(v[4]));
+                epart[(long long)(n - n0) * N + node] = rs[node] * v[1];
             }
-            double *slab = hist + (long long)n * p.hist_stride;
-            slab[node] = v[0];
-            if (node + N < p.P[0]) slab[node + N] = v[0];
-            store_kick_entry(tables + (long long)n * p.table_stride, N, node, float(v[2]), float(v[3]), float(v[4]));
-            epart[(long long)(n - n0) * N + node] = rs[node] * v[1];
         }
         if (!barrier(n)) return;
     }

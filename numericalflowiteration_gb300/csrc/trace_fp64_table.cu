@@ -38,10 +38,20 @@
 //
 // 3D (order 4): a per-cell table would hold 144 doubles per cell, 477 MB
 // for the 16^3 x 32^3, 101-step run, beyond L2; the kernel keeps the 4^3
-// window contraction of trace_fp64.cu on the FP64 slab (55 KB, L2-resident)
-// and takes only the cell-unit drift and locate (4 DADD per axis against
-// about 9 for drift, wrap and locate) and the kick V += -(dt/dx)^2 dS/dxi
-// (one DFMA per axis).
+// window contraction of trace_fp64.cu on the slab (55 KB, L2-resident) and
+// takes the cell-unit drift and locate (4 DADD per axis against about 9 for
+// drift, wrap and locate) and the kick V += -(dt/dx)^2 dS/dxi (one DFMA per
+// axis).  The contraction (188 multiply-adds) and the cubic bases run in
+// double-float arithmetic on the FP32 pipe: each value a pair of floats
+// (hi, lo), hi + lo its value to about 2^-48 relative, with Dekker's and
+// Knuth's error-free sum and product (T. J. Dekker, "A floating-point
+// technique for extending the available precision", Numer. Math. 18, 1971;
+// the product's error term by one FMA).  The slab is read as such pairs
+// (derive_ff3d_kernel writes them beside each FP64 slab), the fractions are
+// split once per substep, and E goes back to FP64 for the kick: 36 FP64
+// and about 3,300 FP32 operations per point-substep instead of about 240
+// FP64 ones.  Each multiply-add's error is below 2^-47 of its operands'
+// magnitudes (FP64: 2^-53), far below the 1e-12 parity bar.
 //
 // Thread mapping and the deterministic rho rows are trace_fp64.cu's: a warp
 // is 32 consecutive spatial nodes at one velocity node, PPT velocity nodes
@@ -81,6 +91,76 @@ __device__ __forceinline__ int cell_of(int U, int N)
         const int J = U % N;
         return J + (J < 0 ? N : 0);
     }
+}
+
+// Double-float arithmetic (see the file comment).  Every operation goes
+// through the _rn intrinsics, which the compiler never contracts into an
+// FMA: the error-free transformations need each rounding as written.
+struct ff {
+    float hi, lo;
+};
+__device__ __forceinline__ ff ff_of(double x)
+{
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - double(h))};
+}
+__device__ __forceinline__ double ff_value(ff a) { return double(a.hi) + double(a.lo); }
+// hi + lo renormalised, |s| >= |e| (Dekker's fast two-sum)
+__device__ __forceinline__ ff ff_norm(float s, float e)
+{
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+// a + b: Knuth's two-sum of the high parts, the low parts added to its error
+__device__ __forceinline__ ff ff_add(ff a, ff b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    return ff_norm(s, e);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.hi, -a.lo}; }
+// a b: the exact product of the high parts (its error by one FMA) plus the
+// cross terms (a.lo b.lo, below 2^-48 of the product, dropped)
+__device__ __forceinline__ ff ff_mul(ff a, ff b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return ff_norm(p, e);
+}
+// a b + c
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float pe = __fmaf_rn(a.hi, b.hi, -p);
+    pe = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, pe));
+    const float s = __fadd_rn(p, c.hi);
+    const float bb = __fsub_rn(s, p);
+    float e = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bb)), __fsub_rn(c.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(pe, c.lo));
+    return ff_norm(s, e);
+}
+// a times a power of two (exact)
+__device__ __forceinline__ ff ff_scale2(ff a, float s) { return {__fmul_rn(a.hi, s), __fmul_rn(a.lo, s)}; }
+
+// cubic_bd_fp64 (nufi_common.cuh) in double-float: the four cubic B-spline
+// values and derivatives on a cell at fraction t; c6 = 1/6, c23 = 2/3.
+__device__ __forceinline__ void cubic_bd_ff(ff t, ff c6, ff c23, ff (&b)[4], ff (&d)[4])
+{
+    const ff one = {1.0f, 0.0f};
+    const ff s = ff_add(one, ff_neg(t));
+    const ff t2 = ff_mul(t, t), s2 = ff_mul(s, s);
+    const ff t3 = ff_mul(t2, t);
+    b[0] = ff_mul(ff_mul(s2, s), c6);
+    b[3] = ff_mul(t3, c6);
+    b[1] = ff_add(ff_scale2(t3, 0.5f), ff_add(c23, ff_neg(t2)));
+    b[2] = ff_add(ff_add(ff_add(one, ff_neg(b[0])), ff_neg(b[1])), ff_neg(b[3]));
+    d[0] = ff_scale2(s2, -0.5f);
+    d[3] = ff_scale2(t2, 0.5f);
+    d[1] = ff_mul(t, ff_add(ff_mul(t, ff{1.5f, 0.0f}), ff{-2.0f, 0.0f}));
+    d[2] = ff_neg(ff_add(ff_add(d[0], d[1]), d[3]));
 }
 
 }  // namespace
@@ -209,15 +289,16 @@ __global__ void __launch_bounds__(256) trace_fp64_2d_table_kernel(const Problem 
 }
 
 template <int PPT, bool POW2>
-__global__ void __launch_bounds__(256, 2) trace_fp64_3d_cells_kernel(const Problem p, const double *__restrict__ hist,
-                                                                  int n, long long q_begin, long long q_end,
-                                                                  int vblocks, double *__restrict__ partial,
-                                                                  unsigned *err)
+__global__ void __launch_bounds__(256, 2) trace_fp64_3d_cells_kernel(const Problem p, const float2 *__restrict__ tff,
+                                                                  long long tstride, int n, long long q_begin,
+                                                                  long long q_end, int vblocks,
+                                                                  double *__restrict__ partial, unsigned *err)
 {
     const int lane = threadIdx.x, warp = threadIdx.y, W = blockDim.y;
     const long long s = (long long)blockIdx.x * 32 + lane;
     const long long Ns = p.Ns;
     const int sy = p.P[0], sz = p.P[0] * p.P[1];
+    const ff c6 = ff_of(1.0 / 6.0), c23 = ff_of(2.0 / 3.0);
     double K[3], vs[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -246,47 +327,50 @@ __global__ void __launch_bounds__(256, 2) trace_fp64_3d_cells_kernel(const Probl
             rm /= p.M[a];
         }
     }
-    auto substep = [&](const double *__restrict__ c, double h) {
+    auto substep = [&](const float2 *__restrict__ c, double h) {
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) drift_cells(U[q][a], X[q][a], V[q][a]);
-            const double *__restrict__ w = c + (long long)cell_of<POW2>(U[q][2], p.N[2]) * sz +
+            const float2 *__restrict__ w = c + (long long)cell_of<POW2>(U[q][2], p.N[2]) * sz +
                                            (long long)cell_of<POW2>(U[q][1], p.N[1]) * sy +
                                            cell_of<POW2>(U[q][0], p.N[0]);
-            double bx[4], dx[4], by[4], dy[4], bz[4], dz[4];
-            cubic_bd_fp64(X[q][0], bx, dx);
-            cubic_bd_fp64(X[q][1], by, dy);
-            cubic_bd_fp64(X[q][2], bz, dz);
-            double ex = 0, ey = 0, ez = 0;
+            // the window contraction of trace_fp64.cu's field_3d<4>, in double-float
+            ff bx[4], dx[4], by[4], dy[4], bz[4], dz[4];
+            cubic_bd_ff(ff_of(X[q][0]), c6, c23, bx, dx);
+            cubic_bd_ff(ff_of(X[q][1]), c6, c23, by, dy);
+            cubic_bd_ff(ff_of(X[q][2]), c6, c23, bz, dz);
+            const ff zero = {0.0f, 0.0f};
+            ff ex = zero, ey = zero, ez = zero;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                double sx = 0, s_y = 0, s_z = 0;
+                ff sx = zero, s_y = zero, s_z = zero;
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    double r0 = 0, r1 = 0;
+                    ff r0 = zero, r1 = zero;
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
-                        const double v = __ldg(w + k * sz + j * sy + i);
-                        r0 = fma(v, bx[i], r0);
-                        r1 = fma(v, dx[i], r1);
+                        const float2 v2 = __ldg(w + k * sz + j * sy + i);
+                        const ff v = {v2.x, v2.y};
+                        r0 = ff_fma(v, bx[i], r0);
+                        r1 = ff_fma(v, dx[i], r1);
                     }
-                    sx = fma(r1, by[j], sx);
-                    s_y = fma(r0, dy[j], s_y);
-                    s_z = fma(r0, by[j], s_z);
+                    sx = ff_fma(r1, by[j], sx);
+                    s_y = ff_fma(r0, dy[j], s_y);
+                    s_z = ff_fma(r0, by[j], s_z);
                 }
-                ex = fma(sx, bz[k], ex);
-                ey = fma(s_y, bz[k], ey);
-                ez = fma(s_z, dz[k], ez);
+                ex = ff_fma(sx, bz[k], ex);
+                ey = ff_fma(s_y, bz[k], ey);
+                ez = ff_fma(s_z, dz[k], ez);
             }
-            V[q][0] = fma(h * K[0], ex, V[q][0]);
-            V[q][1] = fma(h * K[1], ey, V[q][1]);
-            V[q][2] = fma(h * K[2], ez, V[q][2]);
+            V[q][0] = fma(h * K[0], ff_value(ex), V[q][0]);
+            V[q][1] = fma(h * K[1], ff_value(ey), V[q][1]);
+            V[q][2] = fma(h * K[2], ff_value(ez), V[q][2]);
         }
     };
     if (n > 0) {
-        for (int k = n - 1; k >= 1; --k) substep(hist + (long long)k * p.hist_stride, 1.0);
-        substep(hist, 0.5);
+        for (int k = n - 1; k >= 1; --k) substep(tff + (long long)k * tstride, 1.0);
+        substep(tff, 0.5);
     }
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
@@ -304,6 +388,16 @@ __global__ void __launch_bounds__(256, 2) trace_fp64_3d_cells_kernel(const Probl
     }
     }
     write_partial_tiled(acc, s, Ns, partial);
+}
+
+// The double-float pairs of one 3D slab: (hi, lo) with hi the coefficient
+// rounded to FP32 and lo the rest rounded to FP32 (see the file comment).
+__global__ void derive_ff3d_kernel(const Problem p, const double *__restrict__ slab, float2 *__restrict__ out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.stride_t) return;
+    const ff v = ff_of(slab[i]);
+    out[i] = make_float2(v.hi, v.lo);
 }
 
 // The 24 coefficients of every cell of one 2D slab (see the file comment):
@@ -392,14 +486,19 @@ bool fp64_table_supported(const Problem &p, long long Nt)
 
 long long fp64_table_stride(const Problem &p)
 {
-    return p.dim == 1 ? (3LL * p.N[0] + 1) / 2 * 2 : p.dim == 2 ? (24LL * p.Ns + 1) / 2 * 2 : 0;
+    // 3D: the slab's double-float pairs, one float2 (8 bytes) per coefficient
+    return p.dim == 1 ? (3LL * p.N[0] + 1) / 2 * 2 : p.dim == 2 ? (24LL * p.Ns + 1) / 2 * 2 : p.hist_stride;
 }
 
 cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, double *table_slab, cudaStream_t st,
                                   double *hist_out)
 {
     if (hist_out && p.dim != 1) return cudaErrorInvalidValue;  // the copy form is 1D only
-    if (p.dim == 3) return cudaSuccess;                          // no table
+    if (p.dim == 3) {
+        derive_ff3d_kernel<<<unsigned((p.stride_t + 255) / 256), 256, 0, st>>>(p, hist_slab,
+                                                                          reinterpret_cast<float2 *>(table_slab));
+        return cudaGetLastError();
+    }
     if (p.dim == 1) {
         const long long n = hist_out ? p.stride_t : p.N[0];
         derive_table64_kernel<<<unsigned((n + 127) / 128), 128, 0, st>>>(p, hist_slab, table_slab, hist_out);
@@ -420,11 +519,12 @@ cudaError_t launch_trace_fp64_table(const Problem &p, const LaunchShape &ls, con
     bool pow2 = true;
     for (int a = 0; a < p.dim; ++a) pow2 = pow2 && (p.N[a] & (p.N[a] - 1)) == 0;
     if (p.dim == 3) {  // the planner caps 3D at 2 points per thread
+        const float2 *tff = reinterpret_cast<const float2 *>(tables);
 #define NUFI_LAUNCH3(K)                                                                                        \
     if (pow2)                                                                                                  \
-        trace_fp64_3d_cells_kernel<K, true><<<grid, block, 0, st>>>(p, hist, n, qb, qe, vb, partial, err);     \
+        trace_fp64_3d_cells_kernel<K, true><<<grid, block, 0, st>>>(p, tff, ts, n, qb, qe, vb, partial, err);  \
     else                                                                                                       \
-        trace_fp64_3d_cells_kernel<K, false><<<grid, block, 0, st>>>(p, hist, n, qb, qe, vb, partial, err);
+        trace_fp64_3d_cells_kernel<K, false><<<grid, block, 0, st>>>(p, tff, ts, n, qb, qe, vb, partial, err);
         switch (ls.ppt) {
         case 1: NUFI_LAUNCH3(1) break;
         case 2: NUFI_LAUNCH3(2) break;

@@ -85,6 +85,12 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
         shi[q] = nd.sig_hi;
         slo[q] = nd.sig_lo;
     }
+    // the FP64 part of this thread's f~ sum, constant over the run (chain order)
+    double gsum = 0;
+#pragma unroll
+    for (int q = 0; q < PPT; ++q)
+        if (live[q]) gsum += nodes[mv[q]].g;
+
     for (int j = threadIdx.x; j < 5 * N; j += blockDim.x) gs[j] = green[j];
     if (threadIdx.x == 0) {
         for (int r = 0; r < kRing; ++r) {
@@ -226,15 +232,16 @@ __global__ void __launch_bounds__(PPT > 4 ? 256 : 512, 1) run_split_1d_kernel(
         }
         gbase_prev = gbase;
         gbase += nchunks;
-        double acc = 0;
+        float ds = 0.f, dc = 0.f;
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
             if (!live[q]) continue;
             const SplitNode nd = nodes[mv[q]];
             float2 cs = __ldg(phase + I[q]);
             if constexpr (UNWRAP) cs = phase_unwrapped(cs, Wr[q] - n * ((nd.S0u - nd.S0) / N), p.phase_wrap[0]);
-            acc += double(delta_f0(f, nd, cs, xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
+            two_sum_acc(ds, dc, delta_f0(f, nd, cs, xi[q], (dwT[q] - dwTc[q]) - slo[q]));
         }
+        double acc = gsum + (double(ds) + double(dc));
         if (blockDim.x > unsigned(Nr)) {
             if (grp == 1) combine[s] = acc;
             __syncthreads();

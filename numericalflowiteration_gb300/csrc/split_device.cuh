@@ -188,6 +188,19 @@ __device__ __forceinline__ void sincos_small(float a, float &s, float &c)
 
 // f0(foot) - G(u0) in FP32: f0 = (1 + alpha cos kx) G(u), expm1 form so
 // the rounding is relative to the perturbation (see trace_split.cu).
+// A thread's f~ sum over its chains as the FP64 part sum_q g_q (constant
+// over the run) plus the FP32 deviations summed by Knuth's two-sum: the
+// running sum s and the sum c of its exact rounding errors, s + c within
+// about 2^-47 of the terms' magnitudes of the exact sum.  The _rn
+// intrinsics keep every rounding as written (no FMA contraction).
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x)
+{
+    const float t = __fadd_rn(s, x);
+    const float bb = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(x, bb)));
+    s = t;
+}
+
 __device__ __forceinline__ float delta_f0(const F0 &f, const SplitNode &nd, float2 cs, float xi, float dw)
 {
     float sp, cp;

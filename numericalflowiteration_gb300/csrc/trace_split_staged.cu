@@ -140,15 +140,19 @@ __global__ void __launch_bounds__(512, 1) trace_split_1d_staged_kernel(const Pro
     }
 
     const F0 f = make_f0(p);
-    double acc = 0;
+    // f~ summed as the whole-run kernel sums it (two_sum_acc): the same bits
+    double gsum = 0;
+    float ds = 0.f, dc = 0.f;
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
         if (!live[q]) continue;
         const SplitNode nd = nodes[mv[q]];
+        gsum += nd.g;
         float2 cs = __ldg(phase + I[q]);
         if constexpr (UNWRAP) cs = phase_unwrapped(cs, Wr[q] - n * ((nd.S0u - nd.S0) / N), p.phase_wrap[0]);
-        acc += double(delta_f0(f, nd, cs, xi[q], (dwT[q] - dwTc[q]) - slo[q])) + nd.g;
+        two_sum_acc(ds, dc, delta_f0(f, nd, cs, xi[q], (dwT[q] - dwTc[q]) - slo[q]));
     }
+    double acc = gsum + (double(ds) + double(dc));
     // groups of the same node combined in group order
     if (blockDim.x > unsigned(Nr)) {
         if (grp == 1) combine[s] = acc;

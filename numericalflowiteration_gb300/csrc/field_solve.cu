@@ -153,7 +153,10 @@ __device__ __forceinline__ double block_sum_warps(double v, double *red)
 // GB300 issues FP64 at 1/64 of the FP32 rate, so the kernel's time is its
 // FP64 instruction count: NCONV (Ns/32 + 5) warp instructions per node this
 // way, against NCONV (Ns/32 + 6 w) with a node's sum split over w warps.
-template <int NCONV>
+// D1: the 1D instance (the same values in the same order without the other
+// axes' index arithmetic: less code to fetch when the kernel starts cold,
+// as it does right after a trace in the drop-in loop).
+template <int NCONV, bool D1>
 __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     const Problem p, const double *__restrict__ rho, const double *__restrict__ green, int green_in_smem,
     double *__restrict__ slab, float *__restrict__ table, double *__restrict__ energy_partial,
@@ -203,7 +206,27 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     double acc[NCONV];
 #pragma unroll
     for (int c = 0; c < NCONV; ++c) acc[c] = 0;
-    if (i < Ns) {
+    if (D1 && i < Ns) {
+        for (int j = lane; j < Ns; j += kLd * 32) {
+            double g[kLd][NCONV];
+#pragma unroll
+            for (int u = 0; u < kLd; ++u) {
+                const int jj = j + 32 * u;
+                int m = i - jj;
+                m += m < 0 ? N0 : 0;
+#pragma unroll
+                for (int c = 0; c < NCONV; ++c) g[u][c] = jj < Ns ? G[c * Ns + m] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kLd; ++u) {
+                const int jj = j + 32 * u;
+                if (jj >= Ns) break;
+                const double r = rs[jj];
+#pragma unroll
+                for (int c = 0; c < NCONV; ++c) acc[c] = fma(g[u][c], r, acc[c]);
+            }
+        }
+    } else if (i < Ns) {
         const int i0 = i % N0, i1 = (i / N0) % N1, i2 = i / (N0 * N1);
         const int step0 = 32 % N0, step1 = (32 / N0) % N1, step2 = 32 / (N0 * N1);
         int j = lane;
@@ -244,7 +267,14 @@ __global__ void __launch_bounds__(kSolveThreads) circulant_solve_kernel(
     for (int c = 0; c < NCONV; ++c)
         for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
     double e_local = 0;
-    if (lane == 0 && i < Ns) {
+    if (D1 && lane == 0 && i < Ns) {
+        slab[i] = acc[0];
+        if (i + N0 < p.P[0]) slab[i + N0] = acc[0];
+        if constexpr (NCONV == 5) {
+            if (table) store_kick_entry(table, N0, i, float(acc[2]), float(acc[3]), float(acc[4]));
+        }
+        e_local = rs[i] * acc[1];
+    } else if (lane == 0 && i < Ns) {
         const int i0 = i % N0, i1 = (i / N0) % N1, i2 = i / (N0 * N1);
         const double cval = acc[0];
         // every padded position of node i: i_a and i_a + N_a while < P_a
@@ -481,11 +511,11 @@ cudaError_t field_solve_prepare(const SolvePlan &plan)
                                      2 * kSpectralMaxAxis * 16);
         return e;
     }
-    cudaError_t e = cudaFuncSetAttribute(circulant_solve_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(plan.smem));
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(circulant_solve_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(plan.smem));
+    cudaError_t e = cudaSuccess;
+    for (auto fn : {circulant_solve_kernel<2, false>, circulant_solve_kernel<5, false>, circulant_solve_kernel<2, true>,
+                    circulant_solve_kernel<5, true>})
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(plan.smem));
+    return e;
 }
 
 cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const double *rho, double *hist_slab,
@@ -498,14 +528,12 @@ cudaError_t launch_field_solve(const Problem &p, const SolvePlan &plan, const do
     }
     // without a table, c and phi only: the green rows 0 and 1 of either form
     const unsigned threads = 32u * unsigned(plan.nodes_per_block);
-    if (plan.nconv == 5 && table_slab)
-        circulant_solve_kernel<5><<<plan.blocks, threads, plan.smem, st>>>(
-            p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
-            energy_out, err, err_pub, seq_pub, seq);
-    else
-        circulant_solve_kernel<2><<<plan.blocks, threads, plan.smem, st>>>(
-            p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab, plan.energy_partial, plan.energy_counter,
-            energy_out, err, err_pub, seq_pub, seq);
+    const bool five = plan.nconv == 5 && table_slab;
+    auto fn = p.dim == 1 ? (five ? circulant_solve_kernel<5, true> : circulant_solve_kernel<2, true>)
+                         : (five ? circulant_solve_kernel<5, false> : circulant_solve_kernel<2, false>);
+    fn<<<plan.blocks, threads, plan.smem, st>>>(p, rho, plan.green, plan.green_in_smem, hist_slab, table_slab,
+                                               plan.energy_partial, plan.energy_counter, energy_out, err, err_pub,
+                                               seq_pub, seq);
     return cudaGetLastError();
 }
 

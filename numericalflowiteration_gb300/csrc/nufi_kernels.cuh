@@ -122,12 +122,13 @@ cudaError_t launch_trace_fp64(const Problem &p, const LaunchShape &ls, const dou
 bool fp64_order_supported(int dim, int order);
 // FP64 order-4 trace in cell units (trace_fp64_table.cu): 1D and 2D over
 // per-slab FP64 derivative tables of fp64_table_stride doubles per slab
-// (written by launch_derive_table64 from each FP64 slab), 3D on the slabs
-// (stride 0: no table).
+// (written by launch_derive_table64 from each FP64 slab), 3D over each
+// slab's double-float (hi, lo) pairs (one float2 per coefficient, the
+// slab's own stride).
 bool fp64_table_supported(const Problem &p, long long Nt);
 long long fp64_table_stride(const Problem &p);
-// the FP64 derivative table of one slab (1D, 2D); with hist_out (1D), the
-// slab is also copied there
+// the FP64 derivative table of one slab (1D, 2D) or its double-float pairs
+// (3D); with hist_out (1D), the slab is also copied there
 cudaError_t launch_derive_table64(const Problem &p, const double *hist_slab, double *table_slab, cudaStream_t st,
                                   double *hist_out = nullptr);
 cudaError_t launch_trace_fp64_table(const Problem &p, const LaunchShape &ls, const double *tables,

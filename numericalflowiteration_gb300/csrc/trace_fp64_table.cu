@@ -472,7 +472,7 @@ __global__ void derive_table64_kernel(const Problem p, const double *__restrict_
 // count that stays far inside int (|U| grows by at most |V| + 1 per
 // substep; the margin of 4 covers the kicks' change of V).
 // 2D: also a table of at most 4 GiB (24 doubles per cell and slab).  3D:
-// the cell-unit trace on the slab itself (no table).
+// the cell-unit trace on the slab's double-float pairs (the slab's size).
 bool fp64_table_supported(const Problem &p, long long Nt)
 {
     if (p.order != 4) return false;

@@ -373,6 +373,41 @@ def test_dropin_speculative_field_solve(nufi):
     assert rel_max(ea, er) <= 1e-6
 
 
+def test_dropin_speculation_partial_ranges_and_interleaved_calls(nufi):
+    """Partial q ranges (rho summed from two downloads) never equal the last
+    published rho, so the handle does not speculate; once it does, a launch
+    between compute_rho and field_solve (here compute_metrics) discards the
+    pending speculative solve.  Every field_solve equals a second handle's
+    ordinary solve of the same input, bit for bit."""
+    from numericalflowiteration_gb300.config import two_stream_1d
+    cfg = two_stream_1d(Nx=64, Nv=256, Nt=12, precision="fp32split")
+    half = cfg.n_points // 2
+    with nufi.Simulation(cfg) as sim, nufi.Simulation(cfg) as ref:
+        coeffs = np.zeros((cfg.Nt + 1) * sim.stride_t)
+        for n in range(cfg.Nt + 1):
+            l0 = sim.launches
+            if n < 5:
+                rho = np.zeros(cfg.n_spatial)
+                sim.compute_rho(n, 0, half)
+                sim.download_rho(rho)
+                sim.compute_rho(n, half, cfg.n_points)
+                sim.download_rho(rho)
+                assert sim.launches - l0 == 2, n  # no speculative solve behind either trace
+            else:
+                sim.compute_rho(n)
+                # the first full-range step enables the speculation in its field_solve
+                assert sim.launches - l0 == (1 if n == 5 else 2), n
+                rho = sim.download_rho(np.zeros(cfg.n_spatial))
+                if n == 9:
+                    sim.compute_metrics(n)
+                    sim.download_metrics()
+            slab, e = sim.field_solve(rho)
+            want_slab, want_e = ref.field_solve(rho)
+            assert np.array_equal(slab, want_slab) and e == want_e, n
+            coeffs[n * sim.stride_t:(n + 1) * sim.stride_t] = slab
+            sim.upload_phi(n, coeffs)
+
+
 def test_persistent_run_subrange_and_repeat(nufi):
     """Steps in two calls (0..k, k+1..Nt) and a repeated run give the same
     history as one call."""
